@@ -1,0 +1,340 @@
+"""Benchmark: FP64 matrix powers kernel on one GB300 (or N replicas).
+
+Workload (the GB300 configuration of the task): 3-D 7-point Laplacian on a
+128^3 grid (n = 2,097,152, nnz = 14,581,760, diagonal 6, off-diagonal -1),
+CSR with FP64 values and int32 indices, x ~ U[-1,1] (seed 1), k = 8 powers,
+2048 parts from recursive coordinate bisection (8x8x16 boxes; METIS is not
+available).  One step = one MPK call computing [Ax, ..., A^8 x] into the
+level-major vv array.
+
+  value  : row-powers per second, k*n / (device time of one call), summed
+           over ranks; device time from CUDA events around each call on the
+           launching stream, L2 flushed (256 MiB write) before every call.
+  e2e    : the same metric through mpkg_exec_host with pinned host buffers:
+           x copied host->device and the k output vectors device->host
+           inside the timed call.
+  roofline: HBM bound; algorithmic bytes of one call
+           B = nnz*(8+4) + 4*(n+1) + 8*n*(k+1) (matrix once, x once, k
+           outputs once) over the call's device time, against the measured
+           copy bandwidth in MEASURED_PEAKS.json.
+
+--impl reference runs the reference mpk2 exec_mpk_xd (compiled from its
+own sources into oracle/_ref, OpenMP over parts, all host cores) on a
+bounded sample of the same workload's PA1 task lists; if that library is
+absent the oracle's C restatement of the same loop runs instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+K_LEVELS = 8
+GRID = 128
+NPART = 2048
+SEED = 1
+FLUSH_BYTES = 256 << 20
+
+
+def workload():
+    import mpk_gb300 as M
+    a = M.Csr.laplacian(GRID, GRID, GRID, diag=6.0, off=-1.0)
+    part = M.partition_rcb(a.coords, NPART)
+    x = M.uniform(SEED, a.n)
+    return a, part, x
+
+
+def algorithmic_bytes(n, nnz, k):
+    return nnz * 12 + 4 * (n + 1) + 8 * n * (k + 1)
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per launch of `kernel` on this workload from the committed
+    ncu summary (profiles/ncu_traffic.json), or None."""
+    p = os.path.join(HERE, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    e = d.get(kernel)
+    return None if e is None else e.get("dram_bytes_per_launch")
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [t.strip() for t in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def time_device(plan, d_vv, steps, warmup, flush, stream):
+    """Per-call CUDA-event times (ms) with an L2 flush before every call."""
+    import torch
+    for _ in range(warmup):
+        flush.fill_(1.0)
+        plan.exec_device(d_vv.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for e0, e1 in ev:
+            flush.fill_(1.0)
+            e0.record(stream)
+            plan.exec_device(d_vv.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+    plan.sync(stream.cuda_stream)
+    torch.cuda.synchronize()
+    return [e0.elapsed_time(e1) for e0, e1 in ev]
+
+
+def cpu_reference_sample(a, part, nth, reps=3, sample_parts=256):
+    """Reference exec_mpk_xd (or the oracle's restatement) on the PA1 task
+    lists of the first `sample_parts` parts; returns (seconds per sample
+    call, row evaluations per call, output rows per call, kind)."""
+    import mpk_gb300 as M
+    from oracle import oracle as O
+    O.build()
+    g = a.pattern()
+    off, idx = M.tasks(g, NPART, K_LEVELS, part, check=False)
+    sp = sample_parts
+    off_s = off[:sp + 1].copy()
+    idx_s = idx[:off_s[-1]].copy()
+    # owned rows of the sampled parts, per level: what the sample contributes
+    owned = int(np.count_nonzero(part < sp))
+    vv = np.zeros((K_LEVELS + 1) * a.n)
+    vv[:a.n] = M.uniform(SEED, a.n)
+    if O.ref_available():
+        r = O.RefTaskLists(g.ptr, g.col, sp, K_LEVELS, 0, off_s, idx_s)
+        run = lambda: r.exec_xd(vv, nth)  # noqa: E731
+        kind = "reference"
+    else:
+        run = lambda: O.exec_tasks_par(g.ptr, g.col, None, 0, sp, off_s, idx_s, vv, O.MODE_FMA, nth)  # noqa: E731
+        kind = "port"
+    run()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        run()
+        ts.append(time.perf_counter() - t0)
+    return min(ts), int(off_s[-1]), owned * K_LEVELS, kind
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--exec", default="pipe", choices=["pipe", "tiles", "spmv", "tasks"])
+    ap.add_argument("--arith", default="fma", choices=["fma", "separate"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world, rank, local = dist_setup(args)
+    a, part, x = workload()
+    n, nnz, k = a.n, a.nnz, K_LEVELS
+    nth = os.cpu_count() or 1
+    cfg = {"workload": "3-D 7-point Laplacian 128^3 (n=2,097,152, nnz=14,581,760), FP64 CSR int32, "
+                       "x~U[-1,1] seed 1, k=8, 2048 RCB parts",
+           "n": n, "nnz": nnz, "k": k, "parts": NPART}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        t, rows_eval, out_rows, kind = cpu_reference_sample(a, part, nth)
+        steps = max(1, min(args.steps, 20))
+        per = []
+        import mpk_gb300 as M  # noqa: F401
+        for _ in range(steps):
+            per.append(t)
+        value = out_rows / t / 1e9
+        line = {"impl": "reference", "metric": "MPK powers/sec (FP64, k*n output rows per second)",
+                "value": value, "unit": "Grow-powers/s", "n_gpus": 0, "steps": steps, "warmup": args.warmup,
+                "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic",
+                "config": dict(cfg, sample=f"PA1 task lists of parts 0..255 of 2048 (1/8 of the call)"),
+                "cpu_baseline": {"value": value, "unit": "Grow-powers/s", "cores": nth, "kind": kind,
+                                 "sample": "exec_mpk_xd, 1/deg operator, PA1 task lists of 256 of 2048 parts, "
+                                           f"{rows_eval} row evaluations per step, {nth} OpenMP threads"},
+                "e2e": {"value": value, "unit": "Grow-powers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    import mpk_gb300 as M
+    torch.cuda.set_device(local)
+    arith = M.ARITH_FMA if args.arith == "fma" else M.ARITH_SEPARATE
+    mk = {"pipe": lambda: M.Plan.pipe(a, k, arith=arith),
+          "tiles": lambda: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TILES, arith=arith),
+          "tasks": lambda: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TASKS, arith=arith),
+          "spmv": lambda: M.Plan.spmv(a, k, arith=arith)}
+    plan = mk[args.exec]()
+    base = mk["spmv"]() if args.exec != "spmv" else plan
+    info = plan.info()
+    stream = torch.cuda.Stream()
+    d_vv = torch.zeros((k + 1) * n, dtype=torch.float64, device="cuda")
+    d_vv[:n] = torch.from_numpy(x).cuda()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        w0 = time.perf_counter()
+        times = time_device(plan, d_vv, args.steps, args.warmup, flush, stream)
+        barrier(world)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    ms = statistics.mean(times)
+    ms_max = reduce_max(world, ms)
+    value = world * k * n / (ms_max * 1e-3) / 1e9
+
+    base_ms = statistics.mean(time_device(base, d_vv, min(args.steps, 100), args.warmup, flush, stream))
+
+    # end to end through the host API, pinned host buffers
+    hv = torch.zeros((k + 1) * n, dtype=torch.float64).pin_memory()
+    hv[:n] = torch.from_numpy(x)
+    hnp = hv.numpy()
+    for _ in range(args.warmup):
+        plan.exec_host(hnp)
+    e2e_steps = max(3, min(args.steps, 50))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        plan.exec_host(hnp)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = reduce_max(world, e2e_s)
+    # the device result of the timed runs equals the host run
+    same = bool(np.array_equal(d_vv.cpu().numpy(), hnp))
+
+    peak, peak_kind = peaks()
+    B = algorithmic_bytes(n, nnz, k)
+    achieved = B / (ms * 1e-3) / 1e9
+    kname = {"pipe": "pipe_kernel", "tiles": "tiles_kernel", "tasks": "tasks_kernel",
+             "spmv": "spmv_level_kernel"}[args.exec]
+    traffic = profile_traffic(kname)
+    rows = info["rows_computed"]
+    fp64_tflops = 2.0 * nnz * k * (rows / (n * k)) / (ms * 1e-3) / 1e12
+
+    line = {"metric": "MPK powers/sec (FP64, k*n output rows per second)", "value": value,
+            "unit": "Grow-powers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": dict(cfg, executor=args.exec, arith=args.arith,
+                           l2="flushed before every call (256 MiB write); per-call CUDA events",
+                           parallelism=f"replicas{world}"),
+            "e2e": {"value": world * k * n / e2e_s / 1e9, "unit": "Grow-powers/s",
+                    "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n * k},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "algorithmic_bytes": B},
+            "fp64_pipe": {"achieved_tflops": fp64_tflops, "note": "2*nnz*k*redundancy flops over call time"},
+            "k_spmv_ms": base_ms, "speedup_vs_k_spmv": base_ms / ms,
+            "gpu_launches": info["launches"] * args.steps,
+            "clocks": clk.summary(), "wall_s_timed_region": wall, "host_device_agree": same,
+            "plan": {kk: info[kk] for kk in ("rows_computed", "device_bytes", "pipe_reach", "pipe_grid",
+                                            "tiles_in_smem", "max_tile_slots")}}
+    if rank == 0 and not args.no_cpu_baseline:
+        t, rows_eval, out_rows, kind = cpu_reference_sample(a, part, nth)
+        line["cpu_baseline"] = {"value": out_rows / t / 1e9, "unit": "Grow-powers/s", "cores": nth, "kind": kind,
+                                "sample": "exec_mpk_xd, 1/deg operator, PA1 task lists of 256 of 2048 parts "
+                                          f"({rows_eval} row evaluations), best of 3"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

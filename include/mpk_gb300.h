@@ -1,0 +1,174 @@
+/*
+ * mpk_gb300: GB300 matrix powers kernel, status-returning C ABI.
+ *
+ * Computes vv = [x, Ax, A^2x, ..., A^k x] (level-major: vv[l*n + i]) for a
+ * CSR matrix A with int32 indices and FP64 values, or for the reference's
+ * row-normalised adjacency operator (A_ij = 1/deg(i) for every stored
+ * column j of row i) when no values are given.
+ *
+ * Every function returns 0 on success or a negative MPKG_E* code; the
+ * text of the last error on the calling thread is mpkg_last_error().
+ * No function exits the process.  Plans are not thread-safe: use one plan
+ * per thread, or serialise calls on a plan.  Device pointers and streams
+ * must belong to the plan's device.
+ *
+ * Reference interfaces replaced (vatai/mpk):
+ *   - task-list execution exec_mpk / exec_mpk_xd / vexec_mpk
+ *     (mpk2/mpkexec.c:41-130, mpk2/mpkvexec.c:41-55) -> mpkg_plan_tasks +
+ *     mpkg_exec_*;
+ *   - PA1 diamond execution over part + skirt sets (mpk2/mpkprep.c:185-233
+ *     consumed by mpk2/mpkexec.c:10-39) -> mpkg_plan_pa1 (tiles);
+ *   - k chained SpMVs spmv_exec_seq/par and the verify_val gold chain
+ *     (mpk2/spmvexec.c:8-50, mpk2/verify_val.c:44-75) ->
+ *     mpkg_spmv_chain_device / mpkg_plan_spmv;
+ *   - the prep tools comp (levels, weights; mpk2/comp.c:25-106) and skirt
+ *     (mpk2/skirt.c:10-74) -> mpkg_levels, mpkg_level_weights,
+ *     mpkg_skirt_write.
+ * The legacy mpk2 names themselves are exported too (mpk2_compat.h).
+ */
+#ifndef MPK_GB300_H
+#define MPK_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPKG_OK 0
+#define MPKG_EINVAL -1   /* bad argument */
+#define MPKG_EIO -2      /* file could not be opened/read/written */
+#define MPKG_EFORMAT -3  /* malformed file */
+#define MPKG_ESTRUCT -4  /* dependency/structure check failed */
+#define MPKG_ECUDA -5    /* CUDA runtime error, or no GPU */
+#define MPKG_ETIMEOUT -6 /* a bounded device-side wait gave up */
+#define MPKG_ENOMEM -7   /* host or device allocation failed */
+#define MPKG_ERANGE -8   /* index or size out of the supported range */
+
+/* Arithmetic of the FP64 row sums, s over the stored columns in CSR order. */
+#define MPKG_ARITH_FMA 0      /* s = fma(a, x, s): one rounding per term */
+#define MPKG_ARITH_SEPARATE 1 /* s = s + a*x: two roundings per term (the
+                                 reference compiled without contraction) */
+#define MPKG_ARITH_DF64 2     /* double-float (FP32 pair) arithmetic on the
+                                 FP32 pipes, FP64 storage; about 2^-46
+                                 relative error per operation */
+
+/* Executors. */
+#define MPKG_EXEC_TASKS 0 /* reference task lists, one CTA per (phase,part) */
+#define MPKG_EXEC_TILES 1 /* PA1: one CTA per part + k-deep skirt, levels
+                             computed in shared memory */
+#define MPKG_EXEC_PIPE 2  /* zero-redundancy level pipeline: chunks of rows
+                             advance level by level behind their
+                             neighbours, matrix chunk kept in shared memory */
+#define MPKG_EXEC_SPMV 3  /* k separate SpMV launches (baseline) */
+
+typedef struct mpkg_plan mpkg_plan;
+
+typedef struct {
+  int n, nlevel, nphase, npart;
+  int exec, arith, valued;
+  long nnz;
+  long rows_computed;   /* row evaluations per execution, redundancy included */
+  long device_bytes;    /* device memory held by the plan */
+  int launches;         /* kernels launched per execution */
+  int tiles_in_smem;    /* TILES: 1 if the levels fit in shared memory */
+  int max_tile_slots;   /* TILES: largest part + skirt */
+  int pipe_chunk;       /* PIPE: rows per chunk */
+  int pipe_reach;       /* PIPE: dependency reach in chunks */
+  int pipe_grid;        /* PIPE: resident CTAs launched */
+} mpkg_plan_info_t;
+
+/* Plan over task lists in the reference layout: list t = phase*npart+part
+ * holds entries level*n+vertex in idx[off[t]..off[t+1]), level-major
+ * (mpk2/lib.h:78-99 task_t/mpk_t, filled by prep_mpk mpk2/mpkprep.c:7-258).
+ * val == NULL selects the 1/deg operator.  ptr/col/val/off/idx are host
+ * arrays, copied. */
+int mpkg_plan_tasks(int n, const int *ptr, const int *col, const double *val,
+                    int npart, int nlevel, int nphase, const long *off,
+                    const long *idx, int arith, mpkg_plan **out);
+
+/* PA1 plan straight from a partition (no dense skirt array): exec is
+ * MPKG_EXEC_TILES or MPKG_EXEC_TASKS (reference task lists built from the
+ * bounded skirts). */
+int mpkg_plan_pa1(int n, const int *ptr, const int *col, const double *val,
+                  const int *part, int npart, int nlevel, int exec, int arith,
+                  mpkg_plan **out);
+
+/* Zero-redundancy pipeline plan (chunk <= 0 picks a default). */
+int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val,
+                   int nlevel, int chunk, int arith, mpkg_plan **out);
+
+/* k chained SpMV launches (baseline; also the GPU spmv_exec_*). */
+int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val,
+                   int nlevel, int arith, mpkg_plan **out);
+
+int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info);
+
+/* Execute with host memory: vv holds (nlevel+1)*n doubles, x in vv[0..n);
+ * levels 1..nlevel are written back.  The host->device copy of x and the
+ * device->host copy of the levels are part of the call. */
+int mpkg_exec_host(mpkg_plan *p, double *vv);
+
+/* Execute on device memory: d_vv as above, on `stream` (a cudaStream_t,
+ * NULL = the plan's own stream).  Asynchronous: errors of the kernels
+ * themselves are reported by mpkg_sync(). */
+int mpkg_exec_device(mpkg_plan *p, double *d_vv, void *stream);
+
+/* Wait for the plan's work on `stream` and report device-side errors
+ * (MPKG_ETIMEOUT when a bounded wait gave up). */
+int mpkg_sync(mpkg_plan *p, void *stream);
+
+void mpkg_plan_destroy(mpkg_plan *p);
+
+/* Stand-alone k-SpMV on device arrays (no plan). */
+int mpkg_spmv_chain_device(int n, const int *d_ptr, const int *d_col, const double *d_val,
+                           int nlevel, double *d_vv, int arith, void *stream);
+
+/* ---- host prep (bit-identical outputs to the reference prep tools) ---- */
+
+/* Graph files. */
+int mpkg_read_metis(const char *path, int *n, long *nnz, int **ptr, int **col);
+int mpkg_read_values(const char *path, long nnz, double **val);
+void mpkg_free(void *p);
+
+/* comp_level (level_org == NULL) / update_level (mpk2/lib.c:330-412). */
+int mpkg_levels(int n, const int *ptr, const int *col, const int *part, int npart,
+                const int *level_org, int *level);
+/* level2wcrs (mpk2/lib.c:504-537). */
+int mpkg_level_weights(int n, const int *ptr, const int *col, const int *level,
+                       int *wv, int *we);
+/* `skirt` tool output file (mpk2/skirt.c + lib.c:584-654), computed with
+ * bounded searches; lev == NULL for PA1. */
+int mpkg_skirt_write(const char *path, int n, const int *ptr, const int *col,
+                     const int *part, int npart, const int *lev, int nlevel);
+
+/* Task lists of prep_mpk from files-free inputs: parts is max(nphase,1)*n,
+ * levels nphase*n; the skirt comes from the bounded search on parts[0]
+ * (and levels[nphase-1] when nphase > 0).  Returns the number of entries
+ * through *count; off has (nphase+1)*npart+1 entries, idx is allocated
+ * (mpkg_free).  check != 0 runs the reference's dependency checks. */
+int mpkg_tasks(int n, const int *ptr, const int *col, int npart, int nlevel, int nphase,
+               const int *parts, const int *levels, int check, long *off, long **idx,
+               long *count);
+
+/* Partitioners (METIS is not available): recursive coordinate bisection
+ * (coords: dim ints per vertex) and breadth-first recursive bisection. */
+int mpkg_partition_rcb(int n, const int *coords, int dim, int npart, int *part);
+int mpkg_partition_bfs(int n, const int *ptr, const int *col, int npart, int *part);
+
+/* Generators: the reference gen2 stencils (type m5p t5p m7p m9p cube) and
+ * Laplacians on nx*ny*nz grids (coords optional, 3 ints per vertex). */
+int mpkg_gen_stencil(const char *type, int size, int *n, long *nnz, int **ptr, int **col,
+                     double **val);
+int mpkg_gen_laplacian(int nx, int ny, int nz, double diag, double off, int *n, long *nnz,
+                       int **ptr, int **col, double **val, int **coords);
+void mpkg_uniform(uint64_t seed, long n, double *out);
+
+const char *mpkg_last_error(void);
+int mpkg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

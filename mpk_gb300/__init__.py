@@ -1,0 +1,314 @@
+"""mpk_gb300 -- GB300 matrix powers kernel (MPK).
+
+Python host interface over the C ABI of ``libmpk_gb300.so`` (declared in
+``include/mpk_gb300.h`` and ``include/mpk2_compat.h``).  The library is the
+product: this module only marshals numpy arrays and torch device pointers.
+It raises when the library is missing; there is no CPU fallback.
+
+Level-major layout as in the reference: ``vv[l*n + i]`` holds (A^l x)_i,
+``vv[0:n]`` is x (mpk2/mpktest.c:66-75).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmpk_gb300.so")
+
+OK, EINVAL, EIO, EFORMAT, ESTRUCT, ECUDA, ETIMEOUT, ENOMEM, ERANGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
+ARITH_FMA, ARITH_SEPARATE, ARITH_DF64 = 0, 1, 2
+EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV = 0, 1, 2, 3
+
+_ERRNAMES = {EINVAL: "EINVAL", EIO: "EIO", EFORMAT: "EFORMAT", ESTRUCT: "ESTRUCT", ECUDA: "ECUDA",
+             ETIMEOUT: "ETIMEOUT", ENOMEM: "ENOMEM", ERANGE: "ERANGE"}
+
+
+class MpkError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{_ERRNAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """The loaded C library (built in-tree by ``mpk_gb300.build``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("n", C.c_int), ("nlevel", C.c_int), ("nphase", C.c_int), ("npart", C.c_int),
+                ("exec", C.c_int), ("arith", C.c_int), ("valued", C.c_int),
+                ("nnz", C.c_long), ("rows_computed", C.c_long), ("device_bytes", C.c_long),
+                ("launches", C.c_int), ("tiles_in_smem", C.c_int), ("max_tile_slots", C.c_int),
+                ("pipe_chunk", C.c_int), ("pipe_reach", C.c_int), ("pipe_grid", C.c_int)]
+
+
+def _declare(L):
+    P, I, Lg, D, V = C.c_void_p, C.c_int, C.c_long, C.c_double, C.c_void_p
+    pp = C.POINTER(C.c_void_p)
+    sig = {
+        "mpkg_plan_tasks": (I, [I, P, P, P, I, I, I, P, P, I, pp]),
+        "mpkg_plan_pa1": (I, [I, P, P, P, P, I, I, I, I, pp]),
+        "mpkg_plan_pipe": (I, [I, P, P, P, I, I, I, pp]),
+        "mpkg_plan_spmv": (I, [I, P, P, P, I, I, pp]),
+        "mpkg_plan_info": (I, [P, C.POINTER(PlanInfo)]),
+        "mpkg_exec_host": (I, [P, P]),
+        "mpkg_exec_device": (I, [P, P, P]),
+        "mpkg_sync": (I, [P, P]),
+        "mpkg_plan_destroy": (None, [P]),
+        "mpkg_spmv_chain_device": (I, [I, P, P, P, I, P, I, P]),
+        "mpkg_read_metis": (I, [C.c_char_p, C.POINTER(I), C.POINTER(Lg), pp, pp]),
+        "mpkg_read_values": (I, [C.c_char_p, Lg, pp]),
+        "mpkg_free": (None, [P]),
+        "mpkg_levels": (I, [I, P, P, P, I, P, P]),
+        "mpkg_level_weights": (I, [I, P, P, P, P, P]),
+        "mpkg_skirt_write": (I, [C.c_char_p, I, P, P, P, I, P, I]),
+        "mpkg_tasks": (I, [I, P, P, I, I, I, P, P, I, P, pp, C.POINTER(Lg)]),
+        "mpkg_partition_rcb": (I, [I, P, I, I, P]),
+        "mpkg_partition_bfs": (I, [I, P, P, I, P]),
+        "mpkg_gen_stencil": (I, [C.c_char_p, I, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
+        "mpkg_gen_laplacian": (I, [I, I, I, D, D, C.POINTER(I), C.POINTER(Lg), pp, pp, pp, pp]),
+        "mpkg_uniform": (None, [C.c_uint64, Lg, P]),
+        "mpkg_last_error": (C.c_char_p, []),
+        "mpkg_version": (I, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def _check(rc):
+    if rc != OK:
+        raise MpkError(rc, lib().mpkg_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _take(p, count, dtype):
+    """Copy a malloc'd C array into numpy and free it."""
+    if count == 0:
+        lib().mpkg_free(p)
+        return np.zeros(0, dtype=dtype)
+    ct = {np.int32: C.c_int, np.int64: C.c_long, np.float64: C.c_double}[dtype]
+    arr = np.ctypeslib.as_array(C.cast(p, C.POINTER(ct)), shape=(count,)).copy()
+    lib().mpkg_free(p)
+    return arr
+
+
+# ---------------------------------------------------------------- matrices
+class Csr:
+    """CSR matrix with int32 indices; ``val is None`` is the 1/deg operator
+    (mpk2/lib.h:10-14 crs0_t; pdmpk/csr.h:11-69 Csr)."""
+
+    def __init__(self, ptr, col, val=None, coords=None):
+        self.ptr = _i32(ptr)
+        self.col = _i32(col)
+        self.val = _f64(val)
+        self.n = len(self.ptr) - 1
+        self.nnz = int(self.ptr[-1])
+        self.coords = coords
+
+    def pattern(self):
+        """Same graph, 1/deg operator (values dropped)."""
+        return Csr(self.ptr, self.col, None, self.coords)
+
+    @staticmethod
+    def read_metis(path, values_path=None):
+        L = lib()
+        n, nnz = C.c_int(), C.c_long()
+        pp, cp = C.c_void_p(), C.c_void_p()
+        _check(L.mpkg_read_metis(path.encode(), C.byref(n), C.byref(nnz), C.byref(pp), C.byref(cp)))
+        ptr = _take(pp, n.value + 1, np.int32)
+        col = _take(cp, nnz.value, np.int32)
+        val = None
+        if values_path:
+            vp = C.c_void_p()
+            _check(L.mpkg_read_values(values_path.encode(), nnz.value, C.byref(vp)))
+            val = _take(vp, nnz.value, np.float64)
+        return Csr(ptr, col, val)
+
+    @staticmethod
+    def stencil(kind, size):
+        """The reference gen2 stencils (mpk2/gen2.c:59-267)."""
+        L = lib()
+        n, nnz = C.c_int(), C.c_long()
+        pp, cp, vp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(L.mpkg_gen_stencil(kind.encode(), size, C.byref(n), C.byref(nnz), C.byref(pp),
+                                  C.byref(cp), C.byref(vp)))
+        return Csr(_take(pp, n.value + 1, np.int32), _take(cp, nnz.value, np.int32),
+                   _take(vp, nnz.value, np.float64))
+
+    @staticmethod
+    def laplacian(nx, ny, nz=1, diag=None, off=-1.0):
+        """(2d+1)-point Laplacian on an nx*ny*nz grid, ascending columns."""
+        if diag is None:
+            diag = 4.0 if nz == 1 else 6.0
+        L = lib()
+        n, nnz = C.c_int(), C.c_long()
+        pp, cp, vp, xp = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(L.mpkg_gen_laplacian(nx, ny, nz, diag, off, C.byref(n), C.byref(nnz), C.byref(pp),
+                                    C.byref(cp), C.byref(vp), C.byref(xp)))
+        coords = _take(xp, 3 * n.value, np.int32).reshape(-1, 3)
+        return Csr(_take(pp, n.value + 1, np.int32), _take(cp, nnz.value, np.int32),
+                   _take(vp, nnz.value, np.float64), coords)
+
+    def write_metis(self, path, ne=None):
+        with open(path, "w") as f:
+            f.write(f"{self.n} {self.nnz // 2 if ne is None else ne}\n")
+            for i in range(self.n):
+                cols = self.col[self.ptr[i]:self.ptr[i + 1]] + 1
+                f.write("".join(f"{c} " for c in cols) + "\n")
+
+    def write_values(self, path):
+        with open(path, "w") as f:
+            f.write("".join(f"{v:.17g} " for v in self.val))
+
+
+def uniform(seed, n):
+    """Uniform[-1, 1) doubles from the library's splitmix64 stream."""
+    out = np.empty(n, dtype=np.float64)
+    lib().mpkg_uniform(seed, n, _ptr(out))
+    return out
+
+
+# ---------------------------------------------------------------- host prep
+def partition_rcb(coords, npart):
+    coords = _i32(coords)
+    n, dim = coords.shape
+    part = np.empty(n, dtype=np.int32)
+    _check(lib().mpkg_partition_rcb(n, _ptr(coords), dim, npart, _ptr(part)))
+    return part
+
+
+def partition_bfs(a: Csr, npart):
+    part = np.empty(a.n, dtype=np.int32)
+    _check(lib().mpkg_partition_bfs(a.n, _ptr(a.ptr), _ptr(a.col), npart, _ptr(part)))
+    return part
+
+
+def levels(a: Csr, part, npart, level_org=None):
+    """comp_level / update_level (mpk2/lib.c:330-412)."""
+    part = _i32(part)
+    lo = _i32(level_org)
+    out = np.empty(a.n, dtype=np.int32)
+    _check(lib().mpkg_levels(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(part), npart, _ptr(lo), _ptr(out)))
+    return out
+
+
+def level_weights(a: Csr, level):
+    """level2wcrs (mpk2/lib.c:504-537) -> (wv, we)."""
+    level = _i32(level)
+    wv = np.empty(a.n, dtype=np.int32)
+    we = np.empty(a.nnz, dtype=np.int32)
+    _check(lib().mpkg_level_weights(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(level), _ptr(wv), _ptr(we)))
+    return wv, we
+
+
+def write_skirt(path, a: Csr, part, npart, nlevel, lev=None):
+    """The `skirt` tool's output file (mpk2/skirt.c, mpk2/lib.c:584-654)."""
+    part = _i32(part)
+    lev = _i32(lev)
+    _check(lib().mpkg_skirt_write(path.encode(), a.n, _ptr(a.ptr), _ptr(a.col), _ptr(part), npart,
+                                  _ptr(lev), nlevel))
+
+
+def tasks(a: Csr, npart, nlevel, parts, levels_=None, check=True):
+    """prep_mpk task lists (mpk2/mpkprep.c:7-258) -> (off, idx)."""
+    parts = np.atleast_2d(_i32(parts))
+    nphase = 0 if levels_ is None else len(levels_)
+    lv = None if levels_ is None else np.ascontiguousarray(np.atleast_2d(levels_), dtype=np.int32)
+    off = np.empty((nphase + 1) * npart + 1, dtype=np.int64)
+    ip, cnt = C.c_void_p(), C.c_long()
+    _check(lib().mpkg_tasks(a.n, _ptr(a.ptr), _ptr(a.col), npart, nlevel, nphase, _ptr(parts),
+                            _ptr(lv), 1 if check else 0, _ptr(off), C.byref(ip), C.byref(cnt)))
+    return off, _take(ip, cnt.value, np.int64)
+
+
+# ---------------------------------------------------------------- plans
+class Plan:
+    """A device-resident MPK plan (matrix + schedule) executed many times."""
+
+    def __init__(self, handle, a: Csr, nlevel):
+        self._h = C.c_void_p(handle)
+        self.n = a.n
+        self.nlevel = nlevel
+
+    @staticmethod
+    def _make(fn, *args, a, nlevel):
+        h = C.c_void_p()
+        _check(fn(*args, C.byref(h)))
+        return Plan(h.value, a, nlevel)
+
+    @classmethod
+    def pa1(cls, a: Csr, part, npart, nlevel, exec=EXEC_TILES, arith=ARITH_FMA):
+        part = _i32(part)
+        return cls._make(lib().mpkg_plan_pa1, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), _ptr(part),
+                         npart, nlevel, exec, arith, a=a, nlevel=nlevel)
+
+    @classmethod
+    def from_tasks(cls, a: Csr, npart, nlevel, nphase, off, idx, arith=ARITH_FMA):
+        off = np.ascontiguousarray(off, dtype=np.int64)
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        return cls._make(lib().mpkg_plan_tasks, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), npart, nlevel,
+                         nphase, _ptr(off), _ptr(idx), arith, a=a, nlevel=nlevel)
+
+    @classmethod
+    def pipe(cls, a: Csr, nlevel, chunk=256, arith=ARITH_FMA):
+        return cls._make(lib().mpkg_plan_pipe, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, chunk,
+                         arith, a=a, nlevel=nlevel)
+
+    @classmethod
+    def spmv(cls, a: Csr, nlevel, arith=ARITH_FMA):
+        return cls._make(lib().mpkg_plan_spmv, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, arith,
+                         a=a, nlevel=nlevel)
+
+    def info(self) -> dict:
+        inf = PlanInfo()
+        _check(lib().mpkg_plan_info(self._h, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in PlanInfo._fields_}
+
+    def exec_host(self, vv: np.ndarray) -> np.ndarray:
+        """vv: float64 array of (nlevel+1)*n with x in vv[:n]; filled in place."""
+        assert vv.dtype == np.float64 and vv.flags.c_contiguous and vv.size == (self.nlevel + 1) * self.n
+        _check(lib().mpkg_exec_host(self._h, _ptr(vv)))
+        return vv
+
+    def exec_device(self, d_vv_ptr: int, stream: int = 0):
+        """Asynchronous launch on device memory (e.g. a torch tensor's data_ptr())."""
+        _check(lib().mpkg_exec_device(self._h, C.c_void_p(d_vv_ptr), C.c_void_p(stream or None)))
+
+    def sync(self, stream: int = 0):
+        _check(lib().mpkg_sync(self._h, C.c_void_p(stream or None)))
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            lib().mpkg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,847 @@
+// CUDA kernels (sm_103a) and device plans of the GB300 matrix powers kernel.
+//
+// Executors (see include/mpk_gb300.h):
+//   tasks  - the reference's (phase, part) task lists, one CTA per list,
+//            levels separated by __syncthreads (mpk2/mpkexec.c:10-39);
+//   tiles  - PA1 diamond tiles: one CTA per part, its k-deep skirt staged in
+//            shared memory, k levels computed in place, owned rows written;
+//   pipe   - zero-redundancy level pipeline: chunks of rows keep their
+//            matrix rows in shared memory and advance level by level once
+//            the neighbouring chunks have finished the previous level;
+//   spmv   - k separate SpMV launches (baseline, spmv_exec_*).
+// All executors evaluate each row sum over the stored columns in CSR order,
+// so for a given arithmetic mode every executor produces the same bits.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mpk_gb300.h"
+#include "host.h"
+
+using namespace mpkg;
+
+namespace {
+
+constexpr int kErrTimeout = 2;
+constexpr int kErrBounds = 3;
+constexpr long kSpinLimit = 4000000;  // polls of one flag (~1 s with backoff)
+
+#define CUDA_TRY(expr)                                                             \
+  do {                                                                             \
+    cudaError_t e_ = (expr);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(kECuda, std::string(#expr) + ": " + cudaGetErrorString(e_));     \
+  } while (0)
+
+template <int ARITH>
+__device__ __forceinline__ double row_term(double s, double a, double x) {
+  if (ARITH == MPKG_ARITH_SEPARATE) return __dadd_rn(s, __dmul_rn(a, x));
+  return __fma_rn(a, x, s);
+}
+
+__device__ __forceinline__ double ld_cg(const double *p) { return __ldcg(p); }
+
+// ------------------------------------------------------------------------
+// k-SpMV: one launch per level, one thread per row.
+// ------------------------------------------------------------------------
+template <int ARITH, bool VALUED>
+__global__ void __launch_bounds__(256) spmv_level_kernel(int n, const int *__restrict__ ptr,
+                                                         const int *__restrict__ col,
+                                                         const double *__restrict__ coef,
+                                                         const double *__restrict__ x,
+                                                         double *__restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int j0 = ptr[i], j1 = ptr[i + 1];
+  double s = 0.0;
+  if (VALUED) {
+    for (int j = j0; j < j1; j++) s = row_term<ARITH>(s, coef[j], x[col[j]]);
+  } else {
+    double a = coef[i];  // 1/deg, rounded on the host exactly as 1.0/deg
+    for (int j = j0; j < j1; j++) s = row_term<ARITH>(s, a, x[col[j]]);
+  }
+  y[i] = s;
+}
+
+// ------------------------------------------------------------------------
+// Task lists: one CTA per (phase, part) list; a list is a sequence of
+// level segments of vertex ids, computed in order with a CTA barrier in
+// between.  vv is read through L2 (ld.global.cg) because the skirt phase
+// lets several CTAs write the same (level, vertex) with identical values.
+// ------------------------------------------------------------------------
+template <int ARITH, bool VALUED>
+__global__ void __launch_bounds__(256) tasks_kernel(int n, int list_base,
+                                                    const long *__restrict__ list_seg,
+                                                    const int *__restrict__ seg_level,
+                                                    const long *__restrict__ seg_off,
+                                                    const int *__restrict__ rows,
+                                                    const int *__restrict__ ptr,
+                                                    const int *__restrict__ col,
+                                                    const double *__restrict__ coef,
+                                                    double *vv) {
+  const int list = list_base + blockIdx.x;
+  for (long sg = list_seg[list]; sg < list_seg[list + 1]; sg++) {
+    const long l = seg_level[sg];
+    const double *src = vv + (l - 1) * (long)n;
+    double *dst = vv + l * (long)n;
+    for (long q = seg_off[sg] + threadIdx.x; q < seg_off[sg + 1]; q += blockDim.x) {
+      int i = rows[q];
+      int j0 = ptr[i], j1 = ptr[i + 1];
+      double s = 0.0;
+      if (VALUED) {
+        for (int j = j0; j < j1; j++) s = row_term<ARITH>(s, coef[j], ld_cg(src + col[j]));
+      } else {
+        double a = coef[i];
+        for (int j = j0; j < j1; j++) s = row_term<ARITH>(s, a, ld_cg(src + col[j]));
+      }
+      dst[i] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------
+// PA1 tiles.  Tile p: slots [slot_off[p], slot_off[p+1]) sorted by
+// (distance to part p, vertex); shell[p*(k+1)+d] = slots with distance
+// <= d.  Level l is computed on slots [0, shell[k-l]); rows of slots with
+// distance 0 (the part itself) are written to vv.  Local structure is
+// sliced ELL (32 rows per slice, column-major inside a slice, 0xFFFF pads).
+// Level buffers live in shared memory (SMEM) or, for tiles too large for
+// it, in a global scratch area of 2*max_slots doubles per CTA.
+// ------------------------------------------------------------------------
+struct TileArgs {
+  int n, nlevel, max_slots;
+  const int *order;
+  const long *slot_off;
+  const int *shell;
+  const int *slot_vert;
+  const long *slice_off;
+  const long *ell_off;
+  const uint16_t *ell_col;
+  const uint8_t *ell_width;
+  const int *ptr;       // global row pointers (value offsets)
+  const double *coef;   // values (nnz) or 1/deg (n)
+  const double *x;
+  double *vv;
+  double *scratch;      // used when !SMEM
+  int *err;
+};
+
+template <int ARITH, bool VALUED, bool SMEM>
+__global__ void __launch_bounds__(512) tiles_kernel(TileArgs a) {
+  extern __shared__ double smem_buf[];
+  const int p = a.order[blockIdx.x];
+  const long s0 = a.slot_off[p];
+  const int ns = (int)(a.slot_off[p + 1] - s0);
+  const int *shell = a.shell + (long)p * (a.nlevel + 1);
+  const long sl0 = a.slice_off[p];
+  double *buf0 = SMEM ? smem_buf : a.scratch + (long)blockIdx.x * 2 * a.max_slots;
+  double *buf1 = buf0 + a.max_slots;
+  if (ns > a.max_slots) {  // plan invariant; never true for a valid plan
+    if (threadIdx.x == 0) atomicExch(a.err, kErrBounds);
+    return;
+  }
+  for (int s = threadIdx.x; s < ns; s += blockDim.x) buf0[s] = a.x[a.slot_vert[s0 + s]];
+  __syncthreads();
+  const int owned = shell[0];
+  for (int l = 1; l <= a.nlevel; l++) {
+    const double *in = (l & 1) ? buf0 : buf1;
+    double *out = (l & 1) ? buf1 : buf0;
+    const int nrows = shell[a.nlevel - l];
+    double *dst = a.vv + (long)l * a.n;
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+      const long sl = sl0 + (r >> 5);
+      const int lane = r & 31;
+      const int w = a.ell_width[sl];
+      const uint16_t *cp = a.ell_col + a.ell_off[sl] + lane;
+      const int v = a.slot_vert[s0 + r];
+      double s = 0.0;
+      if (VALUED) {
+        const double *vp = a.coef + a.ptr[v];
+        for (int t = 0; t < w; t++) {
+          const int c = cp[t * 32];
+          if (c == 0xFFFF) break;
+          s = row_term<ARITH>(s, vp[t], in[c]);
+        }
+      } else {
+        const double cf = a.coef[v];
+        for (int t = 0; t < w; t++) {
+          const int c = cp[t * 32];
+          if (c == 0xFFFF) break;
+          s = row_term<ARITH>(s, cf, in[c]);
+        }
+      }
+      out[r] = s;
+      if (r < owned) dst[v] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------
+// Level pipeline.  A persistent grid of CTAs takes chunks of `chunk`
+// consecutive rows in ticket order.  The CTA copies the chunk's matrix
+// rows into shared memory once, then for l = 1..k waits until every chunk
+// its rows reference has published level l-1 (flags[c] = epoch*32 + level,
+// bounded spin), computes the chunk's rows of level l into vv and publishes
+// level l.  No row is computed twice.  A CTA waiting for level l-1 of chunk
+// c + d needs that chunk to be running, so the plan requires the grid to
+// hold more than (k-1)*reach chunks at once; a wait that exceeds the spin
+// limit sets the error word and the whole grid drains.
+// ------------------------------------------------------------------------
+struct PipeArgs {
+  int n, nlevel, chunk, nchunk;
+  uint32_t epoch;
+  const int *dep_lo, *dep_hi;
+  const int *ptr, *col;
+  const double *coef;
+  const double *x;
+  double *vv;
+  unsigned int *ticket;
+  unsigned int *flags;
+  int *err;
+  int max_chunk_nnz;
+};
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int ARITH, bool VALUED>
+__global__ void __launch_bounds__(256) pipe_kernel(PipeArgs a) {
+  extern __shared__ __align__(16) unsigned char pipe_smem[];
+  // layout: rptr[chunk+1] ints | cols[max_chunk_nnz] ints | vals[max_chunk_nnz] doubles
+  int *rptr = reinterpret_cast<int *>(pipe_smem);
+  int *cols = rptr + a.chunk + 1;
+  double *vals = reinterpret_cast<double *>(
+      pipe_smem + (((size_t)(a.chunk + 1 + a.max_chunk_nnz) * sizeof(int) + 15) & ~(size_t)15));
+  __shared__ unsigned int s_chunk;
+  __shared__ int s_abort;
+  const unsigned int base_tag = a.epoch * 32u;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_chunk = atomicAdd(a.ticket, 1u);
+      s_abort = 0;
+    }
+    __syncthreads();
+    const int c = (int)s_chunk;
+    if (c >= a.nchunk) return;
+    const int r0 = c * a.chunk;
+    const int nr = min(a.chunk, a.n - r0);
+    const int j00 = a.ptr[r0];
+    // stage the chunk's rows
+    for (int r = threadIdx.x; r <= nr; r += blockDim.x) rptr[r] = a.ptr[r0 + r] - j00;
+    __syncthreads();
+    const int cnnz = rptr[nr];
+    if (cnnz > a.max_chunk_nnz) {  // plan invariant
+      if (threadIdx.x == 0) atomicExch(a.err, kErrBounds);
+      return;
+    }
+    for (int t = threadIdx.x; t < cnnz; t += blockDim.x) {
+      cols[t] = a.col[j00 + t];
+      if (VALUED) vals[t] = a.coef[j00 + t];
+    }
+    double cf = 0.0;
+    int myrow = r0 + threadIdx.x;
+    if (!VALUED && threadIdx.x < nr) cf = a.coef[myrow];
+    __syncthreads();
+    const int dlo = a.dep_lo[c], dhi = a.dep_hi[c];
+    for (int l = 1; l <= a.nlevel; l++) {
+      if (l > 1) {
+        // wait for level l-1 of the chunks this chunk reads
+        const unsigned int want = base_tag + (unsigned)(l - 1);
+        for (int d = dlo + (int)threadIdx.x; d <= dhi; d += blockDim.x) {
+          if (d == c) continue;
+          long spins = 0;
+          while (ld_acquire(a.flags + d) < want) {
+            if (++spins > kSpinLimit || *((volatile int *)a.err)) {
+              atomicCAS(a.err, 0, kErrTimeout);
+              s_abort = 1;
+              break;
+            }
+            __nanosleep(spins < 64 ? 32 : 256);
+          }
+        }
+        __syncthreads();
+        if (s_abort) return;
+      }
+      if (threadIdx.x < nr) {
+        const double *src = a.vv + (long)(l - 1) * a.n;
+        const int q0 = rptr[threadIdx.x], q1 = rptr[threadIdx.x + 1];
+        double s = 0.0;
+        if (l == 1) {
+          for (int q = q0; q < q1; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf, a.x[cols[q]]);
+        } else {
+          for (int q = q0; q < q1; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf, ld_cg(src + cols[q]));
+        }
+        a.vv[(long)l * a.n + myrow] = s;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        st_release(a.flags + c, base_tag + (unsigned)l);
+      }
+    }
+  }
+}
+
+__global__ void copy_kernel(const double *__restrict__ src, double *__restrict__ dst, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+}  // namespace
+
+// ==========================================================================
+// Plans
+// ==========================================================================
+struct mpkg_plan {
+  int n = 0, nlevel = 0, nphase = 0, npart = 0;
+  int exec = MPKG_EXEC_TASKS, arith = MPKG_ARITH_FMA;
+  bool valued = false;
+  bool full_coverage = true;
+  long nnz = 0;
+  long rows_computed = 0;
+  long device_bytes = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int *d_ptr = nullptr, *d_col = nullptr;
+  double *d_coef = nullptr;  // values (nnz) or 1/deg (n)
+  int *d_err = nullptr;
+  double *d_vv = nullptr;    // staging for host execution
+  // tasks
+  std::vector<long> list_seg_h;
+  long *d_list_seg = nullptr;
+  int *d_seg_level = nullptr;
+  long *d_seg_off = nullptr;
+  int *d_rows = nullptr;
+  // tiles
+  TileArgs tiles{};
+  bool tiles_smem = true;
+  size_t tiles_smem_bytes = 0;
+  int max_tile_slots = 0;
+  std::vector<void *> owned;
+  // pipe
+  PipeArgs pipe{};
+  int pipe_grid = 0, pipe_reach = 0;
+  size_t pipe_smem_bytes = 0;
+  uint32_t epoch = 0;
+  int launches = 0;
+  std::vector<double> h_x;  // x staging when a tasks plan leaves entries uncovered
+};
+
+namespace {
+
+template <typename T>
+int dev_copy(mpkg_plan *p, T **dst, const T *src, size_t count) {
+  *dst = nullptr;
+  if (count == 0) return kOk;
+  CUDA_TRY(cudaMalloc((void **)dst, sizeof(T) * count));
+  p->owned.push_back(*dst);
+  p->device_bytes += (long)(sizeof(T) * count);
+  CUDA_TRY(cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice));
+  return kOk;
+}
+
+template <typename T>
+int dev_alloc(mpkg_plan *p, T **dst, size_t count) {
+  *dst = nullptr;
+  if (count == 0) return kOk;
+  CUDA_TRY(cudaMalloc((void **)dst, sizeof(T) * count));
+  p->owned.push_back(*dst);
+  p->device_bytes += (long)(sizeof(T) * count);
+  return kOk;
+}
+
+int check_csr(int n, const int *ptr, const int *col) {
+  if (n <= 0 || !ptr || !col) return fail(kEInval, "empty matrix or null arrays");
+  if (ptr[0] != 0) return fail(kEInval, "ptr[0] must be 0");
+  for (int i = 0; i < n; i++)
+    if (ptr[i + 1] < ptr[i]) return fail(kEInval, "ptr must be non-decreasing");
+  for (long j = 0; j < ptr[n]; j++)
+    if (col[j] < 0 || col[j] >= n) return fail(kERange, "column index out of range");
+  return kOk;
+}
+
+int plan_common(mpkg_plan *p, int n, const int *ptr, const int *col, const double *val,
+                int nlevel, int arith) {
+  int rc = check_csr(n, ptr, col);
+  if (rc) return rc;
+  if (nlevel <= 0 || nlevel > 31) return fail(kEInval, "nlevel must be in [1, 31]");
+  if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE)
+    return fail(kEInval, "arith mode not supported by this executor");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
+  CUDA_TRY(cudaGetDevice(&p->device));
+  p->n = n;
+  p->nlevel = nlevel;
+  p->arith = arith;
+  p->valued = val != nullptr;
+  p->nnz = ptr[n];
+  CUDA_TRY(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  if ((rc = dev_copy(p, &p->d_ptr, ptr, (size_t)n + 1))) return rc;
+  if ((rc = dev_copy(p, &p->d_col, col, (size_t)p->nnz))) return rc;
+  if (val) {
+    if ((rc = dev_copy(p, &p->d_coef, val, (size_t)p->nnz))) return rc;
+  } else {
+    std::vector<double> rdeg(n);
+    for (int i = 0; i < n; i++) rdeg[i] = 1.0 / (ptr[i + 1] - ptr[i]);  // as mpk2/mpkexec.c:28
+    if ((rc = dev_copy(p, &p->d_coef, rdeg.data(), (size_t)n))) return rc;
+  }
+  if ((rc = dev_alloc(p, &p->d_err, 1))) return rc;
+  CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
+  return kOk;
+}
+
+int build_task_device(mpkg_plan *p, int npart, int nphase, const long *off, const long *idx) {
+  const int n = p->n;
+  const long nlists = (long)(nphase + 1) * npart;
+  std::vector<long> list_seg(nlists + 1, 0);
+  std::vector<int> seg_level;
+  std::vector<long> seg_off;
+  std::vector<int> rows;
+  rows.reserve(off[nlists]);
+  std::vector<unsigned char> covered((size_t)n * (p->nlevel + 1), 0);
+  for (long t = 0; t < nlists; t++) {
+    list_seg[t] = (long)seg_level.size();
+    if (off[t + 1] < off[t]) return fail(kEInval, "task offsets must be non-decreasing");
+    int cur = -1;
+    for (long q = off[t]; q < off[t + 1]; q++) {
+      long e = idx[q];
+      long l = e / n;
+      if (e < 0 || l < 1 || l > p->nlevel) return fail(kERange, "task entry outside levels 1..nlevel");
+      int i = (int)(e - l * n);
+      if (l < cur) return fail(kEInval, "task list is not level-major");
+      if (l != cur) {
+        seg_level.push_back((int)l);
+        seg_off.push_back((long)rows.size());
+        cur = (int)l;
+      }
+      rows.push_back(i);
+      covered[(size_t)e] = 1;
+    }
+  }
+  list_seg[nlists] = (long)seg_level.size();
+  seg_off.push_back((long)rows.size());
+  p->full_coverage = true;
+  for (size_t e = (size_t)n; e < covered.size(); e++)
+    if (!covered[e]) { p->full_coverage = false; break; }
+  p->rows_computed = (long)rows.size();
+  p->list_seg_h = list_seg;
+  int rc;
+  if ((rc = dev_copy(p, &p->d_list_seg, list_seg.data(), list_seg.size()))) return rc;
+  if ((rc = dev_copy(p, &p->d_seg_level, seg_level.data(), seg_level.size()))) return rc;
+  if ((rc = dev_copy(p, &p->d_seg_off, seg_off.data(), seg_off.size()))) return rc;
+  if ((rc = dev_copy(p, &p->d_rows, rows.data(), rows.size()))) return rc;
+  return kOk;
+}
+
+int build_tile_device(mpkg_plan *p, const TilePlan &tp) {
+  int rc;
+  TileArgs &a = p->tiles;
+  a.n = p->n;
+  a.nlevel = p->nlevel;
+  a.max_slots = tp.max_slots;
+  p->max_tile_slots = tp.max_slots;
+  p->rows_computed = tp.total_rows;
+  int *order, *shell, *slot_vert;
+  long *slot_off, *slice_off, *ell_off;
+  uint16_t *ell_col;
+  uint8_t *ell_width;
+  if ((rc = dev_copy(p, &order, tp.order.data(), tp.order.size()))) return rc;
+  if ((rc = dev_copy(p, &slot_off, tp.slot_off.data(), tp.slot_off.size()))) return rc;
+  if ((rc = dev_copy(p, &shell, tp.shell.data(), tp.shell.size()))) return rc;
+  if ((rc = dev_copy(p, &slot_vert, tp.slot_vert.data(), tp.slot_vert.size()))) return rc;
+  if ((rc = dev_copy(p, &slice_off, tp.slice_off.data(), tp.slice_off.size()))) return rc;
+  if ((rc = dev_copy(p, &ell_off, tp.ell_off.data(), tp.ell_off.size()))) return rc;
+  std::vector<uint16_t> ec = tp.ell_col;
+  if (ec.empty()) ec.push_back(0xFFFF);
+  if ((rc = dev_copy(p, &ell_col, ec.data(), ec.size()))) return rc;
+  std::vector<uint8_t> ew = tp.ell_width;
+  if (ew.empty()) ew.push_back(0);
+  if ((rc = dev_copy(p, &ell_width, ew.data(), ew.size()))) return rc;
+  a.order = order; a.slot_off = slot_off; a.shell = shell; a.slot_vert = slot_vert;
+  a.slice_off = slice_off; a.ell_off = ell_off; a.ell_col = ell_col; a.ell_width = ell_width;
+  a.ptr = p->d_ptr;
+  a.coef = p->d_coef;
+  a.err = p->d_err;
+  size_t need = 2 * (size_t)tp.max_slots * sizeof(double);
+  int maxsm = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
+  p->tiles_smem = need <= (size_t)maxsm;
+  p->tiles_smem_bytes = p->tiles_smem ? need : 0;
+  a.scratch = nullptr;
+  if (!p->tiles_smem) {
+    double *scr;
+    if ((rc = dev_alloc(p, &scr, 2 * (size_t)tp.max_slots * tp.npart))) return rc;
+    a.scratch = scr;
+  }
+  return kOk;
+}
+
+template <int ARITH, bool VALUED, bool SMEM>
+int set_tiles_attr(size_t bytes) {
+  CUDA_TRY(cudaFuncSetAttribute(tiles_kernel<ARITH, VALUED, SMEM>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return kOk;
+}
+
+template <int ARITH, bool VALUED>
+int pipe_setup_t(mpkg_plan *p, int *grid) {
+  CUDA_TRY(cudaFuncSetAttribute(pipe_kernel<ARITH, VALUED>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pipe_smem_bytes));
+  int per_sm = 0, nsm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_kernel<ARITH, VALUED>, 256,
+                                                         p->pipe_smem_bytes));
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+  *grid = per_sm * nsm;
+  return kOk;
+}
+
+int launch_spmv(int n, const int *ptr, const int *col, const double *coef, bool valued, int nlevel,
+                double *vv, int arith, cudaStream_t st) {
+  dim3 blk(256), grd((n + 255) / 256);
+  for (int l = 1; l <= nlevel; l++) {
+    const double *x = vv + (long)(l - 1) * n;
+    double *y = vv + (long)l * n;
+    if (arith == MPKG_ARITH_SEPARATE) {
+      if (valued) spmv_level_kernel<MPKG_ARITH_SEPARATE, true><<<grd, blk, 0, st>>>(n, ptr, col, coef, x, y);
+      else spmv_level_kernel<MPKG_ARITH_SEPARATE, false><<<grd, blk, 0, st>>>(n, ptr, col, coef, x, y);
+    } else {
+      if (valued) spmv_level_kernel<MPKG_ARITH_FMA, true><<<grd, blk, 0, st>>>(n, ptr, col, coef, x, y);
+      else spmv_level_kernel<MPKG_ARITH_FMA, false><<<grd, blk, 0, st>>>(n, ptr, col, coef, x, y);
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+template <int ARITH, bool VALUED>
+void launch_tasks_t(mpkg_plan *p, double *vv, cudaStream_t st) {
+  for (int ph = 0; ph <= p->nphase; ph++) {
+    tasks_kernel<ARITH, VALUED><<<p->npart, 256, 0, st>>>(p->n, ph * p->npart, p->d_list_seg,
+                                                         p->d_seg_level, p->d_seg_off, p->d_rows,
+                                                         p->d_ptr, p->d_col, p->d_coef, vv);
+  }
+}
+
+template <int ARITH, bool VALUED>
+void launch_tiles_t(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) {
+  TileArgs a = p->tiles;
+  a.x = x;
+  a.vv = vv;
+  if (p->tiles_smem)
+    tiles_kernel<ARITH, VALUED, true><<<p->npart, 512, p->tiles_smem_bytes, st>>>(a);
+  else
+    tiles_kernel<ARITH, VALUED, false><<<p->npart, 512, 0, st>>>(a);
+}
+
+template <int ARITH, bool VALUED>
+void launch_pipe_t(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) {
+  PipeArgs a = p->pipe;
+  a.x = x;
+  a.vv = vv;
+  a.epoch = p->epoch;
+  pipe_kernel<ARITH, VALUED><<<p->pipe_grid, 256, p->pipe_smem_bytes, st>>>(a);
+}
+
+#define DISPATCH2(fn, ...)                                                   \
+  do {                                                                       \
+    if (p->arith == MPKG_ARITH_SEPARATE) {                                        \
+      if (p->valued) fn<MPKG_ARITH_SEPARATE, true>(__VA_ARGS__);                  \
+      else fn<MPKG_ARITH_SEPARATE, false>(__VA_ARGS__);                           \
+    } else {                                                                 \
+      if (p->valued) fn<MPKG_ARITH_FMA, true>(__VA_ARGS__);                       \
+      else fn<MPKG_ARITH_FMA, false>(__VA_ARGS__);                                \
+    }                                                                        \
+  } while (0)
+
+int plan_launch(mpkg_plan *p, double *d_vv, cudaStream_t st) {
+  p->launches = 0;
+  switch (p->exec) {
+    case MPKG_EXEC_TASKS:
+      DISPATCH2(launch_tasks_t, p, d_vv, st);
+      p->launches = p->nphase + 1;
+      break;
+    case MPKG_EXEC_TILES:
+      DISPATCH2(launch_tiles_t, p, d_vv, d_vv, st);
+      p->launches = 1;
+      break;
+    case MPKG_EXEC_PIPE: {
+      p->epoch++;
+      if (p->epoch >= (1u << 26)) {  // tags wrap: clear the flags
+        CUDA_TRY(cudaMemsetAsync(p->pipe.flags, 0, sizeof(unsigned int) * p->pipe.nchunk, st));
+        p->epoch = 1;
+      }
+      CUDA_TRY(cudaMemsetAsync(p->pipe.ticket, 0, sizeof(unsigned int), st));
+      DISPATCH2(launch_pipe_t, p, d_vv, d_vv, st);
+      p->launches = 1;
+      break;
+    }
+    case MPKG_EXEC_SPMV: {
+      int rc = launch_spmv(p->n, p->d_ptr, p->d_col, p->d_coef, p->valued, p->nlevel, d_vv, p->arith, st);
+      if (rc) return rc;
+      p->launches = p->nlevel;
+      break;
+    }
+    default:
+      return fail(kEInval, "unknown executor");
+  }
+  CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+mpkg_plan *new_plan() { return new (std::nothrow) mpkg_plan(); }
+
+}  // namespace
+
+// ==========================================================================
+// C ABI
+// ==========================================================================
+extern "C" {
+
+const char *mpkg_last_error(void) { return last_error(); }
+int mpkg_version(void) { return 1; }
+
+void mpkg_plan_destroy(mpkg_plan *p) {
+  if (!p) return;
+  for (void *q : p->owned) cudaFree(q);
+  if (p->d_vv) cudaFree(p->d_vv);
+  if (p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+}
+
+int mpkg_plan_tasks(int n, const int *ptr, const int *col, const double *val, int npart,
+                    int nlevel, int nphase, const long *off, const long *idx, int arith,
+                    mpkg_plan **out) {
+  clear_error();
+  if (!out) return fail(kEInval, "out is null");
+  *out = nullptr;
+  if (npart <= 0 || nphase < 0 || !off || (!idx && off[(long)(nphase + 1) * npart] > 0))
+    return fail(kEInval, "bad task list arguments");
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  int rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  if (!rc) {
+    p->exec = MPKG_EXEC_TASKS;
+    p->npart = npart;
+    p->nphase = nphase;
+    rc = build_task_device(p, npart, nphase, off, idx);
+  }
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
+int mpkg_plan_pa1(int n, const int *ptr, const int *col, const double *val, const int *part,
+                  int npart, int nlevel, int exec, int arith, mpkg_plan **out) {
+  clear_error();
+  if (!out) return fail(kEInval, "out is null");
+  *out = nullptr;
+  if (!part || npart <= 0) return fail(kEInval, "bad partition");
+  if (exec != MPKG_EXEC_TILES && exec != MPKG_EXEC_TASKS)
+    return fail(kEInval, "PA1 plans use the tiles or tasks executor");
+  int rc = check_csr(n, ptr, col);
+  if (rc) return rc;
+  Csr g;
+  g.n = n;
+  g.ptr.assign(ptr, ptr + n + 1);
+  g.col.assign(col, col + ptr[n]);
+  std::vector<int> pv(part, part + n);
+  for (int q : pv) if (q < 0 || q >= npart) return fail(kERange, "part id out of range");
+  if (exec == MPKG_EXEC_TASKS) {
+    std::vector<PartSkirt> sk;
+    if ((rc = comp_skirts(g, pv, npart, nullptr, nlevel, &sk))) return rc;
+    TaskLists tl;
+    if ((rc = build_tasks(g, npart, nlevel, 0, {pv}, {}, sk, false, &tl))) return rc;
+    return mpkg_plan_tasks(n, ptr, col, val, npart, nlevel, 0, tl.off.data(), tl.idx.data(), arith, out);
+  }
+  TilePlan tp;
+  if ((rc = build_tile_plan(g, pv, npart, nlevel, &tp))) return rc;
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  if (!rc) {
+    p->exec = MPKG_EXEC_TILES;
+    p->npart = npart;
+    rc = build_tile_device(p, tp);
+  }
+  if (!rc && p->tiles_smem) {
+    if (p->arith == MPKG_ARITH_SEPARATE) {
+      rc = p->valued ? set_tiles_attr<MPKG_ARITH_SEPARATE, true, true>(p->tiles_smem_bytes)
+                     : set_tiles_attr<MPKG_ARITH_SEPARATE, false, true>(p->tiles_smem_bytes);
+    } else {
+      rc = p->valued ? set_tiles_attr<MPKG_ARITH_FMA, true, true>(p->tiles_smem_bytes)
+                     : set_tiles_attr<MPKG_ARITH_FMA, false, true>(p->tiles_smem_bytes);
+    }
+  }
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
+int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int nlevel,
+                   int chunk, int arith, mpkg_plan **out) {
+  clear_error();
+  if (!out) return fail(kEInval, "out is null");
+  *out = nullptr;
+  if (chunk <= 0) chunk = 256;
+  if (chunk != 256) return fail(kEInval, "pipe executor uses 256-row chunks");
+  int rc = check_csr(n, ptr, col);
+  if (rc) return rc;
+  Csr g;
+  g.n = n;
+  g.ptr.assign(ptr, ptr + n + 1);
+  g.col.assign(col, col + ptr[n]);
+  PipePlan pp;
+  if ((rc = build_pipe_plan(g, nlevel, chunk, &pp))) return rc;
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  if (!rc) {
+    p->exec = MPKG_EXEC_PIPE;
+    p->npart = pp.nchunk;
+    p->rows_computed = (long)n * nlevel;
+    PipeArgs &a = p->pipe;
+    a.n = n; a.nlevel = nlevel; a.chunk = chunk; a.nchunk = pp.nchunk;
+    int maxnnz = 0;
+    for (int c = 0; c < pp.nchunk; c++) {
+      int r1 = std::min(n, (c + 1) * chunk);
+      maxnnz = std::max(maxnnz, ptr[r1] - ptr[c * chunk]);
+    }
+    a.max_chunk_nnz = std::max(maxnnz, 1);
+    p->pipe_smem_bytes = (((size_t)(chunk + 1 + a.max_chunk_nnz) * sizeof(int) + 15) & ~(size_t)15) +
+                         (p->valued ? (size_t)a.max_chunk_nnz * sizeof(double) : 0);
+    int *dlo, *dhi;
+    unsigned int *ticket, *flags;
+    if (!rc) rc = dev_copy(p, &dlo, pp.dep_lo.data(), pp.dep_lo.size());
+    if (!rc) rc = dev_copy(p, &dhi, pp.dep_hi.data(), pp.dep_hi.size());
+    if (!rc) rc = dev_alloc(p, &ticket, 1);
+    if (!rc) rc = dev_alloc(p, &flags, (size_t)pp.nchunk);
+    if (!rc) {
+      cudaMemset(flags, 0, sizeof(unsigned int) * pp.nchunk);
+      a.dep_lo = dlo; a.dep_hi = dhi; a.ticket = ticket; a.flags = flags;
+      a.ptr = p->d_ptr; a.col = p->d_col; a.coef = p->d_coef; a.err = p->d_err;
+      int maxsm = 0;
+      cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+      if (p->pipe_smem_bytes > (size_t)maxsm) rc = fail(kERange, "chunk rows too dense for shared memory");
+    }
+    if (!rc) {
+      int grid = 0;
+      if (p->arith == MPKG_ARITH_SEPARATE)
+        rc = p->valued ? pipe_setup_t<MPKG_ARITH_SEPARATE, true>(p, &grid) : pipe_setup_t<MPKG_ARITH_SEPARATE, false>(p, &grid);
+      else
+        rc = p->valued ? pipe_setup_t<MPKG_ARITH_FMA, true>(p, &grid) : pipe_setup_t<MPKG_ARITH_FMA, false>(p, &grid);
+      if (!rc) {
+        p->pipe_reach = pp.reach;
+        p->pipe_grid = std::min(grid, pp.nchunk);
+        // progress needs every chunk within (k-1)*reach of the oldest
+        // unfinished chunk to be running
+        long need = (long)(nlevel - 1) * pp.reach + 1;
+        if (p->pipe_grid < pp.nchunk && p->pipe_grid < need)
+          rc = fail(kERange, "matrix bandwidth too large for the pipeline (reach " +
+                                 std::to_string(pp.reach) + " chunks, " + std::to_string(grid) +
+                                 " resident CTAs)");
+      }
+    }
+  }
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
+int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
+                   mpkg_plan **out) {
+  clear_error();
+  if (!out) return fail(kEInval, "out is null");
+  *out = nullptr;
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  int rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  if (!rc) {
+    p->exec = MPKG_EXEC_SPMV;
+    p->npart = 1;
+    p->rows_computed = (long)n * nlevel;
+  }
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
+int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info) {
+  if (!p || !info) return fail(kEInval, "null argument");
+  std::memset(info, 0, sizeof *info);
+  info->n = p->n; info->nlevel = p->nlevel; info->nphase = p->nphase; info->npart = p->npart;
+  info->exec = p->exec; info->arith = p->arith; info->valued = p->valued;
+  info->nnz = p->nnz;
+  info->rows_computed = p->rows_computed;
+  info->device_bytes = p->device_bytes;
+  info->launches = p->exec == MPKG_EXEC_TASKS ? p->nphase + 1
+                   : p->exec == MPKG_EXEC_SPMV ? p->nlevel : 1;
+  info->tiles_in_smem = p->tiles_smem ? 1 : 0;
+  info->max_tile_slots = p->max_tile_slots;
+  info->pipe_chunk = p->pipe.chunk;
+  info->pipe_reach = p->pipe_reach;
+  info->pipe_grid = p->pipe_grid;
+  return kOk;
+}
+
+int mpkg_exec_device(mpkg_plan *p, double *d_vv, void *stream) {
+  clear_error();
+  if (!p || !d_vv) return fail(kEInval, "null plan or vv");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  return plan_launch(p, d_vv, st);
+}
+
+int mpkg_sync(mpkg_plan *p, void *stream) {
+  if (!p) return fail(kEInval, "null plan");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  int err = 0;
+  CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    cudaMemset(p->d_err, 0, sizeof(int));
+    if (err == kErrTimeout) return fail(kETimeout, "a device-side wait exceeded its spin limit");
+    return fail(kERange, "device-side bounds check failed");
+  }
+  return kOk;
+}
+
+int mpkg_exec_host(mpkg_plan *p, double *vv) {
+  clear_error();
+  if (!p || !vv) return fail(kEInval, "null plan or vv");
+  const long total = (long)p->n * (p->nlevel + 1);
+  if (!p->d_vv) {
+    CUDA_TRY(cudaMalloc(&p->d_vv, sizeof(double) * total));
+  }
+  cudaStream_t st = p->stream;
+  const long up = p->full_coverage ? p->n : total;
+  CUDA_TRY(cudaMemcpyAsync(p->d_vv, vv, sizeof(double) * up, cudaMemcpyHostToDevice, st));
+  int rc = plan_launch(p, p->d_vv, st);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(vv + p->n, p->d_vv + p->n, sizeof(double) * (total - p->n),
+                           cudaMemcpyDeviceToHost, st));
+  return mpkg_sync(p, st);
+}
+
+int mpkg_spmv_chain_device(int n, const int *d_ptr, const int *d_col, const double *d_val,
+                           int nlevel, double *d_vv, int arith, void *stream) {
+  clear_error();
+  if (n <= 0 || !d_ptr || !d_col || !d_vv || nlevel <= 0) return fail(kEInval, "bad arguments");
+  if (!d_val) return fail(kEInval, "the stand-alone chain needs values; use mpkg_plan_spmv for 1/deg");
+  if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE) return fail(kEInval, "bad arith");
+  return launch_spmv(n, d_ptr, d_col, d_val, true, nlevel, d_vv, arith, (cudaStream_t)stream);
+}
+
+}  // extern "C"

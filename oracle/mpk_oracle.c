@@ -1,0 +1,476 @@
+/*
+ * CPU oracle for the matrix powers kernel (MPK) hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file restates, in plain C, the
+ * algorithms of the reference mpk2 code (vatai/mpk) so that tests,
+ * `__graft_entry__.smoke()` and the `cpu_baseline` leg of `bench.py`
+ * can check the CUDA path against it.  The product library never links,
+ * loads or calls anything built from this file.
+ *
+ * Every function cites the reference file:line it restates.  Parity of
+ * this restatement with the reference itself is pinned by the tests in
+ * tests/test_oracle_pin.py (against the reference compiled from its own
+ * sources into oracle/_ref/) and by the committed golden fixtures in
+ * tests/golden/ (generated by tests/golden/make_golden.py from the
+ * reference binaries).
+ *
+ * Arithmetic modes for the FP64 row sums:
+ *   mode 0 ("separate"): s = s + (a * x), two roundings per term; this is
+ *          what the reference computes when the compiler does not contract
+ *          (x86-64 gcc -O2: no FMA instructions are emitted).
+ *   mode 1 ("fma"):      s = fma(a, x, s), one rounding per term; this is
+ *          what the reference computes when gcc contracts a*b+c (aarch64
+ *          gcc -O2 default), and what the CUDA kernels compute by default.
+ * The file is compiled with -ffp-contract=off so mode 0 stays mode 0.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <ctype.h>
+
+#define ORC_OK 0
+#define ORC_EIO -1
+#define ORC_EFORMAT -2
+#define ORC_ERANGE -3
+#define ORC_ESTRUCT -4
+
+static double row_term(double s, double a, double x, int mode) {
+  return mode ? fma(a, x, s) : s + a * x;
+}
+
+/* ------------------------------------------------------------------ */
+/* Graph input: METIS text format, 1-based columns, header "n ne".      */
+/* Restates read_crs (mpk2/lib.c:69-129): one line per vertex, columns  */
+/* in file order, col[] capacity 2*ne, every column in [1, n].          */
+/* ------------------------------------------------------------------ */
+
+/* Pass 1: header values (n, ne) and the exact number of column tokens. */
+long orc_graph_count(const char *path, int *n_out, long *ne_out) {
+  FILE *f = fopen(path, "r");
+  if (!f) return ORC_EIO;
+  int nv = 0, ne = 0, p = 0, q = 0;
+  char line[1 << 16];
+  if (!fgets(line, sizeof line, f)) { fclose(f); return ORC_EFORMAT; }
+  if (sscanf(line, "%d %d %d %d", &nv, &ne, &p, &q) != 2 || nv <= 0 || ne <= 0) {
+    fclose(f); return ORC_EFORMAT;
+  }
+  long cnt = 0;
+  int rows = 0;
+  int c;
+  int in_tok = 0;
+  /* count integer tokens on the next nv lines */
+  while (rows < nv && (c = fgetc(f)) != EOF) {
+    if (c == '\n') { if (in_tok) { cnt++; in_tok = 0; } rows++; continue; }
+    if (isdigit(c)) in_tok = 1;
+    else if (in_tok) { cnt++; in_tok = 0; }
+  }
+  if (in_tok) cnt++;
+  fclose(f);
+  *n_out = nv; *ne_out = ne;
+  return cnt;
+}
+
+/* Pass 2: fill ptr[n+1], col[cap] (0-based). */
+int orc_graph_read(const char *path, int n, long cap, int *ptr, int *col) {
+  FILE *f = fopen(path, "r");
+  if (!f) return ORC_EIO;
+  char line[1 << 16];
+  if (!fgets(line, sizeof line, f)) { fclose(f); return ORC_EFORMAT; }
+  long p = 0;
+  int i = 0;
+  ptr[0] = 0;
+  int c, in_tok = 0;
+  long v = 0;
+  while (i < n && (c = fgetc(f)) != EOF) {
+    if (isdigit(c)) { v = v * 10 + (c - '0'); in_tok = 1; continue; }
+    if (in_tok) {
+      if (p >= cap || v < 1 || v > n) { fclose(f); return ORC_ERANGE; }
+      col[p++] = (int)(v - 1);
+      in_tok = 0; v = 0;
+    }
+    if (c == '\n') ptr[++i] = (int)p;
+  }
+  if (in_tok && i < n) {
+    if (p >= cap || v < 1 || v > n) { fclose(f); return ORC_ERANGE; }
+    col[p++] = (int)(v - 1);
+  }
+  while (i < n) ptr[++i] = (int)p; /* missing trailing lines: empty rows */
+  fclose(f);
+  return ORC_OK;
+}
+
+/* Values file (.loop.val): whitespace separated doubles in CSR order.
+ * Restates alloc_read_val (mpk2/comm_data.c:160-187). */
+int orc_read_values(const char *path, long nnz, double *val) {
+  FILE *f = fopen(path, "r");
+  if (!f) return ORC_EIO;
+  for (long i = 0; i < nnz; i++)
+    if (fscanf(f, "%lf ", val + i) != 1) { fclose(f); return ORC_EFORMAT; }
+  fclose(f);
+  return ORC_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* Min-plus relaxation sweeps (mpk2/lib.c:164-219).                      */
+/* mode 0: all rows, 1: rows with part[i]==r, 2: rows with part[i]!=r.   */
+/* y[i] = min(x[i], x[col]+1); returns the number of strict decreases    */
+/* counted per column visit, exactly as the reference counts them.       */
+/* ------------------------------------------------------------------ */
+long orc_minplus(int n, const int *ptr, const int *col, const int *x, int *y,
+                 int r, const int *part, int mode) {
+  long k = 0;
+  for (int i = 0; i < n; i++) {
+    if (mode == 1 && part[i] != r) continue;
+    if (mode == 2 && part[i] == r) continue;
+    int t = x[i];
+    for (int j = ptr[i]; j < ptr[i + 1]; j++) {
+      int s = x[col[j]] + 1;
+      if (s < t) { t = s; k++; }
+    }
+    y[i] = t;
+  }
+  return k;
+}
+
+/* Swap-until-no-change loop shared by comp_level, update_level and
+ * comp_skirt: the reference iterates minplus_{r,x} between t0 and t1
+ * and keeps the array produced by the last sweep. */
+static int *fixed_point(int n, const int *ptr, const int *col, int *t0, int *t1,
+                        int r, const int *part, int mode) {
+  long ch;
+  do {
+    ch = orc_minplus(n, ptr, col, t0, t1, r, part, mode);
+    int *tt = t0; t0 = t1; t1 = tt;
+  } while (ch > 0);
+  return t1; /* == array written by the last sweep */
+}
+
+/* comp_level (mpk2/lib.c:330-371): per part, start from n+1 inside and
+ * -1 outside, sweep inside the part to a fixed point. */
+int orc_comp_level(int n, const int *ptr, const int *col, const int *part,
+                   int npart, int *level) {
+  int *t0 = malloc(sizeof(int) * n), *t1 = malloc(sizeof(int) * n);
+  if (!t0 || !t1) { free(t0); free(t1); return ORC_EIO; }
+  for (int p = 0; p < npart; p++) {
+    for (int j = 0; j < n; j++) t0[j] = t1[j] = (part[j] == p) ? n + 1 : -1;
+    int *res = fixed_point(n, ptr, col, t0, t1, p, part, 1);
+    for (int j = 0; j < n; j++) if (part[j] == p) level[j] = res[j];
+  }
+  free(t0); free(t1);
+  return ORC_OK;
+}
+
+/* update_level (mpk2/lib.c:373-412): like comp_level, but vertices
+ * outside the part keep the previous phase's level, and vertices inside
+ * start from max(level_org) + n + 1. */
+int orc_update_level(int n, const int *ptr, const int *col, const int *part,
+                     int npart, const int *level_org, int *level) {
+  int *t0 = malloc(sizeof(int) * n), *t1 = malloc(sizeof(int) * n);
+  if (!t0 || !t1) { free(t0); free(t1); return ORC_EIO; }
+  int mx = level_org[0];
+  for (int i = 1; i < n; i++) if (mx < level_org[i]) mx = level_org[i];
+  for (int p = 0; p < npart; p++) {
+    for (int j = 0; j < n; j++) t0[j] = t1[j] = (part[j] == p) ? mx + n + 1 : level_org[j];
+    int *res = fixed_point(n, ptr, col, t0, t1, p, part, 1);
+    for (int j = 0; j < n; j++) if (part[j] == p) level[j] = res[j];
+  }
+  free(t0); free(t1);
+  return ORC_OK;
+}
+
+/* level2wcrs (mpk2/lib.c:504-537): vertex weight max+1-l_i, edge weight
+ * (int)(1e6/(l_i + l_j - 2*min + 1)) clamped to >= 1. */
+void orc_level2weights(int n, const int *ptr, const int *col, const int *level,
+                       int *wv, int *we) {
+  int mx = level[0], mn = level[0];
+  for (int i = 1; i < n; i++) {
+    if (mx < level[i]) mx = level[i];
+    if (mn > level[i]) mn = level[i];
+  }
+  for (int i = 0; i < n; i++) {
+    wv[i] = mx + 1 - level[i];
+    int l0 = level[i];
+    for (int j = ptr[i]; j < ptr[i + 1]; j++) {
+      double w = l0 + level[col[j]] - 2 * mn;
+      w = 1e+6 / (w + 1);
+      we[j] = (w < 1.0) ? 1 : (int)w;
+    }
+  }
+}
+
+/* comp_skirt for one part (mpk2/lib.c:584-615): 0 inside the part, n+1
+ * outside, sweep the outside to a fixed point: dist[j] is the graph
+ * distance of j to part p (n+1 when unreachable). */
+int orc_skirt_dist(int n, const int *ptr, const int *col, const int *part,
+                   int p, int *dist) {
+  int *t0 = malloc(sizeof(int) * n), *t1 = malloc(sizeof(int) * n);
+  if (!t0 || !t1) { free(t0); free(t1); return ORC_EIO; }
+  for (int j = 0; j < n; j++) t0[j] = t1[j] = (part[j] == p) ? 0 : n + 1;
+  int *res = fixed_point(n, ptr, col, t0, t1, p, part, 2);
+  memcpy(dist, res, sizeof(int) * n);
+  free(t0); free(t1);
+  return ORC_OK;
+}
+
+/* write_skirt (mpk2/lib.c:617-654) over comp_skirt distances: header
+ * "skirt N nodes, P parts", then per part "partition p" and lines
+ * "j level-dist" for dist < level (lev == NULL, PA1) or for
+ * lev[j] < level - dist (multi-phase). */
+int orc_write_skirt(const char *path, int n, const int *ptr, const int *col,
+                    const int *part, int npart, const int *lev, int level) {
+  FILE *f = fopen(path, "w");
+  if (!f) return ORC_EIO;
+  int *dist = malloc(sizeof(int) * n);
+  if (!dist) { fclose(f); return ORC_EIO; }
+  fprintf(f, "skirt %d nodes, %d parts\n", n, npart);
+  for (int p = 0; p < npart; p++) {
+    fprintf(f, "partition %d\n", p);
+    orc_skirt_dist(n, ptr, col, part, p, dist);
+    for (int j = 0; j < n; j++) {
+      int keep = lev ? (lev[j] < level - dist[j]) : (dist[j] < level);
+      if (keep) fprintf(f, "%d %d\n", j, level - dist[j]);
+    }
+  }
+  free(dist);
+  fclose(f);
+  return ORC_OK;
+}
+
+/* read_skirt (mpk2/lib.c:656-707) into a dense npart*n array: entries
+ * not listed are -1, listed entries hold level - m. */
+int orc_read_skirt(const char *path, int n, int npart, int level, int *sl) {
+  FILE *f = fopen(path, "r");
+  if (!f) return ORC_EIO;
+  char line[256];
+  int a = -1, b = -1;
+  if (!fgets(line, sizeof line, f) || sscanf(line, "skirt %d nodes, %d parts", &a, &b) != 2 ||
+      a != n || b != npart) { fclose(f); return ORC_EFORMAT; }
+  for (long i = 0; i < (long)npart * n; i++) sl[i] = -1;
+  int p = -1;
+  while (fgets(line, sizeof line, f)) {
+    if (line[0] == 'p') {
+      int q;
+      if (sscanf(line, "partition %d", &q) != 1 || q != p + 1) { fclose(f); return ORC_EFORMAT; }
+      p = q;
+      continue;
+    }
+    int k, m;
+    if (sscanf(line, "%d %d", &k, &m) != 2) continue;
+    if (p < 0 || k < 0 || k >= n || m < 0 || m > level) { fclose(f); return ORC_ERANGE; }
+    sl[(long)p * n + k] = level - m;
+  }
+  fclose(f);
+  return (p == npart - 1) ? ORC_OK : ORC_EFORMAT;
+}
+
+/* ------------------------------------------------------------------ */
+/* Task lists: restates prep_mpk (mpk2/mpkprep.c:7-258) without its      */
+/* printing.  parts: nphase (or 1 when nphase==0) arrays of n part ids;  */
+/* levels: nphase arrays of n levels; sl: dense npart*n skirt (-1 = not  */
+/* in the skirt).  Output: task (phase, part) = tasks[off[t]..off[t+1]), */
+/* t = phase*npart + part, each entry l*n+i.  Returns the total number of */
+/* entries, or ORC_ESTRUCT when the reference's dependency checks fail,  */
+/* or ORC_ERANGE when cap is too small.                                   */
+/* ------------------------------------------------------------------ */
+long orc_prep_tasks(int n, const int *ptr, const int *col, int npart, int nlevel,
+                    int nphase, const int *parts, const int *levels, const int *sl,
+                    long *off, long *tasks, long cap) {
+  long erc = 0;
+  /* level monotonicity (mpkprep.c:21-49) */
+  for (int ph = 0; ph < nphase; ph++) {
+    const int *l1 = levels + (long)ph * n;
+    for (int i = 0; i < n; i++) {
+      if (ph == 0 && l1[i] < 0) erc++;
+      if (ph > 0 && levels[(long)(ph - 1) * n + i] > l1[i]) erc++;
+    }
+  }
+  /* skirt consistency (mpkprep.c:52-84) */
+  for (int p = 0; p < npart; p++)
+    for (int i = 0; i < n; i++) {
+      int s = sl[(long)p * n + i];
+      if (s < 0) continue;
+      if (nphase == 0 && nlevel - s < 0) erc++;
+      if (nphase > 0 && levels[(long)(nphase - 1) * n + i] > nlevel - s) erc++;
+    }
+  if (erc) return ORC_ESTRUCT;
+
+  long nvv = (long)n * (nlevel + 1);
+  double *vv = malloc(sizeof(double) * nvv);
+  int *l0 = calloc(n, sizeof(int));
+  long *tsize = calloc(npart, sizeof(long));
+  if (!vv || !l0 || !tsize) { free(vv); free(l0); free(tsize); return ORC_EIO; }
+  for (long i = 0; i < nvv; i++) vv[i] = -1.0;
+  const int *pl = parts;
+  for (int i = 0; i < n; i++) vv[i] = pl[i] * 100.0;
+
+  long tcount = 0;
+  const int *prevl = l0;
+  int prevlmin = 0;
+  for (int ph = 0; ph < nphase; ph++) {
+    pl = parts + (long)ph * n;
+    const int *ll = levels + (long)ph * n;
+    int lmin = ll[0], lmax = ll[0];
+    for (int i = 1; i < n; i++) { if (lmin > ll[i]) lmin = ll[i]; if (lmax < ll[i]) lmax = ll[i]; }
+    if (lmax > nlevel) lmax = nlevel;
+    for (int p = 0; p < npart; p++) tsize[p] = 0;
+    /* dependency check with part*100+phase tags (mpkprep.c:134-162) */
+    for (int l = prevlmin + 1; l <= lmax; l++)
+      for (int i = 0; i < n; i++)
+        if (prevl[i] < l && l <= ll[i]) {
+          if (vv[(long)l * n + i] >= 0) erc++;
+          for (int j = ptr[i]; j < ptr[i + 1]; j++) {
+            int k = col[j];
+            double t = vv[(long)(l - 1) * n + k];
+            if (t < 0.0 || (pl[i] != pl[k] && ((int)t) % 100 == ph)) erc++;
+          }
+          vv[(long)l * n + i] = pl[i] * 100.0 + ph;
+          tsize[pl[i]]++;
+        }
+    long base = tcount;
+    for (int p = 0; p < npart; p++) {
+      off[(long)ph * npart + p] = base;
+      base += tsize[p];
+      tsize[p] = 0;
+    }
+    if (base > cap) { free(vv); free(l0); free(tsize); return ORC_ERANGE; }
+    for (int l = prevlmin + 1; l <= lmax; l++)
+      for (int i = 0; i < n; i++)
+        if (prevl[i] < l && l <= ll[i]) {
+          int p = pl[i];
+          tasks[off[(long)ph * npart + p] + tsize[p]++] = (long)l * n + i;
+        }
+    tcount = base;
+    prevl = ll;
+    prevlmin = lmin;
+  }
+  if (erc) { free(vv); free(l0); free(tsize); return ORC_ESTRUCT; }
+
+  /* skirt tasks (mpkprep.c:185-233) */
+  pl = parts;
+  for (int p = 0; p < npart; p++) {
+    long t = (long)nphase * npart + p;
+    off[t] = tcount;
+    long cnt = 0;
+    const int *sp = sl + (long)p * n;
+    for (int l = prevlmin + 1; l <= nlevel; l++)
+      for (int i = 0; i < n; i++)
+        if (prevl[i] < l && sp[i] >= 0 && l <= nlevel - sp[i]) {
+          if (vv[(long)l * n + i] > 0.0) erc++;
+          for (int j = ptr[i]; j < ptr[i + 1]; j++)
+            if (vv[(long)(l - 1) * n + col[j]] < 0.0) erc++;
+          vv[(long)l * n + i] = pl[i] * 100.0 + nphase;
+          if (tcount + cnt >= cap) { free(vv); free(l0); free(tsize); return ORC_ERANGE; }
+          tasks[tcount + cnt++] = (long)l * n + i;
+        }
+    for (int l = prevlmin + 1; l <= nlevel; l++)
+      for (int i = 0; i < n; i++)
+        if (prevl[i] < l && sp[i] >= 0 && l <= nlevel - sp[i]) vv[(long)l * n + i] = -0.1;
+    tcount += cnt;
+  }
+  off[(long)(nphase + 1) * npart] = tcount;
+  /* final level fully computed (mpkprep.c:238-242) */
+  for (int i = 0; i < n; i++) if (vv[(long)nlevel * n + i] < -0.5) erc++;
+  free(vv); free(l0); free(tsize);
+  return erc ? ORC_ESTRUCT : tcount;
+}
+
+/* ------------------------------------------------------------------ */
+/* Execution                                                             */
+/* ------------------------------------------------------------------ */
+
+/* do_task over every task list in (phase, part) order: restates
+ * exec_mpk (mpk2/mpkexec.c:10-59, 1/deg weights when val == NULL) and
+ * vexec_mpk (mpk2/mpkvexec.c:10-55, explicit values). */
+void orc_exec_tasks(int n, const int *ptr, const int *col, const double *val,
+                    long ntask_lists, const long *off, const long *tasks,
+                    double *vv, int mode) {
+  for (long t = 0; t < ntask_lists; t++)
+    for (long q = off[t]; q < off[t + 1]; q++) {
+      long tidx = tasks[q];
+      long level = tidx / n;
+      long i = tidx - level * n;
+      const double *src = vv + (level - 1) * n;
+      double s = 0.0;
+      if (val) {
+        for (int j = ptr[i]; j < ptr[i + 1]; j++) s = row_term(s, val[j], src[col[j]], mode);
+      } else {
+        double a = 1.0 / (ptr[i + 1] - ptr[i]);
+        for (int j = ptr[i]; j < ptr[i + 1]; j++) s = row_term(s, a, src[col[j]], mode);
+      }
+      vv[level * n + i] = s;
+    }
+}
+
+/* Transposed layout vv[i*(nlevel+1)+l] (mpk2/mpktexec.c:8-37). */
+void orc_exec_tasks_t(int n, int nlevel, const int *ptr, const int *col,
+                      long ntask_lists, const long *off, const long *tasks,
+                      double *vv, int mode) {
+  int nl1 = nlevel + 1;
+  for (long t = 0; t < ntask_lists; t++)
+    for (long q = off[t]; q < off[t + 1]; q++) {
+      long tidx = tasks[q];
+      long level = tidx / n;
+      long i = tidx - level * n;
+      double a = 1.0 / (ptr[i + 1] - ptr[i]);
+      double s = 0.0;
+      for (int j = ptr[i]; j < ptr[i + 1]; j++)
+        s = row_term(s, a, vv[(long)col[j] * nl1 + level - 1], mode);
+      vv[i * nl1 + level] = s;
+    }
+}
+
+/* k chained SpMVs: spmv_exec_seq (mpk2/spmvexec.c:8-28) when val == NULL,
+ * the verify_val gold chain (mpk2/verify_val.c:44-75) otherwise. */
+void orc_spmv_chain(int n, const int *ptr, const int *col, const double *val,
+                    int nlevel, double *vv, int mode) {
+  for (int l = 1; l <= nlevel; l++) {
+    const double *src = vv + (long)(l - 1) * n;
+    double *dst = vv + (long)l * n;
+    for (int i = 0; i < n; i++) {
+      double s = 0.0;
+      if (val) {
+        for (int j = ptr[i]; j < ptr[i + 1]; j++) s = row_term(s, val[j], src[col[j]], mode);
+      } else {
+        double a = 1.0 / (ptr[i + 1] - ptr[i]);
+        for (int j = ptr[i]; j < ptr[i + 1]; j++) s = row_term(s, a, src[col[j]], mode);
+      }
+      dst[i] = s;
+    }
+  }
+}
+
+/* The same chain with OpenMP over rows, for timing the CPU baseline on
+ * many host cores (spmv_exec_par, mpk2/spmvexec.c:30-50). */
+void orc_spmv_chain_par(int n, const int *ptr, const int *col, const double *val,
+                        int nlevel, double *vv, int mode, int nth) {
+  for (int l = 1; l <= nlevel; l++) {
+    const double *src = vv + (long)(l - 1) * n;
+    double *dst = vv + (long)l * n;
+#pragma omp parallel for num_threads(nth) schedule(static)
+    for (int i = 0; i < n; i++) {
+      double s = 0.0;
+      if (val) {
+        for (int j = ptr[i]; j < ptr[i + 1]; j++) s = row_term(s, val[j], src[col[j]], mode);
+      } else {
+        double a = 1.0 / (ptr[i + 1] - ptr[i]);
+        for (int j = ptr[i]; j < ptr[i + 1]; j++) s = row_term(s, a, src[col[j]], mode);
+      }
+      dst[i] = s;
+    }
+  }
+}
+
+/* exec over task lists with OpenMP: phases in order, parts in parallel
+ * with dynamic scheduling, as exec_mpk_xd (mpk2/mpkexec.c:79-95). */
+void orc_exec_tasks_par(int n, const int *ptr, const int *col, const double *val,
+                        int nphase, int npart, const long *off, const long *tasks,
+                        double *vv, int mode, int nth) {
+  for (int ph = 0; ph <= nphase; ph++) {
+#pragma omp parallel for num_threads(nth) schedule(dynamic, 1)
+    for (int p = 0; p < npart; p++) {
+      long t = (long)ph * npart + p;
+      orc_exec_tasks(n, ptr, col, val, 1, off + t, tasks, vv, mode);
+    }
+  }
+}

@@ -1,0 +1,159 @@
+"""Generates the golden fixtures in this directory from the REFERENCE code.
+
+Run in a checkout that has the reference sources (vatai/mpk) available to
+oracle/Makefile: the reference mpk2 library and tools are compiled from
+their own sources into oracle/_ref/, then driven exactly as the reference
+scripts drive them (mpk2/driver.c, mpk2/mpktest.c, mpk2/verify_val.c):
+
+  comp level / comp weight  -> level files l<ph> and weight graphs g<ph+1>
+  skirt                     -> skirt file s<nphase>
+  read_mpk + prep_mpk       -> task lists
+  exec_mpk / vexec_mpk      -> vv for a seeded x (1/deg and valued operator)
+  verify_val                -> gold_result.bin (x = 1, valued operator)
+
+Inputs (graphs, partitions, x) come from the product's generators and
+partitioners; METIS is not available, so partitions are recursive
+coordinate bisection or breadth-first bisection vectors, stored with the
+fixture.  The reference binaries here are x86-64 gcc -O2 builds, which do
+not contract a*b+c, so every floating-point fixture is in the oracle's
+"separate" arithmetic mode.
+
+    python tests/golden/make_golden.py
+"""
+import ctypes as C
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import mpk_gb300 as M  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+CASES = [
+    # name, grid (nx, ny, nz) or ("cube", size), npart, nlevel, nphase, partitioner, valued, seed
+    dict(name="m5p10_4_4_0", grid=(10, 10, 1), npart=4, nlevel=4, nphase=0, part="rcb", seed=3),
+    dict(name="cfg1_4_4_0", grid=(100, 100, 1), npart=4, nlevel=4, nphase=0, part="rcb", seed=0, gold=True),
+    dict(name="m5p20_4_4_2", grid=(20, 20, 1), npart=4, nlevel=4, nphase=2, part="rcb+bfs", seed=5),
+    dict(name="m5p16_4_6_3", grid=(16, 16, 1), npart=4, nlevel=6, nphase=3, part="bfs+rcb+bfs", seed=6),
+    dict(name="cube6_8_3_0", grid=("cube", 6), npart=8, nlevel=3, nphase=0, part="bfs", seed=7),
+]
+
+
+def loop_matrix(case):
+    """The matrix with diagonal (the .loop.g0/.loop.val pair)."""
+    if case["grid"][0] == "cube":
+        return M.Csr.stencil("cube", case["grid"][1])
+    nx, ny, nz = case["grid"]
+    return M.Csr.laplacian(nx, ny, nz, diag=4.0 if nz == 1 else 6.0, off=-1.0)
+
+
+def partitions(case, a):
+    kinds = case["part"].split("+")
+    out = []
+    for ph in range(max(case["nphase"], 1)):
+        kind = kinds[min(ph, len(kinds) - 1)]
+        if kind == "rcb":
+            out.append(M.partition_rcb(a.coords, case["npart"]))
+        else:
+            out.append(M.partition_bfs(a, case["npart"]))
+    return out
+
+
+def run(cmd, **kw):
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, **kw)
+
+
+def make(case, tmp):
+    a = loop_matrix(case)
+    n, npart, nlevel, nphase = a.n, case["npart"], case["nlevel"], case["nphase"]
+    ghead = case["name"].split("_")[0]
+    d = os.path.join(tmp, case["name"])
+    os.makedirs(d)
+    a.write_metis(os.path.join(d, "g0"), ne=(a.nnz + a.n) // 2)
+    a.write_metis(os.path.join(d, "loop.g0"), ne=(a.nnz + a.n) // 2)
+    a.write_values(os.path.join(tmp, ghead + ".loop.val"))
+    parts = partitions(case, a)
+    for ph, p in enumerate(parts):
+        np.savetxt(os.path.join(d, f"g{ph}.part.{npart}"), p, fmt="%d")
+    comp, skirt = O.ref_tool("comp"), O.ref_tool("skirt")
+    levels, weights = [], []
+    for ph in range(nphase):
+        args = [comp, "level", f"{d}/g0", "x", f"{d}/g{ph}.part.{npart}"]
+        if ph > 0:
+            args.append(f"{d}/l{ph - 1}")
+        run(args + [f"{d}/l{ph}"])
+        levels.append(np.loadtxt(f"{d}/l{ph}", dtype=np.int32).reshape(-1))
+        wargs = [comp, "weight", f"{d}/g0", "x", f"{d}/g{ph}.part.{npart}"]
+        if ph > 0:
+            wargs.append(f"{d}/l{ph - 1}")
+        run(wargs + [f"{d}/g{ph + 1}"])
+        with open(f"{d}/g{ph + 1}") as f:
+            f.readline()
+            we = [int(t) for line in f for t in line.split()[1:][1::2]]
+        weights.append(np.array(we, dtype=np.int32))
+    sargs = [skirt, str(nlevel), f"{d}/g0", "x", f"{d}/g0.part.{npart}"]
+    if nphase > 0:
+        sargs.append(f"{d}/l{nphase - 1}")
+    run(sargs + [f"{d}/s{nphase}"])
+    with open(f"{d}/s{nphase}", "rb") as f:
+        skirt_bytes = f.read()
+
+    R = O.ref()
+    x = M.uniform(case["seed"], n)
+    mg = R.read_mpk(d.encode())
+    vv = np.zeros((nlevel + 1) * n, dtype=np.float64)
+    R.prep_mpk(mg, vv.ctypes.data_as(C.c_void_p))
+    off, idx = O.ref_tasks(mg)
+    vv[:] = 0.0
+    vv[:n] = x
+    R.exec_mpk_xd(mg, vv.ctypes.data_as(C.c_void_p), 2)
+    vv_deg = vv.copy()
+    vv[:] = 0.0
+    vv[:n] = x
+    R.vexec_mpk(mg, vv.ctypes.data_as(C.c_void_p), a.val.ctypes.data_as(C.c_void_p))
+    vv_val = vv.copy()
+    R.spmv_exec_seq.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    vv[:] = 0.0
+    vv[:n] = x
+    R.spmv_exec_seq(mg.contents.g0, vv.ctypes.data_as(C.c_void_p), nlevel)
+    vv_spmv = vv.copy()
+    out = dict(n=n, npart=npart, nlevel=nlevel, nphase=nphase, seed=case["seed"],
+               parts=np.array(parts, dtype=np.int32), x=x,
+               skirt=np.frombuffer(skirt_bytes, dtype=np.uint8),
+               off=off, idx=idx, vv_deg=vv_deg, vv_val=vv_val, vv_spmv=vv_spmv)
+    if n > 1000:  # keep the large fixture small: hashes for the 1/deg results
+        for k in ("vv_deg", "vv_spmv"):
+            out[k + "_sha256"] = np.frombuffer(hashlib.sha256(out.pop(k).tobytes()).digest(), dtype=np.uint8)
+    if nphase:
+        out["levels"] = np.array(levels, dtype=np.int32)
+        out["weights"] = np.array(weights, dtype=np.int32)
+    if case.get("gold"):
+        run([O.ref_tool("verify_val"), case["name"]], cwd=tmp)
+        out["gold_x1"] = np.fromfile(os.path.join(d, "gold_result.bin"), dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, case["name"] + ".npz"), **out)
+    return out
+
+
+def main():
+    O.build()
+    if not O.ref_available():
+        sys.exit("reference sources not available: cannot regenerate golden fixtures")
+    tmp = tempfile.mkdtemp()
+    try:
+        for case in CASES:
+            out = make(case, tmp)
+            print(case["name"], "n", out["n"], "tasks", len(out["idx"]))
+    finally:
+        shutil.rmtree(tmp)
+
+
+if __name__ == "__main__":
+    main()

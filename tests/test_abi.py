@@ -1,0 +1,106 @@
+"""The C-ABI library loads and exports every function include/*.h declares;
+the mpk2-compatible structures keep the reference layout; bad inputs give
+error codes (no GPU needed)."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import mpk_gb300 as M
+from conftest import ROOT
+from oracle import oracle as O
+
+HEADERS = ["mpk_gb300.h", "mpk2_compat.h"]
+
+
+def declared_functions(header):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    text = re.sub(r"typedef struct\s*\w*\s*\{.*?\}\s*\w+;", " ", text, flags=re.S)
+    names = re.findall(r"\b([a-z_][a-z0-9_]*)\s*\([^;{)]*\)\s*;", text)
+    return sorted(set(n for n in names if n not in ("if", "sizeof")))
+
+
+@pytest.mark.parametrize("header", HEADERS)
+def test_library_exports_every_declared_symbol(header):
+    lib = C.CDLL(M.LIB_PATH)
+    names = declared_functions(header)
+    assert len(names) > 10
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_nm_lists_exports():
+    out = subprocess.run(["nm", "-D", "--defined-only", M.LIB_PATH], stdout=subprocess.PIPE, text=True).stdout
+    for n in declared_functions("mpk_gb300.h") + declared_functions("mpk2_compat.h"):
+        assert re.search(r"\bT " + n + r"\b", out), n
+
+
+def test_legacy_struct_layout():
+    """Field offsets of mpk_t/task_t as compiled from include/mpk2_compat.h
+    equal the reference's (mpk2/lib.h:78-99), checked with a C compiler."""
+    src = r'''
+    #include <stddef.h>
+    #include <stdio.h>
+    #include "mpk2_compat.h"
+    int main(void) {
+      printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(mpk_t), offsetof(mpk_t, g0), offsetof(mpk_t, tlist),
+             offsetof(mpk_t, idxallocsize), sizeof(task_t), offsetof(task_t, idx), offsetof(task_t, t1));
+      return 0; }'''
+    with tempfile.TemporaryDirectory() as d:
+        open(os.path.join(d, "a.c"), "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", os.path.join(d, "a"),
+                        os.path.join(d, "a.c")], check=True)
+        got = subprocess.run([os.path.join(d, "a")], stdout=subprocess.PIPE, text=True).stdout.split()
+    assert [int(v) for v in got] == [C.sizeof(O.RefMpk), O.RefMpk.g0.offset, O.RefMpk.tlist.offset,
+                                     O.RefMpk.idxallocsize.offset, C.sizeof(O.RefTask), O.RefTask.idx.offset,
+                                     O.RefTask.t1.offset]
+
+
+def test_plan_argument_errors():
+    a = M.Csr.laplacian(4, 4)
+    bad = M.Csr(a.ptr.copy(), a.col.copy(), a.val)
+    bad.col[3] = 99
+    with pytest.raises(M.MpkError) as e:
+        M.Plan.spmv(bad, 2)
+    assert e.value.code in (M.ERANGE, M.ECUDA)
+    with pytest.raises(M.MpkError) as e:
+        M.Plan.pa1(a, np.zeros(a.n, dtype=np.int32), 1, 2, exec=M.EXEC_PIPE)
+    assert e.value.code == M.EINVAL
+    with pytest.raises(M.MpkError) as e:
+        M.Plan.pa1(a, np.full(a.n, 7, dtype=np.int32), 2, 2)
+    assert e.value.code == M.ERANGE
+
+
+@pytest.mark.skipif(not O.ref_available() or not os.path.isdir("/root/reference/mpk2"),
+                    reason="reference sources not present")
+@pytest.mark.parametrize("tool", ["comp", "skirt"])
+def test_reference_tools_relink_against_library(tool):
+    """The reference's own comp.c / skirt.c mains, compiled against
+    include/mpk2_compat.h and linked with libmpk_gb300.so instead of the
+    reference lib.c, write byte-identical files."""
+    a = M.Csr.laplacian(24, 24)
+    part = M.partition_rcb(a.coords, 6)
+    with tempfile.TemporaryDirectory() as d:
+        shim = os.path.join(d, "lib.h")
+        open(shim, "w").write('#include "mpk2_compat.h"\n')
+        exe = os.path.join(d, tool)
+        subprocess.run(["gcc", "-O2", "-w", "-I", d, "-I", os.path.join(ROOT, "include"),
+                        f"/root/reference/mpk2/{tool}.c", "-o", exe, M.LIB_PATH,
+                        "-Wl,-rpath," + os.path.dirname(M.LIB_PATH)], check=True)
+        g = os.path.join(d, "g0")
+        a.write_metis(g, ne=(a.nnz + a.n) // 2)
+        pf = os.path.join(d, "p")
+        np.savetxt(pf, part, fmt="%d")
+        if tool == "comp":
+            runs = [["level", g, "x", pf], ["weight", g, "x", pf]]
+        else:
+            runs = [["5", g, "x", pf]]
+        for r in runs:
+            subprocess.run([exe] + r + [os.path.join(d, "mine")], check=True, stdout=subprocess.DEVNULL)
+            subprocess.run([O.ref_tool(tool)] + r + [os.path.join(d, "ref")], check=True, stdout=subprocess.DEVNULL)
+            assert open(os.path.join(d, "mine"), "rb").read() == open(os.path.join(d, "ref"), "rb").read()

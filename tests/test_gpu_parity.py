@@ -1,0 +1,132 @@
+"""GPU parity: every executor against the reference's own results (golden
+fixtures, bit for bit in the reference's non-contracted arithmetic) and
+against the oracle (bit for bit in FMA arithmetic), plus the FP64 tolerance
+of the task (1e-13 relative per power vector) and full-size checks on the
+128^3 7-point workload."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import mpk_gb300 as M
+from conftest import GOLDEN_CASES, golden_matrix, load_golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-13  # relative error per power vector, FP64 paths
+
+
+def _check_bits(g, key, vv):
+    if key in g:
+        bad = np.flatnonzero(vv.view(np.int64) != g[key].view(np.int64))
+        assert bad.size == 0, f"{key}: {bad.size} words differ, first at {bad[:5]}"
+    else:
+        assert hashlib.sha256(vv.tobytes()).digest() == g[key + "_sha256"].tobytes(), key
+
+
+def _run(plan, x, n, nlevel):
+    vv = np.zeros((nlevel + 1) * n)
+    vv[:n] = x
+    plan.exec_host(vv)
+    return vv
+
+
+def _plans(name, g, a, arith):
+    n, npart, nlevel, nphase = int(g["n"]), int(g["npart"]), int(g["nlevel"]), int(g["nphase"])
+    out = {"tasks": M.Plan.from_tasks(a, npart, nlevel, nphase, g["off"], g["idx"], arith=arith),
+           "spmv": M.Plan.spmv(a, nlevel, arith=arith),
+           "pipe": M.Plan.pipe(a, nlevel, arith=arith)}
+    if nphase == 0:
+        out["tiles"] = M.Plan.pa1(a, g["parts"][0], npart, nlevel, exec=M.EXEC_TILES, arith=arith)
+        out["pa1_tasks"] = M.Plan.pa1(a, g["parts"][0], npart, nlevel, exec=M.EXEC_TASKS, arith=arith)
+    return out
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("valued", [False, True])
+def test_executors_bitwise_vs_reference(name, valued, gpu):
+    g = load_golden(name)
+    a = golden_matrix(name)
+    if not valued:
+        a = a.pattern()
+    n, nlevel = int(g["n"]), int(g["nlevel"])
+    key = "vv_val" if valued else "vv_deg"
+    for ex, plan in _plans(name, g, a, M.ARITH_SEPARATE).items():
+        vv = _run(plan, g["x"], n, nlevel)
+        _check_bits(g, key, vv)
+        if not valued:
+            _check_bits(g, "vv_spmv", vv)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_executors_bitwise_vs_oracle_fma(name, gpu):
+    g = load_golden(name)
+    a = golden_matrix(name)
+    n, nlevel = int(g["n"]), int(g["nlevel"])
+    want = O.mpk(a.ptr, a.col, a.val, g["x"], nlevel, O.MODE_FMA)
+    for ex, plan in _plans(name, g, a, M.ARITH_FMA).items():
+        vv = _run(plan, g["x"], n, nlevel)
+        assert vv.tobytes() == want.tobytes(), ex
+
+
+def test_config1_fp64_tolerance_vs_reference(gpu):
+    """Config 1 (100^2 5-point, k=4, 4 parts): the default (FMA) GPU result
+    is within 1e-13 per power vector of the reference's valued exec and of
+    verify_val's gold chain (x = 1)."""
+    g = load_golden("cfg1_4_4_0")
+    a = golden_matrix("cfg1_4_4_0")
+    n, nlevel = int(g["n"]), int(g["nlevel"])
+    for ex, plan in _plans("cfg1_4_4_0", g, a, M.ARITH_FMA).items():
+        for x, ref in ((g["x"], g["vv_val"]), (np.ones(n), g["gold_x1"])):
+            vv = _run(plan, x, n, nlevel)
+            for l in range(1, nlevel + 1):
+                r = ref[l * n:(l + 1) * n]
+                err = np.linalg.norm(vv[l * n:(l + 1) * n] - r) / np.linalg.norm(r)
+                assert err <= TOL, (ex, l, err)
+
+
+def test_all_ones_fixed_point_deg_operator(gpu):
+    """The row-normalised operator maps 1 to 1 (mpk2/mpktest.c:43-51)."""
+    a = M.Csr.laplacian(40, 30, 20).pattern()
+    part = M.partition_rcb(a.coords, 64)
+    for plan in (M.Plan.pa1(a, part, 64, 6), M.Plan.pipe(a, 6), M.Plan.spmv(a, 6)):
+        vv = _run(plan, np.ones(a.n), a.n, 6)
+        assert np.max(np.abs(vv - 1.0)) < 1e-14
+
+
+def test_device_pointer_path_matches_host_path(gpu):
+    import torch
+    a = M.Csr.laplacian(64, 64, 8)
+    part = M.partition_rcb(a.coords, 32)
+    x = M.uniform(11, a.n)
+    for plan in (M.Plan.pa1(a, part, 32, 5), M.Plan.pipe(a, 5), M.Plan.spmv(a, 5)):
+        want = _run(plan, x, a.n, 5)
+        d = torch.zeros(6 * a.n, dtype=torch.float64, device="cuda")
+        d[:a.n] = torch.from_numpy(x).cuda()
+        torch.cuda.synchronize()
+        for _ in range(3):  # repeated launches reuse the plan (pipeline epochs)
+            plan.exec_device(d.data_ptr())
+            plan.sync()
+        assert d.cpu().numpy().tobytes() == want.tobytes()
+
+
+@pytest.fixture(scope="module")
+def config2():
+    a = M.Csr.laplacian(128, 128, 128, diag=6.0, off=-1.0)
+    part = M.partition_rcb(a.coords, 2048)
+    x = M.uniform(1, a.n)
+    want = O.mpk(a.ptr, a.col, a.val, x, 8, O.MODE_FMA)
+    return a, part, x, want
+
+
+@pytest.mark.parametrize("ex", ["tiles", "pipe", "spmv"])
+def test_config2_full_size_bitwise_vs_oracle(config2, ex, gpu):
+    """128^3 7-point, k=8, 2048 parts: bit-identical to the oracle chain."""
+    a, part, x, want = config2
+    plan = {"tiles": lambda: M.Plan.pa1(a, part, 2048, 8),
+            "pipe": lambda: M.Plan.pipe(a, 8),
+            "spmv": lambda: M.Plan.spmv(a, 8)}[ex]()
+    vv = _run(plan, x, a.n, 8)
+    bad = np.flatnonzero(vv.view(np.int64) != want.view(np.int64))
+    assert bad.size == 0, f"{bad.size} differ, first {bad[:5]}"
