@@ -67,6 +67,7 @@ def _declare(L):
         "mpkg_exec_device": (I, [P, P, P]),
         "mpkg_sync": (I, [P, P]),
         "mpkg_plan_destroy": (None, [P]),
+        "mpkg_debug_pipe_stall": (I, [P, I]),
         "mpkg_spmv_chain_device": (I, [I, P, P, P, I, P, I, P]),
         "mpkg_read_metis": (I, [C.c_char_p, C.POINTER(I), C.POINTER(Lg), pp, pp]),
         "mpkg_read_values": (I, [C.c_char_p, Lg, pp]),
@@ -301,6 +302,11 @@ class Plan:
 
     def sync(self, stream: int = 0):
         _check(lib().mpkg_sync(self._h, C.c_void_p(stream or None)))
+
+    def debug_stall(self, extra_levels):
+        """Test hook: pipeline waits target `extra_levels` beyond the real
+        level (0 restores normal behaviour)."""
+        _check(lib().mpkg_debug_pipe_stall(self._h, extra_levels))
 
     def close(self):
         if self._h is not None and self._h.value:

@@ -198,11 +198,14 @@ __global__ void __launch_bounds__(512) tiles_kernel(TileArgs a) {
 struct PipeArgs {
   int n, nlevel, chunk, nchunk;
   uint32_t epoch;
+  uint32_t stall;     // test hook: waits for a level this far beyond the real one
   const int *dep_lo, *dep_hi;
   const int *ptr, *col;
-  const double *coef;
+  const double *coef;  // FP64 values (nnz) or 1/deg (n)
+  const float2 *coef2; // double-float values (nnz) or 1/deg (n)
   const double *x;
   double *vv;
+  float2 *ring;        // double-float level values, two slots of n
   unsigned int *ticket;
   unsigned int *flags;
   int *err;
@@ -218,82 +221,265 @@ __device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Every thread of the CTA calls this.  Threads poll one dependency flag
+// each with acquire loads until it reaches `want`; a poll count above
+// kSpinLimit, or an error raised elsewhere, aborts the CTA.  Returns false
+// on abort.  After the barrier every thread's plain loads observe the data
+// the producers released (acquire + CTA barrier).
+__device__ __forceinline__ bool pipe_wait(const PipeArgs &a, int c, int dlo, int dhi, unsigned want,
+                                          int *s_abort) {
+  for (int d = dlo + (int)threadIdx.x; d <= dhi; d += blockDim.x) {
+    if (d == c) continue;
+    long spins = 0;
+    while (ld_acquire(a.flags + d) < want) {
+      if (++spins > kSpinLimit || *((volatile int *)a.err)) {
+        atomicCAS(a.err, 0, kErrTimeout);
+        *s_abort = 1;
+        break;
+      }
+      __nanosleep(spins < 64 ? 32 : 256);
+    }
+  }
+  __syncthreads();
+  return *s_abort == 0;
+}
+
+__device__ __forceinline__ void pipe_publish(const PipeArgs &a, int c, unsigned tag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release(a.flags + c, tag);
+  }
+}
+
+// Takes the next chunk and stages its rows (row pointers, columns and, for
+// the valued operator, coefficients of type T) in shared memory.  Returns
+// the chunk id, or -1 when the work is exhausted or a plan invariant fails.
+template <typename T, bool VALUED>
+__device__ __forceinline__ int pipe_take(const PipeArgs &a, const T *coef, int *rptr, int *cols, T *vals,
+                                         unsigned int *s_chunk, int *s_abort) {
+  if (threadIdx.x == 0) {
+    *s_chunk = atomicAdd(a.ticket, 1u);
+    *s_abort = 0;
+  }
+  __syncthreads();
+  const int c = (int)*s_chunk;
+  if (c >= a.nchunk) return -1;
+  const int r0 = c * a.chunk;
+  const int nr = min(a.chunk, a.n - r0);
+  const int j00 = a.ptr[r0];
+  for (int r = threadIdx.x; r <= nr; r += blockDim.x) rptr[r] = a.ptr[r0 + r] - j00;
+  __syncthreads();
+  const int cnnz = rptr[nr];
+  if (cnnz > a.max_chunk_nnz) {  // plan invariant
+    if (threadIdx.x == 0) atomicExch(a.err, kErrBounds);
+    return -1;
+  }
+  for (int t = threadIdx.x; t < cnnz; t += blockDim.x) {
+    cols[t] = a.col[j00 + t];
+    if (VALUED) vals[t] = coef[j00 + t];
+  }
+  __syncthreads();
+  return c;
+}
+
+template <typename T>
+__device__ __forceinline__ T *pipe_vals(unsigned char *smem, const PipeArgs &a) {
+  return reinterpret_cast<T *>(
+      smem + (((size_t)(a.chunk + 1 + a.max_chunk_nnz) * sizeof(int) + 15) & ~(size_t)15));
+}
+
 template <int ARITH, bool VALUED>
 __global__ void __launch_bounds__(256) pipe_kernel(PipeArgs a) {
   extern __shared__ __align__(16) unsigned char pipe_smem[];
-  // layout: rptr[chunk+1] ints | cols[max_chunk_nnz] ints | vals[max_chunk_nnz] doubles
   int *rptr = reinterpret_cast<int *>(pipe_smem);
   int *cols = rptr + a.chunk + 1;
-  double *vals = reinterpret_cast<double *>(
-      pipe_smem + (((size_t)(a.chunk + 1 + a.max_chunk_nnz) * sizeof(int) + 15) & ~(size_t)15));
+  double *vals = pipe_vals<double>(pipe_smem, a);
   __shared__ unsigned int s_chunk;
   __shared__ int s_abort;
   const unsigned int base_tag = a.epoch * 32u;
   for (;;) {
-    if (threadIdx.x == 0) {
-      s_chunk = atomicAdd(a.ticket, 1u);
-      s_abort = 0;
-    }
-    __syncthreads();
-    const int c = (int)s_chunk;
-    if (c >= a.nchunk) return;
+    const int c = pipe_take<double, VALUED>(a, a.coef, rptr, cols, vals, &s_chunk, &s_abort);
+    if (c < 0) return;
     const int r0 = c * a.chunk;
     const int nr = min(a.chunk, a.n - r0);
-    const int j00 = a.ptr[r0];
-    // stage the chunk's rows
-    for (int r = threadIdx.x; r <= nr; r += blockDim.x) rptr[r] = a.ptr[r0 + r] - j00;
-    __syncthreads();
-    const int cnnz = rptr[nr];
-    if (cnnz > a.max_chunk_nnz) {  // plan invariant
-      if (threadIdx.x == 0) atomicExch(a.err, kErrBounds);
-      return;
-    }
-    for (int t = threadIdx.x; t < cnnz; t += blockDim.x) {
-      cols[t] = a.col[j00 + t];
-      if (VALUED) vals[t] = a.coef[j00 + t];
-    }
-    double cf = 0.0;
-    int myrow = r0 + threadIdx.x;
-    if (!VALUED && threadIdx.x < nr) cf = a.coef[myrow];
-    __syncthreads();
+    const int myrow = r0 + threadIdx.x;
+    const double cf = (!VALUED && (int)threadIdx.x < nr) ? a.coef[myrow] : 0.0;
     const int dlo = a.dep_lo[c], dhi = a.dep_hi[c];
     for (int l = 1; l <= a.nlevel; l++) {
-      if (l > 1) {
-        // wait for level l-1 of the chunks this chunk reads
-        const unsigned int want = base_tag + (unsigned)(l - 1);
-        for (int d = dlo + (int)threadIdx.x; d <= dhi; d += blockDim.x) {
-          if (d == c) continue;
-          long spins = 0;
-          while (ld_acquire(a.flags + d) < want) {
-            if (++spins > kSpinLimit || *((volatile int *)a.err)) {
-              atomicCAS(a.err, 0, kErrTimeout);
-              s_abort = 1;
-              break;
-            }
-            __nanosleep(spins < 64 ? 32 : 256);
-          }
-        }
-        __syncthreads();
-        if (s_abort) return;
-      }
-      if (threadIdx.x < nr) {
+      if (l > 1 && !pipe_wait(a, c, dlo, dhi, base_tag + (unsigned)(l - 1) + a.stall, &s_abort)) return;
+      if ((int)threadIdx.x < nr) {
         const double *src = a.vv + (long)(l - 1) * a.n;
         const int q0 = rptr[threadIdx.x], q1 = rptr[threadIdx.x + 1];
         double s = 0.0;
-        if (l == 1) {
-          for (int q = q0; q < q1; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf, a.x[cols[q]]);
-        } else {
-          for (int q = q0; q < q1; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf, ld_cg(src + cols[q]));
-        }
+        for (int q = q0; q < q1; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf, src[cols[q]]);
         a.vv[(long)l * a.n + myrow] = s;
       }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        __threadfence();
-        st_release(a.flags + c, base_tag + (unsigned)l);
-      }
+      pipe_publish(a, c, base_tag + (unsigned)l);
     }
   }
+}
+
+// ------------------------------------------------------------------------
+// Double-float ("df64") arithmetic on the FP32 pipes.  A value is an
+// unevaluated sum h + l of two floats with |l| <= ulp(h)/2 after
+// normalisation (48 significand bits).  Products use the exact FMA
+// residual; sums use Knuth's TwoSum.  Intrinsics (__fmul_rn, __fadd_rn)
+// keep the compiler from contracting the error-free transformations.
+// FP64 <-> df64 conversions use integer bit manipulation so that they do
+// not occupy the narrow FP64 pipe.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ float2 df_split(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  const int E = e - 1023;
+  const unsigned int sgn = (unsigned int)(b >> 63) << 31;
+  if (e == 0x7FF || E > 127) {  // inf/nan or beyond the float range
+    const float h = __double2float_rn(x);
+    return make_float2(h, 0.0f);
+  }
+  if (E < -126) return make_float2(0.0f, 0.0f);  // below the df64 range
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  const float h = __uint_as_float(sgn | ((unsigned)(E + 127) << 23) | (unsigned)(m >> 29));
+  const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull);  // low 29 bits, weight 2^(E-52)
+  float lo = 0.0f;
+  if (rem != 0 && E - 52 >= -126) {
+    lo = __fmul_rn(__uint2float_rn(rem), __uint_as_float((unsigned)(E - 52 + 127) << 23));
+    lo = __uint_as_float(__float_as_uint(lo) | sgn);
+  }
+  return make_float2(h, lo);
+}
+
+__device__ __forceinline__ double df_widen(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xFF;
+  if (e == 0) return __longlong_as_double((long long)((unsigned long long)(u >> 31) << 63));  // +-0
+  if (e == 0xFF) return (double)f;
+  return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
+                                          ((unsigned long long)(e + 896) << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFF) << 29)));
+}
+
+__device__ __forceinline__ double df_to_double(float2 v) { return __dadd_rn(df_widen(v.x), df_widen(v.y)); }
+
+// s += a * x in double-float
+__device__ __forceinline__ void df_mac(float2 a, float2 x, float &sh, float &sl) {
+  const float p = __fmul_rn(a.x, x.x);
+  float e = __fmaf_rn(a.x, x.x, -p);
+  e = __fmaf_rn(a.x, x.y, e);
+  e = __fmaf_rn(a.y, x.x, e);
+  const float s = __fadd_rn(sh, p);
+  const float bp = __fadd_rn(s, -sh);
+  const float t = __fadd_rn(__fadd_rn(sh, -__fadd_rn(s, -bp)), __fadd_rn(p, -bp));
+  sh = s;
+  sl = __fadd_rn(sl, __fadd_rn(t, e));
+}
+
+__device__ __forceinline__ float2 df_norm(float sh, float sl) {
+  const float h = __fadd_rn(sh, sl);
+  const float l = __fadd_rn(sl, -__fadd_rn(h, -sh));
+  return make_float2(h, l);
+}
+
+// Pipeline in double-float: levels travel between chunks through a
+// two-slot ring of df64 values (level l in slot l&1); vv receives the FP64
+// rounding of every level.  Level 0 (the split of x) is a pipeline stage of
+// its own.  A slot is overwritten (level l+2) only after every chunk within
+// reach has finished level l+1, i.e. no longer reads level l.
+template <bool VALUED>
+__global__ void __launch_bounds__(256) pipe_df_kernel(PipeArgs a) {
+  extern __shared__ __align__(16) unsigned char pipe_smem[];
+  int *rptr = reinterpret_cast<int *>(pipe_smem);
+  int *cols = rptr + a.chunk + 1;
+  float2 *vals = pipe_vals<float2>(pipe_smem, a);
+  __shared__ unsigned int s_chunk;
+  __shared__ int s_abort;
+  const unsigned int base_tag = a.epoch * 32u;
+  for (;;) {
+    const int c = pipe_take<float2, VALUED>(a, a.coef2, rptr, cols, vals, &s_chunk, &s_abort);
+    if (c < 0) return;
+    const int r0 = c * a.chunk;
+    const int nr = min(a.chunk, a.n - r0);
+    const int myrow = r0 + threadIdx.x;
+    const bool active = (int)threadIdx.x < nr;
+    const float2 cf = (!VALUED && active) ? a.coef2[myrow] : make_float2(0.f, 0.f);
+    const int dlo = a.dep_lo[c], dhi = a.dep_hi[c];
+    if (active) a.ring[myrow] = df_split(a.x[myrow]);
+    pipe_publish(a, c, base_tag);
+    for (int l = 1; l <= a.nlevel; l++) {
+      if (!pipe_wait(a, c, dlo, dhi, base_tag + (unsigned)(l - 1) + a.stall, &s_abort)) return;
+      if (active) {
+        const float2 *src = a.ring + (long)((l - 1) & 1) * a.n;
+        const int q0 = rptr[threadIdx.x], q1 = rptr[threadIdx.x + 1];
+        float sh = 0.f, sl = 0.f;
+        for (int q = q0; q < q1; q++) df_mac(VALUED ? vals[q] : cf, src[cols[q]], sh, sl);
+        const float2 v = df_norm(sh, sl);
+        a.ring[(long)(l & 1) * a.n + myrow] = v;
+        a.vv[(long)l * a.n + myrow] = df_to_double(v);
+      }
+      pipe_publish(a, c, base_tag + (unsigned)l);
+    }
+  }
+}
+
+// PA1 tiles in double-float: same schedule as tiles_kernel, level buffers
+// of float2 in shared memory.
+template <bool VALUED, bool SMEM>
+__global__ void __launch_bounds__(512) tiles_df_kernel(TileArgs a, const float2 *coef2) {
+  extern __shared__ float2 smem_f2[];
+  const int p = a.order[blockIdx.x];
+  const long s0 = a.slot_off[p];
+  const int ns = (int)(a.slot_off[p + 1] - s0);
+  const int *shell = a.shell + (long)p * (a.nlevel + 1);
+  const long sl0 = a.slice_off[p];
+  float2 *buf0 = SMEM ? smem_f2 : reinterpret_cast<float2 *>(a.scratch) + (long)blockIdx.x * 2 * a.max_slots;
+  float2 *buf1 = buf0 + a.max_slots;
+  if (ns > a.max_slots) {
+    if (threadIdx.x == 0) atomicExch(a.err, kErrBounds);
+    return;
+  }
+  for (int s = threadIdx.x; s < ns; s += blockDim.x) buf0[s] = df_split(a.x[a.slot_vert[s0 + s]]);
+  __syncthreads();
+  const int owned = shell[0];
+  for (int l = 1; l <= a.nlevel; l++) {
+    const float2 *in = (l & 1) ? buf0 : buf1;
+    float2 *out = (l & 1) ? buf1 : buf0;
+    const int nrows = shell[a.nlevel - l];
+    double *dst = a.vv + (long)l * a.n;
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+      const long sl = sl0 + (r >> 5);
+      const int lane = r & 31;
+      const int w = a.ell_width[sl];
+      const uint16_t *cp = a.ell_col + a.ell_off[sl] + lane;
+      const int v = a.slot_vert[s0 + r];
+      float sh = 0.f, slo = 0.f;
+      if (VALUED) {
+        const float2 *vp = coef2 + a.ptr[v];
+        for (int t = 0; t < w; t++) {
+          const int c = cp[t * 32];
+          if (c == 0xFFFF) break;
+          df_mac(vp[t], in[c], sh, slo);
+        }
+      } else {
+        const float2 cf = coef2[v];
+        for (int t = 0; t < w; t++) {
+          const int c = cp[t * 32];
+          if (c == 0xFFFF) break;
+          df_mac(cf, in[c], sh, slo);
+        }
+      }
+      const float2 res = df_norm(sh, slo);
+      out[r] = res;
+      if (r < owned) dst[v] = df_to_double(res);
+    }
+    __syncthreads();
+  }
+}
+
+// FP64 -> double-float conversion of a coefficient array (plan set-up).
+__global__ void split_kernel(const double *__restrict__ src, float2 *__restrict__ dst, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = df_split(src[i]);
 }
 
 __global__ void copy_kernel(const double *__restrict__ src, double *__restrict__ dst, long n) {
@@ -318,6 +504,7 @@ struct mpkg_plan {
   cudaStream_t stream = nullptr;
   int *d_ptr = nullptr, *d_col = nullptr;
   double *d_coef = nullptr;  // values (nnz) or 1/deg (n)
+  float2 *d_coef2 = nullptr; // double-float split of d_coef (ARITH_DF64)
   int *d_err = nullptr;
   double *d_vv = nullptr;    // staging for host execution
   // tasks
@@ -379,8 +566,8 @@ int plan_common(mpkg_plan *p, int n, const int *ptr, const int *col, const doubl
   int rc = check_csr(n, ptr, col);
   if (rc) return rc;
   if (nlevel <= 0 || nlevel > 31) return fail(kEInval, "nlevel must be in [1, 31]");
-  if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE)
-    return fail(kEInval, "arith mode not supported by this executor");
+  if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE && arith != MPKG_ARITH_DF64)
+    return fail(kEInval, "unknown arith mode");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
   CUDA_TRY(cudaGetDevice(&p->device));
@@ -398,6 +585,13 @@ int plan_common(mpkg_plan *p, int n, const int *ptr, const int *col, const doubl
     std::vector<double> rdeg(n);
     for (int i = 0; i < n; i++) rdeg[i] = 1.0 / (ptr[i + 1] - ptr[i]);  // as mpk2/mpkexec.c:28
     if ((rc = dev_copy(p, &p->d_coef, rdeg.data(), (size_t)n))) return rc;
+  }
+  if (arith == MPKG_ARITH_DF64) {
+    const long m = val ? p->nnz : n;
+    if ((rc = dev_alloc(p, &p->d_coef2, (size_t)m))) return rc;
+    split_kernel<<<256, 256, 0, p->stream>>>(p->d_coef, p->d_coef2, m);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(p->stream));
   }
   if ((rc = dev_alloc(p, &p->d_err, 1))) return rc;
   CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
@@ -497,6 +691,24 @@ int set_tiles_attr(size_t bytes) {
   return kOk;
 }
 
+template <bool VALUED>
+int pipe_setup_df(mpkg_plan *p, int *grid) {
+  CUDA_TRY(cudaFuncSetAttribute(pipe_df_kernel<VALUED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)p->pipe_smem_bytes));
+  int per_sm = 0, nsm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_df_kernel<VALUED>, 256, p->pipe_smem_bytes));
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+  *grid = per_sm * nsm;
+  return kOk;
+}
+
+template <bool VALUED, bool SMEM>
+int set_tiles_df_attr(size_t bytes) {
+  CUDA_TRY(cudaFuncSetAttribute(tiles_df_kernel<VALUED, SMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes));
+  return kOk;
+}
+
 template <int ARITH, bool VALUED>
 int pipe_setup_t(mpkg_plan *p, int *grid) {
   CUDA_TRY(cudaFuncSetAttribute(pipe_kernel<ARITH, VALUED>,
@@ -547,6 +759,26 @@ void launch_tiles_t(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) 
     tiles_kernel<ARITH, VALUED, false><<<p->npart, 512, 0, st>>>(a);
 }
 
+template <bool VALUED>
+void launch_tiles_df(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) {
+  TileArgs a = p->tiles;
+  a.x = x;
+  a.vv = vv;
+  if (p->tiles_smem)
+    tiles_df_kernel<VALUED, true><<<p->npart, 512, p->tiles_smem_bytes, st>>>(a, p->d_coef2);
+  else
+    tiles_df_kernel<VALUED, false><<<p->npart, 512, 0, st>>>(a, p->d_coef2);
+}
+
+template <bool VALUED>
+void launch_pipe_df(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) {
+  PipeArgs a = p->pipe;
+  a.x = x;
+  a.vv = vv;
+  a.epoch = p->epoch;
+  pipe_df_kernel<VALUED><<<p->pipe_grid, 256, p->pipe_smem_bytes, st>>>(a);
+}
+
 template <int ARITH, bool VALUED>
 void launch_pipe_t(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) {
   PipeArgs a = p->pipe;
@@ -575,7 +807,12 @@ int plan_launch(mpkg_plan *p, double *d_vv, cudaStream_t st) {
       p->launches = p->nphase + 1;
       break;
     case MPKG_EXEC_TILES:
-      DISPATCH2(launch_tiles_t, p, d_vv, d_vv, st);
+      if (p->arith == MPKG_ARITH_DF64) {
+        if (p->valued) launch_tiles_df<true>(p, d_vv, d_vv, st);
+        else launch_tiles_df<false>(p, d_vv, d_vv, st);
+      } else {
+        DISPATCH2(launch_tiles_t, p, d_vv, d_vv, st);
+      }
       p->launches = 1;
       break;
     case MPKG_EXEC_PIPE: {
@@ -585,7 +822,12 @@ int plan_launch(mpkg_plan *p, double *d_vv, cudaStream_t st) {
         p->epoch = 1;
       }
       CUDA_TRY(cudaMemsetAsync(p->pipe.ticket, 0, sizeof(unsigned int), st));
-      DISPATCH2(launch_pipe_t, p, d_vv, d_vv, st);
+      if (p->arith == MPKG_ARITH_DF64) {
+        if (p->valued) launch_pipe_df<true>(p, d_vv, d_vv, st);
+        else launch_pipe_df<false>(p, d_vv, d_vv, st);
+      } else {
+        DISPATCH2(launch_pipe_t, p, d_vv, d_vv, st);
+      }
       p->launches = 1;
       break;
     }
@@ -632,7 +874,8 @@ int mpkg_plan_tasks(int n, const int *ptr, const int *col, const double *val, in
     return fail(kEInval, "bad task list arguments");
   mpkg_plan *p = new_plan();
   if (!p) return fail(kENoMem, "plan allocation failed");
-  int rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  int rc = arith == MPKG_ARITH_DF64 ? fail(kEInval, "the tasks executor computes in FP64 only")
+                                    : plan_common(p, n, ptr, col, val, nlevel, arith);
   if (!rc) {
     p->exec = MPKG_EXEC_TASKS;
     p->npart = npart;
@@ -677,7 +920,10 @@ int mpkg_plan_pa1(int n, const int *ptr, const int *col, const double *val, cons
     p->npart = npart;
     rc = build_tile_device(p, tp);
   }
-  if (!rc && p->tiles_smem) {
+  if (!rc && p->tiles_smem && p->arith == MPKG_ARITH_DF64) {
+    rc = p->valued ? set_tiles_df_attr<true, true>(p->tiles_smem_bytes)
+                   : set_tiles_df_attr<false, true>(p->tiles_smem_bytes);
+  } else if (!rc && p->tiles_smem) {
     if (p->arith == MPKG_ARITH_SEPARATE) {
       rc = p->valued ? set_tiles_attr<MPKG_ARITH_SEPARATE, true, true>(p->tiles_smem_bytes)
                      : set_tiles_attr<MPKG_ARITH_SEPARATE, false, true>(p->tiles_smem_bytes);
@@ -729,6 +975,12 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
     if (!rc) rc = dev_copy(p, &dhi, pp.dep_hi.data(), pp.dep_hi.size());
     if (!rc) rc = dev_alloc(p, &ticket, 1);
     if (!rc) rc = dev_alloc(p, &flags, (size_t)pp.nchunk);
+    if (!rc && p->arith == MPKG_ARITH_DF64) {
+      float2 *ring;
+      rc = dev_alloc(p, &ring, 2 * (size_t)n);
+      a.ring = ring;
+      a.coef2 = p->d_coef2;
+    }
     if (!rc) {
       cudaMemset(flags, 0, sizeof(unsigned int) * pp.nchunk);
       a.dep_lo = dlo; a.dep_hi = dhi; a.ticket = ticket; a.flags = flags;
@@ -739,7 +991,9 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
     }
     if (!rc) {
       int grid = 0;
-      if (p->arith == MPKG_ARITH_SEPARATE)
+      if (p->arith == MPKG_ARITH_DF64)
+        rc = p->valued ? pipe_setup_df<true>(p, &grid) : pipe_setup_df<false>(p, &grid);
+      else if (p->arith == MPKG_ARITH_SEPARATE)
         rc = p->valued ? pipe_setup_t<MPKG_ARITH_SEPARATE, true>(p, &grid) : pipe_setup_t<MPKG_ARITH_SEPARATE, false>(p, &grid);
       else
         rc = p->valued ? pipe_setup_t<MPKG_ARITH_FMA, true>(p, &grid) : pipe_setup_t<MPKG_ARITH_FMA, false>(p, &grid);
@@ -748,7 +1002,7 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
         p->pipe_grid = std::min(grid, pp.nchunk);
         // progress needs every chunk within (k-1)*reach of the oldest
         // unfinished chunk to be running
-        long need = (long)(nlevel - 1) * pp.reach + 1;
+        long need = (long)(p->arith == MPKG_ARITH_DF64 ? nlevel : nlevel - 1) * pp.reach + 1;
         if (p->pipe_grid < pp.nchunk && p->pipe_grid < need)
           rc = fail(kERange, "matrix bandwidth too large for the pipeline (reach " +
                                  std::to_string(pp.reach) + " chunks, " + std::to_string(grid) +
@@ -768,7 +1022,8 @@ int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val, int
   *out = nullptr;
   mpkg_plan *p = new_plan();
   if (!p) return fail(kENoMem, "plan allocation failed");
-  int rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  int rc = arith == MPKG_ARITH_DF64 ? fail(kEInval, "the k-SpMV baseline computes in FP64 only")
+                                    : plan_common(p, n, ptr, col, val, nlevel, arith);
   if (!rc) {
     p->exec = MPKG_EXEC_SPMV;
     p->npart = 1;
@@ -776,6 +1031,13 @@ int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val, int
   }
   if (rc) { mpkg_plan_destroy(p); return rc; }
   *out = p;
+  return kOk;
+}
+
+int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels) {
+  if (!p || p->exec != MPKG_EXEC_PIPE || extra_levels < 0 || extra_levels > 1000)
+    return fail(kEInval, "stall hook needs a pipeline plan and 0 <= extra <= 1000");
+  p->pipe.stall = (uint32_t)extra_levels;
   return kOk;
 }
 

@@ -130,3 +130,59 @@ def test_config2_full_size_bitwise_vs_oracle(config2, ex, gpu):
     vv = _run(plan, x, a.n, 8)
     bad = np.flatnonzero(vv.view(np.int64) != want.view(np.int64))
     assert bad.size == 0, f"{bad.size} differ, first {bad[:5]}"
+
+
+def _rel_errors(vv, want, n, nlevel):
+    out = []
+    for l in range(1, nlevel + 1):
+        r = want[l * n:(l + 1) * n]
+        out.append(float(np.linalg.norm(vv[l * n:(l + 1) * n] - r) / np.linalg.norm(r)))
+    return out
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("valued", [False, True])
+def test_df64_executors_within_fp64_tolerance(name, valued, gpu):
+    """Double-float arithmetic (FP32 pipes) with FP64 storage stays within
+    the FP64 tolerance of the reference's results."""
+    g = load_golden(name)
+    a = golden_matrix(name)
+    if not valued:
+        a = a.pattern()
+    n, npart, nlevel, nphase = int(g["n"]), int(g["npart"]), int(g["nlevel"]), int(g["nphase"])
+    want = O.mpk(a.ptr, a.col, a.val, g["x"], nlevel, O.MODE_FMA)
+    plans = {"pipe": M.Plan.pipe(a, nlevel, arith=M.ARITH_DF64)}
+    if nphase == 0:
+        plans["tiles"] = M.Plan.pa1(a, g["parts"][0], npart, nlevel, arith=M.ARITH_DF64)
+    for ex, plan in plans.items():
+        vv = _run(plan, g["x"], n, nlevel)
+        assert vv[:n].tobytes() == g["x"].tobytes()
+        errs = _rel_errors(vv, want, n, nlevel)
+        assert max(errs) <= TOL, (ex, errs)
+
+
+@pytest.mark.parametrize("ex", ["tiles", "pipe"])
+def test_config2_df64_within_fp64_tolerance(config2, ex, gpu):
+    a, part, x, want = config2
+    plan = (M.Plan.pa1(a, part, 2048, 8, arith=M.ARITH_DF64) if ex == "tiles"
+            else M.Plan.pipe(a, 8, arith=M.ARITH_DF64))
+    vv = _run(plan, x, a.n, 8)
+    errs = _rel_errors(vv, want, a.n, 8)
+    assert max(errs) <= TOL, errs
+
+
+def test_pipeline_wait_times_out_and_recovers(gpu):
+    """A dependency flag that is never set: the bounded waits give up, the
+    call reports ETIMEOUT, and the same plan then runs correctly."""
+    a = M.Csr.laplacian(64, 64, 4)
+    x = M.uniform(5, a.n)
+    plan = M.Plan.pipe(a, 4)
+    plan.debug_stall(100)
+    vv = np.zeros(5 * a.n)
+    vv[:a.n] = x
+    with pytest.raises(M.MpkError) as e:
+        plan.exec_host(vv)
+    assert e.value.code == M.ETIMEOUT
+    plan.debug_stall(0)
+    want = O.mpk(a.ptr, a.col, a.val, x, 4, O.MODE_FMA)
+    assert _run(plan, x, a.n, 4).tobytes() == want.tobytes()
