@@ -216,7 +216,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--exec", default="pipe", choices=["pipe", "tiles", "spmv", "tasks"])
-    ap.add_argument("--arith", default="fma", choices=["fma", "separate"])
+    ap.add_argument("--arith", default="fma", choices=["fma", "separate", "df64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -254,13 +254,13 @@ def main():
     import torch
     import mpk_gb300 as M
     torch.cuda.set_device(local)
-    arith = M.ARITH_FMA if args.arith == "fma" else M.ARITH_SEPARATE
+    arith = {"fma": M.ARITH_FMA, "separate": M.ARITH_SEPARATE, "df64": M.ARITH_DF64}[args.arith]
     mk = {"pipe": lambda: M.Plan.pipe(a, k, arith=arith),
           "tiles": lambda: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TILES, arith=arith),
           "tasks": lambda: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TASKS, arith=arith),
           "spmv": lambda: M.Plan.spmv(a, k, arith=arith)}
     plan = mk[args.exec]()
-    base = mk["spmv"]() if args.exec != "spmv" else plan
+    base = M.Plan.spmv(a, k, arith=M.ARITH_FMA) if args.exec != "spmv" else plan
     info = plan.info()
     stream = torch.cuda.Stream()
     d_vv = torch.zeros((k + 1) * n, dtype=torch.float64, device="cuda")

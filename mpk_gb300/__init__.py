@@ -276,7 +276,7 @@ class Plan:
                          nphase, _ptr(off), _ptr(idx), arith, a=a, nlevel=nlevel)
 
     @classmethod
-    def pipe(cls, a: Csr, nlevel, chunk=256, arith=ARITH_FMA):
+    def pipe(cls, a: Csr, nlevel, chunk=0, arith=ARITH_FMA):
         return cls._make(lib().mpkg_plan_pipe, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, chunk,
                          arith, a=a, nlevel=nlevel)
 

@@ -121,6 +121,7 @@ struct TileArgs {
   const long *slot_off;
   const int *shell;
   const int *slot_vert;
+  const int *slot_coef;  // per slot: first value offset (valued) or vertex (1/deg)
   const long *slice_off;
   const long *ell_off;
   const uint16_t *ell_col;
@@ -132,6 +133,39 @@ struct TileArgs {
   double *scratch;      // used when !SMEM
   int *err;
 };
+
+// One tile row in FP64: the slice entries are loaded (and their gathers
+// issued) before the first FMA for rows of up to 8 entries; the sum runs
+// over the entries in CSR order.
+template <int ARITH, bool VALUED>
+__device__ __forceinline__ double tile_row_fp64(const TileArgs &a, long sl, int lane, int co, const double *in) {
+  const int w = a.ell_width[sl];
+  const uint16_t *cp = a.ell_col + a.ell_off[sl] + lane;
+  double s = 0.0;
+  if (w <= 8) {
+    double xv[8], cv[8];
+    bool ok[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int c = t < w ? cp[t * 32] : 0xFFFF;
+      ok[t] = c != 0xFFFF;
+      xv[t] = ok[t] ? in[c] : 0.0;
+      cv[t] = ok[t] ? (VALUED ? a.coef[co + t] : 0.0) : 0.0;
+    }
+    const double cf = VALUED ? 0.0 : a.coef[co];
+#pragma unroll
+    for (int t = 0; t < 8; t++)
+      if (ok[t]) s = row_term<ARITH>(s, VALUED ? cv[t] : cf, xv[t]);
+  } else {
+    const double cf = VALUED ? 0.0 : a.coef[co];
+    for (int t = 0; t < w; t++) {
+      const int c = cp[t * 32];
+      if (c == 0xFFFF) break;
+      s = row_term<ARITH>(s, VALUED ? a.coef[co + t] : cf, in[c]);
+    }
+  }
+  return s;
+}
 
 template <int ARITH, bool VALUED, bool SMEM>
 __global__ void __launch_bounds__(512) tiles_kernel(TileArgs a) {
@@ -156,29 +190,9 @@ __global__ void __launch_bounds__(512) tiles_kernel(TileArgs a) {
     const int nrows = shell[a.nlevel - l];
     double *dst = a.vv + (long)l * a.n;
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
-      const long sl = sl0 + (r >> 5);
-      const int lane = r & 31;
-      const int w = a.ell_width[sl];
-      const uint16_t *cp = a.ell_col + a.ell_off[sl] + lane;
-      const int v = a.slot_vert[s0 + r];
-      double s = 0.0;
-      if (VALUED) {
-        const double *vp = a.coef + a.ptr[v];
-        for (int t = 0; t < w; t++) {
-          const int c = cp[t * 32];
-          if (c == 0xFFFF) break;
-          s = row_term<ARITH>(s, vp[t], in[c]);
-        }
-      } else {
-        const double cf = a.coef[v];
-        for (int t = 0; t < w; t++) {
-          const int c = cp[t * 32];
-          if (c == 0xFFFF) break;
-          s = row_term<ARITH>(s, cf, in[c]);
-        }
-      }
-      out[r] = s;
-      if (r < owned) dst[v] = s;
+      const double v = tile_row_fp64<ARITH, VALUED>(a, sl0 + (r >> 5), r & 31, a.slot_coef[s0 + r], in);
+      out[r] = v;
+      if (r < owned) dst[a.slot_vert[s0 + r]] = v;
     }
     __syncthreads();
   }
@@ -196,10 +210,10 @@ __global__ void __launch_bounds__(512) tiles_kernel(TileArgs a) {
 // limit sets the error word and the whole grid drains.
 // ------------------------------------------------------------------------
 struct PipeArgs {
-  int n, nlevel, chunk, nchunk;
+  int n, nlevel, chunk, nchunk, ngroups;
   uint32_t epoch;
-  uint32_t stall;     // test hook: waits for a level this far beyond the real one
-  const int *dep_lo, *dep_hi;
+  uint32_t stall;      // test hook: waits target counts this far beyond the real ones
+  const int *gdep_lo, *gdep_hi;  // per chunk: first/last counter group it reads
   const int *ptr, *col;
   const double *coef;  // FP64 values (nnz) or 1/deg (n)
   const float2 *coef2; // double-float values (nnz) or 1/deg (n)
@@ -207,49 +221,56 @@ struct PipeArgs {
   double *vv;
   float2 *ring;        // double-float level values, two slots of n
   unsigned int *ticket;
-  unsigned int *flags;
+  unsigned int *counts;  // (nlevel+1) x ngroups completion counters
   int *err;
   int max_chunk_nnz;
 };
+
+constexpr int kPipeThreads = 256;
+constexpr int kPipeRows = 2;                        // rows per thread per pass
+constexpr int kPipePass = kPipeThreads * kPipeRows; // rows per pass
+constexpr int kPipeChunk = 2 * kPipePass;           // rows per chunk (two passes per level)
+constexpr int kPipeGroup = 1;                       // chunks per completion counter
 
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
   unsigned int v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+
+__device__ __forceinline__ unsigned int group_size(const PipeArgs &a, int g) {
+  return (unsigned)min(kPipeGroup, a.nchunk - g * kPipeGroup);
 }
 
-// Every thread of the CTA calls this.  Threads poll one dependency flag
-// each with acquire loads until it reaches `want`; a poll count above
-// kSpinLimit, or an error raised elsewhere, aborts the CTA.  Returns false
-// on abort.  After the barrier every thread's plain loads observe the data
-// the producers released (acquire + CTA barrier).
-__device__ __forceinline__ bool pipe_wait(const PipeArgs &a, int c, int dlo, int dhi, unsigned want,
-                                          int *s_abort) {
-  for (int d = dlo + (int)threadIdx.x; d <= dhi; d += blockDim.x) {
-    if (d == c) continue;
+// Every thread of the CTA calls this.  Threads poll one completion counter
+// each (acquire loads) until its group has finished `level` in this call;
+// a poll count above kSpinLimit, or an error raised elsewhere, aborts the
+// CTA.  Returns false on abort.  After the barrier, every thread's plain
+// loads observe the data the producers released (acquire + CTA barrier).
+__device__ __forceinline__ bool pipe_wait(const PipeArgs &a, int glo, int ghi, int level, int *s_abort) {
+  for (int g = glo + (int)threadIdx.x; g <= ghi; g += blockDim.x) {
+    const unsigned int want = a.epoch * group_size(a, g) + a.stall * 1024u;
+    const unsigned int *cp = a.counts + (long)level * a.ngroups + g;
     long spins = 0;
-    while (ld_acquire(a.flags + d) < want) {
+    while (ld_acquire(cp) < want) {
       if (++spins > kSpinLimit || *((volatile int *)a.err)) {
         atomicCAS(a.err, 0, kErrTimeout);
         *s_abort = 1;
         break;
       }
-      __nanosleep(spins < 64 ? 32 : 256);
+      __nanosleep(spins < 16 ? 64 : 512);
     }
   }
   __syncthreads();
   return *s_abort == 0;
 }
 
-__device__ __forceinline__ void pipe_publish(const PipeArgs &a, int c, unsigned tag) {
+// Release of one chunk's level: every writer fences, the CTA synchronises,
+// one thread bumps the group counter.
+__device__ __forceinline__ void pipe_publish(const PipeArgs &a, int c, int level) {
+  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    st_release(a.flags + c, tag);
-  }
+  if (threadIdx.x == 0) atomicAdd(a.counts + (long)level * a.ngroups + c / kPipeGroup, 1u);
 }
 
 // Takes the next chunk and stages its rows (row pointers, columns and, for
@@ -268,7 +289,7 @@ __device__ __forceinline__ int pipe_take(const PipeArgs &a, const T *coef, int *
   const int r0 = c * a.chunk;
   const int nr = min(a.chunk, a.n - r0);
   const int j00 = a.ptr[r0];
-  for (int r = threadIdx.x; r <= nr; r += blockDim.x) rptr[r] = a.ptr[r0 + r] - j00;
+  for (int r = threadIdx.x; r <= a.chunk; r += blockDim.x) rptr[r] = a.ptr[r0 + min(r, nr)] - j00;
   __syncthreads();
   const int cnnz = rptr[nr];
   if (cnnz > a.max_chunk_nnz) {  // plan invariant
@@ -289,33 +310,82 @@ __device__ __forceinline__ T *pipe_vals(unsigned char *smem, const PipeArgs &a) 
       smem + (((size_t)(a.chunk + 1 + a.max_chunk_nnz) * sizeof(int) + 15) & ~(size_t)15));
 }
 
+// Row sums of the thread's kPipeRows rows in FP64.  Rows of up to 8
+// entries take a path that issues every gather before the first FMA; the
+// sum itself always runs over the entries in CSR order.
 template <int ARITH, bool VALUED>
-__global__ void __launch_bounds__(256) pipe_kernel(PipeArgs a) {
+__device__ __forceinline__ void pipe_rows_fp64(const int *rptr, const int *cols, const double *vals,
+                                               const double *cf, const double *src, double *out, int base) {
+  int q0[kPipeRows], q1[kPipeRows];
+  bool small = true;
+#pragma unroll
+  for (int j = 0; j < kPipeRows; j++) {
+    const int r = base + threadIdx.x + j * kPipeThreads;
+    q0[j] = rptr[r];
+    q1[j] = rptr[r + 1];
+    small &= (q1[j] - q0[j] <= 8);
+  }
+  if (small) {
+    double xv[kPipeRows][8], cv[kPipeRows][8];
+#pragma unroll
+    for (int j = 0; j < kPipeRows; j++)
+#pragma unroll
+      for (int t = 0; t < 8; t++)
+        if (q0[j] + t < q1[j]) {
+          xv[j][t] = src[cols[q0[j] + t]];
+          cv[j][t] = VALUED ? vals[q0[j] + t] : cf[j];
+        }
+#pragma unroll
+    for (int j = 0; j < kPipeRows; j++) {
+      double s = 0.0;
+#pragma unroll
+      for (int t = 0; t < 8; t++)
+        if (q0[j] + t < q1[j]) s = row_term<ARITH>(s, cv[j][t], xv[j][t]);
+      out[j] = s;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kPipeRows; j++) {
+      double s = 0.0;
+      for (int q = q0[j]; q < q1[j]; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf[j], src[cols[q]]);
+      out[j] = s;
+    }
+  }
+}
+
+template <int ARITH, bool VALUED>
+__global__ void __launch_bounds__(kPipeThreads, 2) pipe_kernel(PipeArgs a) {
   extern __shared__ __align__(16) unsigned char pipe_smem[];
   int *rptr = reinterpret_cast<int *>(pipe_smem);
   int *cols = rptr + a.chunk + 1;
   double *vals = pipe_vals<double>(pipe_smem, a);
   __shared__ unsigned int s_chunk;
   __shared__ int s_abort;
-  const unsigned int base_tag = a.epoch * 32u;
   for (;;) {
     const int c = pipe_take<double, VALUED>(a, a.coef, rptr, cols, vals, &s_chunk, &s_abort);
     if (c < 0) return;
     const int r0 = c * a.chunk;
     const int nr = min(a.chunk, a.n - r0);
-    const int myrow = r0 + threadIdx.x;
-    const double cf = (!VALUED && (int)threadIdx.x < nr) ? a.coef[myrow] : 0.0;
-    const int dlo = a.dep_lo[c], dhi = a.dep_hi[c];
+    const int glo = a.gdep_lo[c], ghi = a.gdep_hi[c];
     for (int l = 1; l <= a.nlevel; l++) {
-      if (l > 1 && !pipe_wait(a, c, dlo, dhi, base_tag + (unsigned)(l - 1) + a.stall, &s_abort)) return;
-      if ((int)threadIdx.x < nr) {
-        const double *src = a.vv + (long)(l - 1) * a.n;
-        const int q0 = rptr[threadIdx.x], q1 = rptr[threadIdx.x + 1];
-        double s = 0.0;
-        for (int q = q0; q < q1; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf, src[cols[q]]);
-        a.vv[(long)l * a.n + myrow] = s;
+      if (l > 1 && !pipe_wait(a, glo, ghi, l - 1, &s_abort)) return;
+      const double *src = l == 1 ? a.x : a.vv + (long)(l - 1) * a.n;
+      double *dst = a.vv + (long)l * a.n + r0;
+      for (int base = 0; base < nr; base += kPipePass) {
+        double cf[kPipeRows], out[kPipeRows];
+#pragma unroll
+        for (int j = 0; j < kPipeRows; j++) {
+          const int r = base + threadIdx.x + j * kPipeThreads;
+          cf[j] = (!VALUED && r < nr) ? a.coef[r0 + r] : 0.0;
+        }
+        pipe_rows_fp64<ARITH, VALUED>(rptr, cols, vals, cf, src, out, base);
+#pragma unroll
+        for (int j = 0; j < kPipeRows; j++) {
+          const int r = base + threadIdx.x + j * kPipeThreads;
+          if (r < nr) dst[r] = out[j];
+        }
       }
-      pipe_publish(a, c, base_tag + (unsigned)l);
+      pipe_publish(a, c, l);
     }
   }
 }
@@ -387,43 +457,121 @@ __device__ __forceinline__ float2 df_norm(float sh, float sl) {
 // its own.  A slot is overwritten (level l+2) only after every chunk within
 // reach has finished level l+1, i.e. no longer reads level l.
 template <bool VALUED>
-__global__ void __launch_bounds__(256) pipe_df_kernel(PipeArgs a) {
+__device__ __forceinline__ void pipe_rows_df(const int *rptr, const int *cols, const float2 *vals,
+                                             const float2 *cf, const float2 *src, float2 *out, int base) {
+  int q0[kPipeRows], q1[kPipeRows];
+  bool small = true;
+#pragma unroll
+  for (int j = 0; j < kPipeRows; j++) {
+    const int r = base + threadIdx.x + j * kPipeThreads;
+    q0[j] = rptr[r];
+    q1[j] = rptr[r + 1];
+    small &= (q1[j] - q0[j] <= 8);
+  }
+  if (small) {
+    float2 xv[kPipeRows][8], cv[kPipeRows][8];
+#pragma unroll
+    for (int j = 0; j < kPipeRows; j++)
+#pragma unroll
+      for (int t = 0; t < 8; t++)
+        if (q0[j] + t < q1[j]) {
+          xv[j][t] = src[cols[q0[j] + t]];
+          cv[j][t] = VALUED ? vals[q0[j] + t] : cf[j];
+        }
+#pragma unroll
+    for (int j = 0; j < kPipeRows; j++) {
+      float sh = 0.f, sl = 0.f;
+#pragma unroll
+      for (int t = 0; t < 8; t++)
+        if (q0[j] + t < q1[j]) df_mac(cv[j][t], xv[j][t], sh, sl);
+      out[j] = df_norm(sh, sl);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kPipeRows; j++) {
+      float sh = 0.f, sl = 0.f;
+      for (int q = q0[j]; q < q1[j]; q++) df_mac(VALUED ? vals[q] : cf[j], src[cols[q]], sh, sl);
+      out[j] = df_norm(sh, sl);
+    }
+  }
+}
+
+template <bool VALUED>
+__global__ void __launch_bounds__(kPipeThreads, 2) pipe_df_kernel(PipeArgs a) {
   extern __shared__ __align__(16) unsigned char pipe_smem[];
   int *rptr = reinterpret_cast<int *>(pipe_smem);
   int *cols = rptr + a.chunk + 1;
   float2 *vals = pipe_vals<float2>(pipe_smem, a);
   __shared__ unsigned int s_chunk;
   __shared__ int s_abort;
-  const unsigned int base_tag = a.epoch * 32u;
   for (;;) {
     const int c = pipe_take<float2, VALUED>(a, a.coef2, rptr, cols, vals, &s_chunk, &s_abort);
     if (c < 0) return;
     const int r0 = c * a.chunk;
     const int nr = min(a.chunk, a.n - r0);
-    const int myrow = r0 + threadIdx.x;
-    const bool active = (int)threadIdx.x < nr;
-    const float2 cf = (!VALUED && active) ? a.coef2[myrow] : make_float2(0.f, 0.f);
-    const int dlo = a.dep_lo[c], dhi = a.dep_hi[c];
-    if (active) a.ring[myrow] = df_split(a.x[myrow]);
-    pipe_publish(a, c, base_tag);
+    for (int r = threadIdx.x; r < nr; r += kPipeThreads) a.ring[r0 + r] = df_split(a.x[r0 + r]);
+    pipe_publish(a, c, 0);
+    const int glo = a.gdep_lo[c], ghi = a.gdep_hi[c];
     for (int l = 1; l <= a.nlevel; l++) {
-      if (!pipe_wait(a, c, dlo, dhi, base_tag + (unsigned)(l - 1) + a.stall, &s_abort)) return;
-      if (active) {
-        const float2 *src = a.ring + (long)((l - 1) & 1) * a.n;
-        const int q0 = rptr[threadIdx.x], q1 = rptr[threadIdx.x + 1];
-        float sh = 0.f, sl = 0.f;
-        for (int q = q0; q < q1; q++) df_mac(VALUED ? vals[q] : cf, src[cols[q]], sh, sl);
-        const float2 v = df_norm(sh, sl);
-        a.ring[(long)(l & 1) * a.n + myrow] = v;
-        a.vv[(long)l * a.n + myrow] = df_to_double(v);
+      if (!pipe_wait(a, glo, ghi, l - 1, &s_abort)) return;
+      const float2 *src = a.ring + (long)((l - 1) & 1) * a.n;
+      float2 *ring_out = a.ring + (long)(l & 1) * a.n + r0;
+      double *dst = a.vv + (long)l * a.n + r0;
+      for (int base = 0; base < nr; base += kPipePass) {
+        float2 cf[kPipeRows], out[kPipeRows];
+#pragma unroll
+        for (int j = 0; j < kPipeRows; j++) {
+          const int r = base + threadIdx.x + j * kPipeThreads;
+          cf[j] = (!VALUED && r < nr) ? a.coef2[r0 + r] : make_float2(0.f, 0.f);
+        }
+        pipe_rows_df<VALUED>(rptr, cols, vals, cf, src, out, base);
+#pragma unroll
+        for (int j = 0; j < kPipeRows; j++) {
+          const int r = base + threadIdx.x + j * kPipeThreads;
+          if (r < nr) {
+            ring_out[r] = out[j];
+            dst[r] = df_to_double(out[j]);
+          }
+        }
       }
-      pipe_publish(a, c, base_tag + (unsigned)l);
+      pipe_publish(a, c, l);
     }
   }
 }
 
 // PA1 tiles in double-float: same schedule as tiles_kernel, level buffers
 // of float2 in shared memory.
+template <bool VALUED>
+__device__ __forceinline__ float2 tile_row_df(const TileArgs &a, const float2 *coef2, long sl, int lane, int co,
+                                              const float2 *in) {
+  const int w = a.ell_width[sl];
+  const uint16_t *cp = a.ell_col + a.ell_off[sl] + lane;
+  float sh = 0.f, slo = 0.f;
+  if (w <= 8) {
+    float2 xv[8], cv[8];
+    bool ok[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int c = t < w ? cp[t * 32] : 0xFFFF;
+      ok[t] = c != 0xFFFF;
+      xv[t] = ok[t] ? in[c] : make_float2(0.f, 0.f);
+      cv[t] = (ok[t] && VALUED) ? coef2[co + t] : make_float2(0.f, 0.f);
+    }
+    const float2 cf = VALUED ? make_float2(0.f, 0.f) : coef2[co];
+#pragma unroll
+    for (int t = 0; t < 8; t++)
+      if (ok[t]) df_mac(VALUED ? cv[t] : cf, xv[t], sh, slo);
+  } else {
+    const float2 cf = VALUED ? make_float2(0.f, 0.f) : coef2[co];
+    for (int t = 0; t < w; t++) {
+      const int c = cp[t * 32];
+      if (c == 0xFFFF) break;
+      df_mac(VALUED ? coef2[co + t] : cf, in[c], sh, slo);
+    }
+  }
+  return df_norm(sh, slo);
+}
+
 template <bool VALUED, bool SMEM>
 __global__ void __launch_bounds__(512) tiles_df_kernel(TileArgs a, const float2 *coef2) {
   extern __shared__ float2 smem_f2[];
@@ -447,30 +595,9 @@ __global__ void __launch_bounds__(512) tiles_df_kernel(TileArgs a, const float2 
     const int nrows = shell[a.nlevel - l];
     double *dst = a.vv + (long)l * a.n;
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
-      const long sl = sl0 + (r >> 5);
-      const int lane = r & 31;
-      const int w = a.ell_width[sl];
-      const uint16_t *cp = a.ell_col + a.ell_off[sl] + lane;
-      const int v = a.slot_vert[s0 + r];
-      float sh = 0.f, slo = 0.f;
-      if (VALUED) {
-        const float2 *vp = coef2 + a.ptr[v];
-        for (int t = 0; t < w; t++) {
-          const int c = cp[t * 32];
-          if (c == 0xFFFF) break;
-          df_mac(vp[t], in[c], sh, slo);
-        }
-      } else {
-        const float2 cf = coef2[v];
-        for (int t = 0; t < w; t++) {
-          const int c = cp[t * 32];
-          if (c == 0xFFFF) break;
-          df_mac(cf, in[c], sh, slo);
-        }
-      }
-      const float2 res = df_norm(sh, slo);
+      const float2 res = tile_row_df<VALUED>(a, coef2, sl0 + (r >> 5), r & 31, a.slot_coef[s0 + r], in);
       out[r] = res;
-      if (r < owned) dst[v] = df_to_double(res);
+      if (r < owned) dst[a.slot_vert[s0 + r]] = df_to_double(res);
     }
     __syncthreads();
   }
@@ -641,7 +768,7 @@ int build_task_device(mpkg_plan *p, int npart, int nphase, const long *off, cons
   return kOk;
 }
 
-int build_tile_device(mpkg_plan *p, const TilePlan &tp) {
+int build_tile_device(mpkg_plan *p, const TilePlan &tp, const int *ptr_host_) {
   int rc;
   TileArgs &a = p->tiles;
   a.n = p->n;
@@ -657,6 +784,13 @@ int build_tile_device(mpkg_plan *p, const TilePlan &tp) {
   if ((rc = dev_copy(p, &slot_off, tp.slot_off.data(), tp.slot_off.size()))) return rc;
   if ((rc = dev_copy(p, &shell, tp.shell.data(), tp.shell.size()))) return rc;
   if ((rc = dev_copy(p, &slot_vert, tp.slot_vert.data(), tp.slot_vert.size()))) return rc;
+  int *slot_coef;
+  {
+    std::vector<int> sc(tp.slot_vert.size());
+    for (size_t q = 0; q < sc.size(); q++) sc[q] = p->valued ? ptr_host_[tp.slot_vert[q]] : tp.slot_vert[q];
+    if ((rc = dev_copy(p, &slot_coef, sc.data(), sc.size()))) return rc;
+  }
+  a.slot_coef = slot_coef;
   if ((rc = dev_copy(p, &slice_off, tp.slice_off.data(), tp.slice_off.size()))) return rc;
   if ((rc = dev_copy(p, &ell_off, tp.ell_off.data(), tp.ell_off.size()))) return rc;
   std::vector<uint16_t> ec = tp.ell_col;
@@ -696,7 +830,8 @@ int pipe_setup_df(mpkg_plan *p, int *grid) {
   CUDA_TRY(cudaFuncSetAttribute(pipe_df_kernel<VALUED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)p->pipe_smem_bytes));
   int per_sm = 0, nsm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_df_kernel<VALUED>, 256, p->pipe_smem_bytes));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_df_kernel<VALUED>, kPipeThreads,
+                                                         p->pipe_smem_bytes));
   CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
   *grid = per_sm * nsm;
   return kOk;
@@ -714,7 +849,7 @@ int pipe_setup_t(mpkg_plan *p, int *grid) {
   CUDA_TRY(cudaFuncSetAttribute(pipe_kernel<ARITH, VALUED>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pipe_smem_bytes));
   int per_sm = 0, nsm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_kernel<ARITH, VALUED>, 256,
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_kernel<ARITH, VALUED>, kPipeThreads,
                                                          p->pipe_smem_bytes));
   CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
   *grid = per_sm * nsm;
@@ -776,7 +911,7 @@ void launch_pipe_df(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) 
   a.x = x;
   a.vv = vv;
   a.epoch = p->epoch;
-  pipe_df_kernel<VALUED><<<p->pipe_grid, 256, p->pipe_smem_bytes, st>>>(a);
+  pipe_df_kernel<VALUED><<<p->pipe_grid, kPipeThreads, p->pipe_smem_bytes, st>>>(a);
 }
 
 template <int ARITH, bool VALUED>
@@ -785,7 +920,7 @@ void launch_pipe_t(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) {
   a.x = x;
   a.vv = vv;
   a.epoch = p->epoch;
-  pipe_kernel<ARITH, VALUED><<<p->pipe_grid, 256, p->pipe_smem_bytes, st>>>(a);
+  pipe_kernel<ARITH, VALUED><<<p->pipe_grid, kPipeThreads, p->pipe_smem_bytes, st>>>(a);
 }
 
 #define DISPATCH2(fn, ...)                                                   \
@@ -817,8 +952,9 @@ int plan_launch(mpkg_plan *p, double *d_vv, cudaStream_t st) {
       break;
     case MPKG_EXEC_PIPE: {
       p->epoch++;
-      if (p->epoch >= (1u << 26)) {  // tags wrap: clear the flags
-        CUDA_TRY(cudaMemsetAsync(p->pipe.flags, 0, sizeof(unsigned int) * p->pipe.nchunk, st));
+      if (p->epoch >= (1u << 27)) {  // counters would wrap: start over
+        CUDA_TRY(cudaMemsetAsync(p->pipe.counts, 0,
+                                 sizeof(unsigned int) * (size_t)(p->nlevel + 1) * p->pipe.ngroups, st));
         p->epoch = 1;
       }
       CUDA_TRY(cudaMemsetAsync(p->pipe.ticket, 0, sizeof(unsigned int), st));
@@ -918,7 +1054,7 @@ int mpkg_plan_pa1(int n, const int *ptr, const int *col, const double *val, cons
   if (!rc) {
     p->exec = MPKG_EXEC_TILES;
     p->npart = npart;
-    rc = build_tile_device(p, tp);
+    rc = build_tile_device(p, tp, ptr);
   }
   if (!rc && p->tiles_smem && p->arith == MPKG_ARITH_DF64) {
     rc = p->valued ? set_tiles_df_attr<true, true>(p->tiles_smem_bytes)
@@ -942,8 +1078,8 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
   clear_error();
   if (!out) return fail(kEInval, "out is null");
   *out = nullptr;
-  if (chunk <= 0) chunk = 256;
-  if (chunk != 256) return fail(kEInval, "pipe executor uses 256-row chunks");
+  if (chunk <= 0) chunk = kPipeChunk;
+  if (chunk != kPipeChunk) return fail(kEInval, "the pipeline executor uses 1024-row chunks");
   int rc = check_csr(n, ptr, col);
   if (rc) return rc;
   Csr g;
@@ -961,6 +1097,7 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
     p->rows_computed = (long)n * nlevel;
     PipeArgs &a = p->pipe;
     a.n = n; a.nlevel = nlevel; a.chunk = chunk; a.nchunk = pp.nchunk;
+    a.ngroups = (pp.nchunk + kPipeGroup - 1) / kPipeGroup;
     int maxnnz = 0;
     for (int c = 0; c < pp.nchunk; c++) {
       int r1 = std::min(n, (c + 1) * chunk);
@@ -969,12 +1106,22 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
     a.max_chunk_nnz = std::max(maxnnz, 1);
     p->pipe_smem_bytes = (((size_t)(chunk + 1 + a.max_chunk_nnz) * sizeof(int) + 15) & ~(size_t)15) +
                          (p->valued ? (size_t)a.max_chunk_nnz * sizeof(double) : 0);
+    // dependencies in counter groups, and the reach they imply in chunks
+    std::vector<int> glo(pp.nchunk), ghi(pp.nchunk);
+    long reach = 0;
+    for (int c = 0; c < pp.nchunk; c++) {
+      glo[c] = pp.dep_lo[c] / kPipeGroup;
+      ghi[c] = pp.dep_hi[c] / kPipeGroup;
+      long hi_chunk = std::min<long>((long)ghi[c] * kPipeGroup + kPipeGroup - 1, pp.nchunk - 1);
+      reach = std::max(reach, std::max(hi_chunk - c, (long)c - (long)glo[c] * kPipeGroup));
+    }
     int *dlo, *dhi;
-    unsigned int *ticket, *flags;
-    if (!rc) rc = dev_copy(p, &dlo, pp.dep_lo.data(), pp.dep_lo.size());
-    if (!rc) rc = dev_copy(p, &dhi, pp.dep_hi.data(), pp.dep_hi.size());
+    unsigned int *ticket, *counts;
+    const size_t ncount = (size_t)(nlevel + 1) * a.ngroups;
+    if (!rc) rc = dev_copy(p, &dlo, glo.data(), glo.size());
+    if (!rc) rc = dev_copy(p, &dhi, ghi.data(), ghi.size());
     if (!rc) rc = dev_alloc(p, &ticket, 1);
-    if (!rc) rc = dev_alloc(p, &flags, (size_t)pp.nchunk);
+    if (!rc) rc = dev_alloc(p, &counts, ncount);
     if (!rc && p->arith == MPKG_ARITH_DF64) {
       float2 *ring;
       rc = dev_alloc(p, &ring, 2 * (size_t)n);
@@ -982,8 +1129,8 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
       a.coef2 = p->d_coef2;
     }
     if (!rc) {
-      cudaMemset(flags, 0, sizeof(unsigned int) * pp.nchunk);
-      a.dep_lo = dlo; a.dep_hi = dhi; a.ticket = ticket; a.flags = flags;
+      cudaMemset(counts, 0, sizeof(unsigned int) * ncount);
+      a.gdep_lo = dlo; a.gdep_hi = dhi; a.ticket = ticket; a.counts = counts;
       a.ptr = p->d_ptr; a.col = p->d_col; a.coef = p->d_coef; a.err = p->d_err;
       int maxsm = 0;
       cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
@@ -998,15 +1145,14 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
       else
         rc = p->valued ? pipe_setup_t<MPKG_ARITH_FMA, true>(p, &grid) : pipe_setup_t<MPKG_ARITH_FMA, false>(p, &grid);
       if (!rc) {
-        p->pipe_reach = pp.reach;
+        p->pipe_reach = (int)reach;
         p->pipe_grid = std::min(grid, pp.nchunk);
-        // progress needs every chunk within (k-1)*reach of the oldest
-        // unfinished chunk to be running
-        long need = (long)(p->arith == MPKG_ARITH_DF64 ? nlevel : nlevel - 1) * pp.reach + 1;
+        // The oldest unfinished chunk completes once every chunk within
+        // (waiting levels) * reach of it is running (see pipe_kernel).
+        long need = (long)(p->arith == MPKG_ARITH_DF64 ? nlevel : nlevel - 1) * reach + 1;
         if (p->pipe_grid < pp.nchunk && p->pipe_grid < need)
-          rc = fail(kERange, "matrix bandwidth too large for the pipeline (reach " +
-                                 std::to_string(pp.reach) + " chunks, " + std::to_string(grid) +
-                                 " resident CTAs)");
+          rc = fail(kERange, "matrix bandwidth too large for the pipeline (reach " + std::to_string(reach) +
+                                 " chunks, " + std::to_string(grid) + " resident CTAs)");
       }
     }
   }
@@ -1074,6 +1220,10 @@ int mpkg_sync(mpkg_plan *p, void *stream) {
   CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
     cudaMemset(p->d_err, 0, sizeof(int));
+    if (p->exec == MPKG_EXEC_PIPE) {  // counters are inconsistent after an abort
+      cudaMemset(p->pipe.counts, 0, sizeof(unsigned int) * (size_t)(p->nlevel + 1) * p->pipe.ngroups);
+      p->epoch = 0;
+    }
     if (err == kErrTimeout) return fail(kETimeout, "a device-side wait exceeded its spin limit");
     return fail(kERange, "device-side bounds check failed");
   }
