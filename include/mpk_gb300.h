@@ -126,6 +126,26 @@ void mpkg_plan_destroy(mpkg_plan *p);
  * MPKG_ETIMEOUT with the context still usable; 0 restores normal waits. */
 int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels);
 
+/* Allocation-free pipeline (no counterpart in the reference).  For callers
+ * that must not allocate device memory themselves, e.g. a solver plug-in
+ * running inside an application whose memory pool owns the whole device, or
+ * a time-stepping loop that cannot take cudaMalloc's implicit device
+ * synchronisation.  Runs the FP64 (FMA) pipeline on caller-owned device
+ * arrays: CSR d_ptr/d_col/d_val (values required) and d_vv with x in
+ * d_vv[0..n); writes levels 1..nlevel.  Its bookkeeping lives in a
+ * file-scope device array of about 311 KB that every GPU loading this
+ * library holds until the process exits; limits: n <= 4096*1024 rows,
+ * nlevel <= 16 (larger sizes return MPKG_ERANGE / MPKG_EINVAL).  It calls no
+ * allocating routine.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the one array and
+ * it keeps the last call's contents (each call clears what must start at
+ * zero), so calls that overlap on the GPU race.  The call waits for its
+ * kernels (stream may be NULL) and returns MPKG_ETIMEOUT if a bounded wait
+ * gave up. */
+int mpkg_pipe_noalloc(int n, const int *d_ptr, const int *d_col, const double *d_val,
+                      int nlevel, double *d_vv, void *stream);
+
 /* Stand-alone k-SpMV on device arrays (no plan). */
 int mpkg_spmv_chain_device(int n, const int *d_ptr, const int *d_col, const double *d_val,
                            int nlevel, double *d_vv, int arith, void *stream);

@@ -1257,3 +1257,142 @@ int mpkg_spmv_chain_device(int n, const int *d_ptr, const int *d_col, const doub
 }
 
 }  // extern "C"
+
+// ==========================================================================
+// Allocation-free pipeline entry point (mpkg_pipe_noalloc)
+//
+// For callers that must not allocate device memory themselves: a solver
+// plug-in running inside an application whose memory pool owns the whole
+// device, or a time-stepping loop that cannot afford cudaMalloc's implicit
+// device synchronisation.  The caller passes the matrix and vv in device
+// memory; the pipeline's bookkeeping (dependency ranges, completion
+// counters, ticket, error word) lives in the file-scope array below, which
+// every GPU that loads this library holds until the process exits.
+// ==========================================================================
+namespace {
+
+constexpr int kNoAllocMaxChunks = 4096;  // n <= 4096 * 1024 rows
+constexpr int kNoAllocMaxLevels = 16;
+// word layout: [0] ticket, [1] error, [2] max chunk nnz, [3] reach,
+// [4, 4+C) first dependency chunk, [4+C, 4+2C) last dependency chunk,
+// then (kNoAllocMaxLevels+1) * C completion counters.
+constexpr int kNoAllocHeader = 4;
+constexpr long kNoAllocWords =
+    kNoAllocHeader + 2L * kNoAllocMaxChunks + (long)(kNoAllocMaxLevels + 1) * kNoAllocMaxChunks;
+
+static __device__ __align__(256) unsigned int g_noalloc_scratch[kNoAllocWords];
+
+std::mutex g_noalloc_mu;
+unsigned int *g_noalloc_addr[256];  // device address of the array, per device
+
+// Looks up (once per device, with that device current) the device address
+// of g_noalloc_scratch.
+int noalloc_scratch(int dev, unsigned int **out) {
+  if (dev < 0 || dev >= 256) return fail(kEInval, "device id out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *addr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess) return fail(kECuda, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_addr[dev] = static_cast<unsigned int *>(addr);
+  }
+  *out = g_noalloc_addr[dev];
+  return kOk;
+}
+
+// One CTA per chunk: first and last chunk its rows' columns fall in, its
+// entry count, and the largest chunk distance (atomics into the header).
+__global__ void noalloc_deps_kernel(int n, int chunk, const int *__restrict__ ptr,
+                                    const int *__restrict__ col, unsigned int *scr) {
+  __shared__ int s_lo, s_hi;
+  const int c = blockIdx.x;
+  const int r0 = c * chunk, r1 = min(n, r0 + chunk);
+  if (threadIdx.x == 0) { s_lo = c; s_hi = c; }
+  __syncthreads();
+  int lo = c, hi = c;
+  for (int j = ptr[r0] + threadIdx.x; j < ptr[r1]; j += blockDim.x) {
+    const int cc = col[j] / chunk;
+    lo = min(lo, cc);
+    hi = max(hi, cc);
+  }
+  atomicMin(&s_lo, lo);
+  atomicMax(&s_hi, hi);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    scr[kNoAllocHeader + c] = (unsigned)s_lo;
+    scr[kNoAllocHeader + kNoAllocMaxChunks + c] = (unsigned)s_hi;
+    atomicMax(scr + 2, (unsigned)(ptr[r1] - ptr[r0]));
+    atomicMax(scr + 3, (unsigned)max(c - s_lo, s_hi - c));
+  }
+}
+
+}  // namespace
+
+extern "C" int mpkg_pipe_noalloc(int n, const int *d_ptr, const int *d_col, const double *d_val,
+                                 int nlevel, double *d_vv, void *stream) {
+  clear_error();
+  if (n <= 0 || !d_ptr || !d_col || !d_val || !d_vv) return fail(kEInval, "null argument or n <= 0");
+  if (nlevel < 1 || nlevel > kNoAllocMaxLevels)
+    return fail(kEInval, "mpkg_pipe_noalloc: nlevel must be in [1, 16]");
+  const int chunk = kPipeChunk;
+  const long nchunk = ((long)n + chunk - 1) / chunk;
+  if (nchunk > kNoAllocMaxChunks)
+    return fail(kERange, "mpkg_pipe_noalloc: n exceeds the fixed scratch limit of 4096*1024 rows");
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  unsigned int *scr = nullptr;
+  int rc = noalloc_scratch(dev, &scr);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // the array keeps the previous call's contents: clear header and counters
+  CUDA_TRY(cudaMemsetAsync(scr, 0, sizeof(unsigned int) * kNoAllocHeader, st));
+  unsigned int *counts = scr + kNoAllocHeader + 2 * kNoAllocMaxChunks;
+  CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(unsigned int) * (size_t)(nlevel + 1) * nchunk, st));
+  noalloc_deps_kernel<<<(unsigned)nchunk, 256, 0, st>>>(n, chunk, d_ptr, d_col, scr);
+  CUDA_TRY(cudaGetLastError());
+  unsigned int info[2] = {0, 0};
+  CUDA_TRY(cudaMemcpyAsync(info, scr + 2, sizeof info, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  const int max_nnz = std::max<int>((int)info[0], 1);
+  const long reach = info[1];
+  const size_t smem = (((size_t)(chunk + 1 + max_nnz) * sizeof(int) + 15) & ~(size_t)15) +
+                      (size_t)max_nnz * sizeof(double);
+  int maxsm = 0, per_sm = 0, nsm = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (smem > (size_t)maxsm) return fail(kERange, "mpkg_pipe_noalloc: chunk rows too dense for shared memory");
+  CUDA_TRY(cudaFuncSetAttribute(pipe_kernel<MPKG_ARITH_FMA, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_kernel<MPKG_ARITH_FMA, true>,
+                                                         kPipeThreads, smem));
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const long grid = std::min<long>((long)per_sm * nsm, nchunk);
+  if (grid < nchunk && grid < (long)(nlevel - 1) * reach + 1)
+    return fail(kERange, "mpkg_pipe_noalloc: matrix bandwidth too large for the pipeline");
+  PipeArgs a{};
+  a.n = n;
+  a.nlevel = nlevel;
+  a.chunk = chunk;
+  a.nchunk = (int)nchunk;
+  a.ngroups = (int)nchunk;
+  a.epoch = 1;
+  a.stall = 0;
+  a.gdep_lo = reinterpret_cast<const int *>(scr + kNoAllocHeader);
+  a.gdep_hi = reinterpret_cast<const int *>(scr + kNoAllocHeader + kNoAllocMaxChunks);
+  a.ptr = d_ptr;
+  a.col = d_col;
+  a.coef = d_val;
+  a.x = d_vv;
+  a.vv = d_vv;
+  a.ticket = scr;
+  a.counts = counts;
+  a.err = reinterpret_cast<int *>(scr + 1);
+  a.max_chunk_nnz = max_nnz;
+  pipe_kernel<MPKG_ARITH_FMA, true><<<(unsigned)grid, kPipeThreads, smem, st>>>(a);
+  CUDA_TRY(cudaGetLastError());
+  int err = 0;
+  CUDA_TRY(cudaMemcpyAsync(&err, scr + 1, sizeof err, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (err == kErrTimeout) return fail(kETimeout, "mpkg_pipe_noalloc: a device-side wait exceeded its spin limit");
+  if (err) return fail(kERange, "mpkg_pipe_noalloc: device-side bounds check failed");
+  return kOk;
+}
