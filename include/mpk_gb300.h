@@ -133,7 +133,7 @@ int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels);
  * synchronisation.  Runs the FP64 (FMA) pipeline on caller-owned device
  * arrays: CSR d_ptr/d_col/d_val (values required) and d_vv with x in
  * d_vv[0..n); writes levels 1..nlevel.  Its bookkeeping lives in a
- * file-scope device array of about 311 KB that every GPU loading this
+ * file-scope device array of about 1.2 MB that every GPU loading this
  * library holds until the process exits; limits: n <= 4096*1024 rows,
  * nlevel <= 16 (larger sizes return MPKG_ERANGE / MPKG_EINVAL).  It calls no
  * allocating routine.  The first call on a device looks up the array's

@@ -224,13 +224,12 @@ struct PipeArgs {
   unsigned int *counts;  // (nlevel+1) x ngroups completion counters
   int *err;
   int max_chunk_nnz;
+  bool bulk_ok;        // col/coef bases are 16-byte aligned: stage with bulk copies
 };
 
 constexpr int kPipeThreads = 256;
-constexpr int kPipeRows = 2;                        // rows per thread per pass
-constexpr int kPipePass = kPipeThreads * kPipeRows; // rows per pass
-constexpr int kPipeChunk = 2 * kPipePass;           // rows per chunk (two passes per level)
-constexpr int kPipeGroup = 1;                       // chunks per completion counter
+constexpr int kPipeChunk = kPipeThreads;  // rows per chunk, one per thread
+constexpr int kPipeGroup = 1;             // chunks per completion counter
 
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
   unsigned int v;
@@ -258,27 +257,79 @@ __device__ __forceinline__ bool pipe_wait(const PipeArgs &a, int glo, int ghi, i
         *s_abort = 1;
         break;
       }
-      __nanosleep(spins < 16 ? 64 : 512);
+      __nanosleep(spins < 16 ? 32 : 256);
     }
   }
   __syncthreads();
   return *s_abort == 0;
 }
 
-// Release of one chunk's level: every writer fences, the CTA synchronises,
-// one thread bumps the group counter.
+// Release of one chunk's level: the CTA synchronises, then one thread
+// fences (cumulative over the CTA's writes ordered by the barrier) and
+// bumps the chunk's counter.
 __device__ __forceinline__ void pipe_publish(const PipeArgs &a, int c, int level) {
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) atomicAdd(a.counts + (long)level * a.ngroups + c / kPipeGroup, 1u);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(a.counts + (long)level * a.ngroups + c / kPipeGroup, 1u);
+  }
 }
 
-// Takes the next chunk and stages its rows (row pointers, columns and, for
-// the valued operator, coefficients of type T) in shared memory.  Returns
-// the chunk id, or -1 when the work is exhausted or a plan invariant fails.
+// ---- 1-D bulk copies (TMA) of a chunk's CSR slice into shared memory ----
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar) {
+  asm volatile("mbarrier.init.shared.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long *bar, unsigned phase) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok) : "r"(smem_u32(bar)), "r"(phase) : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Element range [g0, g1) of a global array (16-byte aligned base, element
+// size E) goes to smem buffer `dst` (16-byte aligned) so that element g0
+// lands at dst[g0 % (16/E)].  The 16-byte-aligned body [ga, gb) moves by
+// one bulk copy issued by thread 0, the ragged tail by plain loads.
+template <typename T>
+struct StageRange {
+  long ga, gb, g1;
+  __device__ __forceinline__ StageRange(long g0, long g1_, bool bulk_ok) {
+    constexpr int per = 16 / sizeof(T);
+    ga = g0 - (g0 % per);
+    g1 = g1_;
+    gb = bulk_ok ? (g1 / per) * per : ga;
+    if (gb < ga) gb = ga;
+  }
+  __device__ __forceinline__ unsigned bulk_bytes() const { return (unsigned)((gb - ga) * sizeof(T)); }
+  __device__ __forceinline__ void issue(T *dst, const T *src, unsigned long long *bar) const {
+    if (threadIdx.x == 0 && gb > ga) bulk_g2s(dst, src + ga, bulk_bytes(), bar);
+    for (long j = gb + threadIdx.x; j < g1; j += blockDim.x) dst[j - ga] = src[j];
+  }
+};
+
+// Takes the next chunk and stages its rows in shared memory: row pointers
+// by plain loads, columns and (valued operator) coefficients of type T by
+// bulk copies completing on `bar`.  Returns the chunk id, or -1 when the
+// work is exhausted or an error (bounds, copy timeout) occurred.  *cols_out
+// and *vals_out point at the chunk's first entry inside the buffers.
 template <typename T, bool VALUED>
-__device__ __forceinline__ int pipe_take(const PipeArgs &a, const T *coef, int *rptr, int *cols, T *vals,
-                                         unsigned int *s_chunk, int *s_abort) {
+__device__ __forceinline__ int pipe_take(const PipeArgs &a, const T *coef, int *rptr, int *cols_buf, T *vals_buf,
+                                         int **cols_out, T **vals_out, unsigned long long *bar,
+                                         unsigned *phase, unsigned int *s_chunk, int *s_abort) {
   if (threadIdx.x == 0) {
     *s_chunk = atomicAdd(a.ticket, 1u);
     *s_abort = 0;
@@ -288,103 +339,101 @@ __device__ __forceinline__ int pipe_take(const PipeArgs &a, const T *coef, int *
   if (c >= a.nchunk) return -1;
   const int r0 = c * a.chunk;
   const int nr = min(a.chunk, a.n - r0);
-  const int j00 = a.ptr[r0];
-  for (int r = threadIdx.x; r <= a.chunk; r += blockDim.x) rptr[r] = a.ptr[r0 + min(r, nr)] - j00;
-  __syncthreads();
-  const int cnnz = rptr[nr];
-  if (cnnz > a.max_chunk_nnz) {  // plan invariant
+  const long j00 = a.ptr[r0];
+  const long j01 = a.ptr[r0 + nr];
+  if (j01 - j00 > a.max_chunk_nnz) {  // plan invariant
     if (threadIdx.x == 0) atomicExch(a.err, kErrBounds);
     return -1;
   }
-  for (int t = threadIdx.x; t < cnnz; t += blockDim.x) {
-    cols[t] = a.col[j00 + t];
-    if (VALUED) vals[t] = coef[j00 + t];
+  for (int r = threadIdx.x; r <= a.chunk; r += blockDim.x) rptr[r] = (int)(a.ptr[r0 + min(r, nr)] - j00);
+  const bool bulk_ok = a.bulk_ok;
+  if (threadIdx.x == 0 && bulk_ok) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  const StageRange<int> rc(j00, j01, bulk_ok);
+  const StageRange<T> rv(j00, j01, bulk_ok);
+  if (bulk_ok && threadIdx.x == 0) mbar_expect(bar, rc.bulk_bytes() + (VALUED ? rv.bulk_bytes() : 0u));
+  rc.issue(cols_buf, a.col, bar);
+  if (VALUED) rv.issue(vals_buf, coef, bar);
+  *cols_out = cols_buf + (j00 - rc.ga);
+  *vals_out = vals_buf + (j00 - rv.ga);
+  if (bulk_ok) {
+    long spins = 0;
+    while (!mbar_try(bar, *phase)) {
+      if (++spins > kSpinLimit) {  // copy never completed: report, drain with a second bound
+        if (threadIdx.x == 0) atomicCAS(a.err, 0, kErrTimeout);
+        for (long s2 = 0; s2 < kSpinLimit && !mbar_try(bar, *phase); s2++) __nanosleep(256);
+        return -1;
+      }
+    }
+    *phase ^= 1u;
   }
   __syncthreads();
   return c;
 }
 
-template <typename T>
-__device__ __forceinline__ T *pipe_vals(unsigned char *smem, const PipeArgs &a) {
-  return reinterpret_cast<T *>(
-      smem + (((size_t)(a.chunk + 1 + a.max_chunk_nnz) * sizeof(int) + 15) & ~(size_t)15));
+// Shared memory of one pipeline CTA: row pointers, column buffer and value
+// buffer (element size vsize), each 16-byte aligned with 16 bytes of slack
+// for the alignment shift of a bulk copy.
+__host__ __device__ __forceinline__ size_t pipe_cols_offset(int chunk) {
+  return (((size_t)(chunk + 1) * sizeof(int) + 15) & ~(size_t)15);
+}
+__host__ __device__ __forceinline__ size_t pipe_vals_offset(int chunk, int max_nnz) {
+  return pipe_cols_offset(chunk) + (((size_t)(max_nnz + 4) * sizeof(int) + 15) & ~(size_t)15);
+}
+__host__ __device__ __forceinline__ size_t pipe_smem_size(int chunk, int max_nnz, bool valued, size_t vsize) {
+  return pipe_vals_offset(chunk, max_nnz) + (valued ? (((size_t)max_nnz + 2) * vsize + 15) & ~(size_t)15 : 0);
 }
 
-// Row sums of the thread's kPipeRows rows in FP64.  Rows of up to 8
-// entries take a path that issues every gather before the first FMA; the
-// sum itself always runs over the entries in CSR order.
+// One row sum in FP64 over the entries [q0, q1) in CSR order; rows of up
+// to 8 entries issue every gather before the first FMA.
 template <int ARITH, bool VALUED>
-__device__ __forceinline__ void pipe_rows_fp64(const int *rptr, const int *cols, const double *vals,
-                                               const double *cf, const double *src, double *out, int base) {
-  int q0[kPipeRows], q1[kPipeRows];
-  bool small = true;
+__device__ __forceinline__ double pipe_row_fp64(int q0, int q1, const int *cols, const double *vals, double cf,
+                                                const double *src) {
+  double s = 0.0;
+  if (q1 - q0 <= 8) {
+    double xv[8];
 #pragma unroll
-  for (int j = 0; j < kPipeRows; j++) {
-    const int r = base + threadIdx.x + j * kPipeThreads;
-    q0[j] = rptr[r];
-    q1[j] = rptr[r + 1];
-    small &= (q1[j] - q0[j] <= 8);
-  }
-  if (small) {
-    double xv[kPipeRows][8], cv[kPipeRows][8];
+    for (int t = 0; t < 8; t++)
+      if (q0 + t < q1) xv[t] = src[cols[q0 + t]];
 #pragma unroll
-    for (int j = 0; j < kPipeRows; j++)
-#pragma unroll
-      for (int t = 0; t < 8; t++)
-        if (q0[j] + t < q1[j]) {
-          xv[j][t] = src[cols[q0[j] + t]];
-          cv[j][t] = VALUED ? vals[q0[j] + t] : cf[j];
-        }
-#pragma unroll
-    for (int j = 0; j < kPipeRows; j++) {
-      double s = 0.0;
-#pragma unroll
-      for (int t = 0; t < 8; t++)
-        if (q0[j] + t < q1[j]) s = row_term<ARITH>(s, cv[j][t], xv[j][t]);
-      out[j] = s;
-    }
+    for (int t = 0; t < 8; t++)
+      if (q0 + t < q1) s = row_term<ARITH>(s, VALUED ? vals[q0 + t] : cf, xv[t]);
   } else {
-#pragma unroll
-    for (int j = 0; j < kPipeRows; j++) {
-      double s = 0.0;
-      for (int q = q0[j]; q < q1[j]; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf[j], src[cols[q]]);
-      out[j] = s;
-    }
+    for (int q = q0; q < q1; q++) s = row_term<ARITH>(s, VALUED ? vals[q] : cf, src[cols[q]]);
   }
+  return s;
 }
 
 template <int ARITH, bool VALUED>
-__global__ void __launch_bounds__(kPipeThreads, 2) pipe_kernel(PipeArgs a) {
+__global__ void __launch_bounds__(kPipeThreads) pipe_kernel(PipeArgs a) {
   extern __shared__ __align__(16) unsigned char pipe_smem[];
   int *rptr = reinterpret_cast<int *>(pipe_smem);
-  int *cols = rptr + a.chunk + 1;
-  double *vals = pipe_vals<double>(pipe_smem, a);
+  int *cols_buf = reinterpret_cast<int *>(pipe_smem + pipe_cols_offset(a.chunk));
+  double *vals_buf = reinterpret_cast<double *>(pipe_smem + pipe_vals_offset(a.chunk, a.max_chunk_nnz));
   __shared__ unsigned int s_chunk;
   __shared__ int s_abort;
+  __shared__ __align__(8) unsigned long long s_bar;
+  unsigned phase = 0;
+  if (threadIdx.x == 0 && a.bulk_ok) mbar_init(&s_bar);
+  __syncthreads();
   for (;;) {
-    const int c = pipe_take<double, VALUED>(a, a.coef, rptr, cols, vals, &s_chunk, &s_abort);
+    int *cols;
+    double *vals;
+    const int c = pipe_take<double, VALUED>(a, a.coef, rptr, cols_buf, vals_buf, &cols, &vals, &s_bar, &phase,
+                                            &s_chunk, &s_abort);
     if (c < 0) return;
     const int r0 = c * a.chunk;
     const int nr = min(a.chunk, a.n - r0);
+    const int r = threadIdx.x;
+    const bool active = r < nr;
+    const double cf = (!VALUED && active) ? a.coef[r0 + r] : 0.0;
+    const int q0 = rptr[r], q1 = active ? rptr[r + 1] : q0;
     const int glo = a.gdep_lo[c], ghi = a.gdep_hi[c];
     for (int l = 1; l <= a.nlevel; l++) {
       if (l > 1 && !pipe_wait(a, glo, ghi, l - 1, &s_abort)) return;
       const double *src = l == 1 ? a.x : a.vv + (long)(l - 1) * a.n;
-      double *dst = a.vv + (long)l * a.n + r0;
-      for (int base = 0; base < nr; base += kPipePass) {
-        double cf[kPipeRows], out[kPipeRows];
-#pragma unroll
-        for (int j = 0; j < kPipeRows; j++) {
-          const int r = base + threadIdx.x + j * kPipeThreads;
-          cf[j] = (!VALUED && r < nr) ? a.coef[r0 + r] : 0.0;
-        }
-        pipe_rows_fp64<ARITH, VALUED>(rptr, cols, vals, cf, src, out, base);
-#pragma unroll
-        for (int j = 0; j < kPipeRows; j++) {
-          const int r = base + threadIdx.x + j * kPipeThreads;
-          if (r < nr) dst[r] = out[j];
-        }
-      }
+      const double v = pipe_row_fp64<ARITH, VALUED>(q0, q1, cols, vals, cf, src);
+      if (active) a.vv[(long)l * a.n + r0 + r] = v;
       pipe_publish(a, c, l);
     }
   }
@@ -456,83 +505,59 @@ __device__ __forceinline__ float2 df_norm(float sh, float sl) {
 // rounding of every level.  Level 0 (the split of x) is a pipeline stage of
 // its own.  A slot is overwritten (level l+2) only after every chunk within
 // reach has finished level l+1, i.e. no longer reads level l.
+// One row sum in double-float over the entries [q0, q1) in CSR order.
 template <bool VALUED>
-__device__ __forceinline__ void pipe_rows_df(const int *rptr, const int *cols, const float2 *vals,
-                                             const float2 *cf, const float2 *src, float2 *out, int base) {
-  int q0[kPipeRows], q1[kPipeRows];
-  bool small = true;
+__device__ __forceinline__ float2 pipe_row_df(int q0, int q1, const int *cols, const float2 *vals, float2 cf,
+                                              const float2 *src) {
+  float sh = 0.f, sl = 0.f;
+  if (q1 - q0 <= 8) {
+    float2 xv[8];
 #pragma unroll
-  for (int j = 0; j < kPipeRows; j++) {
-    const int r = base + threadIdx.x + j * kPipeThreads;
-    q0[j] = rptr[r];
-    q1[j] = rptr[r + 1];
-    small &= (q1[j] - q0[j] <= 8);
-  }
-  if (small) {
-    float2 xv[kPipeRows][8], cv[kPipeRows][8];
+    for (int t = 0; t < 8; t++)
+      if (q0 + t < q1) xv[t] = src[cols[q0 + t]];
 #pragma unroll
-    for (int j = 0; j < kPipeRows; j++)
-#pragma unroll
-      for (int t = 0; t < 8; t++)
-        if (q0[j] + t < q1[j]) {
-          xv[j][t] = src[cols[q0[j] + t]];
-          cv[j][t] = VALUED ? vals[q0[j] + t] : cf[j];
-        }
-#pragma unroll
-    for (int j = 0; j < kPipeRows; j++) {
-      float sh = 0.f, sl = 0.f;
-#pragma unroll
-      for (int t = 0; t < 8; t++)
-        if (q0[j] + t < q1[j]) df_mac(cv[j][t], xv[j][t], sh, sl);
-      out[j] = df_norm(sh, sl);
-    }
+    for (int t = 0; t < 8; t++)
+      if (q0 + t < q1) df_mac(VALUED ? vals[q0 + t] : cf, xv[t], sh, sl);
   } else {
-#pragma unroll
-    for (int j = 0; j < kPipeRows; j++) {
-      float sh = 0.f, sl = 0.f;
-      for (int q = q0[j]; q < q1[j]; q++) df_mac(VALUED ? vals[q] : cf[j], src[cols[q]], sh, sl);
-      out[j] = df_norm(sh, sl);
-    }
+    for (int q = q0; q < q1; q++) df_mac(VALUED ? vals[q] : cf, src[cols[q]], sh, sl);
   }
+  return df_norm(sh, sl);
 }
 
 template <bool VALUED>
-__global__ void __launch_bounds__(kPipeThreads, 2) pipe_df_kernel(PipeArgs a) {
+__global__ void __launch_bounds__(kPipeThreads) pipe_df_kernel(PipeArgs a) {
   extern __shared__ __align__(16) unsigned char pipe_smem[];
   int *rptr = reinterpret_cast<int *>(pipe_smem);
-  int *cols = rptr + a.chunk + 1;
-  float2 *vals = pipe_vals<float2>(pipe_smem, a);
+  int *cols_buf = reinterpret_cast<int *>(pipe_smem + pipe_cols_offset(a.chunk));
+  float2 *vals_buf = reinterpret_cast<float2 *>(pipe_smem + pipe_vals_offset(a.chunk, a.max_chunk_nnz));
   __shared__ unsigned int s_chunk;
   __shared__ int s_abort;
+  __shared__ __align__(8) unsigned long long s_bar;
+  unsigned phase = 0;
+  if (threadIdx.x == 0 && a.bulk_ok) mbar_init(&s_bar);
+  __syncthreads();
   for (;;) {
-    const int c = pipe_take<float2, VALUED>(a, a.coef2, rptr, cols, vals, &s_chunk, &s_abort);
+    int *cols;
+    float2 *vals;
+    const int c = pipe_take<float2, VALUED>(a, a.coef2, rptr, cols_buf, vals_buf, &cols, &vals, &s_bar, &phase,
+                                            &s_chunk, &s_abort);
     if (c < 0) return;
     const int r0 = c * a.chunk;
     const int nr = min(a.chunk, a.n - r0);
-    for (int r = threadIdx.x; r < nr; r += kPipeThreads) a.ring[r0 + r] = df_split(a.x[r0 + r]);
+    const int r = threadIdx.x;
+    const bool active = r < nr;
+    const float2 cf = (!VALUED && active) ? a.coef2[r0 + r] : make_float2(0.f, 0.f);
+    const int q0 = rptr[r], q1 = active ? rptr[r + 1] : q0;
+    if (active) a.ring[r0 + r] = df_split(a.x[r0 + r]);
     pipe_publish(a, c, 0);
     const int glo = a.gdep_lo[c], ghi = a.gdep_hi[c];
     for (int l = 1; l <= a.nlevel; l++) {
       if (!pipe_wait(a, glo, ghi, l - 1, &s_abort)) return;
       const float2 *src = a.ring + (long)((l - 1) & 1) * a.n;
-      float2 *ring_out = a.ring + (long)(l & 1) * a.n + r0;
-      double *dst = a.vv + (long)l * a.n + r0;
-      for (int base = 0; base < nr; base += kPipePass) {
-        float2 cf[kPipeRows], out[kPipeRows];
-#pragma unroll
-        for (int j = 0; j < kPipeRows; j++) {
-          const int r = base + threadIdx.x + j * kPipeThreads;
-          cf[j] = (!VALUED && r < nr) ? a.coef2[r0 + r] : make_float2(0.f, 0.f);
-        }
-        pipe_rows_df<VALUED>(rptr, cols, vals, cf, src, out, base);
-#pragma unroll
-        for (int j = 0; j < kPipeRows; j++) {
-          const int r = base + threadIdx.x + j * kPipeThreads;
-          if (r < nr) {
-            ring_out[r] = out[j];
-            dst[r] = df_to_double(out[j]);
-          }
-        }
+      const float2 v = pipe_row_df<VALUED>(q0, q1, cols, vals, cf, src);
+      if (active) {
+        a.ring[(long)(l & 1) * a.n + r0 + r] = v;
+        a.vv[(long)l * a.n + r0 + r] = df_to_double(v);
       }
       pipe_publish(a, c, l);
     }
@@ -1079,7 +1104,7 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
   if (!out) return fail(kEInval, "out is null");
   *out = nullptr;
   if (chunk <= 0) chunk = kPipeChunk;
-  if (chunk != kPipeChunk) return fail(kEInval, "the pipeline executor uses 1024-row chunks");
+  if (chunk != kPipeChunk) return fail(kEInval, "the pipeline executor uses 256-row chunks");
   int rc = check_csr(n, ptr, col);
   if (rc) return rc;
   Csr g;
@@ -1104,8 +1129,7 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
       maxnnz = std::max(maxnnz, ptr[r1] - ptr[c * chunk]);
     }
     a.max_chunk_nnz = std::max(maxnnz, 1);
-    p->pipe_smem_bytes = (((size_t)(chunk + 1 + a.max_chunk_nnz) * sizeof(int) + 15) & ~(size_t)15) +
-                         (p->valued ? (size_t)a.max_chunk_nnz * sizeof(double) : 0);
+    p->pipe_smem_bytes = pipe_smem_size(chunk, a.max_chunk_nnz, p->valued, 8);
     // dependencies in counter groups, and the reach they imply in chunks
     std::vector<int> glo(pp.nchunk), ghi(pp.nchunk);
     long reach = 0;
@@ -1132,6 +1156,7 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
       cudaMemset(counts, 0, sizeof(unsigned int) * ncount);
       a.gdep_lo = dlo; a.gdep_hi = dhi; a.ticket = ticket; a.counts = counts;
       a.ptr = p->d_ptr; a.col = p->d_col; a.coef = p->d_coef; a.err = p->d_err;
+      a.bulk_ok = true;  // cudaMalloc'd arrays are 256-byte aligned
       int maxsm = 0;
       cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
       if (p->pipe_smem_bytes > (size_t)maxsm) rc = fail(kERange, "chunk rows too dense for shared memory");
@@ -1271,7 +1296,7 @@ int mpkg_spmv_chain_device(int n, const int *d_ptr, const int *d_col, const doub
 // ==========================================================================
 namespace {
 
-constexpr int kNoAllocMaxChunks = 4096;  // n <= 4096 * 1024 rows
+constexpr int kNoAllocMaxChunks = 16384;  // n <= 16384 * 256 = 4096 * 1024 rows
 constexpr int kNoAllocMaxLevels = 16;
 // word layout: [0] ticket, [1] error, [2] max chunk nnz, [3] reach,
 // [4, 4+C) first dependency chunk, [4+C, 4+2C) last dependency chunk,
@@ -1355,8 +1380,7 @@ extern "C" int mpkg_pipe_noalloc(int n, const int *d_ptr, const int *d_col, cons
   CUDA_TRY(cudaStreamSynchronize(st));
   const int max_nnz = std::max<int>((int)info[0], 1);
   const long reach = info[1];
-  const size_t smem = (((size_t)(chunk + 1 + max_nnz) * sizeof(int) + 15) & ~(size_t)15) +
-                      (size_t)max_nnz * sizeof(double);
+  const size_t smem = pipe_smem_size(chunk, max_nnz, true, sizeof(double));
   int maxsm = 0, per_sm = 0, nsm = 0;
   CUDA_TRY(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   if (smem > (size_t)maxsm) return fail(kERange, "mpkg_pipe_noalloc: chunk rows too dense for shared memory");
@@ -1387,6 +1411,7 @@ extern "C" int mpkg_pipe_noalloc(int n, const int *d_ptr, const int *d_col, cons
   a.counts = counts;
   a.err = reinterpret_cast<int *>(scr + 1);
   a.max_chunk_nnz = max_nnz;
+  a.bulk_ok = ((uintptr_t)d_col % 16 == 0) && ((uintptr_t)d_val % 16 == 0);
   pipe_kernel<MPKG_ARITH_FMA, true><<<(unsigned)grid, kPipeThreads, smem, st>>>(a);
   CUDA_TRY(cudaGetLastError());
   int err = 0;
