@@ -502,9 +502,9 @@ __device__ __forceinline__ float2 df_norm(float sh, float sl) {
 
 // Pipeline in double-float: levels travel between chunks through a
 // two-slot ring of df64 values (level l in slot l&1); vv receives the FP64
-// rounding of every level.  Level 0 (the split of x) is a pipeline stage of
-// its own.  A slot is overwritten (level l+2) only after every chunk within
-// reach has finished level l+1, i.e. no longer reads level l.
+// rounding of every level.  Level 1 splits the gathered FP64 x values.  A
+// slot is overwritten (level l+2) only after every chunk within reach has
+// finished level l+1, i.e. no longer reads level l.
 // One row sum in double-float over the entries [q0, q1) in CSR order.
 template <bool VALUED>
 __device__ __forceinline__ float2 pipe_row_df(int q0, int q1, const int *cols, const float2 *vals, float2 cf,
@@ -525,7 +525,7 @@ __device__ __forceinline__ float2 pipe_row_df(int q0, int q1, const int *cols, c
 }
 
 template <bool VALUED>
-__global__ void __launch_bounds__(kPipeThreads) pipe_df_kernel(PipeArgs a) {
+__global__ void __launch_bounds__(kPipeThreads, 8) pipe_df_kernel(PipeArgs a) {
   extern __shared__ __align__(16) unsigned char pipe_smem[];
   int *rptr = reinterpret_cast<int *>(pipe_smem);
   int *cols_buf = reinterpret_cast<int *>(pipe_smem + pipe_cols_offset(a.chunk));
@@ -548,13 +548,18 @@ __global__ void __launch_bounds__(kPipeThreads) pipe_df_kernel(PipeArgs a) {
     const bool active = r < nr;
     const float2 cf = (!VALUED && active) ? a.coef2[r0 + r] : make_float2(0.f, 0.f);
     const int q0 = rptr[r], q1 = active ? rptr[r + 1] : q0;
-    if (active) a.ring[r0 + r] = df_split(a.x[r0 + r]);
-    pipe_publish(a, c, 0);
     const int glo = a.gdep_lo[c], ghi = a.gdep_hi[c];
     for (int l = 1; l <= a.nlevel; l++) {
-      if (!pipe_wait(a, glo, ghi, l - 1, &s_abort)) return;
-      const float2 *src = a.ring + (long)((l - 1) & 1) * a.n;
-      const float2 v = pipe_row_df<VALUED>(q0, q1, cols, vals, cf, src);
+      if (l > 1 && !pipe_wait(a, glo, ghi, l - 1, &s_abort)) return;
+      float2 v;
+      if (l == 1) {  // level 1 reads x (FP64) and splits each gathered value
+        float sh = 0.f, sl = 0.f;
+        for (int q = q0; q < q1; q++) df_mac(VALUED ? vals[q] : cf, df_split(a.x[cols[q]]), sh, sl);
+        v = df_norm(sh, sl);
+      } else {
+        const float2 *src = a.ring + (long)((l - 1) & 1) * a.n;
+        v = pipe_row_df<VALUED>(q0, q1, cols, vals, cf, src);
+      }
       if (active) {
         a.ring[(long)(l & 1) * a.n + r0 + r] = v;
         a.vv[(long)l * a.n + r0 + r] = df_to_double(v);
@@ -1174,7 +1179,7 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
         p->pipe_grid = std::min(grid, pp.nchunk);
         // The oldest unfinished chunk completes once every chunk within
         // (waiting levels) * reach of it is running (see pipe_kernel).
-        long need = (long)(p->arith == MPKG_ARITH_DF64 ? nlevel : nlevel - 1) * reach + 1;
+        long need = (long)(nlevel - 1) * reach + 1;
         if (p->pipe_grid < pp.nchunk && p->pipe_grid < need)
           rc = fail(kERange, "matrix bandwidth too large for the pipeline (reach " + std::to_string(reach) +
                                  " chunks, " + std::to_string(grid) + " resident CTAs)");

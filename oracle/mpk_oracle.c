@@ -474,3 +474,115 @@ void orc_exec_tasks_par(int n, const int *ptr, const int *col, const double *val
     }
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* MPI-2 rank buffers (mpk2/buffers.h:18-100).                           */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int n, npart, nlevel, nphase, rank, buf_count, buf_scount, mptr_count, mcol_count;
+  int *recvcounts, *sendcounts, *rdispls, *sdispls;           /* npart*(nphase+1) */
+  int *rcount, *mcount, *scount, *rbuf_offsets, *mbuf_offsets, *sbuf_offsets, *mptr_offsets,
+      *mcol_offsets;                                          /* nphase+1 */
+  long *idx_buf, *idx_sbuf, *mptr_buf, *mcol_buf;
+  double *mval_buf;                                           /* NULL when absent */
+} orc_bufs;
+
+/* Reads rank<N>.bufs as written by write_buffers (mpk2/buffers.c:588-631):
+ * nine ints, four int arrays of npart*(nphase+1), eight int arrays of
+ * nphase+1, then idx_buf, idx_sbuf, mptr_buf, mcol_buf (longs) and an
+ * optional mval_buf (doubles). */
+orc_bufs *orc_bufs_read(const char *path) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return NULL;
+  orc_bufs *b = calloc(1, sizeof *b);
+  int hdr[9];
+  if (fread(hdr, sizeof(int), 9, f) != 9) { fclose(f); free(b); return NULL; }
+  b->n = hdr[0]; b->npart = hdr[1]; b->nlevel = hdr[2]; b->nphase = hdr[3]; b->rank = hdr[4];
+  b->buf_count = hdr[5]; b->buf_scount = hdr[6]; b->mptr_count = hdr[7]; b->mcol_count = hdr[8];
+  long np = (long)b->npart * (b->nphase + 1), ph = b->nphase + 1;
+  int **a4[4] = {&b->recvcounts, &b->sendcounts, &b->rdispls, &b->sdispls};
+  for (int i = 0; i < 4; i++) {
+    *a4[i] = malloc(sizeof(int) * np);
+    if (fread(*a4[i], sizeof(int), np, f) != (size_t)np) goto bad;
+  }
+  int **a8[8] = {&b->rcount, &b->mcount, &b->scount, &b->rbuf_offsets, &b->mbuf_offsets, &b->sbuf_offsets,
+                 &b->mptr_offsets, &b->mcol_offsets};
+  for (int i = 0; i < 8; i++) {
+    *a8[i] = malloc(sizeof(int) * ph);
+    if (fread(*a8[i], sizeof(int), ph, f) != (size_t)ph) goto bad;
+  }
+  b->idx_buf = malloc(sizeof(long) * (b->buf_count + 1));
+  b->idx_sbuf = malloc(sizeof(long) * (b->buf_scount + 1));
+  b->mptr_buf = malloc(sizeof(long) * (b->mptr_count + 1));
+  b->mcol_buf = malloc(sizeof(long) * (b->mcol_count + 1));
+  if (fread(b->idx_buf, sizeof(long), b->buf_count, f) != (size_t)b->buf_count) goto bad;
+  if (fread(b->idx_sbuf, sizeof(long), b->buf_scount, f) != (size_t)b->buf_scount) goto bad;
+  if (fread(b->mptr_buf, sizeof(long), b->mptr_count, f) != (size_t)b->mptr_count) goto bad;
+  if (fread(b->mcol_buf, sizeof(long), b->mcol_count, f) != (size_t)b->mcol_count) goto bad;
+  b->mval_buf = malloc(sizeof(double) * (b->mcol_count + 1));
+  if (fread(b->mval_buf, sizeof(double), b->mcol_count, f) < (size_t)b->mcol_count) {
+    free(b->mval_buf);
+    b->mval_buf = NULL;
+  }
+  fclose(f);
+  return b;
+bad:
+  fclose(f);
+  return NULL; /* leaks on malformed input; test infrastructure only */
+}
+
+/* One process's computation for `phase` (mpk2/mpi2_mpkexecbufs_val.c:13-30). */
+static void orc_bufs_task(orc_bufs *b, double *vv_buf, int phase, int mode) {
+  int mcount = b->mcount[phase];
+  long *mptr = b->mptr_buf + b->mptr_offsets[phase];
+  long *mcol = b->mcol_buf + b->mcol_offsets[phase];
+  double *mval = b->mval_buf + b->mcol_offsets[phase];
+  double *vv_mbuf = vv_buf + b->mbuf_offsets[phase];
+  for (int mi = 0; mi < mcount; mi++) {
+    double tmp = 0.0;
+    for (long mj = mptr[mi]; mj < mptr[mi + 1]; mj++) tmp = row_term(tmp, mval[mj], vv_buf[mcol[mj]], mode);
+    vv_mbuf[mi] = tmp;
+  }
+}
+
+/* All ranks of the MPI-2 valued exec in one process: the input placed in
+ * every rank's rbuf[0] (mpi2_mpkexecbufs_val.c:86-87, here vv_buf[i] =
+ * x[idx_buf[i]] instead of 1.0), phase 0 computed, then per phase the
+ * send-buffer gather and the Alltoallv (mpi2_mpkexecbufs_val.c:32-48)
+ * emulated by copies, and finally collect_results (mpk2/mpi2_mpkexec.c:
+ * 122-146): vv[idx_buf[i]] = vv_buf[i], rank 0 first.  Returns 0, or -1
+ * when a buffer has no values. */
+int orc_bufs_exec(int P, orc_bufs **b, const double *x, double *vv, int mode) {
+  double **vb = malloc(sizeof(double *) * P), **sb = malloc(sizeof(double *) * P);
+  for (int p = 0; p < P; p++) {
+    if (!b[p]->mval_buf) { free(vb); free(sb); return -1; }
+    vb[p] = calloc(b[p]->buf_count + 1, sizeof(double));
+    sb[p] = calloc(b[p]->buf_scount + 1, sizeof(double));
+    for (int i = 0; i < b[p]->rcount[0]; i++) vb[p][i] = x[b[p]->idx_buf[i]];
+  }
+  for (int p = 0; p < P; p++) orc_bufs_task(b[p], vb[p], 0, mode);
+  for (int ph = 1; ph <= b[0]->nphase; ph++) {
+    for (int p = 0; p < P; p++) {
+      long *is = b[p]->idx_sbuf + b[p]->sbuf_offsets[ph];
+      double *s = sb[p] + b[p]->sbuf_offsets[ph];
+      for (int i = 0; i < b[p]->scount[ph]; i++) s[i] = vb[p][is[i]];
+    }
+    for (int dst = 0; dst < P; dst++)
+      for (int src = 0; src < P; src++) {
+        int off = P * ph;
+        int cnt = b[dst]->recvcounts[off + src];
+        double *r = vb[dst] + b[dst]->rbuf_offsets[ph] + b[dst]->rdispls[off + src];
+        double *s = sb[src] + b[src]->sbuf_offsets[ph] + b[src]->sdispls[off + dst];
+        memcpy(r, s, sizeof(double) * cnt);
+      }
+    for (int p = 0; p < P; p++) orc_bufs_task(b[p], vb[p], ph, mode);
+  }
+  for (int p = 0; p < P; p++) {
+    for (int i = 0; i < b[p]->buf_count; i++) vv[b[p]->idx_buf[i]] = vb[p][i];
+    free(vb[p]);
+    free(sb[p]);
+  }
+  free(vb);
+  free(sb);
+  return 0;
+}

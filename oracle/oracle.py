@@ -268,3 +268,26 @@ class RefTaskLists:
 
     def exec_xd(self, vv, nth):
         ref().exec_mpk_xd(C.byref(self.mpk), vv.ctypes.data_as(C.c_void_p), nth)
+
+
+# ---------------------------------------------------------------- MPI-2 buffers
+def bufs_exec(paths, x, nlevel, mode=MODE_FMA):
+    """All ranks of the MPI-2 valued exec, emulated in one process
+    (orc_bufs_exec): paths = rank0.bufs ... rank{P-1}.bufs."""
+    o = lib()
+    o.orc_bufs_read.restype = C.c_void_p
+    o.orc_bufs_read.argtypes = [C.c_char_p]
+    o.orc_bufs_exec.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    handles = []
+    for p in paths:
+        h = o.orc_bufs_read(p.encode())
+        if not h:
+            raise ValueError(f"oracle: cannot read {p}")
+        handles.append(h)
+    arr = (C.c_void_p * len(handles))(*handles)
+    n = len(x)
+    vv = np.zeros((nlevel + 1) * n)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    if o.orc_bufs_exec(len(handles), arr, _p(xx), _p(vv), mode) != 0:
+        raise ValueError("oracle: buffers without values")
+    return vv

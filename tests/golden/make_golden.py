@@ -135,6 +135,11 @@ def make(case, tmp):
     if nphase:
         out["levels"] = np.array(levels, dtype=np.int32)
         out["weights"] = np.array(weights, dtype=np.int32)
+    if n <= 1000:  # MPI-2 rank buffers from the reference prep (mpi2_mpkwrtbufs)
+        for r in range(npart):
+            run([O.ref_tool("mpi2_mpkwrtbufs"), case["name"]], cwd=tmp, env=dict(os.environ, MPK_RANK=str(r)))
+            with open(os.path.join(d, f"rank{r}.bufs"), "rb") as f:
+                out[f"bufs{r}"] = np.frombuffer(f.read(), dtype=np.uint8)
     if case.get("gold"):
         run([O.ref_tool("verify_val"), case["name"]], cwd=tmp)
         out["gold_x1"] = np.fromfile(os.path.join(d, "gold_result.bin"), dtype=np.float64)

@@ -138,3 +138,27 @@ def test_oracle_vs_live_reference_random_graphs(seed):
                        check=True, stdout=subprocess.DEVNULL)
         O.write_skirt(os.path.join(d, "s2"), ptr, col, part, npart, nlevel)
         assert open(os.path.join(d, "s"), "rb").read() == open(os.path.join(d, "s2"), "rb").read()
+
+
+def _bufs_files(g, d):
+    paths = []
+    r = 0
+    while f"bufs{r}" in g:
+        p = os.path.join(d, f"rank{r}.bufs")
+        g[f"bufs{r}"].tofile(p)
+        paths.append(p)
+        r += 1
+    return paths
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if c != "cfg1_4_4_0"])
+def test_oracle_mpi2_exec_equals_reference_gold_chain(name):
+    """The reference's own MPI-2 test (mpk2/run_script.sh:21-27): the
+    distributed valued exec over the rank buffers written by
+    mpi2_mpkwrtbufs equals the serial chain bit for bit."""
+    g = load_golden(name)
+    with tempfile.TemporaryDirectory() as d:
+        paths = _bufs_files(g, d)
+        assert len(paths) == int(g["npart"])
+        vv = O.bufs_exec(paths, g["x"], int(g["nlevel"]), O.MODE_SEPARATE)
+    assert vv.tobytes() == g["vv_val"].tobytes()
