@@ -225,6 +225,8 @@ struct PipeArgs {
   int *err;
   int max_chunk_nnz;
   bool bulk_ok;        // col/coef bases are 16-byte aligned: stage with bulk copies
+  const int *items;    // dataflow order: (level << 26) | chunk, topologically sorted
+  int nitems;
 };
 
 constexpr int kPipeThreads = 256;
@@ -569,6 +571,83 @@ __global__ void __launch_bounds__(kPipeThreads, 8) pipe_df_kernel(PipeArgs a) {
   }
 }
 
+// ------------------------------------------------------------------------
+// Dataflow pipeline.  Work items are (chunk, level) pairs in a precomputed
+// topological order: key = chunk + D*(level-1), D larger than the
+// dependency reach, levels ascending within a key.  CTAs take items in
+// ticket order; an item waits (bounded) until the chunks its rows read
+// have published the previous level, computes its 256 rows straight from
+// global memory (the matrix of recent chunks stays in L2) and publishes.
+// Every dependency of an item has a smaller ticket and so belongs to a CTA
+// that is already running: the schedule cannot deadlock, whatever the
+// grid size, and no CTA sits idle holding a chunk.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ int flow_next(const PipeArgs &a, int *s_t) {
+  __syncthreads();
+  const int t = *s_t;
+  __syncthreads();
+  if (t < a.nitems && threadIdx.x == 0) *s_t = (int)atomicAdd(a.ticket, 1u);  // prefetch
+  return t;
+}
+
+template <int ARITH, bool VALUED>
+__global__ void __launch_bounds__(kPipeThreads) flow_kernel(PipeArgs a) {
+  __shared__ int s_t;
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) {
+    s_t = (int)atomicAdd(a.ticket, 1u);
+    s_abort = 0;
+  }
+  for (;;) {
+    const int t = flow_next(a, &s_t);
+    if (t >= a.nitems) return;
+    const int item = a.items[t];
+    const int c = item & ((1 << 26) - 1), l = item >> 26;
+    if (l > 1 && !pipe_wait(a, a.gdep_lo[c], a.gdep_hi[c], l - 1, &s_abort)) return;
+    const int r = c * a.chunk + (int)threadIdx.x;
+    if (r < a.n) {
+      const int q0 = a.ptr[r], q1 = a.ptr[r + 1];
+      const double cf = VALUED ? 0.0 : a.coef[r];
+      const double *src = l == 1 ? a.x : a.vv + (long)(l - 1) * a.n;
+      a.vv[(long)l * a.n + r] = pipe_row_fp64<ARITH, VALUED>(q0, q1, a.col, a.coef, cf, src);
+    }
+    pipe_publish(a, c, l);
+  }
+}
+
+template <bool VALUED>
+__global__ void __launch_bounds__(kPipeThreads, 6) flow_df_kernel(PipeArgs a) {
+  __shared__ int s_t;
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) {
+    s_t = (int)atomicAdd(a.ticket, 1u);
+    s_abort = 0;
+  }
+  for (;;) {
+    const int t = flow_next(a, &s_t);
+    if (t >= a.nitems) return;
+    const int item = a.items[t];
+    const int c = item & ((1 << 26) - 1), l = item >> 26;
+    if (l > 1 && !pipe_wait(a, a.gdep_lo[c], a.gdep_hi[c], l - 1, &s_abort)) return;
+    const int r = c * a.chunk + (int)threadIdx.x;
+    if (r < a.n) {
+      const int q0 = a.ptr[r], q1 = a.ptr[r + 1];
+      const float2 cf = VALUED ? make_float2(0.f, 0.f) : a.coef2[r];
+      float2 v;
+      if (l == 1) {
+        float sh = 0.f, sl = 0.f;
+        for (int q = q0; q < q1; q++) df_mac(VALUED ? a.coef2[q] : cf, df_split(a.x[a.col[q]]), sh, sl);
+        v = df_norm(sh, sl);
+      } else {
+        v = pipe_row_df<VALUED>(q0, q1, a.col, a.coef2, cf, a.ring + (long)((l - 1) & 1) * a.n);
+      }
+      a.ring[(long)(l & 1) * a.n + r] = v;
+      a.vv[(long)l * a.n + r] = df_to_double(v);
+    }
+    pipe_publish(a, c, l);
+  }
+}
+
 // PA1 tiles in double-float: same schedule as tiles_kernel, level buffers
 // of float2 in shared memory.
 template <bool VALUED>
@@ -857,11 +936,8 @@ int set_tiles_attr(size_t bytes) {
 
 template <bool VALUED>
 int pipe_setup_df(mpkg_plan *p, int *grid) {
-  CUDA_TRY(cudaFuncSetAttribute(pipe_df_kernel<VALUED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)p->pipe_smem_bytes));
   int per_sm = 0, nsm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_df_kernel<VALUED>, kPipeThreads,
-                                                         p->pipe_smem_bytes));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, flow_df_kernel<VALUED>, kPipeThreads, 0));
   CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
   *grid = per_sm * nsm;
   return kOk;
@@ -876,11 +952,8 @@ int set_tiles_df_attr(size_t bytes) {
 
 template <int ARITH, bool VALUED>
 int pipe_setup_t(mpkg_plan *p, int *grid) {
-  CUDA_TRY(cudaFuncSetAttribute(pipe_kernel<ARITH, VALUED>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pipe_smem_bytes));
   int per_sm = 0, nsm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_kernel<ARITH, VALUED>, kPipeThreads,
-                                                         p->pipe_smem_bytes));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, flow_kernel<ARITH, VALUED>, kPipeThreads, 0));
   CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
   *grid = per_sm * nsm;
   return kOk;
@@ -941,7 +1014,7 @@ void launch_pipe_df(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) 
   a.x = x;
   a.vv = vv;
   a.epoch = p->epoch;
-  pipe_df_kernel<VALUED><<<p->pipe_grid, kPipeThreads, p->pipe_smem_bytes, st>>>(a);
+  flow_df_kernel<VALUED><<<p->pipe_grid, kPipeThreads, 0, st>>>(a);
 }
 
 template <int ARITH, bool VALUED>
@@ -950,7 +1023,7 @@ void launch_pipe_t(mpkg_plan *p, const double *x, double *vv, cudaStream_t st) {
   a.x = x;
   a.vv = vv;
   a.epoch = p->epoch;
-  pipe_kernel<ARITH, VALUED><<<p->pipe_grid, kPipeThreads, p->pipe_smem_bytes, st>>>(a);
+  flow_kernel<ARITH, VALUED><<<p->pipe_grid, kPipeThreads, 0, st>>>(a);
 }
 
 #define DISPATCH2(fn, ...)                                                   \
@@ -1162,9 +1235,6 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
       a.gdep_lo = dlo; a.gdep_hi = dhi; a.ticket = ticket; a.counts = counts;
       a.ptr = p->d_ptr; a.col = p->d_col; a.coef = p->d_coef; a.err = p->d_err;
       a.bulk_ok = true;  // cudaMalloc'd arrays are 256-byte aligned
-      int maxsm = 0;
-      cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
-      if (p->pipe_smem_bytes > (size_t)maxsm) rc = fail(kERange, "chunk rows too dense for shared memory");
     }
     if (!rc) {
       int grid = 0;
@@ -1176,13 +1246,22 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val, int
         rc = p->valued ? pipe_setup_t<MPKG_ARITH_FMA, true>(p, &grid) : pipe_setup_t<MPKG_ARITH_FMA, false>(p, &grid);
       if (!rc) {
         p->pipe_reach = (int)reach;
-        p->pipe_grid = std::min(grid, pp.nchunk);
-        // The oldest unfinished chunk completes once every chunk within
-        // (waiting levels) * reach of it is running (see pipe_kernel).
-        long need = (long)(nlevel - 1) * reach + 1;
-        if (p->pipe_grid < pp.nchunk && p->pipe_grid < need)
-          rc = fail(kERange, "matrix bandwidth too large for the pipeline (reach " + std::to_string(reach) +
-                                 " chunks, " + std::to_string(grid) + " resident CTAs)");
+        // topological item order: key = chunk + D*(level-1), levels ascending
+        // within a key; D leaves about one grid's worth of items between an
+        // item and its latest dependency
+        const long D = reach + std::max<long>(1, ((long)grid + nlevel - 1) / nlevel);
+        std::vector<int> items;
+        items.reserve((size_t)pp.nchunk * nlevel);
+        for (long K = 0; K < pp.nchunk + D * (nlevel - 1); K++)
+          for (int l = 1; l <= nlevel; l++) {
+            const long c = K - D * (l - 1);
+            if (c >= 0 && c < pp.nchunk) items.push_back((l << 26) | (int)c);
+          }
+        int *ditems = nullptr;
+        rc = dev_copy(p, &ditems, items.data(), items.size());
+        a.items = ditems;
+        a.nitems = (int)items.size();
+        p->pipe_grid = (int)std::min<long>(grid, (long)items.size());
       }
     }
   }

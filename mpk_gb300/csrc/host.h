@@ -150,4 +150,26 @@ struct PipePlan {
 };
 int build_pipe_plan(const Csr &g, int nlevel, int chunk, PipePlan *pp);
 
+// ---- MPI-2 rank buffers (bufs.cc) ----------------------------------------
+// One rank's computation/communication buffers, the layout of buffers_t
+// (mpk2/buffers.h:18-100): per phase an rbuf (received values, phase 0 =
+// the x halo) followed by an mbuf (values computed by this rank),
+// tile-local CSR mptr/mcol whose columns index the rank's own vv_buf, the
+// send list idx_sbuf, and MPI counts/displacements per phase.
+struct RankBuffers {
+  int n = 0, npart = 0, nlevel = 0, nphase = 0, rank = 0;
+  int buf_count = 0, buf_scount = 0, mptr_count = 0, mcol_count = 0;
+  std::vector<int> recvcounts, sendcounts, rdispls, sdispls;  // npart*(nphase+1)
+  std::vector<int> rcount, mcount, scount, rbuf_offsets, mbuf_offsets, sbuf_offsets, mptr_offsets,
+      mcol_offsets;                                          // nphase+1
+  std::vector<long> idx_buf, idx_sbuf, mptr_buf, mcol_buf;
+  std::vector<double> mval_buf;  // empty when the file holds no values
+};
+// rank<N>.bufs as write_buffers writes it (mpk2/buffers.c:588-631).
+int read_rank_buffers(const std::string &path, RankBuffers *b);
+int write_rank_buffers(const std::string &path, const RankBuffers &b);
+// Checks the internal consistency of a set of rank buffers (counts,
+// offsets, index ranges, matching send/receive counts).
+int check_rank_buffers(const std::vector<RankBuffers> &bufs);
+
 }  // namespace mpkg
