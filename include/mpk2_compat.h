@@ -144,6 +144,71 @@ void vexec_mpk(mpk_t *mg, double *vv, double *val);
 /* mpk2/mpktexec.c:39: transposed layout vv[i*(nlevel+1)+l] */
 void exec_mpkt(mpk_t *mg, double *vv, int nth);
 
+/* ---- MPI-2 prep (mpk2/comm_data.h, mpk2/buffers.h) ---------------------- */
+
+/* mpk2/comm_data.h:10-22 */
+typedef struct comm_table {
+  char *dir;
+  int n;
+  int nlevel;
+  int npart;
+  int nphase;
+  int rank;
+  crs0_t *graph;
+  part_t **plist;
+  level_t **llist;
+  skirt_t *skirt;
+} comm_data_t;
+
+/* mpk2/comm_data.h:24 (records the error instead of exiting) */ void dir_name_error(char *dir);
+/* mpk2/comm_data.h:26: dir/loop.g0 */ crs0_t *read_matrix(char *dir);
+/* mpk2/comm_data.h:28: <dir up to its first '_'>.loop.val */ double *alloc_read_val(crs0_t *g0, char *dir);
+/* mpk2/comm_data.h:30 */ comm_data_t *new_comm_data(char *dir, int rank);
+/* mpk2/comm_data.h:32 */ void del_comm_data(comm_data_t *cd);
+
+/* mpk2/buffers.h:18-100 */
+typedef struct buffers_t {
+  int n;
+  int npart;
+  int nlevel;
+  int nphase;
+  int rank;
+  int buf_count;
+  int buf_scount;
+  int mptr_count;
+  int mcol_count;
+  int *recvcounts;
+  int *sendcounts;
+  int *rdispls;
+  int *sdispls;
+  int *rcount;
+  int *mcount;
+  int *scount;
+  int *rbuf_offsets;
+  int *mbuf_offsets;
+  int *sbuf_offsets;
+  int *mptr_offsets;
+  int *mcol_offsets;
+  long *idx_buf;
+  long *idx_sbuf;
+  long *mptr_buf;
+  long *mcol_buf;
+  double *vv_buf;
+  double *vv_sbuf;
+  double *mval_buf;
+} buffers_t;
+
+/* mpk2/buffers.h:107 (a command-line helper: exits on argc != 2, as the
+ * reference) */ void check_args(int argc, char *argv0);
+/* mpk2/buffers.h:120 */ buffers_t *new_bufs(comm_data_t *cd);
+/* mpk2/buffers.h:128 */ void alloc_val_bufs(buffers_t *bufs);
+/* mpk2/buffers.h:136 */ void del_bufs(buffers_t *bufs);
+/* mpk2/buffers.h:158: computed for all ranks with sparse communication
+ * sets; relabels cd->plist for phases > 0 as the reference does */
+void fill_buffers(comm_data_t *cd, buffers_t *bufs);
+/* mpk2/buffers.h:171 */ void write_buffers(buffers_t *bufs, char *dir);
+/* mpk2/buffers.h:183 */ buffers_t *read_buffers(char *dir, int rank);
+
 /* New: text of the last error recorded by the functions above on the
  * calling thread ("" when none). */
 const char *mpk2_last_error(void);

@@ -61,6 +61,7 @@ extern "C" {
                              advance level by level behind their
                              neighbours, matrix chunk kept in shared memory */
 #define MPKG_EXEC_SPMV 3  /* k separate SpMV launches (baseline) */
+#define MPKG_EXEC_BUFS 4  /* MPI-2 rank buffers of all ranks on one GPU */
 
 typedef struct mpkg_plan mpkg_plan;
 
@@ -101,6 +102,15 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val,
 /* k chained SpMV launches (baseline; also the GPU spmv_exec_*). */
 int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val,
                    int nlevel, int arith, mpkg_plan **out);
+
+/* MPI-2 rank buffers rank0.bufs .. rank{npart-1}.bufs in `dir` (the files
+ * mpi2_mpkwrtbufs writes, mpk2/buffers.c:588-631; values required) run on
+ * one GPU: each phase's per-rank computation (mpk2/mpi2_mpkexecbufs_val.c:
+ * 13-30) is one launch over all ranks, each phase's MPI_Alltoallv
+ * (mpi2_mpkexecbufs_val.c:32-48) one device gather.  Execution places x
+ * from vv[0..n) into every rank's phase-0 receive buffer and collects every
+ * rank's values into vv (collect_results, mpk2/mpi2_mpkexec.c:122-146). */
+int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out);
 
 int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info);
 
@@ -176,6 +186,13 @@ int mpkg_skirt_write(const char *path, int n, const int *ptr, const int *col,
 int mpkg_tasks(int n, const int *ptr, const int *col, int npart, int nlevel, int nphase,
                const int *parts, const int *levels, int check, long *off, long **idx,
                long *count);
+
+/* The MPI-2 prep of every rank at once (what mpi2_mpkwrtbufs does rank by
+ * rank, mpk2/mpi2_mpkwrtbufs.c:41-60): reads `dir` (ghead_npart_nlevel_
+ * nphase with loop.g0, g<ph>.part.<npart>, l<ph>, s<nphase>, and
+ * <dir up to its first '_'>.loop.val) and writes dir/rank<r>.bufs for every
+ * rank, byte-compatible with the reference's files. */
+int mpkg_bufs_prepare(const char *dir);
 
 /* Partitioners (METIS is not available): recursive coordinate bisection
  * (coords: dim ints per vertex) and breadth-first recursive bisection. */

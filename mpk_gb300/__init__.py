@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(_HERE, "libmpk_gb300.so")
 
 OK, EINVAL, EIO, EFORMAT, ESTRUCT, ECUDA, ETIMEOUT, ENOMEM, ERANGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
 ARITH_FMA, ARITH_SEPARATE, ARITH_DF64 = 0, 1, 2
-EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV = 0, 1, 2, 3
+EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS = 0, 1, 2, 3, 4
 
 _ERRNAMES = {EINVAL: "EINVAL", EIO: "EIO", EFORMAT: "EFORMAT", ESTRUCT: "ESTRUCT", ECUDA: "ECUDA",
              ETIMEOUT: "ETIMEOUT", ENOMEM: "ENOMEM", ERANGE: "ERANGE"}
@@ -63,6 +63,7 @@ def _declare(L):
         "mpkg_plan_pipe": (I, [I, P, P, P, I, I, I, pp]),
         "mpkg_plan_spmv": (I, [I, P, P, P, I, I, pp]),
         "mpkg_plan_info": (I, [P, C.POINTER(PlanInfo)]),
+        "mpkg_plan_bufs": (I, [C.c_char_p, I, I, pp]),
         "mpkg_exec_host": (I, [P, P]),
         "mpkg_exec_device": (I, [P, P, P]),
         "mpkg_sync": (I, [P, P]),
@@ -279,6 +280,17 @@ class Plan:
     def pipe(cls, a: Csr, nlevel, chunk=0, arith=ARITH_FMA):
         return cls._make(lib().mpkg_plan_pipe, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, chunk,
                          arith, a=a, nlevel=nlevel)
+
+    @classmethod
+    def bufs(cls, directory, npart, arith=ARITH_FMA):
+        """MPI-2 rank buffers (rank<r>.bufs in `directory`) on one GPU."""
+        h = C.c_void_p()
+        _check(lib().mpkg_plan_bufs(directory.encode(), npart, arith, C.byref(h)))
+        p = Plan.__new__(Plan)
+        p._h = h
+        inf = p.info()
+        p.n, p.nlevel = inf["n"], inf["nlevel"]
+        return p
 
     @classmethod
     def spmv(cls, a: Csr, nlevel, arith=ARITH_FMA):

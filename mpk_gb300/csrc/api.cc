@@ -744,3 +744,258 @@ void spmv_exec_seq(crs0_t *g0, double *vv, int nlevel) { legacy_spmv(g0, vv, nle
 void spmv_exec_par(crs0_t *g0, double *vv, int nlevel, int nth) { (void)nth; legacy_spmv(g0, vv, nlevel); }
 
 }  // extern "C"
+
+// ==========================================================================
+// MPI-2 prep: comm_data_t and buffers_t (mpk2/comm_data.h, mpk2/buffers.h)
+// ==========================================================================
+namespace {
+
+// "ghead_npart_nlevel_nphase" parsed from the end of the directory name.
+bool parse_dir(const char *dir, int *npart, int *nlevel, int *nphase) {
+  int len = (int)std::strlen(dir), cnt = 0, j = len;
+  for (; j >= 0; j--)
+    if (dir[j] == '_' && ++cnt == 3) break;
+  *npart = *nlevel = *nphase = -1;
+  return cnt == 3 && j >= 0 && std::sscanf(dir + j, "_%d_%d_%d", npart, nlevel, nphase) == 3 && *npart > 0 &&
+         *nlevel > 0 && *nphase >= 0;
+}
+
+// <dir up to its first '_'>.loop.val (mpk2/comm_data.c:160-187)
+std::string values_path(const char *dir) {
+  std::string d(dir);
+  size_t u = d.find('_');
+  return (u == std::string::npos ? d : d.substr(0, u)) + ".loop.val";
+}
+
+buffers_t *to_legacy(const RankBuffers &b) {
+  buffers_t *o = (buffers_t *)std::calloc(1, sizeof(buffers_t));
+  o->n = b.n; o->npart = b.npart; o->nlevel = b.nlevel; o->nphase = b.nphase; o->rank = b.rank;
+  o->buf_count = b.buf_count; o->buf_scount = b.buf_scount; o->mptr_count = b.mptr_count;
+  o->mcol_count = b.mcol_count;
+  o->recvcounts = dup(b.recvcounts); o->sendcounts = dup(b.sendcounts);
+  o->rdispls = dup(b.rdispls); o->sdispls = dup(b.sdispls);
+  o->rcount = dup(b.rcount); o->mcount = dup(b.mcount); o->scount = dup(b.scount);
+  o->rbuf_offsets = dup(b.rbuf_offsets); o->mbuf_offsets = dup(b.mbuf_offsets);
+  o->sbuf_offsets = dup(b.sbuf_offsets); o->mptr_offsets = dup(b.mptr_offsets);
+  o->mcol_offsets = dup(b.mcol_offsets);
+  o->idx_buf = dup(b.idx_buf); o->idx_sbuf = dup(b.idx_sbuf);
+  o->mptr_buf = dup(b.mptr_buf); o->mcol_buf = dup(b.mcol_buf);
+  o->mval_buf = b.mval_buf.empty() ? nullptr : dup(b.mval_buf);
+  return o;
+}
+
+RankBuffers from_legacy(const buffers_t *o) {
+  RankBuffers b;
+  b.n = o->n; b.npart = o->npart; b.nlevel = o->nlevel; b.nphase = o->nphase; b.rank = o->rank;
+  b.buf_count = o->buf_count; b.buf_scount = o->buf_scount; b.mptr_count = o->mptr_count;
+  b.mcol_count = o->mcol_count;
+  const size_t np = (size_t)o->npart * (o->nphase + 1), ph = (size_t)o->nphase + 1;
+  b.recvcounts.assign(o->recvcounts, o->recvcounts + np); b.sendcounts.assign(o->sendcounts, o->sendcounts + np);
+  b.rdispls.assign(o->rdispls, o->rdispls + np); b.sdispls.assign(o->sdispls, o->sdispls + np);
+  b.rcount.assign(o->rcount, o->rcount + ph); b.mcount.assign(o->mcount, o->mcount + ph);
+  b.scount.assign(o->scount, o->scount + ph);
+  b.rbuf_offsets.assign(o->rbuf_offsets, o->rbuf_offsets + ph);
+  b.mbuf_offsets.assign(o->mbuf_offsets, o->mbuf_offsets + ph);
+  b.sbuf_offsets.assign(o->sbuf_offsets, o->sbuf_offsets + ph);
+  b.mptr_offsets.assign(o->mptr_offsets, o->mptr_offsets + ph);
+  b.mcol_offsets.assign(o->mcol_offsets, o->mcol_offsets + ph);
+  b.idx_buf.assign(o->idx_buf, o->idx_buf + o->buf_count);
+  b.idx_sbuf.assign(o->idx_sbuf, o->idx_sbuf + o->buf_scount);
+  b.mptr_buf.assign(o->mptr_buf, o->mptr_buf + o->mptr_count);
+  b.mcol_buf.assign(o->mcol_buf, o->mcol_buf + o->mcol_count);
+  if (o->mval_buf) b.mval_buf.assign(o->mval_buf, o->mval_buf + o->mcol_count);
+  return b;
+}
+
+// The inputs of the MPI-2 prep from a comm_data_t.
+void comm_inputs(const comm_data_t *cd, Csr *g, std::vector<std::vector<int>> *parts,
+                 std::vector<std::vector<int>> *levels, std::vector<PartSkirt> *sk) {
+  *g = csr_of(cd->graph);
+  const int n = cd->n;
+  parts->clear();
+  levels->clear();
+  for (int ph = 0; ph < std::max(cd->nphase, 1); ph++)
+    parts->emplace_back(cd->plist[ph]->part, cd->plist[ph]->part + n);
+  for (int ph = 0; ph < cd->nphase; ph++) levels->emplace_back(cd->llist[ph]->level, cd->llist[ph]->level + n);
+  sk->assign(cd->npart, PartSkirt());
+  for (int p = 0; p < cd->npart; p++) {
+    const int *s = cd->skirt->levels + (size_t)p * n;
+    for (int i = 0; i < n; i++)
+      if (s[i] >= 0) { (*sk)[p].vert.push_back(i); (*sk)[p].dist.push_back(s[i]); }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void dir_name_error(char *dir) {
+  fail(kEFormat, std::string("unknown directory naming ") + (dir ? dir : "") +
+                     " (expecting ghead_npart_nlevel_nphase)");
+}
+
+crs0_t *read_matrix(char *dir) {
+  clear_error();
+  if (!dir) return nullptr;
+  FILE *f = std::fopen((std::string(dir) + "/loop.g0").c_str(), "r");
+  if (!f) { fail(kEIo, std::string("cannot open ") + dir + "/loop.g0"); return nullptr; }
+  return read_crs(f);
+}
+
+double *alloc_read_val(crs0_t *g0, char *dir) {
+  clear_error();
+  if (!g0 || !dir) return nullptr;
+  std::vector<double> v;
+  if (read_values(values_path(dir), g0->ptr[g0->n], &v)) return nullptr;
+  return dup(v);
+}
+
+comm_data_t *new_comm_data(char *dir, int rank) {
+  clear_error();
+  int npart, nlevel, nphase;
+  if (!dir || !parse_dir(dir, &npart, &nlevel, &nphase)) { dir_name_error(dir); return nullptr; }
+  crs0_t *g = read_matrix(dir);
+  if (!g) return nullptr;
+  comm_data_t *cd = (comm_data_t *)std::calloc(1, sizeof(comm_data_t));
+  cd->dir = dir; cd->rank = rank; cd->npart = npart; cd->nlevel = nlevel; cd->nphase = nphase;
+  cd->graph = g;
+  cd->n = g->n;
+  const int np = nphase == 0 ? 1 : nphase;
+  cd->plist = (part_t **)std::calloc(np, sizeof(part_t *));
+  cd->llist = nphase == 0 ? nullptr : (level_t **)std::calloc(nphase, sizeof(level_t *));
+  std::string d(dir);
+  bool ok = true;
+  for (int ph = 0; ph < np && ok; ph++) {
+    std::string fn = d + "/g" + std::to_string(ph) + ".part." + std::to_string(npart);
+    FILE *f = std::fopen(fn.c_str(), "r");
+    if (!f) { fail(kEIo, "cannot open " + fn); ok = false; break; }
+    cd->plist[ph] = new_part(g);
+    read_part(f, cd->plist[ph]);
+    std::fclose(f);
+    if (nphase > 0) {
+      fn = d + "/l" + std::to_string(ph);
+      f = std::fopen(fn.c_str(), "r");
+      if (!f) { fail(kEIo, "cannot open " + fn); ok = false; break; }
+      cd->llist[ph] = new_level(cd->plist[ph]);
+      read_level(f, cd->llist[ph]);
+    }
+  }
+  if (ok) {
+    std::string fn = d + "/s" + std::to_string(nphase);
+    FILE *f = std::fopen(fn.c_str(), "r");
+    if (!f) { fail(kEIo, "cannot open " + fn); ok = false; }
+    else {
+      cd->plist[0]->n_part = std::max(cd->plist[0]->n_part, npart);
+      cd->skirt = new_skirt(cd->plist[0]);
+      if (!cd->skirt) { std::fclose(f); ok = false; }
+      else read_skirt(f, cd->skirt, nlevel);
+    }
+  }
+  if (!ok) { del_comm_data(cd); return nullptr; }
+  return cd;
+}
+
+void del_comm_data(comm_data_t *cd) {
+  if (!cd) return;
+  const int np = cd->nphase == 0 ? 1 : cd->nphase;
+  for (int ph = 0; ph < np; ph++) if (cd->plist && cd->plist[ph]) del_part(cd->plist[ph]);
+  for (int ph = 0; ph < cd->nphase; ph++) if (cd->llist && cd->llist[ph]) del_level(cd->llist[ph]);
+  std::free(cd->plist);
+  std::free(cd->llist);
+  if (cd->skirt) del_skirt(cd->skirt);
+  if (cd->graph) del_crs(cd->graph);
+  std::free(cd);
+}
+
+void check_args(int argc, char *argv0) {
+  if (argc != 2) {
+    std::fprintf(stderr, "usage: %s dirname\n", argv0 ? argv0 : "prog");
+    std::exit(1);
+  }
+}
+
+buffers_t *new_bufs(comm_data_t *cd) {
+  if (!cd) return nullptr;
+  buffers_t *b = (buffers_t *)std::calloc(1, sizeof(buffers_t));
+  b->n = cd->n; b->npart = cd->npart; b->nlevel = cd->nlevel; b->nphase = cd->nphase; b->rank = cd->rank;
+  return b;
+}
+
+void alloc_val_bufs(buffers_t *b) {
+  if (!b) return;
+  std::free(b->vv_buf);
+  std::free(b->vv_sbuf);
+  b->vv_buf = (double *)std::calloc(std::max(b->buf_count, 1), sizeof(double));
+  b->vv_sbuf = (double *)std::calloc(std::max(b->buf_scount, 1), sizeof(double));
+}
+
+void del_bufs(buffers_t *b) {
+  if (!b) return;
+  for (void *q : {(void *)b->recvcounts, (void *)b->sendcounts, (void *)b->rdispls, (void *)b->sdispls,
+                  (void *)b->rcount, (void *)b->mcount, (void *)b->scount, (void *)b->rbuf_offsets,
+                  (void *)b->mbuf_offsets, (void *)b->sbuf_offsets, (void *)b->mptr_offsets,
+                  (void *)b->mcol_offsets, (void *)b->idx_buf, (void *)b->idx_sbuf, (void *)b->mptr_buf,
+                  (void *)b->mcol_buf, (void *)b->vv_buf, (void *)b->vv_sbuf, (void *)b->mval_buf})
+    std::free(q);
+  std::free(b);
+}
+
+void fill_buffers(comm_data_t *cd, buffers_t *bufs) {
+  clear_error();
+  if (!cd || !bufs) { fail(kEInval, "fill_buffers: null argument"); return; }
+  Csr g;
+  std::vector<std::vector<int>> parts, levels;
+  std::vector<PartSkirt> sk;
+  comm_inputs(cd, &g, &parts, &levels, &sk);
+  std::vector<RankBuffers> all;
+  if (fill_all_buffers(g, cd->npart, cd->nlevel, cd->nphase, &parts, levels, sk, &all)) return;
+  for (int ph = 1; ph < cd->nphase; ph++)  // the relabelling reduce_comm applies
+    std::copy(parts[ph].begin(), parts[ph].end(), cd->plist[ph]->part);
+  buffers_t *o = to_legacy(all[cd->rank]);
+  double *vv = bufs->vv_buf, *vs = bufs->vv_sbuf;
+  for (void *q : {(void *)bufs->recvcounts, (void *)bufs->sendcounts, (void *)bufs->rdispls, (void *)bufs->sdispls,
+                  (void *)bufs->rcount, (void *)bufs->mcount, (void *)bufs->scount, (void *)bufs->rbuf_offsets,
+                  (void *)bufs->mbuf_offsets, (void *)bufs->sbuf_offsets, (void *)bufs->mptr_offsets,
+                  (void *)bufs->mcol_offsets, (void *)bufs->idx_buf, (void *)bufs->idx_sbuf, (void *)bufs->mptr_buf,
+                  (void *)bufs->mcol_buf, (void *)bufs->mval_buf})
+    std::free(q);
+  *bufs = *o;
+  bufs->vv_buf = vv;
+  bufs->vv_sbuf = vs;
+  bufs->mval_buf = nullptr;  // filled by the caller, as mpi2_mpkwrtbufs does
+  std::free(o);
+}
+
+void write_buffers(buffers_t *bufs, char *dir) {
+  clear_error();
+  if (!bufs || !dir) return;
+  write_rank_buffers(std::string(dir) + "/rank" + std::to_string(bufs->rank) + ".bufs", from_legacy(bufs));
+}
+
+buffers_t *read_buffers(char *dir, int rank) {
+  clear_error();
+  if (!dir) return nullptr;
+  RankBuffers b;
+  if (read_rank_buffers(std::string(dir) + "/rank" + std::to_string(rank) + ".bufs", &b)) return nullptr;
+  return to_legacy(b);
+}
+
+int mpkg_bufs_prepare(const char *dir) {
+  clear_error();
+  if (!dir) return fail(kEInval, "null dir");
+  comm_data_t *cd = new_comm_data(const_cast<char *>(dir), 0);
+  if (!cd) return kEIo;
+  Csr g;
+  std::vector<std::vector<int>> parts, levels;
+  std::vector<PartSkirt> sk;
+  comm_inputs(cd, &g, &parts, &levels, &sk);
+  int rc = read_values(values_path(dir), g.nnz(), &g.val);
+  std::vector<RankBuffers> all;
+  if (!rc) rc = fill_all_buffers(g, cd->npart, cd->nlevel, cd->nphase, &parts, levels, sk, &all);
+  for (int r = 0; !rc && r < cd->npart; r++)
+    rc = write_rank_buffers(std::string(dir) + "/rank" + std::to_string(r) + ".bufs", all[r]);
+  del_comm_data(cd);
+  return rc;
+}
+
+}  // extern "C"

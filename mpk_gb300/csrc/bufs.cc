@@ -1,6 +1,8 @@
 // MPI-2 rank buffers: file format and consistency checks.
+#include <algorithm>
 #include <cstdio>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "host.h"
@@ -117,6 +119,251 @@ int check_rank_buffers(const std::vector<RankBuffers> &bufs) {
       if (i < 0 || i >= b.buf_count) return fail(kERange, "mcol entry out of range");
     for (int i = 0; i < b.rcount[0]; i++)
       if (b.idx_buf[b.rbuf_offsets[0] + i] >= b.n) return fail(kEFormat, "phase-0 receive entry is not level 0");
+  }
+  return kOk;
+}
+
+}  // namespace mpkg
+
+namespace mpkg {
+
+// Hungarian algorithm (shortest augmenting paths with potentials) on the
+// cost max(sums) - sums: an optimal assignment of rows (old parts) to
+// columns (new parts) maximising the communication that stays on a rank.
+void assign_max_trace(const std::vector<long> &sums, int np, std::vector<int> *perm) {
+  long mx = 0;
+  for (long v : sums) mx = std::max(mx, v);
+  const long INF = (long)4e18;
+  // 1-based arrays: u (rows), v (cols), match[col] = row
+  std::vector<long> u(np + 1, 0), v(np + 1, 0), minv(np + 1);
+  std::vector<int> match(np + 1, 0), way(np + 1, 0);
+  std::vector<char> used(np + 1);
+  auto cost = [&](int i, int j) { return mx - sums[(long)(i - 1) * np + (j - 1)]; };
+  for (int i = 1; i <= np; i++) {
+    match[0] = i;
+    int j0 = 0;
+    std::fill(minv.begin(), minv.end(), INF);
+    std::fill(used.begin(), used.end(), 0);
+    do {
+      used[j0] = 1;
+      const int i0 = match[j0];
+      long delta = INF;
+      int j1 = 0;
+      for (int j = 1; j <= np; j++)
+        if (!used[j]) {
+          const long cur = cost(i0, j) - u[i0] - v[j];
+          if (cur < minv[j]) { minv[j] = cur; way[j] = j0; }
+          if (minv[j] < delta) { delta = minv[j]; j1 = j; }
+        }
+      for (int j = 0; j <= np; j++) {
+        if (used[j]) { u[match[j]] += delta; v[j] -= delta; }
+        else minv[j] -= delta;
+      }
+      j0 = j1;
+    } while (match[j0] != 0);
+    do {
+      const int j1 = way[j0];
+      match[j0] = match[j1];
+      j0 = j1;
+    } while (j0);
+  }
+  perm->assign(np, 0);
+  for (int j = 1; j <= np; j++) (*perm)[j - 1] = match[j] - 1;
+}
+
+namespace {
+struct Triple {
+  int src, tgt;
+  long v;
+};
+bool by_tgt(const Triple &a, const Triple &b) {
+  return a.tgt != b.tgt ? a.tgt < b.tgt : a.src != b.src ? a.src < b.src : a.v < b.v;
+}
+void unique_triples(std::vector<Triple> *t) {
+  std::sort(t->begin(), t->end(), by_tgt);
+  t->erase(std::unique(t->begin(), t->end(),
+                       [](const Triple &a, const Triple &b) { return a.src == b.src && a.tgt == b.tgt && a.v == b.v; }),
+           t->end());
+}
+}  // namespace
+
+// See host.h.  The phase ranges follow the reference: phase ph computes
+// level l of vertex i when prevl[i] < l <= level_ph[i] (l up to
+// min(max level_ph, nlevel)); the skirt phase computes, for part p, level
+// l of skirt vertex i when prevl[i] < l <= nlevel - dist_p(i).  A needed
+// value (l-1, k) travels from the part that computed it last (store_part)
+// to the computing part unless they coincide (proc_vertex,
+// mpk2/buffers.c:53-66).
+int fill_all_buffers(const Csr &g, int npart, int nlevel, int nphase, std::vector<std::vector<int>> *parts,
+                     const std::vector<std::vector<int>> &levels, const std::vector<PartSkirt> &sk,
+                     std::vector<RankBuffers> *out) {
+  const int n = g.n, P = npart, L = nlevel;
+  if ((int)parts->size() < std::max(nphase, 1) || (int)levels.size() < nphase || (int)sk.size() != P)
+    return fail(kEInval, "missing partitions, levels or skirts");
+  const size_t nvv = (size_t)n * (L + 1);
+  std::vector<int> store(nvv, -1);
+  for (int i = 0; i < n; i++) store[i] = (*parts)[0][i];
+  auto lmin = [&](int ph) {  // min_or_0 (mpk2/buffers.c:68-77)
+    if (nphase == 0 || ph < 0) return 0;
+    return *std::min_element(levels[ph].begin(), levels[ph].end());
+  };
+  auto lmax = [&](int ph) {  // max_or_nlevel (mpk2/buffers.c:79-90)
+    if (ph == nphase) return L;
+    return std::min(L, *std::max_element(levels[ph].begin(), levels[ph].end()));
+  };
+  std::vector<std::vector<Triple>> ct(nphase + 1);
+  std::vector<std::vector<std::vector<long>>> mlist(nphase + 1, std::vector<std::vector<long>>(P));
+  int err = 0;
+  auto proc = [&](int cur, int i, int level, std::vector<Triple> &t) {
+    for (int j = g.ptr[i]; j < g.ptr[i + 1]; j++) {
+      const long kv = (long)n * (level - 1) + g.col[j];
+      const int sp = store[kv];
+      if (sp == -1) err = 1;
+      else if (sp != cur) t.push_back({sp, cur, kv});
+    }
+  };
+  std::vector<Triple> init;
+  for (int i = 0; i < n; i++) init.push_back({(*parts)[0][i], (*parts)[0][i], (long)i});
+  for (int ph = 0; ph < nphase; ph++) {
+    const std::vector<int> &ll = levels[ph];
+    const int *prevl = ph ? levels[ph - 1].data() : nullptr;
+    const int lo = lmin(ph - 1), hi = lmax(ph);
+    if (ph > 0) {  // collect_comm + reduce_comm (mpk2/buffers.c:92-123, reduce_comm.c:44-59)
+      std::vector<Triple> cc;
+      for (int level = lo + 1; level <= hi; level++)
+        for (int i = 0; i < n; i++)
+          if (prevl[i] < level && level <= ll[i]) {
+            const int tgt = (*parts)[ph][i];
+            for (int j = g.ptr[i]; j < g.ptr[i + 1]; j++) {
+              const long kv = (long)n * (level - 1) + g.col[j];
+              if (store[kv] != -1) cc.push_back({store[kv], tgt, kv});
+            }
+          }
+      unique_triples(&cc);
+      std::vector<long> sums((size_t)P * P, 0);
+      for (const Triple &t : cc) sums[(size_t)t.src * P + t.tgt]++;
+      std::vector<int> perm;
+      assign_max_trace(sums, P, &perm);
+      for (int &q : (*parts)[ph]) q = perm[q];
+    }
+    std::vector<Triple> &t = ct[ph];
+    if (ph == 0) t = init;
+    for (int level = lo + 1; level <= hi; level++)
+      for (int i = 0; i < n; i++) {
+        const int pv = prevl ? prevl[i] : 0;
+        if (pv < level && level <= ll[i] && store[(size_t)level * n + i] == -1) {
+          const int cur = (*parts)[ph][i];
+          proc(cur, i, level, t);
+          store[(size_t)level * n + i] = cur;
+          mlist[ph][cur].push_back((long)level * n + i);
+        }
+      }
+  }
+  {  // skirt_comm_table + iterator(skirt_cond) (mpk2/buffers.c:155-179, 203-238)
+    std::vector<Triple> &t = ct[nphase];
+    if (nphase == 0) t = init;
+    const int *prevl = nphase ? levels[nphase - 1].data() : nullptr;
+    const int lo = lmin(nphase - 1);
+    for (int p = 0; p < P; p++)
+      for (int level = lo + 1; level <= L; level++)
+        for (size_t q = 0; q < sk[p].vert.size(); q++) {
+          const int i = sk[p].vert[q], d = sk[p].dist[q];
+          const int pv = prevl ? prevl[i] : 0;
+          if (pv < level && d >= 0 && level <= L - d) {
+            proc(p, i, level, t);
+            store[(size_t)level * n + i] = p;
+            mlist[nphase][p].push_back((long)level * n + i);
+          }
+        }
+  }
+  if (err) return fail(kEStruct, "a needed value is computed by no part (inconsistent levels/skirt)");
+  for (auto &t : ct) unique_triples(&t);
+  out->assign(P, RankBuffers());
+  for (int r = 0; r < P; r++) {
+    RankBuffers &b = (*out)[r];
+    b.n = n; b.npart = P; b.nlevel = L; b.nphase = nphase; b.rank = r;
+    const size_t np = (size_t)P * (nphase + 1), ph1 = nphase + 1;
+    b.recvcounts.assign(np, 0); b.sendcounts.assign(np, 0); b.rdispls.assign(np, 0); b.sdispls.assign(np, 0);
+    for (auto *v : {&b.rcount, &b.mcount, &b.scount, &b.rbuf_offsets, &b.mbuf_offsets, &b.sbuf_offsets,
+                    &b.mptr_offsets, &b.mcol_offsets})
+      v->assign(ph1, 0);
+    std::vector<std::vector<long>> rlist(ph1), slist(ph1);
+    for (int ph = 0; ph <= nphase; ph++) {
+      // fill_idx_rsbuf order (mpk2/buffers.c:354-377): by peer, then vv index
+      for (const Triple &t : ct[ph])
+        if (t.tgt == r) { rlist[ph].push_back(t.v); b.recvcounts[(size_t)P * ph + t.src]++; }
+      std::vector<Triple> sends;
+      for (const Triple &t : ct[ph])
+        if (t.src == r) sends.push_back(t);
+      std::sort(sends.begin(), sends.end(), [](const Triple &a, const Triple &c) {
+        return a.tgt != c.tgt ? a.tgt < c.tgt : a.v < c.v;
+      });
+      for (const Triple &t : sends) { slist[ph].push_back(t.v); b.sendcounts[(size_t)P * ph + t.tgt]++; }
+      // by_tgt sorted the receive list by (src, v) within tgt == r
+      b.rcount[ph] = (int)rlist[ph].size();
+      b.scount[ph] = (int)slist[ph].size();
+      b.mcount[ph] = (int)mlist[ph][r].size();
+      for (int q = 1; q < P; q++) {
+        const size_t k = (size_t)P * ph + q;
+        b.sdispls[k] = b.sdispls[k - 1] + b.sendcounts[k - 1];
+        b.rdispls[k] = b.rdispls[k - 1] + b.recvcounts[k - 1];
+      }
+    }
+    // alloc_bufs (mpk2/buffers.c:317-352)
+    long count = 0, scount = 0, mptrcount = 0;
+    for (int ph = 0; ph <= nphase; ph++) {
+      b.rbuf_offsets[ph] = (int)count;
+      count += b.rcount[ph];
+      b.mbuf_offsets[ph] = (int)count;
+      count += b.mcount[ph];
+      b.sbuf_offsets[ph] = (int)scount;
+      scount += b.scount[ph];
+      b.mptr_offsets[ph] = (int)mptrcount;
+      mptrcount += b.mcount[ph] + 1;
+    }
+    b.buf_count = (int)count;
+    b.buf_scount = (int)scount;
+    b.mptr_count = (int)mptrcount;
+    b.idx_buf.clear();
+    b.idx_sbuf.clear();
+    b.mptr_buf.clear();
+    for (int ph = 0; ph <= nphase; ph++) {
+      b.idx_buf.insert(b.idx_buf.end(), rlist[ph].begin(), rlist[ph].end());
+      b.idx_buf.insert(b.idx_buf.end(), mlist[ph][r].begin(), mlist[ph][r].end());
+      b.idx_sbuf.insert(b.idx_sbuf.end(), slist[ph].begin(), slist[ph].end());
+      long acc = 0;  // fill_mptr (mpk2/buffers.c:379-390)
+      b.mptr_buf.push_back(0);
+      for (long idx : mlist[ph][r]) {
+        const int i = (int)(idx % n);
+        acc += g.ptr[i + 1] - g.ptr[i];
+        b.mptr_buf.push_back(acc);
+      }
+    }
+    // fill_mcol_sbuf (mpk2/buffers.c:413-474): columns and send entries
+    // become positions of the first occurrence in idx_buf
+    std::unordered_map<long, long> find;
+    find.reserve(b.idx_buf.size() * 2);
+    for (size_t i = 0; i < b.idx_buf.size(); i++) find.emplace(b.idx_buf[i], (long)i);
+    auto first = [&](long v) {
+      auto it = find.find(v);
+      return it == find.end() ? -1L : it->second;
+    };
+    long mcol_count = 0;
+    b.mcol_buf.clear();
+    b.mval_buf.clear();
+    for (int ph = 0; ph <= nphase; ph++) {
+      b.mcol_offsets[ph] = (int)mcol_count;
+      for (long idx : mlist[ph][r]) {
+        const long i = idx % n, level = idx / n;
+        for (int j = g.ptr[i]; j < g.ptr[i + 1]; j++) {
+          b.mcol_buf.push_back(first(g.col[j] + (long)n * (level - 1)));
+          if (!g.val.empty()) b.mval_buf.push_back(g.val[j]);  // alloc_fill_mval (mpi2_mpkwrtbufs.c:12-29)
+        }
+      }
+      mcol_count = (long)b.mcol_buf.size();
+    }
+    b.mcol_count = (int)mcol_count;
+    for (long &v : b.idx_sbuf) v = first(v);
   }
   return kOk;
 }

@@ -718,6 +718,37 @@ __global__ void split_kernel(const double *__restrict__ src, float2 *__restrict_
     dst[i] = df_split(src[i]);
 }
 
+// ------------------------------------------------------------------------
+// MPI-2 rank buffers on one GPU.  Every rank's vv_buf lives in one device
+// array; a phase's computation is one launch with one CTA per rank (level
+// segments separated by barriers, rows summed in CSR order), and the
+// phase's MPI_Alltoallv (mpk2/mpi2_mpkexecbufs_val.c:32-48) becomes one
+// gather: receive slot <- the sender's send-list entry.
+// ------------------------------------------------------------------------
+__global__ void gather_map_kernel(const double *__restrict__ src, const long *__restrict__ sidx,
+                                  double *__restrict__ dst, const long *__restrict__ didx, long cnt) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < cnt; t += (long)gridDim.x * blockDim.x)
+    dst[didx[t]] = src[sidx[t]];
+}
+
+template <int ARITH>
+__global__ void __launch_bounds__(256) bufs_phase_kernel(int list_base, const long *__restrict__ list_seg,
+                                                         const long *__restrict__ seg_off,
+                                                         const long *__restrict__ row_dst,
+                                                         const long *__restrict__ row_ptr,
+                                                         const long *__restrict__ gcol,
+                                                         const double *__restrict__ gval, double *vall) {
+  const int list = list_base + blockIdx.x;
+  for (long sg = list_seg[list]; sg < list_seg[list + 1]; sg++) {
+    for (long q = seg_off[sg] + threadIdx.x; q < seg_off[sg + 1]; q += blockDim.x) {
+      double s = 0.0;
+      for (long j = row_ptr[q]; j < row_ptr[q + 1]; j++) s = row_term<ARITH>(s, gval[j], vall[gcol[j]]);
+      vall[row_dst[q]] = s;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void copy_kernel(const double *__restrict__ src, double *__restrict__ dst, long n) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     dst[i] = src[i];
@@ -759,6 +790,15 @@ struct mpkg_plan {
   PipeArgs pipe{};
   int pipe_grid = 0, pipe_reach = 0;
   size_t pipe_smem_bytes = 0;
+  // MPI-2 rank buffers
+  double *b_vall = nullptr;
+  long *b_in_dst = nullptr, *b_in_src = nullptr, *b_out_src = nullptr, *b_out_dst = nullptr;
+  long b_nin = 0, b_nout = 0;
+  long *b_cm_dst = nullptr, *b_cm_src = nullptr;
+  std::vector<long> b_cm_off;  // per phase: range of the comm gather
+  long *b_list_seg = nullptr, *b_seg_off = nullptr, *b_row_dst = nullptr, *b_row_ptr = nullptr,
+       *b_gcol = nullptr;
+  double *b_gval = nullptr;
   uint32_t epoch = 0;
   int launches = 0;
   std::vector<double> h_x;  // x staging when a tasks plan leaves entries uncovered
@@ -1070,6 +1110,25 @@ int plan_launch(mpkg_plan *p, double *d_vv, cudaStream_t st) {
       p->launches = 1;
       break;
     }
+    case MPKG_EXEC_BUFS: {
+      const int P = p->npart;
+      if (p->b_nin) gather_map_kernel<<<592, 256, 0, st>>>(d_vv, p->b_in_src, p->b_vall, p->b_in_dst, p->b_nin);
+      for (int ph = 0; ph <= p->nphase; ph++) {
+        const long c0 = p->b_cm_off[ph], c1 = p->b_cm_off[ph + 1];
+        if (ph > 0 && c1 > c0)
+          gather_map_kernel<<<592, 256, 0, st>>>(p->b_vall, p->b_cm_src + c0, p->b_vall, p->b_cm_dst + c0, c1 - c0);
+        if (p->arith == MPKG_ARITH_SEPARATE)
+          bufs_phase_kernel<MPKG_ARITH_SEPARATE><<<P, 256, 0, st>>>(ph * P, p->b_list_seg, p->b_seg_off,
+                                                                   p->b_row_dst, p->b_row_ptr, p->b_gcol,
+                                                                   p->b_gval, p->b_vall);
+        else
+          bufs_phase_kernel<MPKG_ARITH_FMA><<<P, 256, 0, st>>>(ph * P, p->b_list_seg, p->b_seg_off, p->b_row_dst,
+                                                              p->b_row_ptr, p->b_gcol, p->b_gval, p->b_vall);
+      }
+      if (p->b_nout) gather_map_kernel<<<592, 256, 0, st>>>(p->b_vall, p->b_out_src, d_vv, p->b_out_dst, p->b_nout);
+      p->launches = 2 + 2 * p->nphase + 1;
+      break;
+    }
     case MPKG_EXEC_SPMV: {
       int rc = launch_spmv(p->n, p->d_ptr, p->d_col, p->d_coef, p->valued, p->nlevel, d_vv, p->arith, st);
       if (rc) return rc;
@@ -1289,6 +1348,121 @@ int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val, int
   return kOk;
 }
 
+int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out) {
+  clear_error();
+  if (!out || !dir || npart <= 0) return fail(kEInval, "bad argument");
+  *out = nullptr;
+  if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE)
+    return fail(kEInval, "rank buffers run in FP64 (fma or separate)");
+  std::vector<RankBuffers> bufs(npart);
+  int rc;
+  for (int r = 0; r < npart; r++)
+    if ((rc = read_rank_buffers(std::string(dir) + "/rank" + std::to_string(r) + ".bufs", &bufs[r]))) return rc;
+  if ((rc = check_rank_buffers(bufs))) return rc;
+  const int n = bufs[0].n, nlevel = bufs[0].nlevel, nphase = bufs[0].nphase, P = npart;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  p->exec = MPKG_EXEC_BUFS;
+  p->n = n; p->nlevel = nlevel; p->nphase = nphase; p->npart = P;
+  p->arith = arith; p->valued = true;
+  rc = cudaGetDevice(&p->device) == cudaSuccess ? kOk : fail(kECuda, "cudaGetDevice failed");
+  if (!rc && cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(kECuda, "stream creation failed");
+  std::vector<long> off(P + 1, 0);
+  for (int r = 0; r < P; r++) off[r + 1] = off[r] + bufs[r].buf_count;
+  // input gather, output scatter
+  std::vector<long> in_dst, in_src, out_src, out_dst;
+  for (int r = 0; r < P; r++) {
+    const RankBuffers &b = bufs[r];
+    for (int i = 0; i < b.rcount[0]; i++) {
+      in_dst.push_back(off[r] + b.rbuf_offsets[0] + i);
+      in_src.push_back(b.idx_buf[b.rbuf_offsets[0] + i]);
+    }
+    for (int i = 0; i < b.buf_count; i++) {
+      out_src.push_back(off[r] + i);
+      out_dst.push_back(b.idx_buf[i]);
+    }
+  }
+  // communication per phase: receive slot of dst from src's send list
+  std::vector<long> cm_dst, cm_src, cm_off(nphase + 2, 0);
+  for (int ph = 0; ph <= nphase; ph++) {
+    cm_off[ph] = (long)cm_dst.size();
+    if (ph == 0) continue;
+    for (int dst = 0; dst < P; dst++)
+      for (int src = 0; src < P; src++) {
+        const long k = (long)P * ph;
+        const int cnt = bufs[dst].recvcounts[k + src];
+        for (int t = 0; t < cnt; t++) {
+          cm_dst.push_back(off[dst] + bufs[dst].rbuf_offsets[ph] + bufs[dst].rdispls[k + src] + t);
+          cm_src.push_back(off[src] + bufs[src].idx_sbuf[bufs[src].sbuf_offsets[ph] + bufs[src].sdispls[k + dst] + t]);
+        }
+      }
+  }
+  cm_off[nphase + 1] = (long)cm_dst.size();
+  // computation rows, segmented per (phase, rank) by level
+  std::vector<long> list_seg((size_t)(nphase + 1) * P + 1, 0), seg_off, row_dst, row_ptr(1, 0), gcol;
+  std::vector<double> gval;
+  long rows_total = 0;
+  for (int ph = 0; ph <= nphase; ph++)
+    for (int r = 0; r < P; r++) {
+      const RankBuffers &b = bufs[r];
+      list_seg[(size_t)ph * P + r] = (long)seg_off.size();
+      const long *idx_m = b.idx_buf.data() + b.mbuf_offsets[ph];
+      const long *mptr = b.mptr_buf.data() + b.mptr_offsets[ph];
+      const long *mcol = b.mcol_buf.data() + b.mcol_offsets[ph];
+      const double *mval = b.mval_buf.data() + b.mcol_offsets[ph];
+      long cur = -1;
+      for (int mi = 0; mi < b.mcount[ph]; mi++) {
+        const long level = idx_m[mi] / n;
+        if (level < cur) { rc = rc ? rc : fail(kEFormat, "rank buffer rows are not level-major"); break; }
+        if (level != cur) {
+          seg_off.push_back((long)row_dst.size());
+          cur = level;
+        }
+        row_dst.push_back(off[r] + b.mbuf_offsets[ph] + mi);
+        for (long mj = mptr[mi]; mj < mptr[mi + 1]; mj++) {
+          gcol.push_back(off[r] + mcol[mj]);
+          gval.push_back(mval[mj]);
+        }
+        row_ptr.push_back((long)gcol.size());
+        rows_total++;
+      }
+    }
+  list_seg[(size_t)(nphase + 1) * P] = (long)seg_off.size();
+  seg_off.push_back((long)row_dst.size());
+  p->rows_computed = rows_total;
+  p->nnz = (long)gcol.size();
+  if (!rc) rc = dev_alloc(p, &p->b_vall, std::max<long>(off[P], 1));
+  if (!rc) rc = dev_copy(p, &p->b_in_dst, in_dst.data(), in_dst.size());
+  if (!rc) rc = dev_copy(p, &p->b_in_src, in_src.data(), in_src.size());
+  if (!rc) rc = dev_copy(p, &p->b_out_src, out_src.data(), out_src.size());
+  if (!rc) rc = dev_copy(p, &p->b_out_dst, out_dst.data(), out_dst.size());
+  if (!rc) rc = dev_copy(p, &p->b_cm_dst, cm_dst.data(), cm_dst.size());
+  if (!rc) rc = dev_copy(p, &p->b_cm_src, cm_src.data(), cm_src.size());
+  if (!rc) rc = dev_copy(p, &p->b_list_seg, list_seg.data(), list_seg.size());
+  if (!rc) rc = dev_copy(p, &p->b_seg_off, seg_off.data(), seg_off.size());
+  if (!rc) rc = dev_copy(p, &p->b_row_dst, row_dst.data(), row_dst.size());
+  if (!rc) rc = dev_copy(p, &p->b_row_ptr, row_ptr.data(), row_ptr.size());
+  if (!rc) rc = dev_copy(p, &p->b_gcol, gcol.data(), gcol.size());
+  if (!rc) rc = dev_copy(p, &p->b_gval, gval.data(), gval.size());
+  if (!rc) rc = dev_alloc(p, &p->d_err, 1);
+  if (!rc && cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) rc = fail(kECuda, "memset failed");
+  p->b_nin = (long)in_dst.size();
+  p->b_nout = (long)out_src.size();
+  p->b_cm_off = cm_off;
+  // every (level, vertex) of levels 1..nlevel must be produced by some rank
+  std::vector<unsigned char> cov((size_t)n * (nlevel + 1), 0);
+  for (long v : out_dst) cov[(size_t)v] = 1;
+  p->full_coverage = true;
+  for (size_t e = (size_t)n; e < cov.size(); e++)
+    if (!cov[e]) { p->full_coverage = false; break; }
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
 int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels) {
   if (!p || p->exec != MPKG_EXEC_PIPE || extra_levels < 0 || extra_levels > 1000)
     return fail(kEInval, "stall hook needs a pipeline plan and 0 <= extra <= 1000");
@@ -1305,7 +1479,8 @@ int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info) {
   info->rows_computed = p->rows_computed;
   info->device_bytes = p->device_bytes;
   info->launches = p->exec == MPKG_EXEC_TASKS ? p->nphase + 1
-                   : p->exec == MPKG_EXEC_SPMV ? p->nlevel : 1;
+                   : p->exec == MPKG_EXEC_SPMV ? p->nlevel
+                   : p->exec == MPKG_EXEC_BUFS ? 2 + 2 * p->nphase + 1 : 1;
   info->tiles_in_smem = p->tiles_smem ? 1 : 0;
   info->max_tile_slots = p->max_tile_slots;
   info->pipe_chunk = p->pipe.chunk;

@@ -171,5 +171,18 @@ int write_rank_buffers(const std::string &path, const RankBuffers &b);
 // Checks the internal consistency of a set of rank buffers (counts,
 // offsets, index ranges, matching send/receive counts).
 int check_rank_buffers(const std::vector<RankBuffers> &bufs);
+// The MPI-2 prep of every rank (fill_buffers + alloc_fill_mval,
+// mpk2/buffers.c:573-586, mpk2/mpi2_mpkwrtbufs.c:12-29), computed for all
+// ranks at once with sparse communication sets instead of the reference's
+// dense level*n*P*P table.  g: the matrix with values (loop.g0 +
+// .loop.val); parts: max(nphase,1) partitions (relabelled in place for
+// phases > 0, as reduce_comm does); levels: nphase level arrays; sk: the
+// skirt of every part as read from s<nphase>.
+int fill_all_buffers(const Csr &g, int npart, int nlevel, int nphase, std::vector<std::vector<int>> *parts,
+                     const std::vector<std::vector<int>> &levels, const std::vector<PartSkirt> &sk,
+                     std::vector<RankBuffers> *out);
+// Linear assignment maximising the trace: perm[j] = row assigned to column
+// j of the npart x npart matrix sums (row-major).
+void assign_max_trace(const std::vector<long> &sums, int npart, std::vector<int> *perm);
 
 }  // namespace mpkg

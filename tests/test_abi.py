@@ -104,3 +104,30 @@ def test_reference_tools_relink_against_library(tool):
             subprocess.run([exe] + r + [os.path.join(d, "mine")], check=True, stdout=subprocess.DEVNULL)
             subprocess.run([O.ref_tool(tool)] + r + [os.path.join(d, "ref")], check=True, stdout=subprocess.DEVNULL)
             assert open(os.path.join(d, "mine"), "rb").read() == open(os.path.join(d, "ref"), "rb").read()
+
+
+@pytest.mark.skipif(not O.ref_available() or not os.path.isdir("/root/reference/mpk2"),
+                    reason="reference sources not present")
+def test_reference_mpi2_prep_relinks_against_library(monkeypatch):
+    """The reference's own mpi2_mpkwrtbufs.c main, compiled against
+    include/mpk2_compat.h (plus the single-process mpi.h stand-in) and
+    linked with libmpk_gb300.so, writes the same rank buffers as the
+    reference build."""
+    from conftest import golden_matrix, load_golden
+    name = "m5p20_4_4_2"
+    g = load_golden(name)
+    a = golden_matrix(name)
+    with tempfile.TemporaryDirectory() as d:
+        for hdr in ("lib.h", "comm_data.h", "buffers.h"):
+            open(os.path.join(d, hdr), "w").write('#include "mpk2_compat.h"\n')
+        exe = os.path.join(d, "wrtbufs")
+        subprocess.run(["gcc", "-O2", "-w", "-I", d, "-I", os.path.join(ROOT, "include"), "-I",
+                        os.path.join(ROOT, "oracle", "refshim"), "/root/reference/mpk2/mpi2_mpkwrtbufs.c", "-o", exe,
+                        M.LIB_PATH, "-Wl,-rpath," + os.path.dirname(M.LIB_PATH)], check=True)
+        from test_prep import _case_dir
+        _case_dir(name, g, a, d)
+        monkeypatch.chdir(d)
+        for r in range(int(g["npart"])):
+            subprocess.run([exe, name], check=True, env=dict(os.environ, MPK_RANK=str(r)), stdout=subprocess.DEVNULL)
+            mine = np.fromfile(os.path.join(d, name, f"rank{r}.bufs"), dtype=np.uint8)
+            assert mine.tobytes() == g[f"bufs{r}"].tobytes(), f"rank {r}"

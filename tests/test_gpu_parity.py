@@ -4,6 +4,8 @@ against the oracle (bit for bit in FMA arithmetic), plus the FP64 tolerance
 of the task (1e-13 relative per power vector) and full-size checks on the
 128^3 7-point workload."""
 import hashlib
+import os
+import tempfile
 
 import numpy as np
 import pytest
@@ -186,3 +188,30 @@ def test_pipeline_wait_times_out_and_recovers(gpu):
     plan.debug_stall(0)
     want = O.mpk(a.ptr, a.col, a.val, x, 4, O.MODE_FMA)
     assert _run(plan, x, a.n, 4).tobytes() == want.tobytes()
+
+
+def _bufs_dir(g, d):
+    r = 0
+    while f"bufs{r}" in g:
+        g[f"bufs{r}"].tofile(os.path.join(d, f"rank{r}.bufs"))
+        r += 1
+    return r
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if c != "cfg1_4_4_0"])
+def test_rank_buffers_on_gpu_bitwise(name, gpu):
+    """The reference's MPI-2 rank buffers (written by its mpi2_mpkwrtbufs)
+    executed by one GPU launch per phase: bit-identical to the reference's
+    serial valued chain (the check of mpk2/run_script.sh:27), and to the
+    oracle's emulation of the MPI exec in FMA arithmetic."""
+    g = load_golden(name)
+    n, nlevel = int(g["n"]), int(g["nlevel"])
+    with tempfile.TemporaryDirectory() as d:
+        P = _bufs_dir(g, d)
+        plan = M.Plan.bufs(d, P, arith=M.ARITH_SEPARATE)
+        vv = _run(plan, g["x"], n, nlevel)
+        _check_bits(g, "vv_val", vv)
+        plan = M.Plan.bufs(d, P, arith=M.ARITH_FMA)
+        vv = _run(plan, g["x"], n, nlevel)
+        want = O.bufs_exec([os.path.join(d, f"rank{r}.bufs") for r in range(P)], g["x"], nlevel, O.MODE_FMA)
+        assert vv.tobytes() == want.tobytes()

@@ -164,3 +164,36 @@ def test_empty_part_pa1_tasks():
         sl = O.read_skirt(s, a.n, 4, 3)
     ro = O.prep_tasks(a.ptr, a.col, 4, 3, 0, part, None, sl)
     assert np.array_equal(off, ro[0]) and np.array_equal(idx, ro[1])
+
+
+def _case_dir(name, g, a, parent):
+    """The directory layout the reference's MPI-2 prep reads."""
+    d = os.path.join(parent, name)
+    os.makedirs(d)
+    npart, nphase = int(g["npart"]), int(g["nphase"])
+    a.write_metis(os.path.join(d, "loop.g0"), ne=(a.nnz + a.n) // 2)
+    a.write_values(os.path.join(parent, name.split("_")[0] + ".loop.val"))
+    for ph in range(max(nphase, 1)):
+        np.savetxt(os.path.join(d, f"g{ph}.part.{npart}"), g["parts"][ph], fmt="%d")
+    for ph in range(nphase):
+        np.savetxt(os.path.join(d, f"l{ph}"), g["levels"][ph], fmt="%d")
+    g["skirt"].tofile(os.path.join(d, f"s{nphase}"))
+    return d
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if c != "cfg1_4_4_0"])
+def test_mpi2_rank_buffers_byte_identical(name, monkeypatch):
+    """mpkg_bufs_prepare writes the same rank<r>.bufs files as the
+    reference's mpi2_mpkwrtbufs (fill_buffers + alloc_fill_mval), including
+    the partition relabelling of phases > 0."""
+    g = load_golden(name)
+    a = golden_matrix(name)
+    with tempfile.TemporaryDirectory() as parent:
+        _case_dir(name, g, a, parent)
+        monkeypatch.chdir(parent)
+        M.lib().mpkg_bufs_prepare.argtypes = [M.C.c_char_p]
+        rc = M.lib().mpkg_bufs_prepare(name.encode())
+        assert rc == 0, M.lib().mpkg_last_error().decode()
+        for r in range(int(g["npart"])):
+            mine = np.fromfile(os.path.join(parent, name, f"rank{r}.bufs"), dtype=np.uint8)
+            assert mine.tobytes() == g[f"bufs{r}"].tobytes(), f"rank {r}"
