@@ -62,6 +62,11 @@ extern "C" {
                              neighbours, matrix chunk kept in shared memory */
 #define MPKG_EXEC_SPMV 3  /* k separate SpMV launches (baseline) */
 #define MPKG_EXEC_BUFS 4  /* MPI-2 rank buffers of all ranks on one GPU */
+#define MPKG_EXEC_MIXED 5 /* mixed-precision pipeline (FP32/BF16 values) */
+
+/* Value storage of the mixed-precision form. */
+#define MPKG_VALUE_F32 0
+#define MPKG_VALUE_BF16 1
 
 typedef struct mpkg_plan mpkg_plan;
 
@@ -111,6 +116,23 @@ int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val,
  * from vv[0..n) into every rank's phase-0 receive buffer and collects every
  * rank's values into vv (collect_results, mpk2/mpi2_mpkexec.c:122-146). */
 int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out);
+
+/* Mixed-precision form (no counterpart in the reference's code; the
+ * precision pattern of the task): matrix values stored as FP32 or BF16
+ * (value_type), basis vectors FP32, FP32 accumulation in CSR order, every
+ * level scaled by 2^-e with 2^e >= ||A||_inf so the monomial basis cannot
+ * grow; the scaling is exact, A^l x = 2^(l*e) * v_l.  Same zero-redundancy
+ * pipeline as MPKG_EXEC_PIPE (requires the resident grid to cover
+ * (nlevel-1) x the matrix's dependency reach, else MPKG_ERANGE). */
+int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, int nlevel, int value_type,
+                    mpkg_plan **out);
+/* e of the plan's scaling and the number of values the storage type
+ * cannot represent exactly (0 means lossless, e.g. BF16 on stencils). */
+int mpkg_mixed_scale(const mpkg_plan *p, int *exponent, long *inexact_values);
+/* d_vv: (nlevel+1)*n floats on the device, x (pre-scaled as the caller
+ * wishes) in d_vv[0..n); writes v_1..v_nlevel.  Asynchronous; mpkg_sync
+ * reports device-side errors. */
+int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream);
 
 int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info);
 
@@ -205,6 +227,12 @@ int mpkg_gen_stencil(const char *type, int size, int *n, long *nnz, int **ptr, i
                      double **val);
 int mpkg_gen_laplacian(int nx, int ny, int nz, double diag, double off, int *n, long *nnz,
                        int **ptr, int **col, double **val, int **coords);
+/* Variable-coefficient diffusion with log-normal(0, sigma) edge
+ * coefficients (symmetric, diagonal = (1+dominance) * sum |off-diagonal|):
+ * nz <= 1 gives the 9-point operator on nx*ny with direction weights wx,
+ * wy, wdiag; nz > 1 the 7-point operator on nx*ny*nz (weights ignored). */
+int mpkg_gen_diffusion(int nx, int ny, int nz, double sigma, double wx, double wy, double wdiag,
+                       double dominance, uint64_t seed, int *n, long *nnz, int **ptr, int **col, double **val);
 void mpkg_uniform(uint64_t seed, long n, double *out);
 
 const char *mpkg_last_error(void);

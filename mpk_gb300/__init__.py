@@ -20,7 +20,8 @@ LIB_PATH = os.path.join(_HERE, "libmpk_gb300.so")
 
 OK, EINVAL, EIO, EFORMAT, ESTRUCT, ECUDA, ETIMEOUT, ENOMEM, ERANGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
 ARITH_FMA, ARITH_SEPARATE, ARITH_DF64 = 0, 1, 2
-EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS = 0, 1, 2, 3, 4
+EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS, EXEC_MIXED = 0, 1, 2, 3, 4, 5
+VALUE_F32, VALUE_BF16 = 0, 1
 
 _ERRNAMES = {EINVAL: "EINVAL", EIO: "EIO", EFORMAT: "EFORMAT", ESTRUCT: "ESTRUCT", ECUDA: "ECUDA",
              ETIMEOUT: "ETIMEOUT", ENOMEM: "ENOMEM", ERANGE: "ERANGE"}
@@ -82,6 +83,11 @@ def _declare(L):
         "mpkg_gen_stencil": (I, [C.c_char_p, I, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
         "mpkg_gen_laplacian": (I, [I, I, I, D, D, C.POINTER(I), C.POINTER(Lg), pp, pp, pp, pp]),
         "mpkg_uniform": (None, [C.c_uint64, Lg, P]),
+        "mpkg_gen_diffusion": (I, [I, I, I, D, D, D, D, D, C.c_uint64, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
+        "mpkg_plan_mixed": (I, [I, P, P, P, I, I, pp]),
+        "mpkg_mixed_scale": (I, [P, C.POINTER(I), C.POINTER(Lg)]),
+        "mpkg_exec_mixed_device": (I, [P, P, P]),
+        "mpkg_bufs_prepare": (I, [C.c_char_p]),
         "mpkg_last_error": (C.c_char_p, []),
         "mpkg_version": (I, []),
     }
@@ -175,6 +181,18 @@ class Csr:
         coords = _take(xp, 3 * n.value, np.int32).reshape(-1, 3)
         return Csr(_take(pp, n.value + 1, np.int32), _take(cp, nnz.value, np.int32),
                    _take(vp, nnz.value, np.float64), coords)
+
+    @staticmethod
+    def diffusion(nx, ny, nz=1, sigma=1.0, wx=1.0, wy=1.0, wdiag=1.0, dominance=0.01, seed=0):
+        """Variable-coefficient diffusion, log-normal(0, sigma) edge
+        coefficients: 9-point on nx*ny (nz == 1) or 7-point on nx*ny*nz."""
+        L = lib()
+        n, nnz = C.c_int(), C.c_long()
+        pp, cp, vp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(L.mpkg_gen_diffusion(nx, ny, nz, sigma, wx, wy, wdiag, dominance, seed, C.byref(n), C.byref(nnz),
+                                    C.byref(pp), C.byref(cp), C.byref(vp)))
+        return Csr(_take(pp, n.value + 1, np.int32), _take(cp, nnz.value, np.int32),
+                   _take(vp, nnz.value, np.float64))
 
     def write_metis(self, path, ne=None):
         with open(path, "w") as f:
@@ -291,6 +309,22 @@ class Plan:
         inf = p.info()
         p.n, p.nlevel = inf["n"], inf["nlevel"]
         return p
+
+    @classmethod
+    def mixed(cls, a: Csr, nlevel, value_type=VALUE_F32):
+        """Mixed-precision form: FP32/BF16 values, FP32 basis scaled by 2^-e
+        per level (A^l x = 2^(l e) v_l)."""
+        return cls._make(lib().mpkg_plan_mixed, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, value_type,
+                         a=a, nlevel=nlevel)
+
+    def mixed_scale(self):
+        """(e, number of values the storage type rounds)."""
+        e, inexact = C.c_int(), C.c_long()
+        _check(lib().mpkg_mixed_scale(self._h, C.byref(e), C.byref(inexact)))
+        return e.value, inexact.value
+
+    def exec_mixed_device(self, d_vv_ptr: int, stream: int = 0):
+        _check(lib().mpkg_exec_mixed_device(self._h, C.c_void_p(d_vv_ptr), C.c_void_p(stream or None)))
 
     @classmethod
     def spmv(cls, a: Csr, nlevel, arith=ARITH_FMA):

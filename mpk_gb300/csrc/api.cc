@@ -191,6 +191,19 @@ int mpkg_gen_laplacian(int nx, int ny, int nz, double diag, double offd, int *n,
   return kOk;
 }
 
+int mpkg_gen_diffusion(int nx, int ny, int nz, double sigma, double wx, double wy, double wdiag,
+                       double dominance, uint64_t seed, int *n, long *nnz, int **ptr, int **col, double **val) {
+  clear_error();
+  if (!n || !nnz || !ptr || !col || !val) return fail(kEInval, "null argument");
+  Csr g;
+  int rc = nz <= 1 ? gen_diffusion_9pt(nx, ny, sigma, wx, wy, wdiag, dominance, seed, &g)
+                   : gen_diffusion_7pt(nx, ny, nz, sigma, dominance, seed, &g);
+  if (rc) return rc;
+  *n = g.n; *nnz = g.nnz();
+  *ptr = dup(g.ptr); *col = dup(g.col); *val = dup(g.val);
+  return kOk;
+}
+
 void mpkg_uniform(uint64_t seed, long n, double *out) {
   if (out && n > 0) uniform_vector(seed, n, out);
 }

@@ -11,9 +11,11 @@
 //   spmv   - k separate SpMV launches (baseline, spmv_exec_*).
 // All executors evaluate each row sum over the stored columns in CSR order,
 // so for a given arithmetic mode every executor produces the same bits.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -383,7 +385,8 @@ __host__ __device__ __forceinline__ size_t pipe_vals_offset(int chunk, int max_n
   return pipe_cols_offset(chunk) + (((size_t)(max_nnz + 4) * sizeof(int) + 15) & ~(size_t)15);
 }
 __host__ __device__ __forceinline__ size_t pipe_smem_size(int chunk, int max_nnz, bool valued, size_t vsize) {
-  return pipe_vals_offset(chunk, max_nnz) + (valued ? (((size_t)max_nnz + 2) * vsize + 15) & ~(size_t)15 : 0);
+  return pipe_vals_offset(chunk, max_nnz) +
+         (valued ? (((size_t)max_nnz + 16 / vsize) * vsize + 15) & ~(size_t)15 : 0);
 }
 
 // One row sum in FP64 over the entries [q0, q1) in CSR order; rows of up
@@ -749,6 +752,84 @@ __global__ void __launch_bounds__(256) bufs_phase_kernel(int list_base, const lo
   }
 }
 
+// ------------------------------------------------------------------------
+// Mixed-precision pipeline: matrix values stored as FP32 or BF16, basis
+// vectors FP32, FP32 accumulation (FMA, CSR order).  Each level is scaled by
+// a fixed power of two 2^-e with 2^e >= ||A||_inf, so the stored basis
+// never grows (|v_l| <= |v_(l-1)|) and the scaling itself is exact; the
+// caller recovers A^l x = 2^(l e) v_l.  Chunk-affine schedule as
+// pipe_kernel: the chunk's columns and values are staged in shared memory
+// by bulk copies once and reused for every level.
+// ------------------------------------------------------------------------
+struct MixArgs {
+  int n, nlevel, chunk, nchunk;
+  uint32_t epoch;
+  const int *gdep_lo, *gdep_hi;
+  const int *ptr, *col;
+  const void *val;   // float or __nv_bfloat16, nnz entries
+  float *vv;         // (nlevel+1)*n FP32, x in vv[0..n)
+  float scale;       // 2^-e
+  unsigned int *ticket;
+  unsigned int *counts;
+  int *err;
+  int max_chunk_nnz;
+  bool bulk_ok;
+};
+
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <typename VT>
+__global__ void __launch_bounds__(kPipeThreads) mix_pipe_kernel(MixArgs m) {
+  extern __shared__ __align__(16) unsigned char pipe_smem[];
+  // reuse the FP64 pipeline's take/wait/publish through a PipeArgs view
+  PipeArgs a{};
+  a.n = m.n; a.nlevel = m.nlevel; a.chunk = m.chunk; a.nchunk = m.nchunk; a.ngroups = m.nchunk;
+  a.epoch = m.epoch; a.stall = 0; a.ptr = m.ptr; a.col = m.col; a.ticket = m.ticket; a.counts = m.counts;
+  a.err = m.err; a.max_chunk_nnz = m.max_chunk_nnz; a.bulk_ok = m.bulk_ok;
+  int *rptr = reinterpret_cast<int *>(pipe_smem);
+  int *cols_buf = reinterpret_cast<int *>(pipe_smem + pipe_cols_offset(m.chunk));
+  VT *vals_buf = reinterpret_cast<VT *>(pipe_smem + pipe_vals_offset(m.chunk, m.max_chunk_nnz));
+  __shared__ unsigned int s_chunk;
+  __shared__ int s_abort;
+  __shared__ __align__(8) unsigned long long s_bar;
+  unsigned phase = 0;
+  if (threadIdx.x == 0 && m.bulk_ok) mbar_init(&s_bar);
+  __syncthreads();
+  const VT *val = static_cast<const VT *>(m.val);
+  for (;;) {
+    int *cols;
+    VT *vals;
+    const int c = pipe_take<VT, true>(a, val, rptr, cols_buf, vals_buf, &cols, &vals, &s_bar, &phase, &s_chunk,
+                                      &s_abort);
+    if (c < 0) return;
+    const int r0 = c * m.chunk;
+    const int nr = min(m.chunk, m.n - r0);
+    const int r = threadIdx.x;
+    const bool active = r < nr;
+    const int q0 = rptr[r], q1 = active ? rptr[r + 1] : q0;
+    const int glo = m.gdep_lo[c], ghi = m.gdep_hi[c];
+    for (int l = 1; l <= m.nlevel; l++) {
+      if (l > 1 && !pipe_wait(a, glo, ghi, l - 1, &s_abort)) return;
+      const float *src = m.vv + (long)(l - 1) * m.n;
+      float s = 0.f;
+      if (q1 - q0 <= 12) {
+        float xv[12];
+#pragma unroll
+        for (int t = 0; t < 12; t++)
+          if (q0 + t < q1) xv[t] = src[cols[q0 + t]];
+#pragma unroll
+        for (int t = 0; t < 12; t++)
+          if (q0 + t < q1) s = __fmaf_rn(to_f32(vals[q0 + t]), xv[t], s);
+      } else {
+        for (int q = q0; q < q1; q++) s = __fmaf_rn(to_f32(vals[q]), src[cols[q]], s);
+      }
+      if (active) m.vv[(long)l * m.n + r0 + r] = s * m.scale;
+      pipe_publish(a, c, l);
+    }
+  }
+}
+
 __global__ void copy_kernel(const double *__restrict__ src, double *__restrict__ dst, long n) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     dst[i] = src[i];
@@ -790,6 +871,11 @@ struct mpkg_plan {
   PipeArgs pipe{};
   int pipe_grid = 0, pipe_reach = 0;
   size_t pipe_smem_bytes = 0;
+  // mixed-precision pipeline
+  MixArgs mix{};
+  int mix_vt = 0;    // 0: FP32 values, 1: BF16 values
+  int mix_e = 0;     // levels are scaled by 2^-mix_e
+  long mix_inexact = 0;  // values not exactly representable in the storage type
   // MPI-2 rank buffers
   double *b_vall = nullptr;
   long *b_in_dst = nullptr, *b_in_src = nullptr, *b_out_src = nullptr, *b_out_dst = nullptr;
@@ -1463,6 +1549,154 @@ int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out) {
   return kOk;
 }
 
+int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, int nlevel, int value_type,
+                    mpkg_plan **out) {
+  clear_error();
+  if (!out) return fail(kEInval, "out is null");
+  *out = nullptr;
+  if (!val) return fail(kEInval, "the mixed-precision form needs matrix values");
+  if (value_type != MPKG_VALUE_F32 && value_type != MPKG_VALUE_BF16) return fail(kEInval, "unknown value type");
+  int rc = check_csr(n, ptr, col);
+  if (rc) return rc;
+  if (nlevel <= 0 || nlevel > 31) return fail(kEInval, "nlevel must be in [1, 31]");
+  Csr g;
+  g.n = n;
+  g.ptr.assign(ptr, ptr + n + 1);
+  g.col.assign(col, col + ptr[n]);
+  PipePlan pp;
+  if ((rc = build_pipe_plan(g, nlevel, kPipeChunk, &pp))) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  p->exec = MPKG_EXEC_MIXED;
+  p->n = n; p->nlevel = nlevel; p->npart = pp.nchunk; p->valued = true; p->arith = -1;
+  p->nnz = ptr[n];
+  p->rows_computed = (long)n * nlevel;
+  p->mix_vt = value_type;
+  rc = cudaGetDevice(&p->device) == cudaSuccess ? kOk : fail(kECuda, "cudaGetDevice failed");
+  if (!rc && cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(kECuda, "stream creation failed");
+  // infinity norm -> power-of-two scale
+  double anorm = 0.0;
+  for (int i = 0; i < n; i++) {
+    double r = 0.0;
+    for (int j = ptr[i]; j < ptr[i + 1]; j++) r += std::fabs(val[j]);
+    anorm = std::max(anorm, r);
+  }
+  int e = 0;
+  if (anorm > 0) e = (int)std::ceil(std::log2(anorm));
+  p->mix_e = e;
+  MixArgs &m = p->mix;
+  m.n = n; m.nlevel = nlevel; m.chunk = kPipeChunk; m.nchunk = pp.nchunk;
+  m.scale = std::ldexp(1.0f, -e);
+  int maxnnz = 0;
+  for (int c = 0; c < pp.nchunk; c++) {
+    const int r1 = std::min(n, (c + 1) * kPipeChunk);
+    maxnnz = std::max(maxnnz, ptr[r1] - ptr[c * kPipeChunk]);
+  }
+  m.max_chunk_nnz = std::max(maxnnz, 1);
+  const size_t vsize = value_type == MPKG_VALUE_F32 ? 4 : 2;
+  p->pipe_smem_bytes = pipe_smem_size(kPipeChunk, m.max_chunk_nnz, true, vsize);
+  if (!rc) rc = dev_copy(p, &p->d_ptr, ptr, (size_t)n + 1);
+  if (!rc) rc = dev_copy(p, &p->d_col, col, (size_t)p->nnz);
+  if (!rc) {
+    if (value_type == MPKG_VALUE_F32) {
+      std::vector<float> v(p->nnz);
+      for (long j = 0; j < p->nnz; j++) {
+        v[j] = (float)val[j];
+        if ((double)v[j] != val[j]) p->mix_inexact++;
+      }
+      float *dv;
+      rc = dev_copy(p, &dv, v.data(), v.size());
+      m.val = dv;
+    } else {
+      std::vector<__nv_bfloat16> v(p->nnz);
+      for (long j = 0; j < p->nnz; j++) {
+        v[j] = __double2bfloat16(val[j]);
+        if ((double)__bfloat162float(v[j]) != val[j]) p->mix_inexact++;
+      }
+      __nv_bfloat16 *dv;
+      rc = dev_copy(p, &dv, v.data(), v.size());
+      m.val = dv;
+    }
+  }
+  std::vector<int> glo(pp.nchunk), ghi(pp.nchunk);
+  for (int c = 0; c < pp.nchunk; c++) { glo[c] = pp.dep_lo[c]; ghi[c] = pp.dep_hi[c]; }
+  int *dlo = nullptr, *dhi = nullptr;
+  unsigned *ticket = nullptr, *counts = nullptr;
+  if (!rc) rc = dev_copy(p, &dlo, glo.data(), glo.size());
+  if (!rc) rc = dev_copy(p, &dhi, ghi.data(), ghi.size());
+  if (!rc) rc = dev_alloc(p, &ticket, 1);
+  if (!rc) rc = dev_alloc(p, &counts, (size_t)(nlevel + 1) * pp.nchunk);
+  if (!rc) rc = dev_alloc(p, &p->d_err, 1);
+  if (!rc) {
+    cudaMemset(counts, 0, sizeof(unsigned) * (size_t)(nlevel + 1) * pp.nchunk);
+    cudaMemset(p->d_err, 0, sizeof(int));
+    m.gdep_lo = dlo; m.gdep_hi = dhi; m.ptr = p->d_ptr; m.col = p->d_col; m.ticket = ticket; m.counts = counts;
+    m.err = p->d_err;
+    m.bulk_ok = true;
+    p->pipe.counts = counts;  // reset path on errors
+    p->pipe.ngroups = pp.nchunk;
+    int maxsm = 0, per_sm = 0, nsm = 0;
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
+    if (p->pipe_smem_bytes > (size_t)maxsm) rc = fail(kERange, "chunk rows too dense for shared memory");
+    if (!rc) {
+      cudaError_t e1 = value_type == MPKG_VALUE_F32
+                           ? cudaFuncSetAttribute(mix_pipe_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)p->pipe_smem_bytes)
+                           : cudaFuncSetAttribute(mix_pipe_kernel<__nv_bfloat16>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->pipe_smem_bytes);
+      cudaError_t e2 = value_type == MPKG_VALUE_F32
+                           ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_pipe_kernel<float>, kPipeThreads,
+                                                                           p->pipe_smem_bytes)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_pipe_kernel<__nv_bfloat16>,
+                                                                           kPipeThreads, p->pipe_smem_bytes);
+      if (e1 != cudaSuccess || e2 != cudaSuccess) rc = fail(kECuda, "kernel attribute set-up failed");
+    }
+    if (!rc) {
+      const long grid = std::min<long>((long)per_sm * nsm, pp.nchunk);
+      p->pipe_grid = (int)grid;
+      p->pipe_reach = pp.reach;
+      if (grid < pp.nchunk && grid < (long)(nlevel - 1) * pp.reach + 1)
+        rc = fail(kERange, "matrix bandwidth too large for the mixed pipeline");
+    }
+  }
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
+int mpkg_mixed_scale(const mpkg_plan *p, int *exponent, long *inexact_values) {
+  if (!p || p->exec != MPKG_EXEC_MIXED) return fail(kEInval, "not a mixed-precision plan");
+  if (exponent) *exponent = p->mix_e;
+  if (inexact_values) *inexact_values = p->mix_inexact;
+  return kOk;
+}
+
+int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream) {
+  clear_error();
+  if (!p || p->exec != MPKG_EXEC_MIXED || !d_vv) return fail(kEInval, "not a mixed-precision plan, or null vv");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  p->epoch++;
+  if (p->epoch >= (1u << 30)) {
+    CUDA_TRY(cudaMemsetAsync(p->mix.counts, 0, sizeof(unsigned) * (size_t)(p->nlevel + 1) * p->mix.nchunk, st));
+    p->epoch = 1;
+  }
+  CUDA_TRY(cudaMemsetAsync(p->mix.ticket, 0, sizeof(unsigned), st));
+  MixArgs m = p->mix;
+  m.vv = d_vv;
+  m.epoch = p->epoch;
+  if (p->mix_vt == MPKG_VALUE_F32)
+    mix_pipe_kernel<float><<<p->pipe_grid, kPipeThreads, p->pipe_smem_bytes, st>>>(m);
+  else
+    mix_pipe_kernel<__nv_bfloat16><<<p->pipe_grid, kPipeThreads, p->pipe_smem_bytes, st>>>(m);
+  CUDA_TRY(cudaGetLastError());
+  p->launches = 1;
+  return kOk;
+}
+
 int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels) {
   if (!p || p->exec != MPKG_EXEC_PIPE || extra_levels < 0 || extra_levels > 1000)
     return fail(kEInval, "stall hook needs a pipeline plan and 0 <= extra <= 1000");
@@ -1504,7 +1738,7 @@ int mpkg_sync(mpkg_plan *p, void *stream) {
   CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
     cudaMemset(p->d_err, 0, sizeof(int));
-    if (p->exec == MPKG_EXEC_PIPE) {  // counters are inconsistent after an abort
+    if (p->exec == MPKG_EXEC_PIPE || p->exec == MPKG_EXEC_MIXED) {  // counters are inconsistent after an abort
       cudaMemset(p->pipe.counts, 0, sizeof(unsigned int) * (size_t)(p->nlevel + 1) * p->pipe.ngroups);
       p->epoch = 0;
     }

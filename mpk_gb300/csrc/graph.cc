@@ -1,4 +1,5 @@
 // Graph and matrix input/output and the synthetic matrix generators.
+#include <algorithm>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -302,6 +303,96 @@ void uniform_vector(uint64_t seed, long n, double *out) {
     double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
     out[i] = 2.0 * u - 1.0;
   }
+}
+
+}  // namespace mpkg
+
+namespace mpkg {
+
+namespace {
+// splitmix64 -> standard normal by Box-Muller (one value per call).
+struct Normal {
+  uint64_t s;
+  explicit Normal(uint64_t seed) : s(seed) {}
+  uint64_t next() {
+    s += 0x9E3779B97F4A7C15ULL;
+    uint64_t z = s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+  }
+  double uniform01() { return ((double)(next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+  double operator()() {
+    const double u1 = uniform01(), u2 = uniform01();
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+  }
+};
+
+// Assemble a symmetric operator from per-vertex neighbour offsets with a
+// coefficient per undirected edge.
+int assemble(long n, const std::vector<std::vector<std::pair<long, double>>> &nbr, double dominance, Csr *g) {
+  g->n = (int)n;
+  g->ptr.assign(n + 1, 0);
+  g->col.clear();
+  g->val.clear();
+  for (long i = 0; i < n; i++) {
+    std::vector<std::pair<long, double>> row = nbr[i];
+    double d = 0.0;
+    for (auto &e : row) d += std::fabs(e.second);
+    row.emplace_back(i, (1.0 + dominance) * d);
+    std::sort(row.begin(), row.end());
+    for (auto &e : row) {
+      g->col.push_back((int)e.first);
+      g->val.push_back(e.first == i ? e.second : -std::fabs(e.second));
+    }
+    g->ptr[i + 1] = (int)g->col.size();
+  }
+  return kOk;
+}
+}  // namespace
+
+int gen_diffusion_9pt(int nx, int ny, double sigma, double wx, double wy, double wdiag, double dominance,
+                      uint64_t seed, Csr *g) {
+  if (nx <= 0 || ny <= 0) return fail(kEInval, "grid sizes must be positive");
+  const long n = (long)nx * ny;
+  if (n * 9 > 0x7fffffffL) return fail(kERange, "grid too large for int32 indices");
+  Normal rnd(seed);
+  std::vector<std::vector<std::pair<long, double>>> nbr(n);
+  // forward edges: +x, +y, +x+y, -x+y (each undirected edge once)
+  const int dx[4] = {1, 0, 1, -1}, dy[4] = {0, 1, 1, 1};
+  const double w[4] = {wx, wy, wdiag, wdiag};
+  for (int y = 0; y < ny; y++)
+    for (int x = 0; x < nx; x++)
+      for (int d = 0; d < 4; d++) {
+        const int x2 = x + dx[d], y2 = y + dy[d];
+        if (x2 < 0 || x2 >= nx || y2 >= ny) continue;
+        const double c = w[d] * std::exp(sigma * rnd());
+        const long i = (long)y * nx + x, j = (long)y2 * nx + x2;
+        nbr[i].emplace_back(j, c);
+        nbr[j].emplace_back(i, c);
+      }
+  return assemble(n, nbr, dominance, g);
+}
+
+int gen_diffusion_7pt(int nx, int ny, int nz, double sigma, double dominance, uint64_t seed, Csr *g) {
+  if (nx <= 0 || ny <= 0 || nz <= 0) return fail(kEInval, "grid sizes must be positive");
+  const long n = (long)nx * ny * nz;
+  if (n * 7 > 0x7fffffffL) return fail(kERange, "grid too large for int32 indices");
+  Normal rnd(seed);
+  std::vector<std::vector<std::pair<long, double>>> nbr(n);
+  for (int z = 0; z < nz; z++)
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++) {
+        const long i = ((long)z * ny + y) * nx + x;
+        if (x + 1 < nx) { const double c = std::exp(sigma * rnd()); nbr[i].emplace_back(i + 1, c); nbr[i + 1].emplace_back(i, c); }
+        if (y + 1 < ny) { const double c = std::exp(sigma * rnd()); nbr[i].emplace_back(i + nx, c); nbr[i + nx].emplace_back(i, c); }
+        if (z + 1 < nz) {
+          const double c = std::exp(sigma * rnd());
+          nbr[i].emplace_back(i + (long)nx * ny, c);
+          nbr[i + (long)nx * ny].emplace_back(i, c);
+        }
+      }
+  return assemble(n, nbr, dominance, g);
 }
 
 }  // namespace mpkg

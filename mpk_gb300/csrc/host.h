@@ -59,6 +59,14 @@ int gen_reference_stencil(const std::string &type, int size, Csr *g);
 // when non-null (3 ints per vertex).
 int gen_laplacian(int nx, int ny, int nz, double diag, double off, Csr *g,
                   std::vector<int> *coords);
+// Variable-coefficient diffusion operators with log-normal edge
+// coefficients c_e = exp(sigma * N(0,1)) (seeded), symmetric, off-diagonal
+// -w_d c_e, diagonal (1 + dominance) * sum of |off-diagonals|, columns
+// ascending.  9-point on nx*ny (direction weights wx, wy, wdiag) and
+// 7-point on nx*ny*nz (wx = wy = wz = 1).
+int gen_diffusion_9pt(int nx, int ny, double sigma, double wx, double wy, double wdiag, double dominance,
+                      uint64_t seed, Csr *g);
+int gen_diffusion_7pt(int nx, int ny, int nz, double sigma, double dominance, uint64_t seed, Csr *g);
 // Uniform[-1, 1] doubles from a splitmix64 stream (seeded).
 void uniform_vector(uint64_t seed, long n, double *out);
 

@@ -1,0 +1,58 @@
+"""Mixed-precision form (FP32/BF16 values, FP32 basis with exact
+power-of-two level scaling): error per power against the FP64 oracle."""
+import numpy as np
+import pytest
+
+import mpk_gb300 as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-6  # relative error per power vector vs FP64 (FP32 storage)
+
+
+def run_mixed(a, k, value_type, x):
+    import torch
+    plan = M.Plan.mixed(a, k, value_type)
+    e, inexact = plan.mixed_scale()
+    d = torch.zeros((k + 1) * a.n, dtype=torch.float32, device="cuda")
+    d[:a.n] = torch.from_numpy(x.astype(np.float32)).cuda()
+    torch.cuda.synchronize()
+    plan.exec_mixed_device(d.data_ptr())
+    plan.sync()
+    v = d.cpu().numpy().astype(np.float64).reshape(k + 1, a.n)
+    return v * (2.0 ** (e * np.arange(k + 1)))[:, None], e, inexact
+
+
+def rel_errors(v, want, n, k):
+    w = want.reshape(k + 1, n)
+    return [float(np.linalg.norm(v[l] - w[l]) / np.linalg.norm(w[l])) for l in range(1, k + 1)]
+
+
+def test_mixed_fp32_diffusion_9pt(gpu):
+    a = M.Csr.diffusion(256, 256, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, seed=3)
+    x = M.uniform(4, a.n)
+    v, e, inexact = run_mixed(a, 8, M.VALUE_F32, x)
+    want = O.mpk(a.ptr, a.col, a.val, x, 8, O.MODE_FMA)
+    errs = rel_errors(v, want, a.n, 8)
+    assert max(errs) <= MIXED_TOL, errs
+    assert inexact > 0  # log-normal coefficients are not FP32 numbers
+
+
+def test_mixed_bf16_lossless_on_stencil(gpu):
+    """BF16 values are exact for stencil matrices (diagonal 6, off -1)."""
+    a = M.Csr.laplacian(48, 40, 32, diag=6.0, off=-1.0)
+    x = M.uniform(5, a.n)
+    v, e, inexact = run_mixed(a, 8, M.VALUE_BF16, x)
+    assert inexact == 0 and e == 4  # ||A||_inf = 12 -> 2^4
+    want = O.mpk(a.ptr, a.col, a.val, x, 8, O.MODE_FMA)
+    errs = rel_errors(v, want, a.n, 8)
+    assert max(errs) <= MIXED_TOL, errs
+
+
+def test_mixed_scaling_keeps_basis_bounded(gpu):
+    a = M.Csr.laplacian(64, 64, 16, diag=6.0, off=-1.0)
+    x = np.ones(a.n)
+    v, e, _ = run_mixed(a, 12, M.VALUE_F32, x)
+    raw = v / (2.0 ** (e * np.arange(13)))[:, None]
+    assert np.all(np.abs(raw) <= 1.0 + 1e-6)
