@@ -209,6 +209,72 @@ def cpu_reference_sample(a, part, nth, reps=3, sample_parts=256):
     return min(ts), int(off_s[-1]), owned * K_LEVELS, kind
 
 
+def time_mixed(plan, d_vv, steps, warmup, flush, stream):
+    import torch
+    for _ in range(warmup):
+        flush.fill_(1.0)
+        plan.exec_mixed_device(d_vv.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for e0, e1 in ev:
+            flush.fill_(1.0)
+            e0.record(stream)
+            plan.exec_mixed_device(d_vv.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+    plan.sync(stream.cuda_stream)
+    torch.cuda.synchronize()
+    return [e0.elapsed_time(e1) for e0, e1 in ev]
+
+
+def mixed_errors(v32, e, exact, n, k):
+    v = v32.astype(np.float64).reshape(k + 1, n) * (2.0 ** (e * np.arange(k + 1)))[:, None]
+    w = exact.reshape(k + 1, n)
+    return [float(np.linalg.norm(v[l] - w[l]) / np.linalg.norm(w[l])) for l in range(1, k + 1)]
+
+
+def bench_mixed(M, torch, a, x, k, exact, args, flush, stream):
+    """The precision pattern: FP32 / BF16 values with an FP32 basis on this
+    workload, and the 2048^2 9-point anisotropic diffusion (log-normal
+    coefficients) in FP32 against the plain FP64 pipeline on the same
+    matrix.  Errors are per power, relative, against FP64."""
+    out = {}
+    n = a.n
+    for name, vt in (("f32", M.VALUE_F32), ("bf16", M.VALUE_BF16)):
+        plan = M.Plan.mixed(a, k, vt)
+        e, inexact = plan.mixed_scale()
+        d = torch.zeros((k + 1) * n, dtype=torch.float32, device="cuda")
+        d[:n] = torch.from_numpy(x.astype(np.float32)).cuda()
+        t = statistics.mean(time_mixed(plan, d, min(args.steps, 100), args.warmup, flush, stream))
+        errs = mixed_errors(d.cpu().numpy(), e, exact, n, k)
+        out[f"cube128_{name}"] = {"ms_per_step": t, "value": k * n / (t * 1e-3) / 1e9, "rel_err_per_power": errs,
+                                  "values_rounded": inexact,
+                                  "bytes_per_call": a.nnz * (4 + (4 if vt == M.VALUE_F32 else 2)) + 4 * (n + 1) +
+                                  4 * n * (k + 1)}
+        plan.close()
+    # config 3: 2048^2 9-point anisotropic diffusion, log-normal(0,1) edges
+    b = M.Csr.diffusion(2048, 2048, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=3)
+    xb = M.uniform(3, b.n)
+    p64 = M.Plan.pipe(b, k)
+    d64 = torch.zeros((k + 1) * b.n, dtype=torch.float64, device="cuda")
+    d64[:b.n] = torch.from_numpy(xb).cuda()
+    t64 = statistics.mean(time_device(p64, d64, min(args.steps, 50), args.warmup, flush, stream))
+    ex64 = d64.cpu().numpy()
+    p64.close()
+    del d64
+    p32 = M.Plan.mixed(b, k, M.VALUE_F32)
+    e, inexact = p32.mixed_scale()
+    d32 = torch.zeros((k + 1) * b.n, dtype=torch.float32, device="cuda")
+    d32[:b.n] = torch.from_numpy(xb.astype(np.float32)).cuda()
+    t32 = statistics.mean(time_mixed(p32, d32, min(args.steps, 100), args.warmup, flush, stream))
+    errs = mixed_errors(d32.cpu().numpy(), e, ex64, b.n, k)
+    out["diffusion2048_9pt"] = {"n": b.n, "nnz": b.nnz, "fp64_pipe_ms": t64, "f32_ms": t32,
+                                "speedup_f32_vs_fp64": t64 / t32, "rel_err_per_power": errs,
+                                "value_f32": k * b.n / (t32 * 1e-3) / 1e9}
+    p32.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -218,6 +284,7 @@ def main():
     ap.add_argument("--exec", default="pipe", choices=["pipe", "tiles", "spmv", "tasks"])
     ap.add_argument("--arith", default="fma", choices=["fma", "separate", "df64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="time only the selected executor")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -255,12 +322,11 @@ def main():
     import mpk_gb300 as M
     torch.cuda.set_device(local)
     arith = {"fma": M.ARITH_FMA, "separate": M.ARITH_SEPARATE, "df64": M.ARITH_DF64}[args.arith]
-    mk = {"pipe": lambda: M.Plan.pipe(a, k, arith=arith),
-          "tiles": lambda: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TILES, arith=arith),
-          "tasks": lambda: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TASKS, arith=arith),
-          "spmv": lambda: M.Plan.spmv(a, k, arith=arith)}
-    plan = mk[args.exec]()
-    base = M.Plan.spmv(a, k, arith=M.ARITH_FMA) if args.exec != "spmv" else plan
+    mk = {"pipe": lambda ar: M.Plan.pipe(a, k, arith=ar),
+          "tiles": lambda ar: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TILES, arith=ar),
+          "tasks": lambda ar: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TASKS, arith=ar),
+          "spmv": lambda ar: M.Plan.spmv(a, k, arith=ar)}
+    plan = mk[args.exec](arith)
     info = plan.info()
     stream = torch.cuda.Stream()
     d_vv = torch.zeros((k + 1) * n, dtype=torch.float64, device="cuda")
@@ -279,8 +345,27 @@ def main():
     ms = statistics.mean(times)
     ms_max = reduce_max(world, ms)
     value = world * k * n / (ms_max * 1e-3) / 1e9
+    exact = d_vv.cpu().numpy()
 
-    base_ms = statistics.mean(time_device(base, d_vv, min(args.steps, 100), args.warmup, flush, stream))
+    # the other executors on the same workload, for the record
+    variants = {}
+    if not args.no_variants:
+        want = exact if args.arith != "df64" else None
+        for ex, ar in (("spmv", "fma"), ("pipe", "fma"), ("pipe", "df64"), ("tiles", "fma"), ("tiles", "df64")):
+            if ex == args.exec and ar == args.arith:
+                continue
+            vp = mk[ex]({"fma": M.ARITH_FMA, "df64": M.ARITH_DF64}[ar])
+            d2 = torch.zeros_like(d_vv)
+            d2[:n] = d_vv[:n]
+            t = statistics.mean(time_device(vp, d2, min(args.steps, 50), args.warmup, flush, stream))
+            got = d2.cpu().numpy()
+            ref = exact
+            err = max(float(np.linalg.norm(got[l * n:(l + 1) * n] - ref[l * n:(l + 1) * n]) /
+                            np.linalg.norm(ref[l * n:(l + 1) * n])) for l in range(1, k + 1))
+            variants[f"{ex}_{ar}"] = {"ms_per_step": t, "value": k * n / (t * 1e-3) / 1e9,
+                                      "rel_err_max_vs_headline": err}
+            vp.close()
+            del d2
 
     # end to end through the host API, pinned host buffers
     hv = torch.zeros((k + 1) * n, dtype=torch.float64).pin_memory()
@@ -294,17 +379,21 @@ def main():
         plan.exec_host(hnp)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_s = reduce_max(world, e2e_s)
-    # the device result of the timed runs equals the host run
-    same = bool(np.array_equal(d_vv.cpu().numpy(), hnp))
+    same = bool(np.array_equal(exact, hnp))
+
+    mixed = {} if args.no_variants else bench_mixed(M, torch, a, x, k, exact, args, flush, stream)
 
     peak, peak_kind = peaks()
     B = algorithmic_bytes(n, nnz, k)
     achieved = B / (ms * 1e-3) / 1e9
-    kname = {"pipe": "pipe_kernel", "tiles": "tiles_kernel", "tasks": "tasks_kernel",
+    kname = {"pipe": "flow_kernel", "tiles": "tiles_kernel", "tasks": "tasks_kernel",
              "spmv": "spmv_level_kernel"}[args.exec]
+    if args.arith == "df64":
+        kname = {"pipe": "flow_df_kernel", "tiles": "tiles_df_kernel"}.get(args.exec, kname)
     traffic = profile_traffic(kname)
     rows = info["rows_computed"]
     fp64_tflops = 2.0 * nnz * k * (rows / (n * k)) / (ms * 1e-3) / 1e12
+    base_ms = variants.get("spmv_fma", {}).get("ms_per_step")
 
     line = {"metric": "MPK powers/sec (FP64, k*n output rows per second)", "value": value,
             "unit": "Grow-powers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -317,9 +406,12 @@ def main():
                     "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n * k},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "algorithmic_bytes": B},
-            "fp64_pipe": {"achieved_tflops": fp64_tflops, "note": "2*nnz*k*redundancy flops over call time"},
-            "k_spmv_ms": base_ms, "speedup_vs_k_spmv": base_ms / ms,
+                         "algorithmic_bytes": B, "kernel": kname},
+            "fp64_pipe": {"achieved_tflops": fp64_tflops, "peak_tflops_measured": 1.19,
+                          "note": "2*nnz*k*redundancy FP64 flops over call time; GB300 FP64 FMA measured at "
+                                  "0.60 TFMA/s, so plain FP64 MPK cannot reach the HBM bound"},
+            "k_spmv_ms": base_ms, "speedup_vs_k_spmv": (base_ms / ms) if base_ms else None,
+            "variants": variants, "mixed": mixed,
             "gpu_launches": info["launches"] * args.steps,
             "clocks": clk.summary(), "wall_s_timed_region": wall, "host_device_agree": same,
             "plan": {kk: info[kk] for kk in ("rows_computed", "device_bytes", "pipe_reach", "pipe_grid",
