@@ -586,3 +586,122 @@ int orc_bufs_exec(int P, orc_bufs **b, const double *x, double *vv, int mode) {
   free(sb);
   return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* pdmpk buffers (pdmpk/buffers.h:30-166, written by Buffers::Dump,     */
+/* pdmpk/buffers.cc:194-224; vectors as size_t count + raw elements,   */
+/* pdmpk/utils.hpp DumpVec).                                            */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  size_t max_sbuf_size;
+  int mbuf_idx;
+  size_t n_mbuf_pb; size_t *mbuf_pb;
+  size_t n_home; int *home;
+  size_t n_orig; int *orig;
+  size_t n_pd; short *pd;            /* bottom, mid, top per phase */
+  size_t n_res; int *res_mbuf;
+  size_t n_sc; int *sendcounts, *sdispls, *recvcounts, *rdispls;
+  size_t n_sbi; int *sbuf_idcs; size_t n_sbpb; size_t *sbuf_pb;
+  size_t n_init; int *init; size_t n_initpb; size_t *init_pb;   /* (src, tgt) pairs */
+  size_t n_mptr; int *mptr; size_t n_mptrpb; size_t *mptr_pb;
+  size_t n_mcol; int *mcol; size_t n_mval; double *mval;
+  size_t n_rorig; int *rorig;        /* results.bin: original indices */
+} orc_pd;
+
+static void *rdvec(FILE *f, size_t elem, size_t *count) {
+  if (fread(count, sizeof(size_t), 1, f) != 1) return NULL;
+  void *p = malloc(elem * (*count + 1));
+  if (*count && fread(p, elem, *count, f) != *count) { free(p); return NULL; }
+  return p;
+}
+
+orc_pd *orc_pd_read(const char *buf_path, const char *res_path) {
+  FILE *f = fopen(buf_path, "rb");
+  if (!f) return NULL;
+  orc_pd *b = calloc(1, sizeof *b);
+  int ok = fread(&b->max_sbuf_size, sizeof(size_t), 1, f) == 1 && fread(&b->mbuf_idx, sizeof(int), 1, f) == 1;
+  ok = ok && (b->mbuf_pb = rdvec(f, sizeof(size_t), &b->n_mbuf_pb));
+  ok = ok && (b->home = rdvec(f, sizeof(int), &b->n_home));
+  ok = ok && (b->orig = rdvec(f, sizeof(int), &b->n_orig));
+  ok = ok && (b->pd = rdvec(f, 3 * sizeof(short), &b->n_pd));
+  ok = ok && (b->res_mbuf = rdvec(f, sizeof(int), &b->n_res));
+  size_t c1, c2, c3;
+  ok = ok && (b->sendcounts = rdvec(f, sizeof(int), &b->n_sc));
+  ok = ok && (b->sdispls = rdvec(f, sizeof(int), &c1)) && (b->recvcounts = rdvec(f, sizeof(int), &c2)) &&
+       (b->rdispls = rdvec(f, sizeof(int), &c3));
+  ok = ok && c1 == b->n_sc && c2 == b->n_sc && c3 == b->n_sc;
+  ok = ok && (b->sbuf_idcs = rdvec(f, sizeof(int), &b->n_sbi)) && (b->sbuf_pb = rdvec(f, sizeof(size_t), &b->n_sbpb));
+  ok = ok && (b->init = rdvec(f, 2 * sizeof(int), &b->n_init)) && (b->init_pb = rdvec(f, sizeof(size_t), &b->n_initpb));
+  ok = ok && (b->mptr = rdvec(f, sizeof(int), &b->n_mptr)) && (b->mptr_pb = rdvec(f, sizeof(size_t), &b->n_mptrpb));
+  ok = ok && (b->mcol = rdvec(f, sizeof(int), &b->n_mcol)) && (b->mval = rdvec(f, sizeof(double), &b->n_mval));
+  fclose(f);
+  if (!ok) return NULL;
+  f = fopen(res_path, "rb");
+  if (!f) return NULL;
+  b->rorig = rdvec(f, sizeof(int), &b->n_rorig);
+  fclose(f);
+  return b->rorig ? b : NULL;
+}
+
+/* All ranks of pdmpk's exec in one process: LoadInput with x (the
+ * reference loads 1.0, pdmpk/buffers.cc:353-358, here x[original_idcs]),
+ * then AsyncExec (pdmpk/buffers.cc:286-323) with every batch's
+ * MPI_Ialltoallv emulated by copies before the batch's DoComp
+ * (pdmpk/buffers.cc:242-263, partial sums seeded from init_idcs), then
+ * SendHome (pdmpk/buffers.cc:346-351) and the results scatter
+ * (Results::FillVal/FillResults, pdmpk/results.cc:16-29): out[i] = A^k x.
+ * Returns 0, or -1 on inconsistent buffers. */
+int orc_pd_exec(int P, orc_pd **b, const double *x, double *out, int mode) {
+  double **mb = malloc(sizeof(double *) * P), **sb = malloc(sizeof(double *) * P);
+  for (int p = 0; p < P; p++) {
+    mb[p] = calloc(b[p]->mbuf_idx + 1, sizeof(double));
+    sb[p] = calloc(b[p]->max_sbuf_size + 1, sizeof(double));
+    for (size_t i = 0; i < b[p]->mbuf_pb[0] && i < b[p]->n_orig; i++) mb[p][i] = x[b[p]->orig[i]];
+  }
+  size_t batch = 0;
+  for (size_t ph = 0; ph < b[0]->n_pd; ph++) {
+    const short bottom = b[0]->pd[3 * ph], top = b[0]->pd[3 * ph + 2];
+    for (int lvl = bottom; lvl < top; lvl++, batch++) {
+      const size_t off = (size_t)P * batch;
+      for (int p = 0; p < P; p++) {  /* fill send buffers */
+        if (off + P > b[p]->n_sc || batch + 1 >= b[p]->n_mptrpb) return -1;
+        const size_t sc = (size_t)b[p]->sendcounts[off + P - 1] + b[p]->sdispls[off + P - 1];
+        const int *si = b[p]->sbuf_idcs + b[p]->sbuf_pb[batch];
+        for (size_t i = 0; i < sc; i++) sb[p][i] = mb[p][si[i]];
+      }
+      for (int dst = 0; dst < P; dst++) {  /* Alltoallv into the batch's rbuf */
+        const size_t msz = b[dst]->mptr_pb[batch + 1] - b[dst]->mptr_pb[batch];
+        double *rbuf = mb[dst] + b[dst]->mbuf_pb[batch] + msz;
+        for (int src = 0; src < P; src++) {
+          const int cnt = b[dst]->recvcounts[off + src];
+          memcpy(rbuf + b[dst]->rdispls[off + src], sb[src] + b[src]->sdispls[off + dst], sizeof(double) * cnt);
+        }
+      }
+      for (int p = 0; p < P; p++) {  /* DoComp */
+        orc_pd *q = b[p];
+        const size_t mcount = q->mptr_pb[batch + 1] - q->mptr_pb[batch];
+        double *cur = mb[p] + q->mbuf_pb[batch];
+        const int *mp = q->mptr + q->mptr_pb[batch];
+        size_t ii = q->init_pb[batch];
+        for (size_t mi = 0; mi < mcount; mi++) {
+          double tmp = 0.0;
+          if (ii < q->init_pb[batch + 1] && q->mbuf_pb[batch] + mi == (size_t)q->init[2 * ii + 1]) {
+            tmp = mb[p][q->init[2 * ii]];
+            ii++;
+          }
+          for (int mj = mp[mi]; mj < mp[mi + 1]; mj++) tmp = row_term(tmp, q->mval[mj], mb[p][q->mcol[mj]], mode);
+          cur[mi] = tmp;
+        }
+      }
+    }
+  }
+  for (int p = 0; p < P; p++) {
+    for (size_t i = 0; i < b[p]->n_home; i++) mb[p][i] = mb[p][b[p]->home[i]];
+    for (size_t i = 0; i < b[p]->n_res && i < b[p]->n_rorig; i++) out[b[p]->rorig[i]] = mb[p][b[p]->res_mbuf[i]];
+    free(mb[p]);
+    free(sb[p]);
+  }
+  free(mb);
+  free(sb);
+  return 0;
+}

@@ -291,3 +291,25 @@ def bufs_exec(paths, x, nlevel, mode=MODE_FMA):
     if o.orc_bufs_exec(len(handles), arr, _p(xx), _p(vv), mode) != 0:
         raise ValueError("oracle: buffers without values")
     return vv
+
+
+# ---------------------------------------------------------------- pdmpk buffers
+def pd_exec(buf_paths, res_paths, x, mode=MODE_FMA):
+    """All ranks of pdmpk's exec emulated in one process (orc_pd_exec):
+    returns A^k x."""
+    o = lib()
+    o.orc_pd_read.restype = C.c_void_p
+    o.orc_pd_read.argtypes = [C.c_char_p, C.c_char_p]
+    o.orc_pd_exec.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    hs = []
+    for bp, rp in zip(buf_paths, res_paths):
+        h = o.orc_pd_read(bp.encode(), rp.encode())
+        if not h:
+            raise ValueError(f"oracle: cannot read {bp}")
+        hs.append(h)
+    arr = (C.c_void_p * len(hs))(*hs)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros(len(xx))
+    if o.orc_pd_exec(len(hs), arr, _p(xx), _p(out), mode) != 0:
+        raise ValueError("oracle: inconsistent pdmpk buffers")
+    return out
