@@ -63,6 +63,12 @@ extern "C" {
 #define MPKG_EXEC_SPMV 3  /* k separate SpMV launches (baseline) */
 #define MPKG_EXEC_BUFS 4  /* MPI-2 rank buffers of all ranks on one GPU */
 #define MPKG_EXEC_MIXED 5 /* mixed-precision pipeline (FP32/BF16 values) */
+#define MPKG_EXEC_PDMPK 6 /* pdmpk buffers of all ranks on one GPU */
+
+/* Partition providers of the pdmpk prep (mpkg_pdmpk_prep). */
+#define MPKG_PD_PART_BLOCKSHIFT 0 /* contiguous blocks, shifted by half a
+                                     block per call */
+#define MPKG_PD_PART_BFS 1        /* breadth-first recursive bisection */
 
 /* Value storage of the mixed-precision form. */
 #define MPKG_VALUE_F32 0
@@ -116,6 +122,40 @@ int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val,
  * from vv[0..n) into every rank's phase-0 receive buffer and collects every
  * rank's values into vv (collect_results, mpk2/mpi2_mpkexec.c:122-146). */
 int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out);
+
+/* pdmpk buffers (the buf.bin / results.bin pair of every rank that
+ * pdmpk's prep writes, pdmpk/buffers.cc:194-224, pdmpk/results.cc:36-46)
+ * run on one GPU; replaces loading them rank by rank and running
+ * Buffers::AsyncExec under MPI (apps/exec.cc, pdmpk/buffers.cc:120-191).
+ * Every batch is one device gather (the batch's MPI_Ialltoallv) and one
+ * launch over all ranks' rows (Buffers::DoComp with the init_idcs
+ * partial-sum seeds).  Execution loads x from vv[0..n) into every rank's
+ * mbuf (Buffers::LoadInput with the buffers' original_idcs) and writes
+ * A^nlevel x to vv[nlevel*n ..) (Results::FillResults); levels 1 ..
+ * nlevel-1 of vv are left untouched.  n and nlevel come from the buffers
+ * (plan info).  arith: MPKG_ARITH_SEPARATE is bit-identical to the
+ * reference's exec built without FMA contraction, MPKG_ARITH_FMA to one
+ * built with it. */
+int mpkg_plan_pdmpk(int npart, const char *const *buf_paths, const char *const *results_paths, int arith,
+                    mpkg_plan **out);
+
+/* The pdmpk prep of every rank (CommCompPatterns, pdmpk/
+ * comm_comp_patterns.cc:26-768, as apps/prep.cc runs it), written as
+ * buf_paths[r] / results_paths[r].  mirror_method 0..5 and
+ * weight_update_method 0..3 as the reference's --mirror / --weight;
+ * partitioner MPKG_PD_PART_* stands in for METIS_PartGraphKway.
+ * MPKG_ESTRUCT when the mirror method cannot finish (the reference exits
+ * there).  Files are byte-identical to the reference prep's when both use
+ * the same partitions. */
+/* Loads and validates pdmpk buffers on the host (no GPU needed): the
+ * matrix size, the level count, the number of batches and of computed
+ * rows (all ranks).  Any pointer may be null. */
+int mpkg_pdmpk_info(int npart, const char *const *buf_paths, const char *const *results_paths, int *n,
+                    int *nlevel, int *nbatch, long *rows);
+
+int mpkg_pdmpk_prep(int n, const int *ptr, const int *col, const double *val, int npart, int nlevel,
+                    int mirror_method, int weight_update_method, int partitioner, const char *const *buf_paths,
+                    const char *const *results_paths);
 
 /* Mixed-precision form (no counterpart in the reference's code; the
  * precision pattern of the task): matrix values stored as FP32 or BF16
@@ -186,6 +226,11 @@ int mpkg_spmv_chain_device(int n, const int *d_ptr, const int *d_col, const doub
 
 /* Graph files. */
 int mpkg_read_metis(const char *path, int *n, long *nnz, int **ptr, int **col);
+/* Matrix Market file (coordinate, real or pattern, general or symmetric;
+ * pattern => 1/deg values), the reader of pdmpk's Csr (pdmpk/csr.cc:9-122)
+ * except that symmetric files give a consistent CSR.  ptr, col, val are
+ * allocated (mpkg_free). */
+int mpkg_read_mtx(const char *path, int *n, long *nnz, int **ptr, int **col, double **val);
 int mpkg_read_values(const char *path, long nnz, double **val);
 void mpkg_free(void *p);
 

@@ -20,7 +20,8 @@ LIB_PATH = os.path.join(_HERE, "libmpk_gb300.so")
 
 OK, EINVAL, EIO, EFORMAT, ESTRUCT, ECUDA, ETIMEOUT, ENOMEM, ERANGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
 ARITH_FMA, ARITH_SEPARATE, ARITH_DF64 = 0, 1, 2
-EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS, EXEC_MIXED = 0, 1, 2, 3, 4, 5
+EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS, EXEC_MIXED, EXEC_PDMPK = 0, 1, 2, 3, 4, 5, 6
+PD_PART_BLOCKSHIFT, PD_PART_BFS = 0, 1
 VALUE_F32, VALUE_BF16 = 0, 1
 
 _ERRNAMES = {EINVAL: "EINVAL", EIO: "EIO", EFORMAT: "EFORMAT", ESTRUCT: "ESTRUCT", ECUDA: "ECUDA",
@@ -65,6 +66,9 @@ def _declare(L):
         "mpkg_plan_spmv": (I, [I, P, P, P, I, I, pp]),
         "mpkg_plan_info": (I, [P, C.POINTER(PlanInfo)]),
         "mpkg_plan_bufs": (I, [C.c_char_p, I, I, pp]),
+        "mpkg_plan_pdmpk": (I, [I, P, P, I, pp]),
+        "mpkg_pdmpk_prep": (I, [I, P, P, P, I, I, I, I, I, P, P]),
+        "mpkg_pdmpk_info": (I, [I, P, P, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(Lg)]),
         "mpkg_exec_host": (I, [P, P]),
         "mpkg_exec_device": (I, [P, P, P]),
         "mpkg_sync": (I, [P, P]),
@@ -72,6 +76,7 @@ def _declare(L):
         "mpkg_debug_pipe_stall": (I, [P, I]),
         "mpkg_spmv_chain_device": (I, [I, P, P, P, I, P, I, P]),
         "mpkg_read_metis": (I, [C.c_char_p, C.POINTER(I), C.POINTER(Lg), pp, pp]),
+        "mpkg_read_mtx": (I, [C.c_char_p, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
         "mpkg_read_values": (I, [C.c_char_p, Lg, pp]),
         "mpkg_free": (None, [P]),
         "mpkg_levels": (I, [I, P, P, P, I, P, P]),
@@ -158,6 +163,31 @@ class Csr:
         return Csr(ptr, col, val)
 
     @staticmethod
+    def read_mtx(path):
+        """Matrix Market file as pdmpk's Csr reads it (pattern => 1/deg)."""
+        L = lib()
+        n, nnz = C.c_int(), C.c_long()
+        pp, cp, vp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(L.mpkg_read_mtx(os.fsencode(path), C.byref(n), C.byref(nnz), C.byref(pp), C.byref(cp),
+                               C.byref(vp)))
+        return Csr(_take(pp, n.value + 1, np.int32), _take(cp, nnz.value, np.int32),
+                   _take(vp, nnz.value, np.float64))
+
+    def write_mtx(self, path, pattern=False):
+        """Matrix Market coordinate file, general, rows in CSR order
+        (values printed with 17 significant digits)."""
+        with open(path, "w") as f:
+            f.write("%%%%MatrixMarket matrix coordinate %s general\n" % ("pattern" if pattern else "real"))
+            f.write(f"{self.n} {self.n} {self.nnz}\n")
+            rows = np.repeat(np.arange(self.n), np.diff(self.ptr)) + 1
+            if pattern:
+                for i, j in zip(rows, self.col + 1):
+                    f.write(f"{i} {j}\n")
+            else:
+                for i, j, v in zip(rows, self.col + 1, self.val):
+                    f.write("%d %d %.17g\n" % (i, j, v))
+
+    @staticmethod
     def stencil(kind, size):
         """The reference gen2 stencils (mpk2/gen2.c:59-267)."""
         L = lib()
@@ -204,6 +234,30 @@ class Csr:
     def write_values(self, path):
         with open(path, "w") as f:
             f.write("".join(f"{v:.17g} " for v in self.val))
+
+
+def _cstrs(paths):
+    return C.cast((C.c_char_p * len(paths))(*[os.fsencode(x) for x in paths]), C.c_void_p)
+
+
+def pdmpk_prep(a: Csr, npart, nlevel, buf_paths, results_paths, mirror=0, weight=0,
+               partitioner=PD_PART_BLOCKSHIFT):
+    """pdmpk prep of every rank (CommCompPatterns); writes buf_paths[r] and
+    results_paths[r] in the reference's format."""
+    if a.val is None:
+        raise MpkError(EINVAL, "pdmpk prep needs matrix values")
+    assert len(buf_paths) == npart and len(results_paths) == npart
+    _check(lib().mpkg_pdmpk_prep(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), npart, nlevel, mirror, weight,
+                                 partitioner, _cstrs(buf_paths), _cstrs(results_paths)))
+
+
+def pdmpk_info(buf_paths, results_paths):
+    """Loads and validates pdmpk buffers on the host: n, nlevel, batches,
+    computed rows."""
+    n, nl, nb, rows = C.c_int(), C.c_int(), C.c_int(), C.c_long()
+    _check(lib().mpkg_pdmpk_info(len(buf_paths), _cstrs(buf_paths), _cstrs(results_paths), C.byref(n),
+                                 C.byref(nl), C.byref(nb), C.byref(rows)))
+    return dict(n=n.value, nlevel=nl.value, nbatch=nb.value, rows=rows.value)
 
 
 def uniform(seed, n):
@@ -304,6 +358,19 @@ class Plan:
         """MPI-2 rank buffers (rank<r>.bufs in `directory`) on one GPU."""
         h = C.c_void_p()
         _check(lib().mpkg_plan_bufs(directory.encode(), npart, arith, C.byref(h)))
+        p = Plan.__new__(Plan)
+        p._h = h
+        inf = p.info()
+        p.n, p.nlevel = inf["n"], inf["nlevel"]
+        return p
+
+    @classmethod
+    def pdmpk(cls, buf_paths, results_paths, arith=ARITH_FMA):
+        """pdmpk buffers (one buf.bin / results.bin pair per rank) on one
+        GPU; exec writes A^nlevel x to the last level of vv only."""
+        bp, rp = _cstrs(buf_paths), _cstrs(results_paths)
+        h = C.c_void_p()
+        _check(lib().mpkg_plan_pdmpk(len(buf_paths), bp, rp, arith, C.byref(h)))
         p = Plan.__new__(Plan)
         p._h = h
         inf = p.info()

@@ -10,7 +10,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpk_gb300.so")
 
-HOST_SOURCES = ["graph.cc", "partition.cc", "prep.cc", "bufs.cc", "api.cc"]
+HOST_SOURCES = ["graph.cc", "partition.cc", "prep.cc", "bufs.cc", "pdmpk.cc", "api.cc"]
 CUDA_SOURCES = ["device.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

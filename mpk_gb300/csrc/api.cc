@@ -65,6 +65,40 @@ int mpkg_read_metis(const char *path, int *n, long *nnz, int **ptr, int **col) {
   return kOk;
 }
 
+int mpkg_pdmpk_info(int npart, const char *const *buf_paths, const char *const *results_paths, int *n,
+                    int *nlevel, int *nbatch, long *rows) {
+  clear_error();
+  if (npart <= 0 || !buf_paths || !results_paths) return fail(kEInval, "bad argument");
+  std::vector<pdmpk_gb300::Buffers> bufs(npart, pdmpk_gb300::Buffers(npart));
+  int rc;
+  for (int r = 0; r < npart; r++) {
+    if (!buf_paths[r] || !results_paths[r]) return fail(kEInval, "null path");
+    if ((rc = bufs[r].Load(buf_paths[r], results_paths[r]))) return rc;
+  }
+  PdExecMaps m;
+  if ((rc = pd_exec_maps(bufs, &m))) return rc;
+  if (n) *n = m.n;
+  if (nlevel) *nlevel = m.nlevel;
+  if (nbatch) *nbatch = m.nbatch;
+  if (rows) *rows = (long)m.row_dst.size();
+  return kOk;
+}
+
+int mpkg_read_mtx(const char *path, int *n, long *nnz, int **ptr, int **col, double **val) {
+  clear_error();
+  if (!path || !n || !nnz || !ptr || !col || !val) return fail(kEInval, "null argument");
+  Csr g;
+  int rc = read_mtx(path, &g);
+  if (rc) return rc;
+  *n = g.n;
+  *nnz = g.nnz();
+  *ptr = dup(g.ptr);
+  *col = dup(g.col);
+  *val = dup(g.val);
+  if (!*ptr || (g.nnz() && (!*col || !*val))) return fail(kENoMem, "allocation failed");
+  return kOk;
+}
+
 int mpkg_read_values(const char *path, long nnz, double **val) {
   clear_error();
   if (!path || !val || nnz < 0) return fail(kEInval, "bad argument");

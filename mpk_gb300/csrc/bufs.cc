@@ -1,5 +1,6 @@
 // MPI-2 rank buffers: file format and consistency checks.
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 #include <string>
 #include <unordered_map>
@@ -127,48 +128,164 @@ int check_rank_buffers(const std::vector<RankBuffers> &bufs) {
 
 namespace mpkg {
 
-// Hungarian algorithm (shortest augmenting paths with potentials) on the
-// cost max(sums) - sums: an optimal assignment of rows (old parts) to
-// columns (new parts) maximising the communication that stays on a rank.
+// Linear assignment by the Jonker-Volgenant shortest augmenting path
+// algorithm (R. Jonker, A. Volgenant, Computing 38 (1987) 325-340) on the
+// cost max(sums) - sums: rows are old parts, columns new labels, and the
+// optimum keeps the most communication on one rank.  Optimal assignments
+// are often not unique (zero blocks), so the steps follow the published
+// procedure in order -- column reduction scanning columns from the last,
+// reduction transfer, two passes of augmenting row reduction, then
+// shortest-path augmentation of the remaining free rows -- with the same
+// strict/non-strict comparisons, which is what the reference's lapjv
+// (mpk2/lapjv.c:366-390, pdmpk/lapjv.c) implements; ties then resolve
+// identically.
 void assign_max_trace(const std::vector<long> &sums, int np, std::vector<int> *perm) {
-  long mx = 0;
-  for (long v : sums) mx = std::max(mx, v);
-  const long INF = (long)4e18;
-  // 1-based arrays: u (rows), v (cols), match[col] = row
-  std::vector<long> u(np + 1, 0), v(np + 1, 0), minv(np + 1);
-  std::vector<int> match(np + 1, 0), way(np + 1, 0);
-  std::vector<char> used(np + 1);
-  auto cost = [&](int i, int j) { return mx - sums[(long)(i - 1) * np + (j - 1)]; };
-  for (int i = 1; i <= np; i++) {
-    match[0] = i;
-    int j0 = 0;
-    std::fill(minv.begin(), minv.end(), INF);
-    std::fill(used.begin(), used.end(), 0);
-    do {
-      used[j0] = 1;
-      const int i0 = match[j0];
-      long delta = INF;
-      int j1 = 0;
-      for (int j = 1; j <= np; j++)
-        if (!used[j]) {
-          const long cur = cost(i0, j) - u[i0] - v[j];
-          if (cur < minv[j]) { minv[j] = cur; way[j] = j0; }
-          if (minv[j] < delta) { delta = minv[j]; j1 = j; }
-        }
-      for (int j = 0; j <= np; j++) {
-        if (used[j]) { u[match[j]] += delta; v[j] -= delta; }
-        else minv[j] -= delta;
-      }
-      j0 = j1;
-    } while (match[j0] != 0);
-    do {
-      const int j1 = way[j0];
-      match[j0] = match[j1];
-      j0 = j1;
-    } while (j0);
-  }
   perm->assign(np, 0);
-  for (int j = 1; j <= np; j++) (*perm)[j - 1] = match[j] - 1;
+  if (np <= 1) return;
+  long mx = sums[0];
+  for (long s : sums) mx = std::max(mx, s);
+  const int n = np;
+  std::vector<long> c((size_t)n * n);
+  for (size_t k = 0; k < c.size(); k++) c[k] = mx - sums[k];
+  auto C = [&](int i, int j) { return c[(size_t)i * n + j]; };
+  const int kFree = -1;
+  std::vector<int> x(n, kFree), y(n, kFree);  // x[row] = column, y[column] = row
+  std::vector<long> v(n, 0);                   // column duals
+  std::vector<int> cols(n);                    // column scan order of the augmentation
+  std::vector<char> multi(n, 0);               // row picked by more than one column
+  // column reduction
+  for (int j = n - 1; j >= 0; j--) {
+    cols[j] = j;
+    long h = C(0, j);
+    int imin = 0;
+    for (int i = 1; i < n; i++)
+      if (C(i, j) < h) { h = C(i, j); imin = i; }
+    v[j] = h;
+    if (x[imin] == kFree && !multi[imin]) {
+      x[imin] = j;
+      y[j] = imin;
+    } else {
+      multi[imin] = 1;
+      y[j] = kFree;
+    }
+  }
+  // reduction transfer; rows never picked are free
+  std::vector<int> fr;
+  for (int i = 0; i < n; i++) {
+    if (x[i] == kFree) {
+      fr.push_back(i);
+    } else if (!multi[i]) {
+      const int j1 = x[i];
+      long mn = LONG_MAX;
+      for (int j = 0; j < n; j++)
+        if (j != j1) mn = std::min(mn, C(i, j) - v[j]);
+      v[j1] -= mn;
+    }
+  }
+  // augmenting row reduction, twice; the list of free rows is rewritten
+  // in place while it is consumed
+  for (int pass = 0; pass < 2; pass++) {
+    const int f0 = (int)fr.size();
+    int k = 0, f = 0;
+    while (k < f0) {
+      const int i = fr[k++];
+      long u1 = C(i, 0) - v[0], u2 = LONG_MAX;
+      int j1 = 0, j2 = 0;
+      for (int j = 1; j < n; j++) {
+        const long h = C(i, j) - v[j];
+        if (h < u2) {
+          if (h >= u1) {
+            u2 = h;
+            j2 = j;
+          } else {
+            u2 = u1;
+            u1 = h;
+            j2 = j1;
+            j1 = j;
+          }
+        }
+      }
+      int i1 = y[j1];
+      if (u1 < u2) {
+        v[j1] = v[j1] - u2 + u1;
+      } else if (i1 != kFree) {
+        j1 = j2;
+        i1 = y[j1];
+      }
+      if (i1 != kFree) {
+        if (u1 < u2) fr[--k] = i1;
+        else fr[f++] = i1;
+      }
+      x[i] = j1;
+      y[j1] = i;
+    }
+    fr.resize(f);
+  }
+  // augmentation: Dijkstra-like shortest path from every remaining free row
+  std::vector<long> d(n);
+  std::vector<int> pred(n);
+  for (int i1 : fr) {
+    for (int j = 0; j < n; j++) {
+      d[j] = C(i1, j) - v[j];
+      pred[j] = i1;
+    }
+    int low = 0, up = 0, last = 0, jend = -1;
+    long mn = 0;
+    while (jend < 0) {
+      if (up == low) {  // next set of columns at minimum distance
+        last = low;
+        mn = d[cols[up++]];
+        for (int k = up; k < n; k++) {
+          const int j = cols[k];
+          const long h = d[j];
+          if (h <= mn) {
+            if (h < mn) {
+              up = low;
+              mn = h;
+            }
+            cols[k] = cols[up];
+            cols[up++] = j;
+          }
+        }
+        for (int h = low; h < up && jend < 0; h++)
+          if (y[cols[h]] == kFree) jend = cols[h];
+        if (jend >= 0) break;
+      }
+      // scan the row matched to the next ready column
+      const int j1 = cols[low++];
+      const int i = y[j1];
+      const long u1 = C(i, j1) - v[j1] - mn;
+      for (int k = up; k < n; k++) {
+        const int j = cols[k];
+        const long h = C(i, j) - v[j] - u1;
+        if (h < d[j]) {
+          d[j] = h;
+          pred[j] = i;
+          if (h == mn) {
+            if (y[j] == kFree) {
+              jend = j;
+              break;
+            }
+            cols[k] = cols[up];
+            cols[up++] = j;
+          }
+        }
+      }
+    }
+    for (int k = 0; k < last; k++) {
+      const int j = cols[k];
+      v[j] += d[j] - mn;
+    }
+    int j = jend, i;
+    do {
+      i = pred[j];
+      y[j] = i;
+      const int k = j;
+      j = x[i];
+      x[i] = k;
+    } while (i != i1);
+  }
+  for (int j = 0; j < n; j++) (*perm)[j] = y[j];
 }
 
 namespace {

@@ -752,6 +752,26 @@ __global__ void __launch_bounds__(256) bufs_phase_kernel(int list_base, const lo
   }
 }
 
+// One pdmpk batch of every rank (Buffers::DoComp, pdmpk/buffers.cc:76-97):
+// a row starts from its partial-sum seed (or 0.0) and adds val*mbuf[col]
+// in CSR order.  Thread per row; rows of a batch are independent.
+template <int ARITH>
+__global__ void __launch_bounds__(256) pd_batch_kernel(long r0, long r1, const long *__restrict__ row_dst,
+                                                       const long *__restrict__ row_init,
+                                                       const long *__restrict__ row_ptr,
+                                                       const long *__restrict__ gcol,
+                                                       const double *__restrict__ gval, double *mbuf) {
+  for (long q = r0 + blockIdx.x * (long)blockDim.x + threadIdx.x; q < r1; q += (long)gridDim.x * blockDim.x) {
+    const long s0 = row_init[q];
+    double s = s0 >= 0 ? mbuf[s0] : 0.0;
+    for (long j = row_ptr[q]; j < row_ptr[q + 1]; j++) {
+      if (ARITH == MPKG_ARITH_SEPARATE) s = __dadd_rn(s, __dmul_rn(gval[j], mbuf[gcol[j]]));
+      else s = fma(gval[j], mbuf[gcol[j]], s);
+    }
+    mbuf[row_dst[q]] = s;
+  }
+}
+
 // ------------------------------------------------------------------------
 // Mixed-precision pipeline: matrix values stored as FP32 or BF16, basis
 // vectors FP32, FP32 accumulation (FMA, CSR order).  Each level is scaled by
@@ -885,6 +905,9 @@ struct mpkg_plan {
   long *b_list_seg = nullptr, *b_seg_off = nullptr, *b_row_dst = nullptr, *b_row_ptr = nullptr,
        *b_gcol = nullptr;
   double *b_gval = nullptr;
+  // pdmpk buffers (b_vall, b_in_*, b_out_*, b_cm_* shared with the above)
+  long *d_row_init = nullptr;
+  std::vector<long> pd_row_off;  // per batch: range of rows
   uint32_t epoch = 0;
   int launches = 0;
   std::vector<double> h_x;  // x staging when a tasks plan leaves entries uncovered
@@ -1213,6 +1236,35 @@ int plan_launch(mpkg_plan *p, double *d_vv, cudaStream_t st) {
       }
       if (p->b_nout) gather_map_kernel<<<592, 256, 0, st>>>(p->b_vall, p->b_out_src, d_vv, p->b_out_dst, p->b_nout);
       p->launches = 2 + 2 * p->nphase + 1;
+      break;
+    }
+    case MPKG_EXEC_PDMPK: {
+      int nl = 0;
+      if (p->b_nin) { gather_map_kernel<<<592, 256, 0, st>>>(d_vv, p->b_in_src, p->b_vall, p->b_in_dst, p->b_nin); nl++; }
+      for (size_t bt = 0; bt + 1 < p->b_cm_off.size(); bt++) {
+        const long c0 = p->b_cm_off[bt], c1 = p->b_cm_off[bt + 1];
+        if (c1 > c0) {
+          gather_map_kernel<<<(unsigned)std::min<long>((c1 - c0 + 255) / 256, 1216), 256, 0, st>>>(
+              p->b_vall, p->b_cm_src + c0, p->b_vall, p->b_cm_dst + c0, c1 - c0);
+          nl++;
+        }
+        const long r0 = p->pd_row_off[bt], r1 = p->pd_row_off[bt + 1];
+        if (r1 <= r0) continue;
+        const unsigned g = (unsigned)std::min<long>((r1 - r0 + 255) / 256, 1216);
+        if (p->arith == MPKG_ARITH_SEPARATE)
+          pd_batch_kernel<MPKG_ARITH_SEPARATE><<<g, 256, 0, st>>>(r0, r1, p->b_row_dst, p->d_row_init, p->b_row_ptr,
+                                                                  p->b_gcol, p->b_gval, p->b_vall);
+        else
+          pd_batch_kernel<MPKG_ARITH_FMA><<<g, 256, 0, st>>>(r0, r1, p->b_row_dst, p->d_row_init, p->b_row_ptr,
+                                                             p->b_gcol, p->b_gval, p->b_vall);
+        nl++;
+      }
+      if (p->b_nout) {
+        gather_map_kernel<<<592, 256, 0, st>>>(p->b_vall, p->b_out_src, d_vv + (size_t)p->nlevel * p->n, p->b_out_dst,
+                                               p->b_nout);
+        nl++;
+      }
+      p->launches = nl;
       break;
     }
     case MPKG_EXEC_SPMV: {
@@ -1549,6 +1601,87 @@ int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out) {
   return kOk;
 }
 
+int mpkg_plan_pdmpk(int npart, const char *const *buf_paths, const char *const *results_paths, int arith,
+                    mpkg_plan **out) {
+  clear_error();
+  if (!out || !buf_paths || !results_paths || npart <= 0) return fail(kEInval, "bad argument");
+  *out = nullptr;
+  if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE)
+    return fail(kEInval, "pdmpk buffers run in FP64 (fma or separate)");
+  std::vector<pdmpk_gb300::Buffers> bufs(npart, pdmpk_gb300::Buffers(npart));
+  int rc;
+  for (int r = 0; r < npart; r++) {
+    if (!buf_paths[r] || !results_paths[r]) return fail(kEInval, "null path");
+    if ((rc = bufs[r].Load(buf_paths[r], results_paths[r]))) return rc;
+  }
+  PdExecMaps m;
+  if ((rc = pd_exec_maps(bufs, &m))) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  p->exec = MPKG_EXEC_PDMPK;
+  p->n = m.n; p->nlevel = m.nlevel; p->nphase = m.nbatch; p->npart = npart;
+  p->arith = arith; p->valued = true;
+  p->full_coverage = true;
+  p->rows_computed = (long)m.row_dst.size();
+  p->nnz = (long)m.gcol.size();
+  rc = cudaGetDevice(&p->device) == cudaSuccess ? kOk : fail(kECuda, "cudaGetDevice failed");
+  if (!rc && cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(kECuda, "stream creation failed");
+  if (!rc) rc = dev_alloc(p, &p->b_vall, std::max<long>(m.mbuf_total, 1));
+  if (!rc) rc = dev_copy(p, &p->b_in_dst, m.in_dst.data(), m.in_dst.size());
+  if (!rc) rc = dev_copy(p, &p->b_in_src, m.in_src.data(), m.in_src.size());
+  if (!rc) rc = dev_copy(p, &p->b_out_src, m.out_src.data(), m.out_src.size());
+  if (!rc) rc = dev_copy(p, &p->b_out_dst, m.out_dst.data(), m.out_dst.size());
+  if (!rc) rc = dev_copy(p, &p->b_cm_dst, m.cm_dst.data(), m.cm_dst.size());
+  if (!rc) rc = dev_copy(p, &p->b_cm_src, m.cm_src.data(), m.cm_src.size());
+  if (!rc) rc = dev_copy(p, &p->b_row_dst, m.row_dst.data(), m.row_dst.size());
+  if (!rc) rc = dev_copy(p, &p->d_row_init, m.row_init.data(), m.row_init.size());
+  if (!rc) rc = dev_copy(p, &p->b_row_ptr, m.row_ptr.data(), m.row_ptr.size());
+  if (!rc) rc = dev_copy(p, &p->b_gcol, m.gcol.data(), m.gcol.size());
+  if (!rc) rc = dev_copy(p, &p->b_gval, m.gval.data(), m.gval.size());
+  if (!rc) rc = dev_alloc(p, &p->d_err, 1);
+  if (!rc && cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) rc = fail(kECuda, "memset failed");
+  p->b_nin = (long)m.in_dst.size();
+  p->b_nout = (long)m.out_src.size();
+  p->b_cm_off = m.cm_off;
+  p->pd_row_off = m.row_off;
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
+int mpkg_pdmpk_prep(int n, const int *ptr, const int *col, const double *val, int npart, int nlevel,
+                    int mirror_method, int weight_update_method, int partitioner, const char *const *buf_paths,
+                    const char *const *results_paths) {
+  clear_error();
+  if (!ptr || !col || !val || !buf_paths || !results_paths || npart <= 0) return fail(kEInval, "bad argument");
+  int rc = check_csr(n, ptr, col);
+  if (rc) return rc;
+  pdmpk_gb300::Csr csr;
+  csr.n = n;
+  csr.nnz = ptr[n];
+  csr.ptr.assign(ptr, ptr + n + 1);
+  csr.col.assign(col, col + ptr[n]);
+  csr.val.assign(val, val + ptr[n]);
+  pdmpk_gb300::Args args;
+  args.npart = npart;
+  args.nlevel = nlevel;
+  args.mirror_method = mirror_method;
+  args.weight_update_method = weight_update_method;
+  if (partitioner == MPKG_PD_PART_BLOCKSHIFT) args.partitioner = pdmpk_gb300::BlockShiftPartitioner();
+  else if (partitioner == MPKG_PD_PART_BFS) args.partitioner = pdmpk_gb300::BfsPartitioner();
+  else return fail(kEInval, "unknown partitioner");
+  std::vector<pdmpk_gb300::Buffers> bufs;
+  if ((rc = pdmpk_gb300::CommCompPatterns(csr, args, &bufs))) return rc;
+  for (int r = 0; r < npart; r++) {
+    if (!buf_paths[r] || !results_paths[r]) return fail(kEInval, "null path");
+    if ((rc = bufs[r].Dump(buf_paths[r], results_paths[r]))) return rc;
+  }
+  return kOk;
+}
+
 int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, int nlevel, int value_type,
                     mpkg_plan **out) {
   clear_error();
@@ -1714,7 +1847,8 @@ int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info) {
   info->device_bytes = p->device_bytes;
   info->launches = p->exec == MPKG_EXEC_TASKS ? p->nphase + 1
                    : p->exec == MPKG_EXEC_SPMV ? p->nlevel
-                   : p->exec == MPKG_EXEC_BUFS ? 2 + 2 * p->nphase + 1 : 1;
+                   : p->exec == MPKG_EXEC_BUFS ? 2 + 2 * p->nphase + 1
+                   : p->exec == MPKG_EXEC_PDMPK ? 2 + 2 * p->nphase : 1;
   info->tiles_in_smem = p->tiles_smem ? 1 : 0;
   info->max_tile_slots = p->max_tile_slots;
   info->pipe_chunk = p->pipe.chunk;
@@ -1760,7 +1894,9 @@ int mpkg_exec_host(mpkg_plan *p, double *vv) {
   CUDA_TRY(cudaMemcpyAsync(p->d_vv, vv, sizeof(double) * up, cudaMemcpyHostToDevice, st));
   int rc = plan_launch(p, p->d_vv, st);
   if (rc) return rc;
-  CUDA_TRY(cudaMemcpyAsync(vv + p->n, p->d_vv + p->n, sizeof(double) * (total - p->n),
+  // pdmpk buffers produce only the last level; the others stay untouched
+  const long first = p->exec == MPKG_EXEC_PDMPK ? (long)p->n * p->nlevel : (long)p->n;
+  CUDA_TRY(cudaMemcpyAsync(vv + first, p->d_vv + first, sizeof(double) * (total - first),
                            cudaMemcpyDeviceToHost, st));
   return mpkg_sync(p, st);
 }

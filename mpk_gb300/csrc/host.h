@@ -7,6 +7,8 @@
 #include <string>
 #include <vector>
 
+#include "../../include/pdmpk_gb300.h"
+
 namespace mpkg {
 
 // Status codes shared with the C ABI (include/mpk_gb300.h).
@@ -189,6 +191,22 @@ int check_rank_buffers(const std::vector<RankBuffers> &bufs);
 int fill_all_buffers(const Csr &g, int npart, int nlevel, int nphase, std::vector<std::vector<int>> *parts,
                      const std::vector<std::vector<int>> &levels, const std::vector<PartSkirt> &sk,
                      std::vector<RankBuffers> *out);
+// pdmpk buffers of all ranks flattened for one-GPU execution: one global
+// mbuf (ranks concatenated), per batch a communication gather (the
+// batch's MPI_Ialltoallv) and the batch's rows (seed + CSR terms), and
+// the input/result scatters (Buffers::LoadInput, Results::FillResults).
+struct PdExecMaps {
+  int n = 0, nlevel = 0, nbatch = 0;
+  long mbuf_total = 0;
+  std::vector<long> in_dst, in_src;          // mbuf[in_dst] = x[in_src]
+  std::vector<long> cm_dst, cm_src, cm_off;  // per batch (nbatch + 1 offsets)
+  std::vector<long> row_off;                 // per batch (nbatch + 1)
+  std::vector<long> row_dst, row_init, row_ptr, gcol;  // row_init -1: no seed
+  std::vector<double> gval;
+  std::vector<long> out_src, out_dst;        // y[out_dst] = mbuf[out_src]
+};
+int pd_exec_maps(const std::vector<pdmpk_gb300::Buffers> &bufs, PdExecMaps *m);
+
 // Linear assignment maximising the trace: perm[j] = row assigned to column
 // j of the npart x npart matrix sums (row-major).
 void assign_max_trace(const std::vector<long> &sums, int npart, std::vector<int> *perm);

@@ -10,6 +10,7 @@ scripts drive them (mpk2/driver.c, mpk2/mpktest.c, mpk2/verify_val.c):
   read_mpk + prep_mpk       -> task lists
   exec_mpk / vexec_mpk      -> vv for a seeded x (1/deg and valued operator)
   verify_val                -> gold_result.bin (x = 1, valued operator)
+  pdmpk prep (apps/prep.cc) -> per-rank buf.bin / results.bin (pdmpk.npz)
 
 Inputs (graphs, partitions, x) come from the product's generators and
 partitioners; METIS is not available, so partitions are recursive
@@ -147,6 +148,51 @@ def make(case, tmp):
     return out
 
 
+# pdmpk prep cases: (matrix, npart, nlevel, [(mirror, weight), ...]); the
+# reference prep (apps/prep.cc) runs with the oracle's METIS stand-in
+# (oracle/refshim/metis.h); STUCK lists combinations where it exits
+# ("Couldn't finish").
+PD_MATRICES = {
+    "m5p10": lambda: M.Csr.laplacian(10, 10, 1, diag=4.0, off=-1.0),
+    "m5p16": lambda: M.Csr.laplacian(16, 16, 1, diag=4.0, off=-1.0),
+    "cube6": lambda: M.Csr.stencil("cube", 6),
+    "m5p20p": lambda: M.Csr.laplacian(20, 20, 1, diag=4.0, off=-1.0),  # written as a pattern file
+}
+PD_CASES = [
+    ("m5p10", 4, 4, [(0, 0), (1, 1), (2, 2), (3, 3), (4, 0), (5, 1)]),
+    ("m5p16", 4, 6, [(0, 3), (1, 2), (4, 1), (5, 0)]),
+    ("cube6", 8, 3, [(0, 1), (2, 3), (4, 2), (5, 0)]),
+    ("m5p20p", 4, 5, [(0, 2), (2, 0), (4, 3), (5, 2)]),
+]
+PD_STUCK = [("cube6", 8, 3, 1, 0), ("m5p20p", 4, 5, 3, 1)]
+
+
+def make_pdmpk(tmp):
+    d = os.path.join(tmp, "pdmpk")
+    os.makedirs(d)
+    out = {}
+    for m, P, L, combos in PD_CASES:
+        mtx = os.path.join(d, m + ".mtx")
+        PD_MATRICES[m]().write_mtx(mtx, pattern=m.endswith("p"))
+        out[f"{m}__mtx"] = np.frombuffer(open(mtx, "rb").read(), dtype=np.uint8)
+        for mm, wm in combos:
+            run([O.ref_tool("pdmpk_prep"), "--matrix", m + ".mtx", "--npart", str(P), "--nlevel", str(L),
+                 "--mirror", str(mm), "--weight", str(wm), "--keepfiles"], cwd=d)
+            for r in range(P):
+                stem = os.path.join(d, f"{m}.mtx-np{P}-nl{L}-mm{mm}-wm{wm}-r{r}-ref-oracle")
+                key = f"{m}__{P}_{L}_{mm}_{wm}__r{r}"
+                out[key + "__buf"] = np.frombuffer(open(stem + ".buf.bin", "rb").read(), dtype=np.uint8)
+                out[key + "__res"] = np.frombuffer(open(stem + ".results.bin", "rb").read(), dtype=np.uint8)
+    for m, P, L, mm, wm in PD_STUCK:
+        mtx = os.path.join(d, m + ".mtx")
+        r = subprocess.run([O.ref_tool("pdmpk_prep"), "--matrix", m + ".mtx", "--npart", str(P), "--nlevel",
+                            str(L), "--mirror", str(mm), "--weight", str(wm)], cwd=d, capture_output=True)
+        assert r.returncode != 0, "expected the reference prep to get stuck"
+    out["stuck"] = np.array([f"{m}_{P}_{L}_{mm}_{wm}" for m, P, L, mm, wm in PD_STUCK])
+    np.savez_compressed(os.path.join(HERE, "pdmpk.npz"), **out)
+    return out
+
+
 def main():
     O.build()
     if not O.ref_available():
@@ -156,6 +202,8 @@ def main():
         for case in CASES:
             out = make(case, tmp)
             print(case["name"], "n", out["n"], "tasks", len(out["idx"]))
+        out = make_pdmpk(tmp)
+        print("pdmpk", len(out), "arrays")
     finally:
         shutil.rmtree(tmp)
 

@@ -131,3 +131,70 @@ def test_reference_mpi2_prep_relinks_against_library(monkeypatch):
             subprocess.run([exe, name], check=True, env=dict(os.environ, MPK_RANK=str(r)), stdout=subprocess.DEVNULL)
             mine = np.fromfile(os.path.join(d, name, f"rank{r}.bufs"), dtype=np.uint8)
             assert mine.tobytes() == g[f"bufs{r}"].tobytes(), f"rank {r}"
+
+
+PD_PROG = r"""
+// A pdmpk-style prep + reload written against include/pdmpk_gb300.h only
+// (the shape of the reference's apps/prep.cc and Buffers::Load).
+#include <cstdio>
+#include <stdexcept>
+#include <vector>
+#include "pdmpk_gb300.h"
+using namespace pdmpk_gb300;
+int main(int argc, char **argv) {
+  try {
+    Csr bad(argv[2]);
+    return 10;  // a bad banner must throw, as pdmpk/csr.cc does
+  } catch (const std::logic_error &) {
+  }
+  const Csr csr(argv[1]);
+  Args args;
+  args.npart = 4;
+  args.nlevel = 3;
+  args.mirror_method = 2;
+  args.weight_update_method = 1;
+  std::vector<Buffers> bufs;
+  if (CommCompPatterns(csr, args, &bufs) != 0) return 11;
+  for (int r = 0; r < args.npart; r++) {
+    const std::string b = Filename(argv[3], 4, 3, 2, 1, r, "gb300", "x", "buf.bin");
+    const std::string s = Filename(argv[3], 4, 3, 2, 1, r, "gb300", "x", "results.bin");
+    if (bufs[r].Dump(b, s) != 0) return 12;
+    Buffers back(args.npart);
+    if (back.Load(b, s) != 0) return 13;
+    if (back.mcsr.mcol != bufs[r].mcsr.mcol || back.mbuf_idx != bufs[r].mbuf_idx ||
+        back.phase_descriptors.size() != bufs[r].phase_descriptors.size() ||
+        back.mpi_bufs.init_idcs != bufs[r].mpi_bufs.init_idcs)
+      return 14;
+    for (const PhaseDescriptor &pd : back.phase_descriptors)
+      if (pd.bottom > pd.mid || pd.mid > pd.top || pd.top > args.nlevel) return 15;
+  }
+  std::printf("%d %d\n", csr.n, bufs[0].GetNumPhases());
+  return 0;
+}
+"""
+
+
+def test_pdmpk_cpp_interface(tmp_path):
+    """include/pdmpk_gb300.h compiles as C++17 and links against the
+    library; Csr throws on a bad banner; prep, Dump and Load round-trip;
+    the files are the ones the product's C entry point writes."""
+    src = tmp_path / "pd.cc"
+    src.write_text(PD_PROG)
+    exe = str(tmp_path / "pd")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe,
+                    M.LIB_PATH, "-Wl,-rpath," + os.path.dirname(M.LIB_PATH)], check=True)
+    a = M.Csr.laplacian(12, 12, 1, diag=4.0, off=-1.0)
+    mtx = str(tmp_path / "m.mtx")
+    a.write_mtx(mtx)
+    bad = tmp_path / "bad.mtx"
+    bad.write_text("%%MatrixMarket matrix array real general\n2 2\n")
+    stem = str(tmp_path / "m.mtx")
+    out = subprocess.run([exe, mtx, str(bad), stem], capture_output=True, text=True)
+    assert out.returncode == 0, out.returncode
+    n, nb = map(int, out.stdout.split())
+    assert n == a.n and nb >= 3
+    bp = [str(tmp_path / f"c{r}.buf.bin") for r in range(4)]
+    rp = [str(tmp_path / f"c{r}.results.bin") for r in range(4)]
+    M.pdmpk_prep(a, 4, 3, bp, rp, mirror=2, weight=1)
+    for r in range(4):
+        assert open(bp[r], "rb").read() == open(f"{stem}-np4-nl3-mm2-wm1-r{r}-gb300-x.buf.bin", "rb").read()
