@@ -64,6 +64,10 @@ extern "C" {
 #define MPKG_EXEC_BUFS 4  /* MPI-2 rank buffers of all ranks on one GPU */
 #define MPKG_EXEC_MIXED 5 /* mixed-precision pipeline (FP32/BF16 values) */
 #define MPKG_EXEC_PDMPK 6 /* pdmpk buffers of all ranks on one GPU */
+#define MPKG_EXEC_WAVE 7  /* wavefront: one persistent launch, each CTA owns
+                             a row range at every level and waits only for
+                             the CTAs owning its columns */
+#define MPKG_EXEC_BATCH 8 /* batched block-vector form (FP32), many matrices */
 
 /* Partition providers of the pdmpk prep (mpkg_pdmpk_prep). */
 #define MPKG_PD_PART_BLOCKSHIFT 0 /* contiguous blocks, shifted by half a
@@ -113,6 +117,48 @@ int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val,
 /* k chained SpMV launches (baseline; also the GPU spmv_exec_*). */
 int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val,
                    int nlevel, int arith, mpkg_plan **out);
+
+/* Wavefront executor (no counterpart in the reference: the GB300 form of
+ * exec_mpk for a matrix whose slices stay in L2).  One cooperative launch
+ * per call; CTA b computes its contiguous rows (equal nonzeros) at level l
+ * once the CTAs owning the columns of those rows have published level
+ * l-1 (bounded waits: MPKG_ETIMEOUT instead of a hang).  Computes every
+ * row once per level.  arith MPKG_ARITH_DF64 runs the rows in
+ * double-float on the FP32 pipes (1/deg operator: row sum then one
+ * scaling; valued: multiply-add per entry) and writes the FP64 rounding of
+ * each level. */
+int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
+                   mpkg_plan **out);
+
+/* Batched block-vector form (no counterpart in the reference; the
+ * batching pattern of the task): nmat independent matrices (host CSR
+ * arrays, FP32 values), nrhs right-hand sides each (a power of two <=
+ * 128), nlevel powers, all in ONE persistent cooperative launch that the
+ * plan replays as a CUDA graph.  Vectors: one float buffer of
+ * (nlevel+1) * N * nrhs, N = sum of n[m]; level l of matrix m starts at
+ * (l*N + row0[m]) * nrhs, row0[m] = n[0] + ... + n[m-1], each row's nrhs
+ * values contiguous; level 0 is the input.  Entries are accumulated with
+ * FP32 FMA in CSR order.  tune != 0 times every kernel configuration
+ * (lanes per row x vector width, L2 group size, CTAs per SM) on these
+ * matrices at plan time and keeps the fastest. */
+int mpkg_plan_batch(int nmat, const int *n, const int *const *ptr, const int *const *col, const float *const *val,
+                    int nrhs, int nlevel, int tune, mpkg_plan **out);
+typedef struct {
+  int nmat, nrhs, nlevel;
+  long rows, nnz;
+  int lanes_per_row, vector_width; /* chosen kernel: lanes x floats = nrhs */
+  long group_bytes;                /* L2 budget of a group of matrices */
+  int ngroup, grid;                /* groups, CTAs of the persistent launch */
+  int graph;                       /* 1: replayed as a CUDA graph */
+  int candidates;                  /* configurations timed by the autotuner */
+  double tune_ms;                  /* autotuning time at plan creation */
+  long device_bytes;
+} mpkg_batch_info_t;
+int mpkg_batch_info(const mpkg_plan *p, mpkg_batch_info_t *info);
+/* d_vb: device buffer as above (16-byte aligned), level 0 filled. */
+int mpkg_exec_batch_device(mpkg_plan *p, float *d_vb, void *stream);
+/* vb: host buffer as above; copies level 0 in and levels 1..nlevel out. */
+int mpkg_exec_batch_host(mpkg_plan *p, float *vb);
 
 /* MPI-2 rank buffers rank0.bufs .. rank{npart-1}.bufs in `dir` (the files
  * mpi2_mpkwrtbufs writes, mpk2/buffers.c:588-631; values required) run on
@@ -276,6 +322,14 @@ int mpkg_gen_laplacian(int nx, int ny, int nz, double diag, double off, int *n, 
  * coefficients (symmetric, diagonal = (1+dominance) * sum |off-diagonal|):
  * nz <= 1 gives the 9-point operator on nx*ny with direction weights wx,
  * wy, wdiag; nz > 1 the 7-point operator on nx*ny*nz (weights ignored). */
+/* Random banded operator (no counterpart in the reference; the batching
+ * workload's "banded" half): row i has its diagonal and m-1 distinct
+ * off-diagonals drawn from [i-bw, i+bw], m uniform in [nmin, nmax], values
+ * N(0,1), diagonal N(0,1) + sum|off| + 1; columns ascending; seeded.
+ * Arrays allocated (mpkg_free). */
+int mpkg_gen_banded(long n, int bw, int nmin, int nmax, uint64_t seed, int *nout, long *nnz, int **ptr, int **col,
+                    double **val);
+
 int mpkg_gen_diffusion(int nx, int ny, int nz, double sigma, double wx, double wy, double wdiag,
                        double dominance, uint64_t seed, int *n, long *nnz, int **ptr, int **col, double **val);
 void mpkg_uniform(uint64_t seed, long n, double *out);

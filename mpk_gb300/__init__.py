@@ -20,7 +20,8 @@ LIB_PATH = os.path.join(_HERE, "libmpk_gb300.so")
 
 OK, EINVAL, EIO, EFORMAT, ESTRUCT, ECUDA, ETIMEOUT, ENOMEM, ERANGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
 ARITH_FMA, ARITH_SEPARATE, ARITH_DF64 = 0, 1, 2
-EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS, EXEC_MIXED, EXEC_PDMPK = 0, 1, 2, 3, 4, 5, 6
+EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS, EXEC_MIXED, EXEC_PDMPK, EXEC_WAVE, EXEC_BATCH = \
+    0, 1, 2, 3, 4, 5, 6, 7, 8
 PD_PART_BLOCKSHIFT, PD_PART_BFS = 0, 1
 VALUE_F32, VALUE_BF16 = 0, 1
 
@@ -48,6 +49,13 @@ def lib():
     return _lib
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("nmat", C.c_int), ("nrhs", C.c_int), ("nlevel", C.c_int), ("rows", C.c_long), ("nnz", C.c_long),
+                ("lanes_per_row", C.c_int), ("vector_width", C.c_int), ("group_bytes", C.c_long),
+                ("ngroup", C.c_int), ("grid", C.c_int), ("graph", C.c_int), ("candidates", C.c_int),
+                ("tune_ms", C.c_double), ("device_bytes", C.c_long)]
+
+
 class PlanInfo(C.Structure):
     _fields_ = [("n", C.c_int), ("nlevel", C.c_int), ("nphase", C.c_int), ("npart", C.c_int),
                 ("exec", C.c_int), ("arith", C.c_int), ("valued", C.c_int),
@@ -64,6 +72,11 @@ def _declare(L):
         "mpkg_plan_pa1": (I, [I, P, P, P, P, I, I, I, I, pp]),
         "mpkg_plan_pipe": (I, [I, P, P, P, I, I, I, pp]),
         "mpkg_plan_spmv": (I, [I, P, P, P, I, I, pp]),
+        "mpkg_plan_wave": (I, [I, P, P, P, I, I, pp]),
+        "mpkg_plan_batch": (I, [I, P, P, P, P, I, I, I, pp]),
+        "mpkg_batch_info": (I, [P, C.POINTER(BatchInfo)]),
+        "mpkg_exec_batch_device": (I, [P, P, P]),
+        "mpkg_exec_batch_host": (I, [P, P]),
         "mpkg_plan_info": (I, [P, C.POINTER(PlanInfo)]),
         "mpkg_plan_bufs": (I, [C.c_char_p, I, I, pp]),
         "mpkg_plan_pdmpk": (I, [I, P, P, I, pp]),
@@ -89,6 +102,7 @@ def _declare(L):
         "mpkg_gen_laplacian": (I, [I, I, I, D, D, C.POINTER(I), C.POINTER(Lg), pp, pp, pp, pp]),
         "mpkg_uniform": (None, [C.c_uint64, Lg, P]),
         "mpkg_gen_diffusion": (I, [I, I, I, D, D, D, D, D, C.c_uint64, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
+        "mpkg_gen_banded": (I, [Lg, I, I, I, C.c_uint64, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
         "mpkg_plan_mixed": (I, [I, P, P, P, I, I, pp]),
         "mpkg_mixed_scale": (I, [P, C.POINTER(I), C.POINTER(Lg)]),
         "mpkg_exec_mixed_device": (I, [P, P, P]),
@@ -224,6 +238,17 @@ class Csr:
         return Csr(_take(pp, n.value + 1, np.int32), _take(cp, nnz.value, np.int32),
                    _take(vp, nnz.value, np.float64))
 
+    @staticmethod
+    def banded(n, bandwidth=64, nnz_min=5, nnz_max=30, seed=0):
+        """Random banded, diagonally dominant operator (N(0,1) values)."""
+        L = lib()
+        nn, nnz = C.c_int(), C.c_long()
+        pp, cp, vp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(L.mpkg_gen_banded(n, bandwidth, nnz_min, nnz_max, seed, C.byref(nn), C.byref(nnz), C.byref(pp),
+                                 C.byref(cp), C.byref(vp)))
+        return Csr(_take(pp, nn.value + 1, np.int32), _take(cp, nnz.value, np.int32),
+                   _take(vp, nnz.value, np.float64))
+
     def write_metis(self, path, ne=None):
         with open(path, "w") as f:
             f.write(f"{self.n} {self.nnz // 2 if ne is None else ne}\n")
@@ -258,6 +283,35 @@ def pdmpk_info(buf_paths, results_paths):
     _check(lib().mpkg_pdmpk_info(len(buf_paths), _cstrs(buf_paths), _cstrs(results_paths), C.byref(n),
                                  C.byref(nl), C.byref(nb), C.byref(rows)))
     return dict(n=n.value, nlevel=nl.value, nbatch=nb.value, rows=rows.value)
+
+
+def batch_workload(count=256, nmin=1000, nmax=200000, seed=0):
+    """The batching workload: `count` matrices with n log-uniform in
+    [nmin, nmax]; even indices random 2-D/3-D stencils (5-point or 9-point
+    diffusion in 2-D, 7-point Laplacian or diffusion in 3-D), odd indices
+    random banded (bandwidth 64, 5-30 entries per row, N(0,1) values,
+    diagonally dominant).  Seeded per matrix."""
+    rng = np.random.default_rng(seed)
+    mats = []
+    for m in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        s = int(rng.integers(1 << 62))
+        if m % 2 == 1:
+            mats.append(Csr.banded(n, 64, 5, 30, seed=s))
+            continue
+        kind = int(rng.integers(4))
+        if kind < 2:  # 2-D
+            nx = max(2, int(round(np.sqrt(n))))
+            ny = max(2, n // nx)
+            mats.append(Csr.laplacian(nx, ny, 1, diag=4.0, off=-1.0) if kind == 0
+                        else Csr.diffusion(nx, ny, 1, sigma=0.5, seed=s))
+        else:  # 3-D
+            nx = max(2, int(round(n ** (1.0 / 3.0))))
+            ny = nx
+            nz = max(2, n // (nx * ny))
+            mats.append(Csr.laplacian(nx, ny, nz, diag=6.0, off=-1.0) if kind == 2
+                        else Csr.diffusion(nx, ny, nz, sigma=0.5, seed=s))
+    return mats
 
 
 def uniform(seed, n):
@@ -392,6 +446,50 @@ class Plan:
 
     def exec_mixed_device(self, d_vv_ptr: int, stream: int = 0):
         _check(lib().mpkg_exec_mixed_device(self._h, C.c_void_p(d_vv_ptr), C.c_void_p(stream or None)))
+
+    @classmethod
+    def wave(cls, a: Csr, nlevel, arith=ARITH_FMA):
+        """Wavefront executor: one persistent launch, neighbour-only waits."""
+        return cls._make(lib().mpkg_plan_wave, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, arith,
+                         a=a, nlevel=nlevel)
+
+    @classmethod
+    def batch(cls, mats, nrhs, nlevel, tune=True):
+        """Batched block-vector form over a list of Csr (values cast to
+        FP32): one persistent launch replayed as a CUDA graph."""
+        keep = []
+        n = np.array([m.n for m in mats], dtype=np.int32)
+        arrs = []
+        for m in mats:
+            if m.val is None:
+                raise MpkError(EINVAL, "the batched form needs matrix values")
+            t = (_i32(m.ptr), _i32(m.col), np.ascontiguousarray(m.val, dtype=np.float32))
+            keep.append(t)
+        ptrs = (C.c_void_p * len(mats))(*[t[0].ctypes.data for t in keep])
+        cols = (C.c_void_p * len(mats))(*[t[1].ctypes.data for t in keep])
+        vals = (C.c_void_p * len(mats))(*[t[2].ctypes.data for t in keep])
+        h = C.c_void_p()
+        _check(lib().mpkg_plan_batch(len(mats), _ptr(n), C.cast(ptrs, C.c_void_p), C.cast(cols, C.c_void_p),
+                                     C.cast(vals, C.c_void_p), nrhs, nlevel, 1 if tune else 0, C.byref(h)))
+        p = Plan.__new__(Plan)
+        p._h = h
+        p.n, p.nlevel, p.nrhs = int(n.sum()), nlevel, nrhs
+        p.row0 = np.concatenate([[0], np.cumsum(n.astype(np.int64))])
+        return p
+
+    def batch_info(self) -> dict:
+        inf = BatchInfo()
+        _check(lib().mpkg_batch_info(self._h, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in BatchInfo._fields_}
+
+    def exec_batch_host(self, vb: np.ndarray) -> np.ndarray:
+        """vb: float32 (nlevel+1, N, nrhs) with level 0 filled; in place."""
+        assert vb.dtype == np.float32 and vb.flags.c_contiguous and vb.size == (self.nlevel + 1) * self.n * self.nrhs
+        _check(lib().mpkg_exec_batch_host(self._h, _ptr(vb)))
+        return vb
+
+    def exec_batch_device(self, d_vb_ptr: int, stream: int = 0):
+        _check(lib().mpkg_exec_batch_device(self._h, C.c_void_p(d_vb_ptr), C.c_void_p(stream or None)))
 
     @classmethod
     def spmv(cls, a: Csr, nlevel, arith=ARITH_FMA):

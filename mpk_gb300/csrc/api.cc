@@ -238,6 +238,18 @@ int mpkg_gen_diffusion(int nx, int ny, int nz, double sigma, double wx, double w
   return kOk;
 }
 
+int mpkg_gen_banded(long n, int bw, int nmin, int nmax, uint64_t seed, int *nout, long *nnz, int **ptr, int **col,
+                    double **val) {
+  clear_error();
+  if (!nout || !nnz || !ptr || !col || !val) return fail(kEInval, "null argument");
+  Csr g;
+  int rc = gen_banded(n, bw, nmin, nmax, seed, &g);
+  if (rc) return rc;
+  *nout = g.n; *nnz = g.nnz();
+  *ptr = dup(g.ptr); *col = dup(g.col); *val = dup(g.val);
+  return kOk;
+}
+
 void mpkg_uniform(uint64_t seed, long n, double *out) {
   if (out && n > 0) uniform_vector(seed, n, out);
 }

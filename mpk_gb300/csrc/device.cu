@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -505,6 +506,24 @@ __device__ __forceinline__ float2 df_norm(float sh, float sl) {
   return make_float2(h, l);
 }
 
+// s += x in double-float (two-sum of the high parts, low parts added)
+__device__ __forceinline__ void df_acc(float2 x, float &sh, float &sl) {
+  const float s = __fadd_rn(sh, x.x);
+  const float bp = __fadd_rn(s, -sh);
+  const float t = __fadd_rn(__fadd_rn(sh, -__fadd_rn(s, -bp)), __fadd_rn(x.x, -bp));
+  sh = s;
+  sl = __fadd_rn(sl, __fadd_rn(t, x.y));
+}
+
+// a * v in double-float (v normalised)
+__device__ __forceinline__ float2 df_scale(float2 a, float2 v) {
+  const float p = __fmul_rn(a.x, v.x);
+  float e = __fmaf_rn(a.x, v.x, -p);
+  e = __fmaf_rn(a.x, v.y, e);
+  e = __fmaf_rn(a.y, v.x, e);
+  return df_norm(p, e);
+}
+
 // Pipeline in double-float: levels travel between chunks through a
 // two-slot ring of df64 values (level l in slot l&1); vv receives the FP64
 // rounding of every level.  Level 1 splits the gathered FP64 x values.  A
@@ -752,6 +771,303 @@ __global__ void __launch_bounds__(256) bufs_phase_kernel(int list_base, const lo
   }
 }
 
+// ------------------------------------------------------------------------
+// Wavefront executor: one persistent (cooperative) launch; CTA b owns the
+// contiguous rows [row_lo[b], row_lo[b+1]) (equal nonzeros) at every level
+// and computes level l as soon as the CTAs owning the columns those rows
+// read (dep_lo[b]..dep_hi[b]) have published level l-1.  No grid-wide
+// barrier and no redundant rows; the matrix slices stay in L2 across
+// levels.  Every level is written to a fresh address range (vv, and in
+// double-float mode one float2 shadow level per level), so L1 never holds
+// a stale copy of data another SM produced during the launch.
+// ------------------------------------------------------------------------
+struct WaveArgs {
+  int n, nlevel, nblk;
+  uint32_t base;               // flags of this call start at base (level l publishes base + l)
+  uint32_t stall;              // test hook: extra levels to wait for (never published)
+  // matrix in sliced ELL (32 rows per slice, entry t of row 32s+j at
+  // sell_off[s] + 32t + j, CSR order within the row), so that a warp's
+  // column and value loads are 128-byte coalesced
+  const long *sell_off;        // nslice + 1
+  const int *len;              // entries per row
+  const int *scol;             // column of each slot
+  const double *sval;          // value of each slot (valued) ...
+  const float2 *sval2;         // ... or its double-float split
+  const double *rdeg;          // 1/deg per row (1/deg operator) ...
+  const float2 *rdeg2;         // ... or its double-float split
+  double *vv;
+  float2 *shadow;              // (nlevel + 1) * n, double-float copies of the levels
+  const int *row_lo;           // nblk + 1
+  const int *dep_lo, *dep_hi;  // per CTA
+  unsigned int *flags;         // per CTA: last level published
+  int *err;
+};
+
+__device__ __forceinline__ bool wave_wait(const WaveArgs &a, int b, unsigned int want, int *s_abort) {
+  const int lo = a.dep_lo[b], hi = a.dep_hi[b];
+  for (int c = lo + (int)threadIdx.x; c <= hi; c += blockDim.x) {
+    long spins = 0;
+    while (ld_acquire(a.flags + c) < want + a.stall) {
+      if (++spins > kSpinLimit || *((volatile int *)a.err)) {
+        atomicCAS(a.err, 0, kErrTimeout);
+        *s_abort = 1;
+        break;
+      }
+      __nanosleep(spins < 16 ? 32 : 256);
+    }
+  }
+  __syncthreads();
+  return *s_abort == 0;
+}
+
+__device__ __forceinline__ void wave_publish(const WaveArgs &a, int b, unsigned int v) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.flags + b), "r"(v) : "memory");
+  }
+}
+
+// FP64 rows (fma or separate multiply/add, CSR order as the reference).
+// A warp computes one 32-row slice; CTA row ranges start on slices.
+template <int ARITH, bool VALUED>
+__global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = 0;
+  __syncthreads();
+  const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int l = 1; l <= a.nlevel; l++) {
+    if (l > 1 && !wave_wait(a, b, a.base + (unsigned)(l - 1), &s_abort)) return;
+    const double *src = a.vv + (size_t)(l - 1) * a.n;
+    double *dst = a.vv + (size_t)l * a.n;
+    for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
+      const int i = (sl << 5) + lane;
+      if (i >= r1) continue;
+      const int len = __ldg(a.len + i);
+      const long e0 = __ldg(a.sell_off + sl) + lane;
+      const double cf = VALUED ? 0.0 : __ldg(a.rdeg + i);
+      double s = 0.0;
+      int t = 0;
+      if (len <= 8) {  // all column loads, then all gathers, in flight together
+        int c[8];
+        double x[8], v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) c[u] = u < len ? __ldg(a.scol + e0 + 32L * u) : 0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          x[u] = u < len ? src[c[u]] : 0.0;
+          v[u] = VALUED ? (u < len ? __ldg(a.sval + e0 + 32L * u) : 0.0) : cf;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+          if (u < len) s = row_term<ARITH>(s, v[u], x[u]);
+        t = len;
+      }
+      for (; t + 4 <= len; t += 4) {
+        int c[4];
+        double x[4], v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) c[u] = __ldg(a.scol + e0 + 32L * (t + u));
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          x[u] = src[c[u]];
+          v[u] = VALUED ? __ldg(a.sval + e0 + 32L * (t + u)) : cf;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) s = row_term<ARITH>(s, v[u], x[u]);
+      }
+      for (; t < len; t++)
+        s = row_term<ARITH>(s, VALUED ? __ldg(a.sval + e0 + 32L * t) : cf, src[__ldg(a.scol + e0 + 32L * t)]);
+      __stcs(dst + i, s);
+    }
+    wave_publish(a, b, a.base + (unsigned)l);
+  }
+}
+
+// Double-float rows.  1/deg operator: the row's values are summed in
+// double-float, then scaled once by 1/deg; valued operator: double-float
+// multiply-add per entry.  Level 0 first splits the CTA's own rows of x.
+template <bool VALUED>
+__global__ void __launch_bounds__(256) wave_df_kernel(WaveArgs a) {
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = 0;
+  __syncthreads();
+  const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) a.shadow[i] = df_split(a.vv[i]);
+  wave_publish(a, b, a.base);
+  for (int l = 1; l <= a.nlevel; l++) {
+    if (!wave_wait(a, b, a.base + (unsigned)(l - 1), &s_abort)) return;
+    const float2 *src = a.shadow + (size_t)(l - 1) * a.n;
+    float2 *sdst = a.shadow + (size_t)l * a.n;
+    double *dst = a.vv + (size_t)l * a.n;
+    for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
+      const int i = (sl << 5) + lane;
+      if (i >= r1) continue;
+      const int len = __ldg(a.len + i);
+      const long e0 = __ldg(a.sell_off + sl) + lane;
+      float sh = 0.f, sl_ = 0.f;
+      int t = 0;
+      if (len <= 8) {  // all column loads, then all gathers, in flight together
+        int c[8];
+        float2 x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) c[u] = u < len ? __ldg(a.scol + e0 + 32L * u) : 0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) x[u] = u < len ? src[c[u]] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          if (u < len) {
+            if (VALUED) df_mac(a.sval2[e0 + 32L * u], x[u], sh, sl_);
+            else df_acc(x[u], sh, sl_);
+          }
+        }
+        t = len;
+      }
+      for (; t + 4 <= len; t += 4) {
+        int c[4];
+        float2 x[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) c[u] = __ldg(a.scol + e0 + 32L * (t + u));
+#pragma unroll
+        for (int u = 0; u < 4; u++) x[u] = src[c[u]];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if (VALUED) df_mac(a.sval2[e0 + 32L * (t + u)], x[u], sh, sl_);
+          else df_acc(x[u], sh, sl_);
+        }
+      }
+      for (; t < len; t++) {
+        const float2 x = src[__ldg(a.scol + e0 + 32L * t)];
+        if (VALUED) df_mac(a.sval2[e0 + 32L * t], x, sh, sl_);
+        else df_acc(x, sh, sl_);
+      }
+      float2 v = df_norm(sh, sl_);
+      if (!VALUED) v = df_scale(a.rdeg2[i], v);
+      sdst[i] = v;
+      __stcs(dst + i, df_to_double(v));
+    }
+    wave_publish(a, b, a.base + (unsigned)l);
+  }
+}
+
+// ------------------------------------------------------------------------
+// Batched block-vector MPK (FP32): many independent matrices, nrhs
+// right-hand sides each, in ONE persistent cooperative launch.  The
+// matrices are concatenated into one block-diagonal CSR and cut into
+// groups whose matrix + two levels of vectors fit in L2; every CTA owns a
+// row range of every group and walks (group, level) in order, waiting
+// only for the CTAs that own its columns (the wavefront rule), so a group's
+// matrix is read from HBM once for all levels.  A row is computed by LPR
+// lanes, each holding VW consecutive right-hand sides (vector loads);
+// entries are accumulated with single-precision FMA in CSR order.
+// ------------------------------------------------------------------------
+struct BatchArgs {
+  long N;                      // rows of all matrices
+  int nrhs, nlevel, nblk, ngroup;
+  uint32_t base, stall;
+  const int *ptr, *col;        // block-diagonal CSR (global columns)
+  const float *val;
+  float *vb;                   // (nlevel + 1) * N * nrhs, level 0 = input
+  const int *row_lo;           // ngroup * (nblk + 1)
+  const int *dep_lo, *dep_hi;  // ngroup * nblk
+  unsigned int *flags;
+  int *err;
+};
+
+template <int VW>
+struct VecF;
+template <>
+struct VecF<1> {
+  static __device__ __forceinline__ void ld(const float *p, float *v) { v[0] = *p; }
+  static __device__ __forceinline__ void st(float *p, const float *v) { __stcs(p, v[0]); }
+};
+template <>
+struct VecF<2> {
+  static __device__ __forceinline__ void ld(const float *p, float *v) {
+    const float2 t = *reinterpret_cast<const float2 *>(p);
+    v[0] = t.x; v[1] = t.y;
+  }
+  static __device__ __forceinline__ void st(float *p, const float *v) {
+    __stcs(reinterpret_cast<float2 *>(p), make_float2(v[0], v[1]));
+  }
+};
+template <>
+struct VecF<4> {
+  static __device__ __forceinline__ void ld(const float *p, float *v) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  }
+  static __device__ __forceinline__ void st(float *p, const float *v) {
+    __stcs(reinterpret_cast<float4 *>(p), make_float4(v[0], v[1], v[2], v[3]));
+  }
+};
+
+template <int LPR, int VW>
+__global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = 0;
+  __syncthreads();
+  const int b = blockIdx.x, nrhs = LPR * VW;
+  const int lane = (int)threadIdx.x % LPR, rpp = (int)blockDim.x / LPR;
+  for (int g = 0; g < a.ngroup; g++) {
+    const int r0 = a.row_lo[(size_t)g * (a.nblk + 1) + b], r1 = a.row_lo[(size_t)g * (a.nblk + 1) + b + 1];
+    const unsigned tag = a.base + (unsigned)g * (unsigned)(a.nlevel + 1);
+    const int dlo = a.dep_lo[(size_t)g * a.nblk + b], dhi = a.dep_hi[(size_t)g * a.nblk + b];
+    for (int l = 1; l <= a.nlevel; l++) {
+      if (l > 1) {  // the CTAs owning this range's columns have published level l-1 of group g
+        for (int c = dlo + (int)threadIdx.x; c <= dhi; c += blockDim.x) {
+          long spins = 0;
+          while (ld_acquire(a.flags + c) < tag + (unsigned)(l - 1) + a.stall) {
+            if (++spins > kSpinLimit || *((volatile int *)a.err)) {
+              atomicCAS(a.err, 0, kErrTimeout);
+              s_abort = 1;
+              break;
+            }
+            __nanosleep(spins < 16 ? 32 : 256);
+          }
+        }
+        __syncthreads();
+        if (s_abort) return;
+      }
+      const float *src = a.vb + (size_t)(l - 1) * a.N * nrhs + lane * VW;
+      float *dst = a.vb + (size_t)l * a.N * nrhs + lane * VW;
+      for (int i = r0 + (int)threadIdx.x / LPR; i < r1; i += rpp) {
+        float acc[VW];
+#pragma unroll
+        for (int u = 0; u < VW; u++) acc[u] = 0.0f;
+        const int q0 = __ldg(a.ptr + i), q1 = __ldg(a.ptr + i + 1);
+        int q = q0;
+        for (; q + 2 <= q1; q += 2) {
+          const int c0 = __ldg(a.col + q), c1 = __ldg(a.col + q + 1);
+          const float v0 = __ldg(a.val + q), v1 = __ldg(a.val + q + 1);
+          float x0[VW], x1[VW];
+          VecF<VW>::ld(src + (size_t)c0 * nrhs, x0);
+          VecF<VW>::ld(src + (size_t)c1 * nrhs, x1);
+#pragma unroll
+          for (int u = 0; u < VW; u++) acc[u] = __fmaf_rn(v0, x0[u], acc[u]);
+#pragma unroll
+          for (int u = 0; u < VW; u++) acc[u] = __fmaf_rn(v1, x1[u], acc[u]);
+        }
+        if (q < q1) {
+          float x0[VW];
+          const float v0 = __ldg(a.val + q);
+          VecF<VW>::ld(src + (size_t)__ldg(a.col + q) * nrhs, x0);
+#pragma unroll
+          for (int u = 0; u < VW; u++) acc[u] = __fmaf_rn(v0, x0[u], acc[u]);
+        }
+        VecF<VW>::st(dst + (size_t)i * nrhs, acc);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.flags + b), "r"(tag + (unsigned)l) : "memory");
+      }
+    }
+  }
+}
+
 // One pdmpk batch of every rank (Buffers::DoComp, pdmpk/buffers.cc:76-97):
 // a row starts from its partial-sum seed (or 0.0) and adds val*mbuf[col]
 // in CSR order.  Thread per row; rows of a batch are independent.
@@ -905,6 +1221,20 @@ struct mpkg_plan {
   long *b_list_seg = nullptr, *b_seg_off = nullptr, *b_row_dst = nullptr, *b_row_ptr = nullptr,
        *b_gcol = nullptr;
   double *b_gval = nullptr;
+  // wavefront executor
+  WaveArgs wave{};
+  int wave_grid = 0;
+  // batched block-vector form
+  BatchArgs batch{};
+  int batch_lpr = 0, batch_vw = 0, batch_nmat = 0;
+  long batch_group_bytes = 0;
+  double batch_tune_ms = 0.0;
+  int batch_candidates = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  const void *graph_key = nullptr;
+  bool graph_ok = false;
+  float *d_fb = nullptr;  // staging of mpkg_exec_batch_host
   // pdmpk buffers (b_vall, b_in_*, b_out_*, b_cm_* shared with the above)
   long *d_row_init = nullptr;
   std::vector<long> pd_row_off;  // per batch: range of rows
@@ -1108,6 +1438,176 @@ int pipe_setup_t(mpkg_plan *p, int *grid) {
   return kOk;
 }
 
+template <typename K>
+int wave_occupancy(mpkg_plan *p, K kernel, int *grid) {
+  int per_sm = 0, nsm = 0, coop = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, p->device));
+  if (!coop) return fail(kECuda, "device does not support cooperative launches");
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0));
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+  if (per_sm <= 0) return fail(kECuda, "wavefront kernel cannot be resident");
+  *grid = per_sm * nsm;
+  return kOk;
+}
+
+void *wave_kernel_ptr(const mpkg_plan *p) {
+  if (p->arith == MPKG_ARITH_DF64)
+    return p->valued ? (void *)wave_df_kernel<true> : (void *)wave_df_kernel<false>;
+  if (p->arith == MPKG_ARITH_SEPARATE)
+    return p->valued ? (void *)wave_kernel<MPKG_ARITH_SEPARATE, true> : (void *)wave_kernel<MPKG_ARITH_SEPARATE, false>;
+  return p->valued ? (void *)wave_kernel<MPKG_ARITH_FMA, true> : (void *)wave_kernel<MPKG_ARITH_FMA, false>;
+}
+
+int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st) {
+  WaveArgs &w = p->wave;
+  const unsigned step = (unsigned)p->nlevel + 1;
+  if (w.base == 0 || w.base > (1u << 30)) {  // first call, or the flags would wrap: start over
+    CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(unsigned int) * (size_t)w.nblk, st));
+    w.base = 1;
+  } else {
+    w.base += step;
+  }
+  WaveArgs a = w;
+  a.vv = d_vv;
+  void *args[] = {&a};
+  CUDA_TRY(cudaLaunchCooperativeKernel(wave_kernel_ptr(p), dim3(w.nblk), dim3(256), args, 0, st));
+  return kOk;
+}
+
+// ---- batched form: kernel choice, layout, launch -------------------------
+typedef void (*BatchKernel)(BatchArgs);
+
+BatchKernel batch_kernel_for(int lpr, int vw) {
+#define MPKG_BK(L, V) if (lpr == L && vw == V) return batch_kernel<L, V>;
+  MPKG_BK(1, 1) MPKG_BK(2, 1) MPKG_BK(4, 1) MPKG_BK(8, 1) MPKG_BK(16, 1) MPKG_BK(32, 1)
+  MPKG_BK(1, 2) MPKG_BK(2, 2) MPKG_BK(4, 2) MPKG_BK(8, 2) MPKG_BK(16, 2) MPKG_BK(32, 2)
+  MPKG_BK(1, 4) MPKG_BK(2, 4) MPKG_BK(4, 4) MPKG_BK(8, 4) MPKG_BK(16, 4) MPKG_BK(32, 4)
+#undef MPKG_BK
+  return nullptr;
+}
+
+// Host description of the concatenated matrices.
+struct BatchHost {
+  long N = 0;
+  std::vector<int> ptr, col;
+  std::vector<float> val;
+  std::vector<long> mat_row0;  // nmat + 1
+};
+
+// Groups of consecutive matrices within `budget` bytes (matrix + two
+// levels of vectors); per group, CTA row ranges of equal nonzeros and the
+// CTAs owning each range's columns.
+void batch_layout(const BatchHost &h, int nrhs, long budget, int grid, std::vector<int> *row_lo,
+                  std::vector<int> *dlo, std::vector<int> *dhi, int *ngroup) {
+  const int nmat = (int)h.mat_row0.size() - 1;
+  std::vector<long> g0(1, 0);
+  long bytes = 0;
+  for (int m = 0; m < nmat; m++) {
+    const long r0 = h.mat_row0[m], r1 = h.mat_row0[m + 1];
+    const long mb = (long)(h.ptr[r1] - h.ptr[r0]) * 8 + (r1 - r0) * (4 + 8L * nrhs);
+    if (bytes > 0 && bytes + mb > budget) {
+      g0.push_back(r0);
+      bytes = 0;
+    }
+    bytes += mb;
+  }
+  g0.push_back(h.N);
+  *ngroup = (int)g0.size() - 1;
+  row_lo->assign((size_t)*ngroup * (grid + 1), 0);
+  dlo->assign((size_t)*ngroup * grid, 0);
+  dhi->assign((size_t)*ngroup * grid, 0);
+  for (int g = 0; g < *ngroup; g++) {
+    int *lo = row_lo->data() + (size_t)g * (grid + 1);
+    const long a = g0[g], z = g0[g + 1];
+    const long q0 = h.ptr[a], nz = h.ptr[z] - q0;
+    lo[0] = (int)a;
+    for (int b = 1; b < grid; b++) {
+      const long target = q0 + nz * b / grid;
+      const int r = (int)(std::lower_bound(h.ptr.begin() + a, h.ptr.begin() + z + 1, (int)target) - h.ptr.begin());
+      lo[b] = std::max(std::min(r, (int)z), lo[b - 1]);
+    }
+    lo[grid] = (int)z;
+    for (int b = 0; b < grid; b++) {
+      int cmin = INT32_MAX, cmax = -1;
+      for (long q = h.ptr[lo[b]]; q < h.ptr[lo[b + 1]]; q++) {
+        cmin = std::min(cmin, h.col[q]);
+        cmax = std::max(cmax, h.col[q]);
+      }
+      int &L = (*dlo)[(size_t)g * grid + b], &H = (*dhi)[(size_t)g * grid + b];
+      if (cmax < 0) { L = H = b; continue; }
+      L = (int)(std::upper_bound(lo, lo + grid, cmin) - lo) - 1;
+      H = (int)(std::upper_bound(lo, lo + grid, cmax) - lo) - 1;
+    }
+  }
+}
+
+int batch_launch_raw(mpkg_plan *p, float *d_vb, cudaStream_t st, bool capture) {
+  BatchArgs a = p->batch;
+  a.vb = d_vb;
+  if (capture) {
+    a.base = 1;  // the graph resets the flags before every replay
+  } else {
+    BatchArgs &w = p->batch;
+    const unsigned step = (unsigned)w.ngroup * (unsigned)(w.nlevel + 1);
+    if (w.base == 0 || w.base > (1u << 30)) {
+      CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(unsigned int) * (size_t)w.nblk, st));
+      w.base = 1;
+    } else {
+      w.base += step;
+    }
+    a.base = w.base;
+  }
+  if (capture) CUDA_TRY(cudaMemsetAsync(a.flags, 0, sizeof(unsigned int) * (size_t)a.nblk, st));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(a.nblk);
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CUDA_TRY(cudaLaunchKernelEx(&cfg, batch_kernel_for(p->batch_lpr, p->batch_vw), a));
+  return kOk;
+}
+
+// One replayable graph per output buffer: flag reset + the persistent
+// kernel.  Falls back to a direct launch when capture is not possible.
+int batch_launch(mpkg_plan *p, float *d_vb, cudaStream_t st) {
+  if (p->graph_ok && p->graph_key == d_vb) {
+    CUDA_TRY(cudaGraphLaunch(p->graph_exec, st));
+    return kOk;
+  }
+  if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
+  if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+  p->graph_ok = false;
+  cudaStream_t cs = nullptr;
+  bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+  if (ok) ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    const int rc = batch_launch_raw(p, d_vb, cs, true);
+    cudaGraph_t g = nullptr;
+    const bool ended = cudaStreamEndCapture(cs, &g) == cudaSuccess;
+    ok = rc == kOk && ended && g != nullptr;
+    if (ok) {
+      p->graph = g;
+      ok = cudaGraphInstantiate(&p->graph_exec, g, 0) == cudaSuccess;
+    } else if (g) {
+      cudaGraphDestroy(g);
+    }
+  }
+  if (cs) cudaStreamDestroy(cs);
+  cudaGetLastError();  // a failed capture leaves no sticky error
+  clear_error();
+  if (ok) {
+    p->graph_ok = true;
+    p->graph_key = d_vb;
+    CUDA_TRY(cudaGraphLaunch(p->graph_exec, st));
+    return kOk;
+  }
+  return batch_launch_raw(p, d_vb, st, false);
+}
+
 int launch_spmv(int n, const int *ptr, const int *col, const double *coef, bool valued, int nlevel,
                 double *vv, int arith, cudaStream_t st) {
   dim3 blk(256), grd((n + 255) / 256);
@@ -1238,6 +1738,14 @@ int plan_launch(mpkg_plan *p, double *d_vv, cudaStream_t st) {
       p->launches = 2 + 2 * p->nphase + 1;
       break;
     }
+    case MPKG_EXEC_BATCH:
+      return fail(kEInval, "batch plans run through mpkg_exec_batch_device / mpkg_exec_batch_host");
+    case MPKG_EXEC_WAVE: {
+      int rc = launch_wave(p, d_vv, st);
+      if (rc) return rc;
+      p->launches = 1;
+      break;
+    }
     case MPKG_EXEC_PDMPK: {
       int nl = 0;
       if (p->b_nin) { gather_map_kernel<<<592, 256, 0, st>>>(d_vv, p->b_in_src, p->b_vall, p->b_in_dst, p->b_nin); nl++; }
@@ -1293,9 +1801,12 @@ const char *mpkg_last_error(void) { return last_error(); }
 int mpkg_version(void) { return 1; }
 
 void mpkg_plan_destroy(mpkg_plan *p) {
+  if (p && p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+  if (p && p->graph) cudaGraphDestroy(p->graph);
   if (!p) return;
   for (void *q : p->owned) cudaFree(q);
   if (p->d_vv) cudaFree(p->d_vv);
+  if (p->d_fb) cudaFree(p->d_fb);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;
 }
@@ -1601,6 +2112,288 @@ int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out) {
   return kOk;
 }
 
+int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
+                   mpkg_plan **out) {
+  clear_error();
+  if (!out) return fail(kEInval, "out is null");
+  *out = nullptr;
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  p->exec = MPKG_EXEC_WAVE;
+  int rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  int grid = 0;
+  if (!rc) rc = wave_occupancy(p, (const void *)wave_kernel_ptr(p), &grid);
+  if (!rc) {
+    const long nnz = ptr[n];
+    const int nslice = (n + 31) / 32;
+    grid = (int)std::max<long>(1, std::min<long>(grid, nslice));
+    // contiguous row ranges of (nearly) equal nonzeros, starting on slices
+    std::vector<int> lo(grid + 1, 0);
+    for (int b = 1; b < grid; b++) {
+      const long target = nnz * b / grid;
+      int r = (int)(std::lower_bound(ptr, ptr + n + 1, (int)target) - ptr);
+      r = std::min(n, (r + 16) / 32 * 32);
+      lo[b] = std::max(r, lo[b - 1]);
+    }
+    lo[grid] = n;
+    // sliced ELL copy of the matrix
+    std::vector<long> soff(nslice + 1, 0);
+    std::vector<int> len(n);
+    for (int sl = 0; sl < nslice; sl++) {
+      int w = 0;
+      for (int i = sl * 32; i < std::min(n, sl * 32 + 32); i++) w = std::max(w, ptr[i + 1] - ptr[i]);
+      soff[sl + 1] = soff[sl] + 32L * w;
+    }
+    std::vector<int> scol(soff[nslice], 0);
+    std::vector<double> sval(val ? soff[nslice] : 0, 0.0);
+    for (int i = 0; i < n; i++) {
+      len[i] = ptr[i + 1] - ptr[i];
+      const long e0 = soff[i / 32] + (i % 32);
+      for (int t = 0; t < len[i]; t++) {
+        scol[e0 + 32L * t] = col[ptr[i] + t];
+        if (val) sval[e0 + 32L * t] = val[ptr[i] + t];
+      }
+    }
+    std::vector<int> dlo(grid), dhi(grid);
+    for (int b = 0; b < grid; b++) {
+      int cmin = INT32_MAX, cmax = -1;
+      for (long q = ptr[lo[b]]; q < ptr[lo[b + 1]]; q++) {
+        cmin = std::min(cmin, col[q]);
+        cmax = std::max(cmax, col[q]);
+      }
+      if (cmax < 0) { dlo[b] = b; dhi[b] = b; continue; }
+      // CTA owning column c: the last b' with lo[b'] <= c (empty ranges skipped)
+      dlo[b] = (int)(std::upper_bound(lo.begin(), lo.end() - 1, cmin) - lo.begin()) - 1;
+      dhi[b] = (int)(std::upper_bound(lo.begin(), lo.end() - 1, cmax) - lo.begin()) - 1;
+    }
+    p->wave_grid = grid;
+    p->pipe_grid = grid;
+    WaveArgs &w = p->wave;
+    w.n = n; w.nlevel = nlevel; w.nblk = grid; w.base = 0; w.err = p->d_err;
+    if (val) { w.sval2 = nullptr; } else { w.rdeg = p->d_coef; w.rdeg2 = p->d_coef2; }
+    int *d_lo = nullptr, *d_dlo = nullptr, *d_dhi = nullptr;
+    rc = dev_copy(p, (long **)&w.sell_off, soff.data(), soff.size());
+    if (!rc) rc = dev_copy(p, (int **)&w.len, len.data(), len.size());
+    if (!rc) rc = dev_copy(p, (int **)&w.scol, scol.data(), scol.size());
+    if (!rc && val) rc = dev_copy(p, (double **)&w.sval, sval.data(), sval.size());
+    if (!rc && val && arith == MPKG_ARITH_DF64) {
+      float2 *sv2 = nullptr;
+      rc = dev_alloc(p, &sv2, sval.size());
+      if (!rc) {
+        split_kernel<<<256, 256, 0, p->stream>>>(w.sval, sv2, (long)sval.size());
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(p->stream) != cudaSuccess)
+          rc = fail(kECuda, "split of the sliced values failed");
+      }
+      w.sval2 = sv2;
+    }
+    if (!rc) rc = dev_copy(p, &d_lo, lo.data(), lo.size());
+    if (!rc) rc = dev_copy(p, &d_dlo, dlo.data(), dlo.size());
+    if (!rc) rc = dev_copy(p, &d_dhi, dhi.data(), dhi.size());
+    if (!rc) rc = dev_alloc(p, &w.flags, (size_t)grid);
+    if (!rc && arith == MPKG_ARITH_DF64) rc = dev_alloc(p, &w.shadow, (size_t)(nlevel + 1) * n);
+    w.row_lo = d_lo; w.dep_lo = d_dlo; w.dep_hi = d_dhi;
+    long reach = 0;
+    for (int b = 0; b < grid; b++) reach = std::max<long>(reach, std::max(b - dlo[b], dhi[b] - b));
+    p->pipe_reach = (int)reach;
+    p->rows_computed = (long)n * nlevel;
+  }
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
+namespace {
+
+// Device state of one (lpr, vw, budget, grid) configuration of a batch plan.
+int batch_configure(mpkg_plan *p, const BatchHost &h, int lpr, int vw, long budget, int grid) {
+  std::vector<int> lo, dlo, dhi;
+  int ngroup = 0;
+  batch_layout(h, p->batch.nrhs, budget, grid, &lo, &dlo, &dhi, &ngroup);
+  BatchArgs &a = p->batch;
+  // previous layout arrays are freed with the plan (owned list); small
+  int *d_lo = nullptr, *d_dlo = nullptr, *d_dhi = nullptr;
+  unsigned int *d_flags = nullptr;
+  int rc = dev_copy(p, &d_lo, lo.data(), lo.size());
+  if (!rc) rc = dev_copy(p, &d_dlo, dlo.data(), dlo.size());
+  if (!rc) rc = dev_copy(p, &d_dhi, dhi.data(), dhi.size());
+  if (!rc) rc = dev_alloc(p, &d_flags, (size_t)grid);
+  if (rc) return rc;
+  a.row_lo = d_lo; a.dep_lo = d_dlo; a.dep_hi = d_dhi; a.flags = d_flags;
+  a.nblk = grid; a.ngroup = ngroup; a.base = 0;
+  p->batch_lpr = lpr; p->batch_vw = vw; p->batch_group_bytes = budget;
+  p->pipe_grid = grid;
+  if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
+  if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+  p->graph_ok = false;
+  p->graph_key = nullptr;
+  return kOk;
+}
+
+}  // namespace
+
+int mpkg_plan_batch(int nmat, const int *n, const int *const *ptr, const int *const *col, const float *const *val,
+                    int nrhs, int nlevel, int tune, mpkg_plan **out) {
+  clear_error();
+  if (!out || nmat <= 0 || !n || !ptr || !col || !val) return fail(kEInval, "bad argument");
+  *out = nullptr;
+  if (nlevel <= 0 || nlevel > 64) return fail(kEInval, "nlevel must be in [1, 64]");
+  if (nrhs <= 0 || nrhs > 128 || (nrhs & (nrhs - 1)) != 0) return fail(kEInval, "nrhs must be a power of two <= 128");
+  BatchHost h;
+  h.mat_row0.assign(nmat + 1, 0);
+  long nnz = 0;
+  for (int m = 0; m < nmat; m++) {
+    int rc = check_csr(n[m], ptr[m], col[m]);
+    if (rc) return rc;
+    if (!val[m]) return fail(kEInval, "the batched form needs matrix values");
+    h.mat_row0[m + 1] = h.mat_row0[m] + n[m];
+    nnz += ptr[m][n[m]];
+  }
+  h.N = h.mat_row0[nmat];
+  if (h.N > INT32_MAX / 2 || nnz > INT32_MAX) return fail(kERange, "batch exceeds 2^30 rows or 2^31 nonzeros");
+  if ((double)(nlevel + 1) * h.N * nrhs * 4 > 1.5e11) return fail(kERange, "batch vectors exceed 150 GB");
+  h.ptr.resize(h.N + 1);
+  h.col.resize(nnz);
+  h.val.resize(nnz);
+  long q = 0;
+  for (int m = 0; m < nmat; m++) {
+    const long r0 = h.mat_row0[m];
+    for (int i = 0; i < n[m]; i++) {
+      h.ptr[r0 + i] = (int)q;
+      for (int t = ptr[m][i]; t < ptr[m][i + 1]; t++, q++) {
+        h.col[q] = (int)(col[m][t] + r0);
+        h.val[q] = val[m][t];
+      }
+    }
+  }
+  h.ptr[h.N] = (int)q;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  p->exec = MPKG_EXEC_BATCH;
+  p->n = (int)h.N; p->nlevel = nlevel; p->valued = true; p->arith = MPKG_ARITH_FMA;
+  p->nnz = nnz;
+  p->rows_computed = h.N * nlevel;
+  p->batch_nmat = nmat;
+  int rc = cudaGetDevice(&p->device) == cudaSuccess ? kOk : fail(kECuda, "cudaGetDevice failed");
+  if (!rc && cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(kECuda, "stream creation failed");
+  BatchArgs &a = p->batch;
+  a.N = h.N; a.nrhs = nrhs; a.nlevel = nlevel;
+  int *d_ptr = nullptr, *d_col = nullptr;
+  float *d_val = nullptr;
+  if (!rc) rc = dev_copy(p, &d_ptr, h.ptr.data(), h.ptr.size());
+  if (!rc) rc = dev_copy(p, &d_col, h.col.data(), h.col.size());
+  if (!rc) rc = dev_copy(p, &d_val, h.val.data(), h.val.size());
+  if (!rc) rc = dev_alloc(p, &p->d_err, 1);
+  if (!rc && cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) rc = fail(kECuda, "memset failed");
+  a.ptr = d_ptr; a.col = d_col; a.val = d_val; a.err = p->d_err;
+  int nsm = 0;
+  if (!rc && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
+    rc = fail(kECuda, "device query failed");
+  // candidates: lanes x vector width covering nrhs, group budget, CTAs per SM
+  struct Cand { int lpr, vw; long budget; int grid; };
+  std::vector<Cand> cands;
+  for (int vw : {4, 2, 1}) {
+    if (nrhs % vw) continue;
+    const int lpr = nrhs / vw;
+    if (lpr > 32) continue;
+    int per_sm = 0;
+    if (!rc && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_for(lpr, vw), 256, 0) != cudaSuccess)
+      rc = fail(kECuda, "occupancy query failed");
+    if (rc || per_sm <= 0) continue;
+    for (long budget : {32L << 20, 64L << 20, 1L << 40})
+      for (int occ : {per_sm, std::max(1, per_sm / 2)}) {
+        cands.push_back({lpr, vw, budget, std::max(1, std::min<int>(occ * nsm, (int)std::min<long>(h.N, INT32_MAX)))});
+        if (occ == std::max(1, per_sm / 2)) break;
+      }
+  }
+  if (!rc && cands.empty()) rc = fail(kEInval, "no kernel configuration for this nrhs");
+  Cand best = cands.empty() ? Cand{1, 1, 0, 1} : cands[0];
+  if (!rc && tune && cands.size() > 1) {
+    // time every candidate on the plan's own matrices (zero input; the
+    // arithmetic does not depend on the values)
+    float *scratch = nullptr;
+    const size_t total = (size_t)(nlevel + 1) * h.N * nrhs;
+    if (cudaMalloc(&scratch, sizeof(float) * total) != cudaSuccess) rc = fail(kENoMem, "autotune scratch");
+    if (!rc && cudaMemsetAsync(scratch, 0, sizeof(float) * total, p->stream) != cudaSuccess)
+      rc = fail(kECuda, "memset failed");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+      rc = fail(kECuda, "event creation failed");
+    float best_ms = 1e30f;
+    auto t_start = std::chrono::steady_clock::now();
+    for (const Cand &c : cands) {
+      if (rc) break;
+      if ((rc = batch_configure(p, h, c.lpr, c.vw, c.budget, c.grid))) break;
+      for (int w = 0; w < 2 && !rc; w++) rc = batch_launch_raw(p, scratch, p->stream, false);
+      if (!rc && cudaEventRecord(e0, p->stream) != cudaSuccess) rc = fail(kECuda, "event record");
+      for (int w = 0; w < 3 && !rc; w++) rc = batch_launch_raw(p, scratch, p->stream, false);
+      if (!rc && cudaEventRecord(e1, p->stream) != cudaSuccess) rc = fail(kECuda, "event record");
+      if (!rc) rc = mpkg_sync(p, p->stream);
+      float ms = 0.f;
+      if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = fail(kECuda, "event time");
+      if (!rc && ms < best_ms) { best_ms = ms; best = c; }
+    }
+    p->batch_tune_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (scratch) cudaFree(scratch);
+  }
+  p->batch_candidates = (int)cands.size();
+  if (!rc) rc = batch_configure(p, h, best.lpr, best.vw, best.budget, best.grid);
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
+int mpkg_batch_info(const mpkg_plan *p, mpkg_batch_info_t *info) {
+  if (!p || !info || p->exec != MPKG_EXEC_BATCH) return fail(kEInval, "not a batch plan");
+  std::memset(info, 0, sizeof *info);
+  info->nmat = p->batch_nmat;
+  info->rows = p->batch.N;
+  info->nnz = p->nnz;
+  info->nrhs = p->batch.nrhs;
+  info->nlevel = p->nlevel;
+  info->lanes_per_row = p->batch_lpr;
+  info->vector_width = p->batch_vw;
+  info->group_bytes = p->batch_group_bytes;
+  info->ngroup = p->batch.ngroup;
+  info->grid = p->batch.nblk;
+  info->graph = p->graph_ok ? 1 : 0;
+  info->candidates = p->batch_candidates;
+  info->tune_ms = p->batch_tune_ms;
+  info->device_bytes = p->device_bytes;
+  return kOk;
+}
+
+int mpkg_exec_batch_device(mpkg_plan *p, float *d_vb, void *stream) {
+  clear_error();
+  if (!p || !d_vb || p->exec != MPKG_EXEC_BATCH) return fail(kEInval, "bad plan or buffer");
+  if (((uintptr_t)d_vb) % 16) return fail(kEInval, "the basis buffer must be 16-byte aligned");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  p->launches = 1;
+  const int rc = batch_launch(p, d_vb, st);
+  if (rc) return rc;
+  CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+int mpkg_exec_batch_host(mpkg_plan *p, float *vb) {
+  clear_error();
+  if (!p || !vb || p->exec != MPKG_EXEC_BATCH) return fail(kEInval, "bad plan or buffer");
+  const size_t lv = (size_t)p->batch.N * p->batch.nrhs, total = lv * (p->nlevel + 1);
+  if (!p->d_fb) CUDA_TRY(cudaMalloc(&p->d_fb, sizeof(float) * total));
+  float *d = p->d_fb;
+  cudaStream_t st = p->stream;
+  CUDA_TRY(cudaMemcpyAsync(d, vb, sizeof(float) * lv, cudaMemcpyHostToDevice, st));
+  int rc = mpkg_exec_batch_device(p, d, st);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(vb + lv, d + lv, sizeof(float) * (total - lv), cudaMemcpyDeviceToHost, st));
+  return mpkg_sync(p, st);
+}
+
 int mpkg_plan_pdmpk(int npart, const char *const *buf_paths, const char *const *results_paths, int arith,
                     mpkg_plan **out) {
   clear_error();
@@ -1831,9 +2624,10 @@ int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream) {
 }
 
 int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels) {
-  if (!p || p->exec != MPKG_EXEC_PIPE || extra_levels < 0 || extra_levels > 1000)
-    return fail(kEInval, "stall hook needs a pipeline plan and 0 <= extra <= 1000");
+  if (!p || (p->exec != MPKG_EXEC_PIPE && p->exec != MPKG_EXEC_WAVE) || extra_levels < 0 || extra_levels > 1000)
+    return fail(kEInval, "stall hook needs a pipeline or wavefront plan and 0 <= extra <= 1000");
   p->pipe.stall = (uint32_t)extra_levels;
+  p->wave.stall = (uint32_t)extra_levels;
   return kOk;
 }
 
@@ -1849,6 +2643,7 @@ int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info) {
                    : p->exec == MPKG_EXEC_SPMV ? p->nlevel
                    : p->exec == MPKG_EXEC_BUFS ? 2 + 2 * p->nphase + 1
                    : p->exec == MPKG_EXEC_PDMPK ? 2 + 2 * p->nphase : 1;
+  if (p->exec == MPKG_EXEC_WAVE) info->pipe_grid = p->wave_grid;
   info->tiles_in_smem = p->tiles_smem ? 1 : 0;
   info->max_tile_slots = p->max_tile_slots;
   info->pipe_chunk = p->pipe.chunk;

@@ -395,4 +395,48 @@ int gen_diffusion_7pt(int nx, int ny, int nz, double sigma, double dominance, ui
   return assemble(n, nbr, dominance, g);
 }
 
+// Random banded operator: row i holds its diagonal plus m-1 distinct
+// off-diagonal columns drawn uniformly from [i-bw, i+bw] (m uniform in
+// [nmin, nmax], capped by the band), values N(0,1); the diagonal is
+// N(0,1) + sum |off-diagonals| + 1 (diagonally dominant).  Columns
+// ascending; seeded.
+int gen_banded(long n, int bw, int nmin, int nmax, uint64_t seed, Csr *g) {
+  if (n <= 0 || n > INT32_MAX / 2 || bw < 1 || nmin < 1 || nmax < nmin) return fail(kEInval, "bad banded parameters");
+  Normal rng(seed);
+  g->n = (int)n;
+  g->ptr.assign(n + 1, 0);
+  g->col.clear();
+  g->val.clear();
+  std::vector<long> pool;
+  std::vector<std::pair<long, double>> row;
+  for (long i = 0; i < n; i++) {
+    const long lo = std::max(0L, i - bw), hi = std::min(n - 1, i + (long)bw);
+    const long avail = hi - lo;  // off-diagonal candidates
+    long m = nmin + (long)(rng.next() % (uint64_t)(nmax - nmin + 1));
+    m = std::min(m - 1, avail);
+    pool.clear();
+    for (long j = lo; j <= hi; j++)
+      if (j != i) pool.push_back(j);
+    for (long k = 0; k < m; k++) {  // partial Fisher-Yates
+      const long r = k + (long)(rng.next() % (uint64_t)(pool.size() - k));
+      std::swap(pool[k], pool[r]);
+    }
+    row.clear();
+    double off = 0.0;
+    for (long k = 0; k < m; k++) {
+      const double v = rng();
+      off += std::fabs(v);
+      row.emplace_back(pool[k], v);
+    }
+    row.emplace_back(i, rng() + off + 1.0);
+    std::sort(row.begin(), row.end());
+    for (auto &e : row) {
+      g->col.push_back((int)e.first);
+      g->val.push_back(e.second);
+    }
+    g->ptr[i + 1] = (int)g->col.size();
+  }
+  return kOk;
+}
+
 }  // namespace mpkg

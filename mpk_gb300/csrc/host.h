@@ -69,6 +69,8 @@ int gen_laplacian(int nx, int ny, int nz, double diag, double off, Csr *g,
 int gen_diffusion_9pt(int nx, int ny, double sigma, double wx, double wy, double wdiag, double dominance,
                       uint64_t seed, Csr *g);
 int gen_diffusion_7pt(int nx, int ny, int nz, double sigma, double dominance, uint64_t seed, Csr *g);
+// Random banded, diagonally dominant operator (see graph.cc).
+int gen_banded(long n, int bw, int nmin, int nmax, uint64_t seed, Csr *g);
 // Uniform[-1, 1] doubles from a splitmix64 stream (seeded).
 void uniform_vector(uint64_t seed, long n, double *out);
 

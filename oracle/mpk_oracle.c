@@ -705,3 +705,25 @@ int orc_pd_exec(int P, orc_pd **b, const double *x, double *out, int mode) {
   free(sb);
   return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Batched block-vector MPK in FP32 (no reference counterpart: the      */
+/* batching form of the task).  V_l = A V_(l-1) for nrhs right-hand     */
+/* sides stored row-major (row i: V[i*nrhs .. i*nrhs+nrhs)), each row a  */
+/* single-precision fused multiply-add per entry in CSR order starting  */
+/* from 0 -- the arithmetic the GPU kernel performs.  vb holds          */
+/* (nlevel+1) levels of n*nrhs floats, level 0 = input.                 */
+/* ------------------------------------------------------------------ */
+void orc_spmm_f32(int n, const int *ptr, const int *col, const float *val, int nrhs, int nlevel, float *vb) {
+  const size_t lv = (size_t)n * nrhs;
+  for (int l = 1; l <= nlevel; l++) {
+    const float *src = vb + (l - 1) * lv;
+    float *dst = vb + l * lv;
+    for (int i = 0; i < n; i++)
+      for (int r = 0; r < nrhs; r++) {
+        float s = 0.0f;
+        for (int q = ptr[i]; q < ptr[i + 1]; q++) s = fmaf(val[q], src[(size_t)col[q] * nrhs + r], s);
+        dst[(size_t)i * nrhs + r] = s;
+      }
+  }
+}

@@ -313,3 +313,18 @@ def pd_exec(buf_paths, res_paths, x, mode=MODE_FMA):
     if o.orc_pd_exec(len(hs), arr, _p(xx), _p(out), mode) != 0:
         raise ValueError("oracle: inconsistent pdmpk buffers")
     return out
+
+
+def spmm_f32(ptr, col, val, X, nlevel):
+    """Batched FP32 block-vector chain, fmaf per entry in CSR order
+    (orc_spmm_f32); X: (n, nrhs) float32.  Returns (nlevel+1, n, nrhs)."""
+    o = lib()
+    o.orc_spmm_f32.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    n, nrhs = X.shape
+    p = np.ascontiguousarray(ptr, dtype=np.int32)
+    c = np.ascontiguousarray(col, dtype=np.int32)
+    v = np.ascontiguousarray(val, dtype=np.float32)
+    vb = np.zeros((nlevel + 1, n, nrhs), dtype=np.float32)
+    vb[0] = X
+    o.orc_spmm_f32(n, _p(p), _p(c), _p(v), nrhs, nlevel, _p(vb))
+    return vb

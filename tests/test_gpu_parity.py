@@ -38,7 +38,8 @@ def _plans(name, g, a, arith):
     n, npart, nlevel, nphase = int(g["n"]), int(g["npart"]), int(g["nlevel"]), int(g["nphase"])
     out = {"tasks": M.Plan.from_tasks(a, npart, nlevel, nphase, g["off"], g["idx"], arith=arith),
            "spmv": M.Plan.spmv(a, nlevel, arith=arith),
-           "pipe": M.Plan.pipe(a, nlevel, arith=arith)}
+           "pipe": M.Plan.pipe(a, nlevel, arith=arith),
+           "wave": M.Plan.wave(a, nlevel, arith=arith)}
     if nphase == 0:
         out["tiles"] = M.Plan.pa1(a, g["parts"][0], npart, nlevel, exec=M.EXEC_TILES, arith=arith)
         out["pa1_tasks"] = M.Plan.pa1(a, g["parts"][0], npart, nlevel, exec=M.EXEC_TASKS, arith=arith)
@@ -92,7 +93,8 @@ def test_all_ones_fixed_point_deg_operator(gpu):
     """The row-normalised operator maps 1 to 1 (mpk2/mpktest.c:43-51)."""
     a = M.Csr.laplacian(40, 30, 20).pattern()
     part = M.partition_rcb(a.coords, 64)
-    for plan in (M.Plan.pa1(a, part, 64, 6), M.Plan.pipe(a, 6), M.Plan.spmv(a, 6)):
+    for plan in (M.Plan.pa1(a, part, 64, 6), M.Plan.pipe(a, 6), M.Plan.spmv(a, 6), M.Plan.wave(a, 6),
+                 M.Plan.wave(a, 6, arith=M.ARITH_DF64)):
         vv = _run(plan, np.ones(a.n), a.n, 6)
         assert np.max(np.abs(vv - 1.0)) < 1e-14
 
@@ -102,7 +104,8 @@ def test_device_pointer_path_matches_host_path(gpu):
     a = M.Csr.laplacian(64, 64, 8)
     part = M.partition_rcb(a.coords, 32)
     x = M.uniform(11, a.n)
-    for plan in (M.Plan.pa1(a, part, 32, 5), M.Plan.pipe(a, 5), M.Plan.spmv(a, 5)):
+    for plan in (M.Plan.pa1(a, part, 32, 5), M.Plan.pipe(a, 5), M.Plan.spmv(a, 5), M.Plan.wave(a, 5),
+                 M.Plan.wave(a, 5, arith=M.ARITH_DF64)):
         want = _run(plan, x, a.n, 5)
         d = torch.zeros(6 * a.n, dtype=torch.float64, device="cuda")
         d[:a.n] = torch.from_numpy(x).cuda()
@@ -122,13 +125,14 @@ def config2():
     return a, part, x, want
 
 
-@pytest.mark.parametrize("ex", ["tiles", "pipe", "spmv"])
+@pytest.mark.parametrize("ex", ["tiles", "pipe", "spmv", "wave"])
 def test_config2_full_size_bitwise_vs_oracle(config2, ex, gpu):
     """128^3 7-point, k=8, 2048 parts: bit-identical to the oracle chain."""
     a, part, x, want = config2
     plan = {"tiles": lambda: M.Plan.pa1(a, part, 2048, 8),
             "pipe": lambda: M.Plan.pipe(a, 8),
-            "spmv": lambda: M.Plan.spmv(a, 8)}[ex]()
+            "spmv": lambda: M.Plan.spmv(a, 8),
+            "wave": lambda: M.Plan.wave(a, 8)}[ex]()
     vv = _run(plan, x, a.n, 8)
     bad = np.flatnonzero(vv.view(np.int64) != want.view(np.int64))
     assert bad.size == 0, f"{bad.size} differ, first {bad[:5]}"
@@ -153,7 +157,7 @@ def test_df64_executors_within_fp64_tolerance(name, valued, gpu):
         a = a.pattern()
     n, npart, nlevel, nphase = int(g["n"]), int(g["npart"]), int(g["nlevel"]), int(g["nphase"])
     want = O.mpk(a.ptr, a.col, a.val, g["x"], nlevel, O.MODE_FMA)
-    plans = {"pipe": M.Plan.pipe(a, nlevel, arith=M.ARITH_DF64)}
+    plans = {"pipe": M.Plan.pipe(a, nlevel, arith=M.ARITH_DF64), "wave": M.Plan.wave(a, nlevel, arith=M.ARITH_DF64)}
     if nphase == 0:
         plans["tiles"] = M.Plan.pa1(a, g["parts"][0], npart, nlevel, arith=M.ARITH_DF64)
     for ex, plan in plans.items():
@@ -163,22 +167,24 @@ def test_df64_executors_within_fp64_tolerance(name, valued, gpu):
         assert max(errs) <= TOL, (ex, errs)
 
 
-@pytest.mark.parametrize("ex", ["tiles", "pipe"])
+@pytest.mark.parametrize("ex", ["tiles", "pipe", "wave"])
 def test_config2_df64_within_fp64_tolerance(config2, ex, gpu):
     a, part, x, want = config2
-    plan = (M.Plan.pa1(a, part, 2048, 8, arith=M.ARITH_DF64) if ex == "tiles"
-            else M.Plan.pipe(a, 8, arith=M.ARITH_DF64))
+    plan = {"tiles": lambda: M.Plan.pa1(a, part, 2048, 8, arith=M.ARITH_DF64),
+            "pipe": lambda: M.Plan.pipe(a, 8, arith=M.ARITH_DF64),
+            "wave": lambda: M.Plan.wave(a, 8, arith=M.ARITH_DF64)}[ex]()
     vv = _run(plan, x, a.n, 8)
     errs = _rel_errors(vv, want, a.n, 8)
     assert max(errs) <= TOL, errs
 
 
-def test_pipeline_wait_times_out_and_recovers(gpu):
+@pytest.mark.parametrize("kind", ["pipe", "wave"])
+def test_pipeline_wait_times_out_and_recovers(kind, gpu):
     """A dependency flag that is never set: the bounded waits give up, the
     call reports ETIMEOUT, and the same plan then runs correctly."""
     a = M.Csr.laplacian(64, 64, 4)
     x = M.uniform(5, a.n)
-    plan = M.Plan.pipe(a, 4)
+    plan = M.Plan.pipe(a, 4) if kind == "pipe" else M.Plan.wave(a, 4)
     plan.debug_stall(100)
     vv = np.zeros(5 * a.n)
     vv[:a.n] = x
