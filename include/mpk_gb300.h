@@ -160,6 +160,63 @@ int mpkg_exec_batch_device(mpkg_plan *p, float *d_vb, void *stream);
 /* vb: host buffer as above; copies level 0 in and levels 1..nlevel out. */
 int mpkg_exec_batch_host(mpkg_plan *p, float *vb);
 
+/* ---- s-step CG and its basis shifts (no counterpart in the reference) ----
+ * The consumer of the MPK basis.  Precision: FP32 matrix values and
+ * basis vectors, FP64 Gram matrix Y^T Y and coefficient-space iteration on
+ * the GPU, FP64 x and true residual (recomputed every outer iteration). */
+typedef struct {
+  int iterations;   /* outer iterations (s-step) or CG iterations */
+  int mpk_steps;    /* inner CG steps taken (s per outer iteration) */
+  int converged;    /* relres <= tol */
+  int breakdowns;   /* inner loops stopped early (non-positive curvature) */
+  double relres;    /* final true relative residual |b - A x| / |b| */
+  double basis_cond;/* largest condition number of the s+1 vectors
+                       p, rho_1(A) p, ..., rho_s(A) p over the outer iterations */
+  double ms;        /* wall time of the call */
+} mpkg_cg_info_t;
+
+/* Standard FP64 conjugate gradients on the GPU (the reference iteration
+ * count).  x: initial guess in, solution out. */
+int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const double *b, double *x, double tol,
+            int max_iter, mpkg_cg_info_t *info);
+/* s-step CG (s <= 10): Newton basis rho_(j+1) = (A - shifts[j]) rho_j /
+ * scale (shifts NULL: monomial basis), 2s+1 FP32 basis vectors per outer
+ * iteration, FP64 Gram + coefficient solve, FP64 residual replacement. */
+int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, const double *b, double *x, int s,
+                  const double *shifts, double scale, double tol, int max_outer, mpkg_cg_info_t *info);
+/* m steps of Lanczos (FP64, GPU) from a seeded uniform start vector: the m
+ * Ritz values ascending (and the tridiagonal when alpha/beta are given). */
+int mpkg_lanczos(int n, const int *ptr, const int *col, const double *val, int m, uint64_t seed, double *ritz,
+                 double *alpha, double *beta);
+/* Eigenvalues of a symmetric tridiagonal matrix (bisection), ascending. */
+void mpkg_tridiag_eigs(int m, const double *alpha, const double *beta, double *out);
+/* Leja ordering of k points (in place): largest modulus first, then each
+ * next point maximises the product of distances to those chosen. */
+void mpkg_leja_order(int k, double *x);
+
+/* Cheap matrix features (GPU): Gershgorin bounds, diagonal, off-diagonal
+ * and row-norm statistics, degrees, diagonal dominance; normalised by the
+ * Gershgorin upper bound.  glo/ghi receive the bounds. */
+#define MPKG_NFEAT 12
+int mpkg_features(int n, const int *ptr, const int *col, const double *val, float *feat, double *glo, double *ghi);
+
+/* MLP nin -> width -> width -> nout (ReLU, linear output, MSE), FP32,
+ * trained and evaluated by the library's own GPU kernels. */
+typedef struct mpkg_mlp mpkg_mlp;
+int mpkg_mlp_create(int nin, int width, int nout, uint64_t seed, mpkg_mlp **out);
+void mpkg_mlp_destroy(mpkg_mlp *m);
+int mpkg_mlp_nparams(const mpkg_mlp *m);
+/* parameters flat: W1 (width x nin), b1, W2 (width x width), b2,
+ * W3 (nout x width), b3; row-major */
+int mpkg_mlp_get_params(const mpkg_mlp *m, float *params);
+int mpkg_mlp_set_params(mpkg_mlp *m, const float *params);
+int mpkg_mlp_forward(mpkg_mlp *m, int nsamples, const float *X, float *Y);
+/* gradient of the mean squared error over the samples (and the loss) */
+int mpkg_mlp_gradient(mpkg_mlp *m, int nsamples, const float *X, const float *T, float *grad, float *loss);
+/* Adam over shuffled minibatches (seeded); loss_curve: mean loss per epoch */
+int mpkg_mlp_train(mpkg_mlp *m, int nsamples, const float *X, const float *T, int epochs, int batch, float lr,
+                   uint64_t seed, float *loss_curve);
+
 /* MPI-2 rank buffers rank0.bufs .. rank{npart-1}.bufs in `dir` (the files
  * mpi2_mpkwrtbufs writes, mpk2/buffers.c:588-631; values required) run on
  * one GPU: each phase's per-rank computation (mpk2/mpi2_mpkexecbufs_val.c:

@@ -56,6 +56,11 @@ class BatchInfo(C.Structure):
                 ("tune_ms", C.c_double), ("device_bytes", C.c_long)]
 
 
+class CgInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("mpk_steps", C.c_int), ("converged", C.c_int), ("breakdowns", C.c_int),
+                ("relres", C.c_double), ("basis_cond", C.c_double), ("ms", C.c_double)]
+
+
 class PlanInfo(C.Structure):
     _fields_ = [("n", C.c_int), ("nlevel", C.c_int), ("nphase", C.c_int), ("npart", C.c_int),
                 ("exec", C.c_int), ("arith", C.c_int), ("valued", C.c_int),
@@ -74,6 +79,20 @@ def _declare(L):
         "mpkg_plan_spmv": (I, [I, P, P, P, I, I, pp]),
         "mpkg_plan_wave": (I, [I, P, P, P, I, I, pp]),
         "mpkg_plan_batch": (I, [I, P, P, P, P, I, I, I, pp]),
+        "mpkg_cg": (I, [I, P, P, P, P, P, D, I, C.POINTER(CgInfo)]),
+        "mpkg_sstep_cg": (I, [I, P, P, P, P, P, I, P, D, D, I, C.POINTER(CgInfo)]),
+        "mpkg_lanczos": (I, [I, P, P, P, I, C.c_uint64, P, P, P]),
+        "mpkg_tridiag_eigs": (None, [I, P, P, P]),
+        "mpkg_leja_order": (None, [I, P]),
+        "mpkg_features": (I, [I, P, P, P, P, C.POINTER(D), C.POINTER(D)]),
+        "mpkg_mlp_create": (I, [I, I, I, C.c_uint64, pp]),
+        "mpkg_mlp_destroy": (None, [P]),
+        "mpkg_mlp_nparams": (I, [P]),
+        "mpkg_mlp_get_params": (I, [P, P]),
+        "mpkg_mlp_set_params": (I, [P, P]),
+        "mpkg_mlp_forward": (I, [P, I, P, P]),
+        "mpkg_mlp_gradient": (I, [P, I, P, P, P, P]),
+        "mpkg_mlp_train": (I, [P, I, P, P, I, I, C.c_float, C.c_uint64, P]),
         "mpkg_batch_info": (I, [P, C.POINTER(BatchInfo)]),
         "mpkg_exec_batch_device": (I, [P, P, P]),
         "mpkg_exec_batch_host": (I, [P, P]),
@@ -522,6 +541,122 @@ class Plan:
     def close(self):
         if self._h is not None and self._h.value:
             lib().mpkg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- s-step CG
+NFEAT = 12
+
+
+def _info_dict(inf):
+    return {k: getattr(inf, k) for k, _ in CgInfo._fields_}
+
+
+def cg(a: Csr, b, x0=None, tol=1e-8, max_iter=10000):
+    """Standard FP64 CG on the GPU: (x, info)."""
+    x = np.zeros(a.n) if x0 is None else np.array(x0, dtype=np.float64)
+    b = _f64(b)
+    inf = CgInfo()
+    _check(lib().mpkg_cg(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), _ptr(b), _ptr(x), tol, max_iter,
+                         C.byref(inf)))
+    return x, _info_dict(inf)
+
+
+def sstep_cg(a: Csr, b, s=8, shifts=None, scale=None, x0=None, tol=1e-8, max_outer=2000):
+    """s-step CG with an FP32 Newton basis (shifts None: monomial) scaled
+    by `scale` per step (default: the Gershgorin upper bound / 2)."""
+    x = np.zeros(a.n) if x0 is None else np.array(x0, dtype=np.float64)
+    b = _f64(b)
+    if scale is None:
+        _, glo, ghi = features(a)
+        scale = ghi / 2.0
+    sh = None if shifts is None else _f64(np.asarray(shifts, dtype=np.float64))
+    inf = CgInfo()
+    _check(lib().mpkg_sstep_cg(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), _ptr(b), _ptr(x), s,
+                               None if sh is None else _ptr(sh), float(scale), tol, max_outer, C.byref(inf)))
+    return x, _info_dict(inf)
+
+
+def lanczos(a: Csr, m, seed=0):
+    """Ritz values (ascending) of m Lanczos steps, and the tridiagonal."""
+    r, al, be = np.zeros(m), np.zeros(m), np.zeros(max(m - 1, 1))
+    _check(lib().mpkg_lanczos(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), m, seed, _ptr(r), _ptr(al), _ptr(be)))
+    return r, al, be
+
+
+def tridiag_eigs(alpha, beta):
+    al, be = _f64(alpha), _f64(beta if len(beta) else np.zeros(1))
+    out = np.zeros(len(al))
+    lib().mpkg_tridiag_eigs(len(al), _ptr(al), _ptr(be), _ptr(out))
+    return out
+
+
+def leja(points):
+    x = np.array(points, dtype=np.float64)
+    lib().mpkg_leja_order(len(x), _ptr(x))
+    return x
+
+
+def features(a: Csr):
+    """(features[NFEAT] float32, Gershgorin lower, upper)."""
+    f = np.zeros(NFEAT, dtype=np.float32)
+    lo, hi = C.c_double(), C.c_double()
+    _check(lib().mpkg_features(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), _ptr(f), C.byref(lo), C.byref(hi)))
+    return f, lo.value, hi.value
+
+
+class Mlp:
+    """nin -> width -> width -> nout MLP trained by the library's GPU kernels."""
+
+    def __init__(self, nin=NFEAT, width=64, nout=8, seed=0):
+        h = C.c_void_p()
+        _check(lib().mpkg_mlp_create(nin, width, nout, seed, C.byref(h)))
+        self._h, self.nin, self.width, self.nout = h, nin, width, nout
+
+    @property
+    def nparams(self):
+        return lib().mpkg_mlp_nparams(self._h)
+
+    def params(self):
+        p = np.zeros(self.nparams, dtype=np.float32)
+        _check(lib().mpkg_mlp_get_params(self._h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparams
+        _check(lib().mpkg_mlp_set_params(self._h, _ptr(p)))
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.nout), dtype=np.float32)
+        _check(lib().mpkg_mlp_forward(self._h, X.shape[0], _ptr(X), _ptr(Y)))
+        return Y
+
+    def gradient(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        g = np.zeros(self.nparams, dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().mpkg_mlp_gradient(self._h, X.shape[0], _ptr(X), _ptr(T), _ptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, X, T, epochs=200, batch=64, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        curve = np.zeros(epochs, dtype=np.float32)
+        _check(lib().mpkg_mlp_train(self._h, X.shape[0], _ptr(X), _ptr(T), epochs, batch, lr, seed, _ptr(curve)))
+        return curve
+
+    def close(self):
+        if self._h:
+            lib().mpkg_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):

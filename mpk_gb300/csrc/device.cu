@@ -787,18 +787,22 @@ struct WaveArgs {
   uint32_t stall;              // test hook: extra levels to wait for (never published)
   // matrix in sliced ELL (32 rows per slice, entry t of row 32s+j at
   // sell_off[s] + 32t + j, CSR order within the row), so that a warp's
-  // column and value loads are 128-byte coalesced
+  // column and value loads are coalesced; columns as int16 offsets from
+  // the row when every |col - row| < 32768, else int32
   const long *sell_off;        // nslice + 1
-  const int *len;              // entries per row
-  const int *scol;             // column of each slot
+  const unsigned short *len;   // entries per row
+  const int *scol;             // column of each slot (int32 form) ...
+  const short *srel;           // ... or col - row (int16 form)
   const double *sval;          // value of each slot (valued) ...
   const float2 *sval2;         // ... or its double-float split
   const double *rdeg;          // 1/deg per row (1/deg operator) ...
   const float2 *rdeg2;         // ... or its double-float split
+  const double *lut;           // 1/d for d < 256 (exactly the rows' 1/deg) ...
+  const float2 *lut2;          // ... and its double-float split
   double *vv;
-  float2 *shadow;              // (nlevel + 1) * n, double-float copies of the levels
+  float2 *ring;                // 2 * n: double-float copies of levels l-1 and l
   const int *row_lo;           // nblk + 1
-  const int *dep_lo, *dep_hi;  // per CTA
+  const int *dep_lo, *dep_hi;  // per CTA: CTAs it reads from or that read from it
   unsigned int *flags;         // per CTA: last level published
   int *err;
 };
@@ -828,12 +832,21 @@ __device__ __forceinline__ void wave_publish(const WaveArgs &a, int b, unsigned 
   }
 }
 
+template <bool REL>
+__device__ __forceinline__ int wave_col(const WaveArgs &a, long e, int i) {
+  return REL ? i + (int)__ldg(a.srel + e) : __ldg(a.scol + e);
+}
+
 // FP64 rows (fma or separate multiply/add, CSR order as the reference).
-// A warp computes one 32-row slice; CTA row ranges start on slices.
-template <int ARITH, bool VALUED>
+// A warp computes one 32-row slice; CTA row ranges start on slices.  The
+// previous level is read from vv: every address of it is fresh in this
+// launch, so L1 holds no stale copy.
+template <int ARITH, bool VALUED, bool REL>
 __global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
   __shared__ int s_abort;
+  __shared__ double s_lut[256];
   if (threadIdx.x == 0) s_abort = 0;
+  if (!VALUED) s_lut[threadIdx.x] = a.lut[threadIdx.x];
   __syncthreads();
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -846,14 +859,14 @@ __global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
       if (i >= r1) continue;
       const int len = __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
-      const double cf = VALUED ? 0.0 : __ldg(a.rdeg + i);
+      const double cf = VALUED ? 0.0 : (len < 256 ? s_lut[len] : __ldg(a.rdeg + i));
       double s = 0.0;
       int t = 0;
       if (len <= 8) {  // all column loads, then all gathers, in flight together
         int c[8];
         double x[8], v[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) c[u] = u < len ? __ldg(a.scol + e0 + 32L * u) : 0;
+        for (int u = 0; u < 8; u++) c[u] = u < len ? wave_col<REL>(a, e0 + 32L * u, i) : 0;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
           x[u] = u < len ? src[c[u]] : 0.0;
@@ -864,21 +877,8 @@ __global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
           if (u < len) s = row_term<ARITH>(s, v[u], x[u]);
         t = len;
       }
-      for (; t + 4 <= len; t += 4) {
-        int c[4];
-        double x[4], v[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) c[u] = __ldg(a.scol + e0 + 32L * (t + u));
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          x[u] = src[c[u]];
-          v[u] = VALUED ? __ldg(a.sval + e0 + 32L * (t + u)) : cf;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) s = row_term<ARITH>(s, v[u], x[u]);
-      }
       for (; t < len; t++)
-        s = row_term<ARITH>(s, VALUED ? __ldg(a.sval + e0 + 32L * t) : cf, src[__ldg(a.scol + e0 + 32L * t)]);
+        s = row_term<ARITH>(s, VALUED ? __ldg(a.sval + e0 + 32L * t) : cf, src[wave_col<REL>(a, e0 + 32L * t, i)]);
       __stcs(dst + i, s);
     }
     wave_publish(a, b, a.base + (unsigned)l);
@@ -887,20 +887,26 @@ __global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
 
 // Double-float rows.  1/deg operator: the row's values are summed in
 // double-float, then scaled once by 1/deg; valued operator: double-float
-// multiply-add per entry.  Level 0 first splits the CTA's own rows of x.
-template <bool VALUED>
-__global__ void __launch_bounds__(256) wave_df_kernel(WaveArgs a) {
+// multiply-add per entry.  Levels travel through a two-slot ring of
+// double-float copies (level l in slot l&1); a CTA overwrites a slot only
+// after every CTA that reads its rows has finished the level before, which
+// the symmetric dependency ranges guarantee.  Level 0 splits the CTA's
+// own rows of x.
+template <bool VALUED, bool REL>
+__global__ void __launch_bounds__(256, 4) wave_df_kernel(WaveArgs a) {
   __shared__ int s_abort;
+  __shared__ float2 s_lut[256];
   if (threadIdx.x == 0) s_abort = 0;
+  if (!VALUED) s_lut[threadIdx.x] = a.lut2[threadIdx.x];
   __syncthreads();
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) a.shadow[i] = df_split(a.vv[i]);
+  for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) a.ring[i] = df_split(a.vv[i]);
   wave_publish(a, b, a.base);
   for (int l = 1; l <= a.nlevel; l++) {
     if (!wave_wait(a, b, a.base + (unsigned)(l - 1), &s_abort)) return;
-    const float2 *src = a.shadow + (size_t)(l - 1) * a.n;
-    float2 *sdst = a.shadow + (size_t)l * a.n;
+    const float2 *src = a.ring + (size_t)((l - 1) & 1) * a.n;
+    float2 *sdst = a.ring + (size_t)(l & 1) * a.n;
     double *dst = a.vv + (size_t)l * a.n;
     for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
       const int i = (sl << 5) + lane;
@@ -913,7 +919,7 @@ __global__ void __launch_bounds__(256) wave_df_kernel(WaveArgs a) {
         int c[8];
         float2 x[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) c[u] = u < len ? __ldg(a.scol + e0 + 32L * u) : 0;
+        for (int u = 0; u < 8; u++) c[u] = u < len ? wave_col<REL>(a, e0 + 32L * u, i) : 0;
 #pragma unroll
         for (int u = 0; u < 8; u++) x[u] = u < len ? src[c[u]] : make_float2(0.f, 0.f);
 #pragma unroll
@@ -925,26 +931,13 @@ __global__ void __launch_bounds__(256) wave_df_kernel(WaveArgs a) {
         }
         t = len;
       }
-      for (; t + 4 <= len; t += 4) {
-        int c[4];
-        float2 x[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) c[u] = __ldg(a.scol + e0 + 32L * (t + u));
-#pragma unroll
-        for (int u = 0; u < 4; u++) x[u] = src[c[u]];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          if (VALUED) df_mac(a.sval2[e0 + 32L * (t + u)], x[u], sh, sl_);
-          else df_acc(x[u], sh, sl_);
-        }
-      }
       for (; t < len; t++) {
-        const float2 x = src[__ldg(a.scol + e0 + 32L * t)];
+        const float2 x = src[wave_col<REL>(a, e0 + 32L * t, i)];
         if (VALUED) df_mac(a.sval2[e0 + 32L * t], x, sh, sl_);
         else df_acc(x, sh, sl_);
       }
       float2 v = df_norm(sh, sl_);
-      if (!VALUED) v = df_scale(a.rdeg2[i], v);
+      if (!VALUED) v = df_scale(len < 256 ? s_lut[len] : a.rdeg2[i], v);
       sdst[i] = v;
       __stcs(dst + i, df_to_double(v));
     }
@@ -1224,6 +1217,7 @@ struct mpkg_plan {
   // wavefront executor
   WaveArgs wave{};
   int wave_grid = 0;
+  bool wave_rel = false;
   // batched block-vector form
   BatchArgs batch{};
   int batch_lpr = 0, batch_vw = 0, batch_nmat = 0;
@@ -1451,11 +1445,17 @@ int wave_occupancy(mpkg_plan *p, K kernel, int *grid) {
 }
 
 void *wave_kernel_ptr(const mpkg_plan *p) {
-  if (p->arith == MPKG_ARITH_DF64)
-    return p->valued ? (void *)wave_df_kernel<true> : (void *)wave_df_kernel<false>;
-  if (p->arith == MPKG_ARITH_SEPARATE)
-    return p->valued ? (void *)wave_kernel<MPKG_ARITH_SEPARATE, true> : (void *)wave_kernel<MPKG_ARITH_SEPARATE, false>;
-  return p->valued ? (void *)wave_kernel<MPKG_ARITH_FMA, true> : (void *)wave_kernel<MPKG_ARITH_FMA, false>;
+  const bool rel = p->wave_rel;
+#define MPKG_WK(REL)                                                                                        \
+  if (p->arith == MPKG_ARITH_DF64)                                                                          \
+    return p->valued ? (void *)wave_df_kernel<true, REL> : (void *)wave_df_kernel<false, REL>;             \
+  if (p->arith == MPKG_ARITH_SEPARATE)                                                                      \
+    return p->valued ? (void *)wave_kernel<MPKG_ARITH_SEPARATE, true, REL>                                  \
+                     : (void *)wave_kernel<MPKG_ARITH_SEPARATE, false, REL>;                                \
+  return p->valued ? (void *)wave_kernel<MPKG_ARITH_FMA, true, REL> : (void *)wave_kernel<MPKG_ARITH_FMA, false, REL>;
+  if (rel) { MPKG_WK(true) }
+  MPKG_WK(false)
+#undef MPKG_WK
 }
 
 int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st) {
@@ -2121,6 +2121,15 @@ int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int
   if (!p) return fail(kENoMem, "plan allocation failed");
   p->exec = MPKG_EXEC_WAVE;
   int rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  if (!rc) {
+    bool rel = true;
+    for (int i = 0; i < n && rel; i++) {
+      if (ptr[i + 1] - ptr[i] > 65535) rc = fail(kERange, "wavefront executor: a row has more than 65535 entries");
+      for (int q = ptr[i]; q < ptr[i + 1]; q++)
+        if (col[q] - i < -32768 || col[q] - i > 32767) { rel = false; break; }
+    }
+    p->wave_rel = rel;
+  }
   int grid = 0;
   if (!rc) rc = wave_occupancy(p, (const void *)wave_kernel_ptr(p), &grid);
   if (!rc) {
@@ -2138,22 +2147,26 @@ int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int
     lo[grid] = n;
     // sliced ELL copy of the matrix
     std::vector<long> soff(nslice + 1, 0);
-    std::vector<int> len(n);
+    std::vector<unsigned short> len(n);
     for (int sl = 0; sl < nslice; sl++) {
       int w = 0;
       for (int i = sl * 32; i < std::min(n, sl * 32 + 32); i++) w = std::max(w, ptr[i + 1] - ptr[i]);
       soff[sl + 1] = soff[sl] + 32L * w;
     }
-    std::vector<int> scol(soff[nslice], 0);
+    std::vector<int> scol(p->wave_rel ? 0 : soff[nslice], 0);
+    std::vector<short> srel(p->wave_rel ? soff[nslice] : 0, 0);
     std::vector<double> sval(val ? soff[nslice] : 0, 0.0);
     for (int i = 0; i < n; i++) {
-      len[i] = ptr[i + 1] - ptr[i];
+      len[i] = (unsigned short)(ptr[i + 1] - ptr[i]);
       const long e0 = soff[i / 32] + (i % 32);
       for (int t = 0; t < len[i]; t++) {
-        scol[e0 + 32L * t] = col[ptr[i] + t];
+        if (p->wave_rel) srel[e0 + 32L * t] = (short)(col[ptr[i] + t] - i);
+        else scol[e0 + 32L * t] = col[ptr[i] + t];
         if (val) sval[e0 + 32L * t] = val[ptr[i] + t];
       }
     }
+    // CTA owning column c: the last b' with lo[b'] <= c (empty ranges skipped)
+    auto owner = [&](int c) { return (int)(std::upper_bound(lo.begin(), lo.end() - 1, c) - lo.begin()) - 1; };
     std::vector<int> dlo(grid), dhi(grid);
     for (int b = 0; b < grid; b++) {
       int cmin = INT32_MAX, cmax = -1;
@@ -2161,21 +2174,44 @@ int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int
         cmin = std::min(cmin, col[q]);
         cmax = std::max(cmax, col[q]);
       }
-      if (cmax < 0) { dlo[b] = b; dhi[b] = b; continue; }
-      // CTA owning column c: the last b' with lo[b'] <= c (empty ranges skipped)
-      dlo[b] = (int)(std::upper_bound(lo.begin(), lo.end() - 1, cmin) - lo.begin()) - 1;
-      dhi[b] = (int)(std::upper_bound(lo.begin(), lo.end() - 1, cmax) - lo.begin()) - 1;
+      dlo[b] = dhi[b] = b;
+      if (cmax >= 0) {
+        dlo[b] = std::min(b, owner(cmin));
+        dhi[b] = std::max(b, owner(cmax));
+      }
     }
+    // symmetric closure: also wait for the CTAs that read this one's rows
+    // (the double-float ring reuses a slot two levels later)
+    std::vector<int> slo(dlo), shi(dhi);
+    for (int c = 0; c < grid; c++)
+      for (int b = dlo[c]; b <= dhi[c]; b++) {
+        slo[b] = std::min(slo[b], c);
+        shi[b] = std::max(shi[b], c);
+      }
     p->wave_grid = grid;
     p->pipe_grid = grid;
     WaveArgs &w = p->wave;
     w.n = n; w.nlevel = nlevel; w.nblk = grid; w.base = 0; w.err = p->d_err;
-    if (val) { w.sval2 = nullptr; } else { w.rdeg = p->d_coef; w.rdeg2 = p->d_coef2; }
+    if (!val) { w.rdeg = p->d_coef; w.rdeg2 = p->d_coef2; }
+    std::vector<double> lut(256, 0.0);
+    for (int d = 1; d < 256; d++) lut[d] = 1.0 / d;  // as the plan's 1/deg (mpk2/mpkexec.c:28)
     int *d_lo = nullptr, *d_dlo = nullptr, *d_dhi = nullptr;
     rc = dev_copy(p, (long **)&w.sell_off, soff.data(), soff.size());
-    if (!rc) rc = dev_copy(p, (int **)&w.len, len.data(), len.size());
-    if (!rc) rc = dev_copy(p, (int **)&w.scol, scol.data(), scol.size());
+    if (!rc) rc = dev_copy(p, (unsigned short **)&w.len, len.data(), len.size());
+    if (!rc && !scol.empty()) rc = dev_copy(p, (int **)&w.scol, scol.data(), scol.size());
+    if (!rc && !srel.empty()) rc = dev_copy(p, (short **)&w.srel, srel.data(), srel.size());
     if (!rc && val) rc = dev_copy(p, (double **)&w.sval, sval.data(), sval.size());
+    if (!rc) rc = dev_copy(p, (double **)&w.lut, lut.data(), lut.size());
+    if (!rc && arith == MPKG_ARITH_DF64) {
+      float2 *l2 = nullptr;
+      rc = dev_alloc(p, &l2, 256);
+      if (!rc) {
+        split_kernel<<<1, 256, 0, p->stream>>>(w.lut, l2, 256);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(p->stream) != cudaSuccess)
+          rc = fail(kECuda, "split of the degree table failed");
+      }
+      w.lut2 = l2;
+    }
     if (!rc && val && arith == MPKG_ARITH_DF64) {
       float2 *sv2 = nullptr;
       rc = dev_alloc(p, &sv2, sval.size());
@@ -2186,14 +2222,16 @@ int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int
       }
       w.sval2 = sv2;
     }
+    const bool df = arith == MPKG_ARITH_DF64;
     if (!rc) rc = dev_copy(p, &d_lo, lo.data(), lo.size());
-    if (!rc) rc = dev_copy(p, &d_dlo, dlo.data(), dlo.size());
-    if (!rc) rc = dev_copy(p, &d_dhi, dhi.data(), dhi.size());
+    if (!rc) rc = dev_copy(p, &d_dlo, (df ? slo : dlo).data(), dlo.size());
+    if (!rc) rc = dev_copy(p, &d_dhi, (df ? shi : dhi).data(), dhi.size());
     if (!rc) rc = dev_alloc(p, &w.flags, (size_t)grid);
-    if (!rc && arith == MPKG_ARITH_DF64) rc = dev_alloc(p, &w.shadow, (size_t)(nlevel + 1) * n);
+    if (!rc && df) rc = dev_alloc(p, &w.ring, (size_t)2 * n);
     w.row_lo = d_lo; w.dep_lo = d_dlo; w.dep_hi = d_dhi;
     long reach = 0;
-    for (int b = 0; b < grid; b++) reach = std::max<long>(reach, std::max(b - dlo[b], dhi[b] - b));
+    for (int b = 0; b < grid; b++)
+      reach = std::max<long>(reach, std::max(b - (df ? slo : dlo)[b], (df ? shi : dhi)[b] - b));
     p->pipe_reach = (int)reach;
     p->rows_computed = (long)n * nlevel;
   }

@@ -1,0 +1,696 @@
+// s-step conjugate gradients around the matrix powers kernel, with the
+// pieces that choose its basis: Lanczos Ritz values (Newton shifts), cheap
+// matrix features, and a small MLP that maps the features to shifts,
+// trained and evaluated by the kernels below.  No counterpart in the
+// reference's code (its only s-step material is a numpy notebook with a
+// monomial basis); this is the consumer that gives the MPK basis a use.
+//
+// Precision: the s-step basis is FP32 (values and vectors), the Gram
+// matrix Y^T Y and the small coefficient-space iteration are FP64 on the
+// GPU, x and the true residual are FP64 (the residual is recomputed from x
+// every outer iteration, so the FP32 basis does not limit the attainable
+// accuracy).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../../include/mpk_gb300.h"
+#include "host.h"
+
+using namespace mpkg;
+
+#define SS_TRY(expr)                                                             \
+  do {                                                                           \
+    cudaError_t e_ = (expr);                                                     \
+    if (e_ != cudaSuccess) return fail(kECuda, std::string(#expr ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxS = 10;              // basis length limit (Gram pairs <= threads)
+constexpr int kMaxCols = 2 * kMaxS + 1;
+
+int check_csr(int n, const int *ptr, const int *col) {
+  if (n <= 0 || !ptr || !col) return fail(kEInval, "empty matrix or null arrays");
+  if (ptr[0] != 0) return fail(kEInval, "ptr[0] must be 0");
+  for (int i = 0; i < n; i++)
+    if (ptr[i + 1] < ptr[i]) return fail(kEInval, "ptr must be non-decreasing");
+  for (long j = 0; j < ptr[n]; j++)
+    if (col[j] < 0 || col[j] >= n) return fail(kERange, "column index out of range");
+  return kOk;
+}
+
+int blocks_for(long n) { return (int)std::max<long>(1, std::min<long>((n + kThreads - 1) / kThreads, 1216)); }
+
+// ---- FP64 vector kernels -------------------------------------------------
+
+// r = b - A x, and per-CTA partial sums of r.r (deterministic reduction).
+__global__ void resid_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                             const double *__restrict__ val, const double *__restrict__ x,
+                             const double *__restrict__ b, double *__restrict__ r, double *__restrict__ part) {
+  __shared__ double red[kThreads];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int q = ptr[i]; q < ptr[i + 1]; q++) s = fma(val[q], x[col[q]], s);
+    const double ri = b[i] - s;
+    r[i] = ri;
+    acc = fma(ri, ri, acc);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// y = A x (FP64), optionally y -= beta * z; partial sums of y.x
+__global__ void spmv64_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                              const double *__restrict__ val, const double *__restrict__ x, double *__restrict__ y,
+                              const double *__restrict__ z, double beta, double *__restrict__ part) {
+  __shared__ double red[kThreads];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int q = ptr[i]; q < ptr[i + 1]; q++) s = fma(val[q], x[col[q]], s);
+    if (z) s = fma(-beta, z[i], s);
+    y[i] = s;
+    acc = fma(s, x[i], acc);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && part) part[blockIdx.x] = red[0];
+}
+
+// y = y + a * x; partial sums of y.y
+__global__ void axpy_norm_kernel(int n, double a, const double *__restrict__ x, double *__restrict__ y,
+                                 double *__restrict__ part) {
+  __shared__ double red[kThreads];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = fma(a, x[i], y[i]);
+    y[i] = v;
+    acc = fma(v, v, acc);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// y = a * x + b * y (no reduction)
+__global__ void axpby_kernel(int n, double a, const double *__restrict__ x, double b, double *__restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = fma(a, x[i], b * y[i]);
+}
+
+// ---- s-step basis (FP32) ---------------------------------------------------
+
+// Column c of the basis Y (column-major, n floats each).  P block: columns
+// 0..s, R block: columns s+1..2s.  Start columns: p / |p| and r / |r|.
+__global__ void basis_start_kernel(int n, const double *__restrict__ p, double ip, const double *__restrict__ r,
+                                   double ir, float *__restrict__ y0, float *__restrict__ yr) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    y0[i] = (float)(p[i] * ip);
+    yr[i] = (float)(r[i] * ir);
+  }
+}
+
+// One Newton step of both blocks: out = (A in - theta in) / sigma, FP32
+// values and accumulation in CSR order; the R block stops one step early.
+__global__ void basis_step_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                                  const float *__restrict__ val, const float *__restrict__ pin, float *__restrict__ pout,
+                                  const float *__restrict__ rin, float *__restrict__ rout, float theta, float rsigma) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float sp = 0.f, sr = 0.f;
+    for (int q = ptr[i]; q < ptr[i + 1]; q++) {
+      const int c = col[q];
+      const float v = val[q];
+      sp = __fmaf_rn(v, pin[c], sp);
+      if (rout) sr = __fmaf_rn(v, rin[c], sr);
+    }
+    pout[i] = (sp - theta * pin[i]) * rsigma;
+    if (rout) rout[i] = (sr - theta * rin[i]) * rsigma;
+  }
+}
+
+// Gram matrix G = Y^T Y in FP64 (products of FP32 values are exact in
+// FP64).  A CTA stages a tile of rows of all columns in shared memory;
+// thread t accumulates pair t of the upper triangle; per-CTA partials are
+// summed in a fixed order by gram_reduce_kernel.
+constexpr int kGramRows = 64;
+__global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const float *__restrict__ y,
+                                                        double *__restrict__ part) {
+  __shared__ float tile[kMaxCols][kGramRows];
+  const int npair = ncol * (ncol + 1) / 2;
+  int pa = 0, pb = 0;
+  {
+    int t = threadIdx.x, a = 0;
+    while (a < ncol && t >= ncol - a) { t -= ncol - a; a++; }
+    pa = a;
+    pb = a + t;
+  }
+  double acc = 0.0;
+  for (long r0 = (long)blockIdx.x * kGramRows; r0 < n; r0 += (long)gridDim.x * kGramRows) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < ncol * kGramRows; e += blockDim.x) {
+      const int c = e / kGramRows, rr = e % kGramRows;
+      tile[c][rr] = r0 + rr < n ? y[(size_t)c * n + r0 + rr] : 0.f;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < npair) {
+#pragma unroll 8
+      for (int rr = 0; rr < kGramRows; rr++) acc = fma((double)tile[pa][rr], (double)tile[pb][rr], acc);
+    }
+  }
+  if ((int)threadIdx.x < npair) part[(size_t)blockIdx.x * npair + threadIdx.x] = acc;
+}
+
+__global__ void gram_reduce_kernel(int nblk, int ncol, const double *__restrict__ part, double *__restrict__ g) {
+  const int npair = ncol * (ncol + 1) / 2;
+  for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; b++) s += part[(size_t)b * npair + t];
+    int a = 0, u = t;
+    while (u >= ncol - a) { u -= ncol - a; a++; }
+    g[a * ncol + a + u] = s;
+    g[(a + u) * ncol + a] = s;
+  }
+}
+
+// The s inner CG steps in coefficient space (FP64, one warp): p = Y ph,
+// r = Y rh, A Y = Y B on the columns in use.  Outputs xh, ph (and rh).
+// Returns through flag[0] = 1 when a breakdown (non-positive curvature or
+// residual) stopped the inner loop early; flag[1] = steps taken.
+__global__ void coeff_kernel(int s, const double *__restrict__ g, const double *__restrict__ theta,
+                             const double *__restrict__ sigma, double pnorm, double rnorm, double *__restrict__ xh,
+                             double *__restrict__ ph, double *__restrict__ rh, int *__restrict__ flag) {
+  if (threadIdx.x != 0) return;
+  const int m = 2 * s + 1;
+  double p[kMaxCols], r[kMaxCols], x[kMaxCols], bp[kMaxCols], gv[kMaxCols];
+  for (int c = 0; c < m; c++) { p[c] = 0.0; r[c] = 0.0; x[c] = 0.0; }
+  p[0] = pnorm;
+  r[s + 1] = rnorm;
+  auto apply_b = [&](const double *v, double *out) {
+    for (int c = 0; c < m; c++) out[c] = 0.0;
+    for (int j = 0; j < s; j++) {  // P block columns 0..s-1
+      out[j] += theta[j] * v[j];
+      out[j + 1] += sigma[j] * v[j];
+    }
+    for (int j = 0; j + 1 < s; j++) {  // R block columns s+1 .. 2s-1
+      const int c = s + 1 + j;
+      out[c] += theta[j] * v[c];
+      out[c + 1] += sigma[j] * v[c];
+    }
+  };
+  auto gdot = [&](const double *u, const double *v) {
+    double t = 0.0;
+    for (int a = 0; a < m; a++) {
+      double w = 0.0;
+      for (int b = 0; b < m; b++) w += g[a * m + b] * v[b];
+      t += u[a] * w;
+    }
+    return t;
+  };
+  int steps = 0, brk = 0;
+  double rr = gdot(r, r);
+  for (int j = 0; j < s; j++) {
+    apply_b(p, bp);
+    const double pap = gdot(p, bp);
+    if (!(pap > 0.0) || !(rr > 0.0)) { brk = 1; break; }
+    const double alpha = rr / pap;
+    for (int c = 0; c < m; c++) {
+      x[c] += alpha * p[c];
+      gv[c] = r[c] - alpha * bp[c];
+    }
+    const double rr2 = gdot(gv, gv);
+    const double beta = rr2 / rr;
+    for (int c = 0; c < m; c++) {
+      r[c] = gv[c];
+      p[c] = gv[c] + beta * p[c];
+    }
+    rr = rr2;
+    steps++;
+  }
+  for (int c = 0; c < m; c++) { xh[c] = x[c]; ph[c] = p[c]; rh[c] = r[c]; }
+  flag[0] = brk;
+  flag[1] = steps;
+}
+
+// x += Y xh, p = Y ph (FP64 accumulation of the FP32 basis)
+__global__ void combine_kernel(int n, int m, const float *__restrict__ y, const double *__restrict__ xh,
+                               const double *__restrict__ ph, double *__restrict__ x, double *__restrict__ p) {
+  __shared__ double cx[kMaxCols], cp[kMaxCols];
+  if ((int)threadIdx.x < m) { cx[threadIdx.x] = xh[threadIdx.x]; cp[threadIdx.x] = ph[threadIdx.x]; }
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double sx = x[i], sp = 0.0;
+    for (int c = 0; c < m; c++) {
+      const double v = (double)y[(size_t)c * n + i];
+      sx = fma(cx[c], v, sx);
+      sp = fma(cp[c], v, sp);
+    }
+    x[i] = sx;
+    p[i] = sp;
+  }
+}
+
+// ---- matrix features ---------------------------------------------------------
+// Per row: diagonal, sum of |off-diagonals|, 2-norm, degree; per CTA
+// partial min/max/sums (fixed-order final reduction on the host).
+struct FeatPart {
+  double glo, ghi, dmin, dmax, dsum, osum, omax, nsum, nsq, degmax, degsum, dommin, domsum;
+};
+__global__ void features_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                                const double *__restrict__ val, FeatPart *__restrict__ part) {
+  __shared__ FeatPart red[kThreads];
+  FeatPart f = {1e300, -1e300, 1e300, -1e300, 0, 0, 0, 0, 0, 0, 0, 1e300, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double d = 0.0, o = 0.0, n2 = 0.0;
+    for (int q = ptr[i]; q < ptr[i + 1]; q++) {
+      const double v = val[q];
+      n2 = fma(v, v, n2);
+      if (col[q] == i) d += v;
+      else o += fabs(v);
+    }
+    const double deg = ptr[i + 1] - ptr[i];
+    f.glo = fmin(f.glo, d - o);
+    f.ghi = fmax(f.ghi, d + o);
+    f.dmin = fmin(f.dmin, d);
+    f.dmax = fmax(f.dmax, d);
+    f.dsum += d;
+    f.osum += o;
+    f.omax = fmax(f.omax, o);
+    const double nr = sqrt(n2);
+    f.nsum += nr;
+    f.nsq += n2;
+    f.degmax = fmax(f.degmax, deg);
+    f.degsum += deg;
+    const double dom = o > 0.0 ? fabs(d) / o : 10.0;
+    f.dommin = fmin(f.dommin, dom);
+    f.domsum += fmin(dom, 10.0);
+  }
+  red[threadIdx.x] = f;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      FeatPart &a = red[threadIdx.x];
+      const FeatPart &b = red[threadIdx.x + w];
+      a.glo = fmin(a.glo, b.glo); a.ghi = fmax(a.ghi, b.ghi);
+      a.dmin = fmin(a.dmin, b.dmin); a.dmax = fmax(a.dmax, b.dmax);
+      a.dsum += b.dsum; a.osum += b.osum; a.omax = fmax(a.omax, b.omax);
+      a.nsum += b.nsum; a.nsq += b.nsq; a.degmax = fmax(a.degmax, b.degmax); a.degsum += b.degsum;
+      a.dommin = fmin(a.dommin, b.dommin); a.domsum += b.domsum;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// ---- device copy of a CSR matrix ------------------------------------------
+struct DevCsr {
+  int n = 0;
+  long nnz = 0;
+  int *ptr = nullptr, *col = nullptr;
+  double *val = nullptr;
+  float *valf = nullptr;
+  ~DevCsr() {
+    cudaFree(ptr); cudaFree(col); cudaFree(val); cudaFree(valf);
+  }
+  int upload(int n_, const int *p, const int *c, const double *v, bool f32) {
+    int rc = check_csr(n_, p, c);
+    if (rc) return rc;
+    n = n_;
+    nnz = p[n_];
+    SS_TRY(cudaMalloc(&ptr, sizeof(int) * (n + 1)));
+    SS_TRY(cudaMalloc(&col, sizeof(int) * std::max<long>(nnz, 1)));
+    SS_TRY(cudaMalloc(&val, sizeof(double) * std::max<long>(nnz, 1)));
+    SS_TRY(cudaMemcpy(ptr, p, sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+    SS_TRY(cudaMemcpy(col, c, sizeof(int) * nnz, cudaMemcpyHostToDevice));
+    SS_TRY(cudaMemcpy(val, v, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+    if (f32) {
+      std::vector<float> vf(v, v + nnz);
+      SS_TRY(cudaMalloc(&valf, sizeof(float) * std::max<long>(nnz, 1)));
+      SS_TRY(cudaMemcpy(valf, vf.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice));
+    }
+    return kOk;
+  }
+};
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  ~DevBuf() { cudaFree(p); }
+  int alloc(size_t n) {
+    SS_TRY(cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)));
+    return kOk;
+  }
+};
+
+int sum_parts(const double *d_part, int nblk, double *out) {
+  std::vector<double> h(nblk);
+  SS_TRY(cudaMemcpy(h.data(), d_part, sizeof(double) * nblk, cudaMemcpyDeviceToHost));
+  double s = 0.0;
+  for (double v : h) s += v;
+  *out = s;
+  return kOk;
+}
+
+// Eigenvalues of the symmetric tridiagonal (alpha diag, beta off) by
+// bisection on Sturm sequence counts, ascending.
+void tridiag_eigs(int m, const double *alpha, const double *beta, double *out) {
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < m; i++) {
+    const double r = (i > 0 ? std::fabs(beta[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(beta[i]) : 0.0);
+    lo = std::min(lo, alpha[i] - r);
+    hi = std::max(hi, alpha[i] + r);
+  }
+  auto count_below = [&](double x) {  // eigenvalues < x
+    int c = 0;
+    double d = 1.0;
+    for (int i = 0; i < m; i++) {
+      const double b2 = i > 0 ? beta[i - 1] * beta[i - 1] : 0.0;
+      d = alpha[i] - x - (i > 0 ? b2 / d : 0.0);
+      if (d == 0.0) d = -1e-300;
+      if (d < 0.0) c++;
+    }
+    return c;
+  };
+  for (int k = 0; k < m; k++) {
+    double a = lo, b = hi;
+    for (int it = 0; it < 200 && b - a > 1e-15 * std::max(1.0, std::fabs(a) + std::fabs(b)); it++) {
+      const double mid = 0.5 * (a + b);
+      if (count_below(mid) > k) b = mid;
+      else a = mid;
+    }
+    out[k] = 0.5 * (a + b);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void mpkg_tridiag_eigs(int m, const double *alpha, const double *beta, double *out) {
+  if (m > 0 && alpha && out && (m == 1 || beta)) tridiag_eigs(m, alpha, beta, out);
+}
+
+void mpkg_leja_order(int k, double *x) {
+  if (!x || k <= 1) return;
+  std::vector<double> v(x, x + k), o;
+  std::vector<char> used(k, 0);
+  int first = 0;
+  for (int i = 1; i < k; i++)
+    if (std::fabs(v[i]) > std::fabs(v[first])) first = i;
+  o.push_back(v[first]);
+  used[first] = 1;
+  while ((int)o.size() < k) {
+    int best = -1;
+    double bv = -1.0;
+    for (int i = 0; i < k; i++) {
+      if (used[i]) continue;
+      double prod = 0.0;  // log of the product of distances (robust to under/overflow)
+      for (double c : o) prod += std::log(std::fabs(v[i] - c) + 1e-300);
+      if (best < 0 || prod > bv) { bv = prod; best = i; }
+    }
+    used[best] = 1;
+    o.push_back(v[best]);
+  }
+  std::copy(o.begin(), o.end(), x);
+}
+
+int mpkg_features(int n, const int *ptr, const int *col, const double *val, float *feat, double *glo, double *ghi) {
+  clear_error();
+  if (!val || !feat) return fail(kEInval, "null argument");
+  DevCsr a;
+  int rc = a.upload(n, ptr, col, val, false);
+  if (rc) return rc;
+  const int nb = blocks_for(n);
+  DevBuf<FeatPart> part;
+  if ((rc = part.alloc(nb))) return rc;
+  features_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, part.p);
+  SS_TRY(cudaGetLastError());
+  std::vector<FeatPart> h(nb);
+  SS_TRY(cudaMemcpy(h.data(), part.p, sizeof(FeatPart) * nb, cudaMemcpyDeviceToHost));
+  FeatPart f = h[0];
+  for (int b = 1; b < nb; b++) {
+    const FeatPart &o = h[b];
+    f.glo = std::min(f.glo, o.glo); f.ghi = std::max(f.ghi, o.ghi);
+    f.dmin = std::min(f.dmin, o.dmin); f.dmax = std::max(f.dmax, o.dmax);
+    f.dsum += o.dsum; f.osum += o.osum; f.omax = std::max(f.omax, o.omax);
+    f.nsum += o.nsum; f.nsq += o.nsq; f.degmax = std::max(f.degmax, o.degmax); f.degsum += o.degsum;
+    f.dommin = std::min(f.dommin, o.dommin); f.domsum += o.domsum;
+  }
+  const double s = f.ghi > 0 ? f.ghi : 1.0, nn = n;
+  const double nmean = f.nsum / nn, nstd = std::sqrt(std::max(0.0, f.nsq / nn - nmean * nmean));
+  const double fv[MPKG_NFEAT] = {f.glo / s,           f.dsum / nn / s,    f.dmin / s,          f.dmax / s,
+                                 f.osum / nn / s,     f.omax / s,         nmean / s,           nstd / s,
+                                 f.degsum / nn / 32., f.degmax / 32.,     std::min(f.dommin, 10.0) / 10.,
+                                 f.domsum / nn / 10.};
+  for (int k = 0; k < MPKG_NFEAT; k++) feat[k] = (float)fv[k];
+  if (glo) *glo = f.glo;
+  if (ghi) *ghi = f.ghi;
+  return kOk;
+}
+
+int mpkg_lanczos(int n, const int *ptr, const int *col, const double *val, int m, uint64_t seed, double *ritz,
+                 double *alpha_out, double *beta_out) {
+  clear_error();
+  if (!val || !ritz || m <= 0 || m > 256 || m > n) return fail(kEInval, "bad argument");
+  DevCsr a;
+  int rc = a.upload(n, ptr, col, val, false);
+  if (rc) return rc;
+  const int nb = blocks_for(n);
+  DevBuf<double> v0, v1, w, part;
+  if ((rc = v0.alloc(n)) || (rc = v1.alloc(n)) || (rc = w.alloc(n)) || (rc = part.alloc(nb))) return rc;
+  std::vector<double> h(n);
+  uniform_vector(seed, n, h.data());
+  double nrm = 0.0;
+  for (double t : h) nrm += t * t;
+  nrm = std::sqrt(nrm);
+  for (double &t : h) t /= nrm;
+  SS_TRY(cudaMemcpy(v1.p, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  SS_TRY(cudaMemset(v0.p, 0, sizeof(double) * n));
+  std::vector<double> alpha(m), beta(m);
+  double bprev = 0.0;
+  double *vp = v0.p, *vc = v1.p;
+  int steps = 0;
+  for (int j = 0; j < m; j++) {
+    // w = A v_j - beta_j v_(j-1);  alpha_j = w . v_j
+    spmv64_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, vc, w.p, j ? vp : nullptr, bprev, part.p);
+    SS_TRY(cudaGetLastError());
+    double al;
+    if ((rc = sum_parts(part.p, nb, &al))) return rc;
+    alpha[j] = al;
+    steps = j + 1;
+    if (j + 1 == m) break;
+    // w -= alpha_j v_j;  beta_(j+1) = |w|
+    axpy_norm_kernel<<<nb, kThreads>>>(n, -al, vc, w.p, part.p);
+    double b2;
+    if ((rc = sum_parts(part.p, nb, &b2))) return rc;
+    const double bt = std::sqrt(b2);
+    beta[j] = bt;
+    if (!(bt > 1e-300)) break;  // invariant subspace
+    // v_(j-1) <- w / beta (becomes v_(j+1))
+    axpby_kernel<<<nb, kThreads>>>(n, 1.0 / bt, w.p, 0.0, vp);
+    std::swap(vp, vc);
+    bprev = bt;
+  }
+  SS_TRY(cudaDeviceSynchronize());
+  std::vector<double> ev(steps);
+  tridiag_eigs(steps, alpha.data(), beta.data(), ev.data());
+  for (int k = 0; k < m; k++) ritz[k] = k < steps ? ev[k] : ev[steps - 1];
+  if (alpha_out) std::copy(alpha.begin(), alpha.begin() + steps, alpha_out);
+  if (beta_out) std::copy(beta.begin(), beta.begin() + std::max(0, steps - 1), beta_out);
+  return steps == m ? kOk : kOk;
+}
+
+int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const double *b, double *x, double tol,
+            int max_iter, mpkg_cg_info_t *info) {
+  clear_error();
+  if (!val || !b || !x || max_iter <= 0) return fail(kEInval, "bad argument");
+  auto t0 = std::chrono::steady_clock::now();
+  DevCsr a;
+  int rc = a.upload(n, ptr, col, val, false);
+  if (rc) return rc;
+  const int nb = blocks_for(n);
+  DevBuf<double> dx, db, dr, dp, dq, part;
+  if ((rc = dx.alloc(n)) || (rc = db.alloc(n)) || (rc = dr.alloc(n)) || (rc = dp.alloc(n)) || (rc = dq.alloc(n)) ||
+      (rc = part.alloc(nb)))
+    return rc;
+  SS_TRY(cudaMemcpy(dx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice));
+  SS_TRY(cudaMemcpy(db.p, b, sizeof(double) * n, cudaMemcpyHostToDevice));
+  double bb = 0.0;
+  for (int i = 0; i < n; i++) bb += b[i] * b[i];
+  const double bnorm = std::sqrt(bb);
+  resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+  double rr;
+  if ((rc = sum_parts(part.p, nb, &rr))) return rc;
+  SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+  int it = 0;
+  while (it < max_iter && std::sqrt(rr) > tol * bnorm) {
+    spmv64_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dp.p, dq.p, nullptr, 0.0, part.p);
+    double pq;
+    if ((rc = sum_parts(part.p, nb, &pq))) return rc;
+    if (!(pq > 0.0)) break;
+    const double alpha = rr / pq;
+    axpby_kernel<<<nb, kThreads>>>(n, alpha, dp.p, 1.0, dx.p);
+    axpy_norm_kernel<<<nb, kThreads>>>(n, -alpha, dq.p, dr.p, part.p);
+    double rr2;
+    if ((rc = sum_parts(part.p, nb, &rr2))) return rc;
+    axpby_kernel<<<nb, kThreads>>>(n, 1.0, dr.p, rr2 / rr, dp.p);
+    rr = rr2;
+    it++;
+  }
+  // true residual
+  resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+  double rt;
+  if ((rc = sum_parts(part.p, nb, &rt))) return rc;
+  SS_TRY(cudaMemcpy(x, dx.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (info) {
+    std::memset(info, 0, sizeof *info);
+    info->iterations = it;
+    info->mpk_steps = it;
+    info->relres = std::sqrt(rt) / bnorm;
+    info->converged = info->relres <= tol;
+    info->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return kOk;
+}
+
+int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, const double *b, double *x, int s,
+                  const double *shifts, double scale, double tol, int max_outer, mpkg_cg_info_t *info) {
+  clear_error();
+  if (!val || !b || !x || s < 1 || s > kMaxS || max_outer <= 0 || !(scale > 0.0))
+    return fail(kEInval, "bad argument");
+  auto t0 = std::chrono::steady_clock::now();
+  DevCsr a;
+  int rc = a.upload(n, ptr, col, val, true);
+  if (rc) return rc;
+  const int nb = blocks_for(n), m = 2 * s + 1, npair = m * (m + 1) / 2;
+  const int gblk = (int)std::min<long>(1216, (n + kGramRows - 1) / kGramRows);
+  DevBuf<double> dx, db, dr, dp, part, gpart, dg, dth, dsg, dxh, dph, drh;
+  DevBuf<float> y;
+  DevBuf<int> dflag;
+  if ((rc = dx.alloc(n)) || (rc = db.alloc(n)) || (rc = dr.alloc(n)) || (rc = dp.alloc(n)) || (rc = part.alloc(nb)) ||
+      (rc = gpart.alloc((size_t)gblk * npair)) || (rc = dg.alloc(m * m)) || (rc = dth.alloc(s)) ||
+      (rc = dsg.alloc(s)) || (rc = dxh.alloc(m)) || (rc = dph.alloc(m)) || (rc = drh.alloc(m)) ||
+      (rc = y.alloc((size_t)m * n)) || (rc = dflag.alloc(2)))
+    return rc;
+  std::vector<double> th(s, 0.0), sg(s, scale);
+  if (shifts) std::copy(shifts, shifts + s, th.begin());
+  SS_TRY(cudaMemcpy(dth.p, th.data(), sizeof(double) * s, cudaMemcpyHostToDevice));
+  SS_TRY(cudaMemcpy(dsg.p, sg.data(), sizeof(double) * s, cudaMemcpyHostToDevice));
+  SS_TRY(cudaMemcpy(dx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice));
+  SS_TRY(cudaMemcpy(db.p, b, sizeof(double) * n, cudaMemcpyHostToDevice));
+  double bb = 0.0;
+  for (int i = 0; i < n; i++) bb += b[i] * b[i];
+  const double bnorm = std::sqrt(bb);
+  resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+  double rr;
+  if ((rc = sum_parts(part.p, nb, &rr))) return rc;
+  SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+  double pp = rr;
+  int outer = 0, steps = 0, breakdowns = 0;
+  double cond_max = 0.0;
+  std::vector<double> hg(m * m);
+  while (outer < max_outer && std::sqrt(rr) > tol * bnorm) {
+    const double pn = std::sqrt(pp), rn = std::sqrt(rr);
+    float *Y = y.p;
+    basis_start_kernel<<<nb, kThreads>>>(n, dp.p, 1.0 / pn, dr.p, 1.0 / rn, Y, Y + (size_t)(s + 1) * n);
+    for (int j = 0; j < s; j++) {
+      const bool rstep = j + 1 < s;
+      basis_step_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.valf, Y + (size_t)j * n, Y + (size_t)(j + 1) * n,
+                                          rstep ? Y + (size_t)(s + 1 + j) * n : nullptr,
+                                          rstep ? Y + (size_t)(s + 2 + j) * n : nullptr, (float)th[j],
+                                          (float)(1.0 / sg[j]));
+    }
+    gram_kernel<<<gblk, kThreads>>>(n, m, Y, gpart.p);
+    gram_reduce_kernel<<<1, kThreads>>>(gblk, m, gpart.p, dg.p);
+    coeff_kernel<<<1, 32>>>(s, dg.p, dth.p, dsg.p, pn, rn, dxh.p, dph.p, drh.p, dflag.p);
+    combine_kernel<<<nb, kThreads>>>(n, m, Y, dxh.p, dph.p, dx.p, dp.p);
+    SS_TRY(cudaGetLastError());
+    int flag[2];
+    SS_TRY(cudaMemcpy(flag, dflag.p, sizeof flag, cudaMemcpyDeviceToHost));
+    if (info) {  // condition number of the P block (the s-step polynomial basis) from its Gram eigenvalues
+      SS_TRY(cudaMemcpy(hg.data(), dg.p, sizeof(double) * m * m, cudaMemcpyDeviceToHost));
+      const int mp = s + 1;
+      std::vector<double> A((size_t)mp * mp);
+      for (int r2 = 0; r2 < mp; r2++)
+        for (int c2 = 0; c2 < mp; c2++) A[r2 * mp + c2] = hg[r2 * m + c2];
+      const int m = mp;  // Jacobi sweeps on the leading (s+1) x (s+1) block
+      for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0.0;
+        for (int p2 = 0; p2 < m; p2++)
+          for (int q2 = p2 + 1; q2 < m; q2++) off += A[p2 * m + q2] * A[p2 * m + q2];
+        if (off < 1e-30) break;
+        for (int p2 = 0; p2 < m; p2++)
+          for (int q2 = p2 + 1; q2 < m; q2++) {
+            const double apq = A[p2 * m + q2];
+            if (std::fabs(apq) < 1e-300) continue;
+            const double tau = (A[q2 * m + q2] - A[p2 * m + p2]) / (2.0 * apq);
+            const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+            const double c = 1.0 / std::sqrt(1.0 + t * t), sn = t * c;
+            for (int k = 0; k < m; k++) {
+              const double akp = A[k * m + p2], akq = A[k * m + q2];
+              A[k * m + p2] = c * akp - sn * akq;
+              A[k * m + q2] = sn * akp + c * akq;
+            }
+            for (int k = 0; k < m; k++) {
+              const double apk = A[p2 * m + k], aqk = A[q2 * m + k];
+              A[p2 * m + k] = c * apk - sn * aqk;
+              A[q2 * m + k] = sn * apk + c * aqk;
+            }
+          }
+      }
+      double emin = 1e300, emax = 0.0;
+      for (int k = 0; k < m; k++) {
+        emin = std::min(emin, A[k * m + k]);
+        emax = std::max(emax, A[k * m + k]);
+      }
+      const double cnd = emin > 0 ? std::sqrt(emax / emin) : 1e300;
+      cond_max = std::max(cond_max, cnd);
+    }
+    breakdowns += flag[0];
+    steps += flag[1];
+    outer++;
+    // true residual (FP64) and |p|^2
+    resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+    if ((rc = sum_parts(part.p, nb, &rr))) return rc;
+    axpy_norm_kernel<<<nb, kThreads>>>(n, 0.0, dp.p, dp.p, part.p);
+    if ((rc = sum_parts(part.p, nb, &pp))) return rc;
+    if (flag[1] == 0 || !(pp > 0.0)) {  // no progress possible with this basis: restart from r
+      SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+      pp = rr;
+      if (flag[1] == 0) break;
+    }
+  }
+  SS_TRY(cudaMemcpy(x, dx.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (info) {
+    std::memset(info, 0, sizeof *info);
+    info->iterations = outer;
+    info->mpk_steps = steps;
+    info->relres = std::sqrt(rr) / bnorm;
+    info->converged = info->relres <= tol;
+    info->basis_cond = cond_max;
+    info->breakdowns = breakdowns;
+    info->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return kOk;
+}
+
+}  // extern "C"

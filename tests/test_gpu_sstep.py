@@ -1,0 +1,76 @@
+"""s-step CG on the GPU and the pieces that choose its basis: features,
+Lanczos (against the numpy oracle), the MLP's forward pass and gradient
+(against the numpy oracle), its training, and what the learned shifts gain
+over the monomial basis."""
+import numpy as np
+import pytest
+
+import mpk_gb300 as M
+from mpk_gb300 import shifts as S
+from oracle import mlp_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_forward_and_gradient_match_oracle(gpu):
+    m = M.Mlp(M.NFEAT, 64, 8, seed=3)
+    rng = np.random.default_rng(0)
+    X = rng.normal(size=(48, M.NFEAT)).astype(np.float32)
+    T = rng.uniform(size=(48, 8)).astype(np.float32)
+    p = m.params()
+    Y = m.forward(X)
+    Yo = mlp_ref.forward(p, X, M.NFEAT, 64, 8)[0]
+    assert np.linalg.norm(Y - Yo) / np.linalg.norm(Yo) < 1e-5
+    g, loss = m.gradient(X, T)
+    go, lo = mlp_ref.gradient(p, X, T, M.NFEAT, 64, 8)
+    assert np.linalg.norm(g - go) / np.linalg.norm(go) < 1e-4
+    assert abs(loss - lo) / lo < 1e-5
+
+
+def test_mlp_training_reduces_loss(gpu):
+    X, T = S.training_set(200, seed=5)
+    mlp, curve = S.train(X, T, epochs=150)
+    assert curve[-1] < curve[0] / 10
+
+
+def test_features_match_numpy(gpu):
+    a = M.Csr.diffusion(30, 20, 1, sigma=0.8, seed=2)
+    f, glo, ghi = M.features(a)
+    d = np.array([a.val[a.ptr[i]:a.ptr[i + 1]][a.col[a.ptr[i]:a.ptr[i + 1]] == i].sum() for i in range(a.n)])
+    o = np.array([np.abs(a.val[a.ptr[i]:a.ptr[i + 1]][a.col[a.ptr[i]:a.ptr[i + 1]] != i]).sum() for i in range(a.n)])
+    assert np.isclose(glo, (d - o).min()) and np.isclose(ghi, (d + o).max())
+    assert np.isclose(f[1], d.mean() / ghi, rtol=1e-6) and np.isclose(f[5], o.max() / ghi, rtol=1e-6)
+
+
+def test_lanczos_matches_oracle(gpu):
+    a = M.Csr.diffusion(40, 40, 1, sigma=1.0, seed=5)
+    r, al, be = M.lanczos(a, 8, seed=2)
+    alo, beo = mlp_ref.lanczos(a.ptr, a.col, a.val, 8, M.uniform(2, a.n))
+    assert np.allclose(al, alo, rtol=1e-12, atol=1e-12) and np.allclose(be, beo, rtol=1e-12)
+    T = np.diag(alo) + np.diag(beo, 1) + np.diag(beo, -1)
+    assert np.allclose(r, np.linalg.eigvalsh(T), rtol=1e-12)
+
+
+@pytest.fixture(scope="module")
+def trained_mlp():
+    X, T = S.training_set(400, seed=11)
+    return S.train(X, T, epochs=200)[0]
+
+
+@pytest.mark.parametrize("dims", [(96, 96, 1), (36, 36, 36)])
+def test_sstep_cg_bases(dims, trained_mlp, gpu):
+    """All bases reach 1e-8 (true residual); the learned shifts (no Lanczos
+    run) need no more outer iterations than the monomial basis and stay
+    within 20 % of the Lanczos-shift basis; standard CG agrees."""
+    a = M.Csr.diffusion(*dims, sigma=1.0, seed=77)
+    b = M.uniform(3, a.n)
+    x_cg, cg = M.cg(a, b)
+    assert cg["converged"]
+    _, mono = M.sstep_cg(a, b, 8)
+    x_l, lan = M.sstep_cg(a, b, 8, shifts=S.from_lanczos(a, 8))
+    _, lrn = M.sstep_cg(a, b, 8, shifts=S.predict(trained_mlp, a))
+    for inf in (mono, lan, lrn):
+        assert inf["converged"] and inf["relres"] <= 1e-8
+    assert lrn["iterations"] <= mono["iterations"]
+    assert lrn["iterations"] <= 1.2 * lan["iterations"]
+    assert np.linalg.norm(x_l - x_cg) / np.linalg.norm(x_cg) < 1e-6
