@@ -52,8 +52,10 @@ def workload():
     return a, part, x
 
 
-def algorithmic_bytes(n, nnz, k):
-    return nnz * 12 + 4 * (n + 1) + 8 * n * (k + 1)
+def algorithmic_bytes(n, nnz, k, valued=False):
+    """Matrix once (int32 columns, FP64 values when valued), row pointers,
+    x once and k FP64 output levels written once."""
+    return nnz * (12 if valued else 4) + 4 * (n + 1) + 8 * n * (k + 1)
 
 
 def peaks():
@@ -255,23 +257,116 @@ def bench_mixed(M, torch, a, x, k, exact, args, flush, stream):
     # config 3: 2048^2 9-point anisotropic diffusion, log-normal(0,1) edges
     b = M.Csr.diffusion(2048, 2048, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=3)
     xb = M.uniform(3, b.n)
-    p64 = M.Plan.pipe(b, k)
-    d64 = torch.zeros((k + 1) * b.n, dtype=torch.float64, device="cuda")
-    d64[:b.n] = torch.from_numpy(xb).cuda()
-    t64 = statistics.mean(time_device(p64, d64, min(args.steps, 50), args.warmup, flush, stream))
-    ex64 = d64.cpu().numpy()
-    p64.close()
-    del d64
+    fp64 = {}
+    for ex, mkp in (("spmv_fma", lambda: M.Plan.spmv(b, k)), ("wave_fma", lambda: M.Plan.wave(b, k)),
+                    ("pipe_fma", lambda: M.Plan.pipe(b, k))):
+        p64 = mkp()
+        d64 = torch.zeros((k + 1) * b.n, dtype=torch.float64, device="cuda")
+        d64[:b.n] = torch.from_numpy(xb).cuda()
+        fp64[ex] = statistics.mean(time_device(p64, d64, min(args.steps, 50), args.warmup, flush, stream))
+        ex64 = d64.cpu().numpy()  # all three are bit-identical (FP64 FMA in CSR order)
+        p64.close()
+        del d64
+    best64 = min(fp64, key=fp64.get)
+    t64 = fp64[best64]
     p32 = M.Plan.mixed(b, k, M.VALUE_F32)
     e, inexact = p32.mixed_scale()
     d32 = torch.zeros((k + 1) * b.n, dtype=torch.float32, device="cuda")
     d32[:b.n] = torch.from_numpy(xb.astype(np.float32)).cuda()
     t32 = statistics.mean(time_mixed(p32, d32, min(args.steps, 100), args.warmup, flush, stream))
     errs = mixed_errors(d32.cpu().numpy(), e, ex64, b.n, k)
-    out["diffusion2048_9pt"] = {"n": b.n, "nnz": b.nnz, "fp64_pipe_ms": t64, "f32_ms": t32,
+    out["diffusion2048_9pt"] = {"n": b.n, "nnz": b.nnz, "fp64_ms": fp64, "fp64_best": best64, "f32_ms": t32,
                                 "speedup_f32_vs_fp64": t64 / t32, "rel_err_per_power": errs,
                                 "value_f32": k * b.n / (t32 * 1e-3) / 1e9}
     p32.close()
+    return out
+
+
+def bench_batch(M, torch, args, flush, stream):
+    """Batching workload: 256 matrices (n log-uniform in [1e3, 2e5], half
+    random 2-D/3-D stencils, half random banded), 16 right-hand sides, FP32,
+    k=6, one persistent graph-replayed launch, autotuned."""
+    import scipy.sparse as sp
+    k, nrhs = 6, 16
+    mats = M.batch_workload(256, seed=0)
+    N = sum(m.n for m in mats)
+    nnz = sum(m.nnz for m in mats)
+    t0 = time.perf_counter()
+    plan = M.Plan.batch(mats, nrhs, k, tune=True)
+    plan_s = time.perf_counter() - t0
+    X = M.uniform(1, N * nrhs).astype(np.float32)
+    d = torch.zeros((k + 1) * N * nrhs, dtype=torch.float32, device="cuda")
+    d[:N * nrhs] = torch.from_numpy(X).cuda()
+    torch.cuda.synchronize()
+    for _ in range(3):
+        plan.exec_batch_device(d.data_ptr(), stream.cuda_stream)
+    plan.sync(stream.cuda_stream)
+    times = []
+    for _ in range(max(3, min(args.steps, 20))):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.exec_batch_device(d.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        plan.sync(stream.cuda_stream)
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    vb = d.view(k + 1, N, nrhs)
+    errs = [0.0] * k
+    sample = [0, 1, 2, 3, 128, 129, 254, 255]
+    row0 = np.concatenate([[0], np.cumsum([m.n for m in mats])])
+    for j in sample:  # error of the FP32 form against FP64, per power
+        m = mats[j]
+        A = sp.csr_matrix((m.val, m.col, m.ptr), shape=(m.n, m.n))
+        v = X.reshape(N, nrhs)[row0[j]:row0[j + 1]].astype(np.float64)
+        for l in range(1, k + 1):
+            v = A @ v
+            got = vb[l, row0[j]:row0[j + 1]].double().cpu().numpy()
+            errs[l - 1] = max(errs[l - 1], float(np.linalg.norm(got - v) / np.linalg.norm(v)))
+    B = nnz * 8 + 4 * (N + 256) + 4 * N * nrhs * (1 + k)
+    peak, _ = peaks()
+    info = plan.batch_info()
+    plan.close()
+    return {"workload": "256 matrices, n log-uniform [1e3, 2e5] (half random 2-D/3-D stencils, half random banded "
+                        "bw 64, 5-30 nnz/row), 16 RHS FP32, k=6", "rows": N, "nnz": nnz, "ms_per_step": ms,
+            "value": N * nrhs * k / (ms * 1e-3) / 1e9, "unit": "G row-RHS powers/s",
+            "algorithmic_bytes": B, "achieved_gbs": B / (ms * 1e-3) / 1e9, "frac_hbm": B / (ms * 1e-3) / 1e9 / peak,
+            "rel_err_per_power_vs_fp64": errs, "error_sample": "8 of the 256 matrices, all 16 RHS",
+            "plan_s": plan_s, "tuned": {kk: info[kk] for kk in ("lanes_per_row", "vector_width", "group_bytes",
+                                                               "ngroup", "grid", "graph", "candidates", "tune_ms")},
+            "gpu_launches_per_step": 1}
+
+
+def bench_sstep(M):
+    """s-step CG (s=8) on the 96^3 7-point variable-coefficient diffusion
+    matrix (log-normal sigma=1), b ~ U[-1,1], tol 1e-8: monomial,
+    Lanczos-shift and learned-shift bases next to standard FP64 CG."""
+    from mpk_gb300 import shifts as S
+    a = M.Csr.diffusion(96, 96, 96, sigma=1.0, dominance=0.01, seed=5)
+    b = M.uniform(7, a.n)
+    out = {"workload": "96^3 7-point diffusion, log-normal(sigma=1) coefficients, dominance 0.01, n=884736, "
+                       "s=8, tol 1e-8 (true residual)"}
+    _, out["cg_fp64"] = M.cg(a, b)
+    _, out["monomial"] = M.sstep_cg(a, b, 8)
+    t0 = time.perf_counter()
+    sh = S.from_lanczos(a, 8)
+    lan_ms = (time.perf_counter() - t0) * 1e3
+    _, out["lanczos_shifts"] = M.sstep_cg(a, b, 8, shifts=sh)
+    out["lanczos_shifts"]["shift_ms"] = lan_ms
+    wpath = os.path.join(HERE, "mpk_gb300", "shift_mlp.npz")
+    if os.path.exists(wpath):
+        from mpk_gb300.train_shifts import load
+        mlp, src = load(wpath), "mpk_gb300/shift_mlp.npz (trained on 2000 synthetic matrices)"
+    else:
+        X, T = S.training_set(400, seed=11)
+        mlp, src = S.train(X, T, epochs=200)[0], "trained here on 400 synthetic matrices"
+    t0 = time.perf_counter()
+    sh = S.predict(mlp, a)
+    pred_ms = (time.perf_counter() - t0) * 1e3
+    _, out["learned_shifts"] = M.sstep_cg(a, b, 8, shifts=sh)
+    out["learned_shifts"]["shift_ms"] = pred_ms
+    out["learned_shifts"]["model"] = src
     return out
 
 
@@ -281,8 +376,8 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--exec", default="pipe", choices=["pipe", "tiles", "spmv", "tasks"])
-    ap.add_argument("--arith", default="fma", choices=["fma", "separate", "df64"])
+    ap.add_argument("--exec", default="wave", choices=["pipe", "wave", "tiles", "spmv", "tasks"])
+    ap.add_argument("--arith", default="df64", choices=["fma", "separate", "df64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="time only the selected executor")
     args = ap.parse_args()
@@ -292,9 +387,9 @@ def main():
     a, part, x = workload()
     n, nnz, k = a.n, a.nnz, K_LEVELS
     nth = os.cpu_count() or 1
-    cfg = {"workload": "3-D 7-point Laplacian 128^3 (n=2,097,152, nnz=14,581,760), FP64 CSR int32, "
-                       "x~U[-1,1] seed 1, k=8, 2048 RCB parts",
-           "n": n, "nnz": nnz, "k": k, "parts": NPART}
+    cfg = {"workload": "3-D 7-point Laplacian 128^3 (n=2,097,152, nnz=14,581,760), CSR int32, 1/deg operator "
+                       "(the reference exec_mpk), FP64 vectors, x~U[-1,1] seed 1, k=8, 2048 RCB parts",
+           "n": n, "nnz": nnz, "k": k, "parts": NPART, "operator": "1/deg (mpk2/mpkexec.c)"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -322,11 +417,16 @@ def main():
     import mpk_gb300 as M
     torch.cuda.set_device(local)
     arith = {"fma": M.ARITH_FMA, "separate": M.ARITH_SEPARATE, "df64": M.ARITH_DF64}[args.arith]
-    mk = {"pipe": lambda ar: M.Plan.pipe(a, k, arith=ar),
-          "tiles": lambda ar: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TILES, arith=ar),
-          "tasks": lambda ar: M.Plan.pa1(a, part, NPART, k, exec=M.EXEC_TASKS, arith=ar),
-          "spmv": lambda ar: M.Plan.spmv(a, k, arith=ar)}
-    plan = mk[args.exec](arith)
+    g = a.pattern()  # the 1/deg operator of the reference's exec_mpk
+
+    def mk(ex, ar, mat=None):
+        mat = g if mat is None else mat
+        return {"pipe": lambda: M.Plan.pipe(mat, k, arith=ar),
+                "wave": lambda: M.Plan.wave(mat, k, arith=ar),
+                "tiles": lambda: M.Plan.pa1(mat, part, NPART, k, exec=M.EXEC_TILES, arith=ar),
+                "tasks": lambda: M.Plan.pa1(mat, part, NPART, k, exec=M.EXEC_TASKS, arith=ar),
+                "spmv": lambda: M.Plan.spmv(mat, k, arith=ar)}[ex]()
+    plan = mk(args.exec, arith)
     info = plan.info()
     stream = torch.cuda.Stream()
     d_vv = torch.zeros((k + 1) * n, dtype=torch.float64, device="cuda")
@@ -347,23 +447,40 @@ def main():
     value = world * k * n / (ms_max * 1e-3) / 1e9
     exact = d_vv.cpu().numpy()
 
+    # FP64 reference result (k chained SpMVs in FP64 FMA, bit-identical to
+    # the oracle's chain) and the headline's error against it
+    def relerr(got, ref):
+        return max(float(np.linalg.norm(got[l * n:(l + 1) * n] - ref[l * n:(l + 1) * n]) /
+                         np.linalg.norm(ref[l * n:(l + 1) * n])) for l in range(1, k + 1))
+
+    rp = mk("spmv", M.ARITH_FMA)
+    ref64 = np.zeros((k + 1) * n)
+    ref64[:n] = x
+    rp.exec_host(ref64)
+    rp.close()
+    headline_err = relerr(exact, ref64)
+
     # the other executors on the same workload, for the record
     variants = {}
     if not args.no_variants:
-        want = exact if args.arith != "df64" else None
-        for ex, ar in (("spmv", "fma"), ("pipe", "fma"), ("pipe", "df64"), ("tiles", "fma"), ("tiles", "df64")):
-            if ex == args.exec and ar == args.arith:
+        runs = [(ex, ar, None) for ex, ar in (("spmv", "fma"), ("wave", "fma"), ("wave", "df64"), ("pipe", "fma"),
+                                              ("pipe", "df64"), ("tiles", "fma"), ("tiles", "df64"))]
+        runs += [("spmv", "fma", "valued"), ("wave", "fma", "valued"), ("wave", "df64", "valued")]
+        ref_val = None
+        for ex, ar, op in runs:
+            if ex == args.exec and ar == args.arith and op is None:
                 continue
-            vp = mk[ex]({"fma": M.ARITH_FMA, "df64": M.ARITH_DF64}[ar])
+            vp = mk(ex, {"fma": M.ARITH_FMA, "df64": M.ARITH_DF64}[ar], a if op else None)
             d2 = torch.zeros_like(d_vv)
             d2[:n] = d_vv[:n]
             t = statistics.mean(time_device(vp, d2, min(args.steps, 50), args.warmup, flush, stream))
             got = d2.cpu().numpy()
-            ref = exact
-            err = max(float(np.linalg.norm(got[l * n:(l + 1) * n] - ref[l * n:(l + 1) * n]) /
-                            np.linalg.norm(ref[l * n:(l + 1) * n])) for l in range(1, k + 1))
-            variants[f"{ex}_{ar}"] = {"ms_per_step": t, "value": k * n / (t * 1e-3) / 1e9,
-                                      "rel_err_max_vs_headline": err}
+            if op and ref_val is None:
+                ref_val = got  # spmv fma valued runs first among the valued
+            variants[f"{ex}_{ar}" + ("_valued" if op else "")] = {
+                "ms_per_step": t, "value": k * n / (t * 1e-3) / 1e9,
+                "rel_err_max_vs_fp64": relerr(got, ref_val if op else ref64),
+                "algorithmic_bytes": algorithmic_bytes(n, nnz, k, valued=bool(op))}
             vp.close()
             del d2
 
@@ -381,15 +498,24 @@ def main():
     e2e_s = reduce_max(world, e2e_s)
     same = bool(np.array_equal(exact, hnp))
 
-    mixed = {} if args.no_variants else bench_mixed(M, torch, a, x, k, exact, args, flush, stream)
+    mixed = {}
+    if not args.no_variants:  # the mixed form runs the valued operator; its FP64 reference:
+        vp = M.Plan.spmv(a, k, arith=M.ARITH_FMA)
+        exact_val = np.zeros((k + 1) * n)
+        exact_val[:n] = x
+        vp.exec_host(exact_val)
+        vp.close()
+        mixed = bench_mixed(M, torch, a, x, k, exact_val, args, flush, stream)
+    batched = {} if args.no_variants else bench_batch(M, torch, args, flush, stream)
+    sstep = {} if args.no_variants else bench_sstep(M)
 
     peak, peak_kind = peaks()
-    B = algorithmic_bytes(n, nnz, k)
+    B = algorithmic_bytes(n, nnz, k, valued=False)
     achieved = B / (ms * 1e-3) / 1e9
-    kname = {"pipe": "flow_kernel", "tiles": "tiles_kernel", "tasks": "tasks_kernel",
+    kname = {"pipe": "flow_kernel", "wave": "wave_kernel", "tiles": "tiles_kernel", "tasks": "tasks_kernel",
              "spmv": "spmv_level_kernel"}[args.exec]
     if args.arith == "df64":
-        kname = {"pipe": "flow_df_kernel", "tiles": "tiles_df_kernel"}.get(args.exec, kname)
+        kname = {"pipe": "flow_df_kernel", "wave": "wave_df_kernel", "tiles": "tiles_df_kernel"}.get(args.exec, kname)
     traffic = profile_traffic(kname)
     rows = info["rows_computed"]
     fp64_tflops = 2.0 * nnz * k * (rows / (n * k)) / (ms * 1e-3) / 1e12
@@ -398,7 +524,8 @@ def main():
     line = {"metric": "MPK powers/sec (FP64, k*n output rows per second)", "value": value,
             "unit": "Grow-powers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
+            "dtype": {"df64": "df64", "fma": "f64", "separate": "f64"}[args.arith], "data": "synthetic",
+            "rel_err_max_vs_fp64": headline_err, "tolerance": 1e-13,
             "config": dict(cfg, executor=args.exec, arith=args.arith,
                            l2="flushed before every call (256 MiB write); per-call CUDA events",
                            parallelism=f"replicas{world}"),
@@ -408,10 +535,11 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "algorithmic_bytes": B, "kernel": kname},
             "fp64_pipe": {"achieved_tflops": fp64_tflops, "peak_tflops_measured": 1.19,
-                          "note": "2*nnz*k*redundancy FP64 flops over call time; GB300 FP64 FMA measured at "
-                                  "0.60 TFMA/s, so plain FP64 MPK cannot reach the HBM bound"},
+                          "note": "2*nnz*k*redundancy flops over call time; GB300 FP64 FMA measured at 0.60 TFMA/s "
+                                  "caps plain FP64 at ~195 us for this workload, so the headline runs the rows in "
+                                  "double-float on the FP32 pipes (FP64 storage, error vs FP64 stated)"},
             "k_spmv_ms": base_ms, "speedup_vs_k_spmv": (base_ms / ms) if base_ms else None,
-            "variants": variants, "mixed": mixed,
+            "variants": variants, "mixed": mixed, "batched": batched, "sstep": sstep,
             "gpu_launches": info["launches"] * args.steps,
             "clocks": clk.summary(), "wall_s_timed_region": wall, "host_device_agree": same,
             "plan": {kk: info[kk] for kk in ("rows_computed", "device_bytes", "pipe_reach", "pipe_grid",

@@ -842,7 +842,7 @@ __device__ __forceinline__ int wave_col(const WaveArgs &a, long e, int i) {
 // previous level is read from vv: every address of it is fresh in this
 // launch, so L1 holds no stale copy.
 template <int ARITH, bool VALUED, bool REL>
-__global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
+__global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
   __shared__ int s_abort;
   __shared__ double s_lut[256];
   if (threadIdx.x == 0) s_abort = 0;
@@ -860,17 +860,20 @@ __global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
       const int len = __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
       const double cf = VALUED ? 0.0 : (len < 256 ? s_lut[len] : __ldg(a.rdeg + i));
+      const short *cr = a.srel + e0;
+      const int *cc = a.scol + e0;
+      const double *cv = a.sval + e0;
+      const double *xb = src + i;
       double s = 0.0;
       int t = 0;
       if (len <= 8) {  // all column loads, then all gathers, in flight together
-        int c[8];
         double x[8], v[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) c[u] = u < len ? wave_col<REL>(a, e0 + 32L * u, i) : 0;
-#pragma unroll
         for (int u = 0; u < 8; u++) {
-          x[u] = u < len ? src[c[u]] : 0.0;
-          v[u] = VALUED ? (u < len ? __ldg(a.sval + e0 + 32L * u) : 0.0) : cf;
+          if (u < len) {
+            x[u] = REL ? xb[__ldg(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
+            v[u] = VALUED ? __ldg(cv + 32 * u) : cf;
+          }
         }
 #pragma unroll
         for (int u = 0; u < 8; u++)
@@ -878,7 +881,8 @@ __global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
         t = len;
       }
       for (; t < len; t++)
-        s = row_term<ARITH>(s, VALUED ? __ldg(a.sval + e0 + 32L * t) : cf, src[wave_col<REL>(a, e0 + 32L * t, i)]);
+        s = row_term<ARITH>(s, VALUED ? __ldg(cv + 32L * t) : cf,
+                            REL ? xb[__ldg(cr + 32L * t)] : src[__ldg(cc + 32L * t)]);
       __stcs(dst + i, s);
     }
     wave_publish(a, b, a.base + (unsigned)l);
@@ -893,7 +897,7 @@ __global__ void __launch_bounds__(256) wave_kernel(WaveArgs a) {
 // the symmetric dependency ranges guarantee.  Level 0 splits the CTA's
 // own rows of x.
 template <bool VALUED, bool REL>
-__global__ void __launch_bounds__(256, 4) wave_df_kernel(WaveArgs a) {
+__global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
   __shared__ int s_abort;
   __shared__ float2 s_lut[256];
   if (threadIdx.x == 0) s_abort = 0;
@@ -913,27 +917,32 @@ __global__ void __launch_bounds__(256, 4) wave_df_kernel(WaveArgs a) {
       if (i >= r1) continue;
       const int len = __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
+      // per-lane bases: slot t of this row is 32*t elements further, an
+      // immediate offset of the load
+      const short *cr = a.srel + e0;
+      const int *cc = a.scol + e0;
+      const float2 *cv = a.sval2 + e0;
+      const float2 *xb = src + i;
       float sh = 0.f, sl_ = 0.f;
       int t = 0;
       if (len <= 8) {  // all column loads, then all gathers, in flight together
-        int c[8];
         float2 x[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) c[u] = u < len ? wave_col<REL>(a, e0 + 32L * u, i) : 0;
-#pragma unroll
-        for (int u = 0; u < 8; u++) x[u] = u < len ? src[c[u]] : make_float2(0.f, 0.f);
+        for (int u = 0; u < 8; u++) {
+          if (u < len) x[u] = REL ? xb[__ldg(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
+        }
 #pragma unroll
         for (int u = 0; u < 8; u++) {
           if (u < len) {
-            if (VALUED) df_mac(a.sval2[e0 + 32L * u], x[u], sh, sl_);
+            if (VALUED) df_mac(cv[32 * u], x[u], sh, sl_);
             else df_acc(x[u], sh, sl_);
           }
         }
         t = len;
       }
       for (; t < len; t++) {
-        const float2 x = src[wave_col<REL>(a, e0 + 32L * t, i)];
-        if (VALUED) df_mac(a.sval2[e0 + 32L * t], x, sh, sl_);
+        const float2 x = REL ? xb[__ldg(cr + 32L * t)] : src[__ldg(cc + 32L * t)];
+        if (VALUED) df_mac(cv[32L * t], x, sh, sl_);
         else df_acc(x, sh, sl_);
       }
       float2 v = df_norm(sh, sl_);
@@ -1032,18 +1041,24 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
         for (int u = 0; u < VW; u++) acc[u] = 0.0f;
         const int q0 = __ldg(a.ptr + i), q1 = __ldg(a.ptr + i + 1);
         int q = q0;
-        for (; q + 2 <= q1; q += 2) {
-          const int c0 = __ldg(a.col + q), c1 = __ldg(a.col + q + 1);
-          const float v0 = __ldg(a.val + q), v1 = __ldg(a.val + q + 1);
-          float x0[VW], x1[VW];
-          VecF<VW>::ld(src + (size_t)c0 * nrhs, x0);
-          VecF<VW>::ld(src + (size_t)c1 * nrhs, x1);
+        // four entries in flight: column and value loads first, then the
+        // four vector loads, then the FMAs in CSR order
+        for (; q + 4 <= q1; q += 4) {
+          int c[4];
+          float v[4], xv[4][VW];
 #pragma unroll
-          for (int u = 0; u < VW; u++) acc[u] = __fmaf_rn(v0, x0[u], acc[u]);
+          for (int u = 0; u < 4; u++) {
+            c[u] = __ldg(a.col + q + u);
+            v[u] = __ldg(a.val + q + u);
+          }
 #pragma unroll
-          for (int u = 0; u < VW; u++) acc[u] = __fmaf_rn(v1, x1[u], acc[u]);
+          for (int u = 0; u < 4; u++) VecF<VW>::ld(src + (size_t)c[u] * nrhs, xv[u]);
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int w = 0; w < VW; w++) acc[w] = __fmaf_rn(v[u], xv[u][w], acc[w]);
         }
-        if (q < q1) {
+        for (; q < q1; q++) {
           float x0[VW];
           const float v0 = __ldg(a.val + q);
           VecF<VW>::ld(src + (size_t)__ldg(a.col + q) * nrhs, x0);
