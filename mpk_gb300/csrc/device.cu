@@ -781,6 +781,9 @@ __global__ void __launch_bounds__(256) bufs_phase_kernel(int list_base, const lo
 // double-float mode one float2 shadow level per level), so L1 never holds
 // a stale copy of data another SM produced during the launch.
 // ------------------------------------------------------------------------
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
+
 struct WaveArgs {
   int n, nlevel, nblk;
   uint32_t base;               // flags of this call start at base (level l publishes base + l)
@@ -917,10 +920,10 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
       if (i >= r1) continue;
       const int len = __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
-      // per-lane bases: slot t of this row is 32*t elements further, an
-      // immediate offset of the load
       const short *cr = a.srel + e0;
       const int *cc = a.scol + e0;
+      // per-lane bases: slot t of this row is 32*t elements further, an
+      // immediate offset of the load
       const float2 *cv = a.sval2 + e0;
       const float2 *xb = src + i;
       float sh = 0.f, sl_ = 0.f;
@@ -949,6 +952,55 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
       if (!VALUED) v = df_scale(len < 256 ? s_lut[len] : a.rdeg2[i], v);
       sdst[i] = v;
       __stcs(dst + i, df_to_double(v));
+    }
+    wave_publish(a, b, a.base + (unsigned)l);
+  }
+}
+
+// Mixed-precision rows on the wavefront schedule: FP32 or BF16 values in
+// the sliced layout, FP32 basis, FP32 FMA in CSR order from 0, each level
+// scaled by the exact power of two `scale` (the same arithmetic as
+// mix_pipe_kernel, so both give identical bits).  Levels live at fresh
+// addresses of the FP32 vv.
+template <typename VT, bool REL>
+__global__ void __launch_bounds__(256) wave_mix_kernel(WaveArgs a, const VT *__restrict__ sv, float *vf, float scale) {
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = 0;
+  __syncthreads();
+  const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int l = 1; l <= a.nlevel; l++) {
+    if (l > 1 && !wave_wait(a, b, a.base + (unsigned)(l - 1), &s_abort)) return;
+    const float *src = vf + (size_t)(l - 1) * a.n;
+    float *dst = vf + (size_t)l * a.n;
+    for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
+      const int i = (sl << 5) + lane;
+      if (i >= r1) continue;
+      const int len = __ldg(a.len + i);
+      const long e0 = __ldg(a.sell_off + sl) + lane;
+      const short *cr = a.srel + e0;
+      const int *cc = a.scol + e0;
+      const VT *cv = sv + e0;
+      const float *xb = src + i;
+      float s = 0.f;
+      int t = 0;
+      if (len <= 12) {  // all loads in flight together (12 covers 9- and 7-point stencils)
+        float x[12], v[12];
+#pragma unroll
+        for (int u = 0; u < 12; u++) {
+          if (u < len) {
+            x[u] = REL ? xb[__ldg(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
+            v[u] = to_f32(cv[32 * u]);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 12; u++)
+          if (u < len) s = __fmaf_rn(v[u], x[u], s);
+        t = len;
+      }
+      for (; t < len; t++)
+        s = __fmaf_rn(to_f32(cv[32L * t]), REL ? xb[__ldg(cr + 32L * t)] : src[__ldg(cc + 32L * t)], s);
+      __stcs(dst + i, s * scale);
     }
     wave_publish(a, b, a.base + (unsigned)l);
   }
@@ -1120,8 +1172,6 @@ struct MixArgs {
   bool bulk_ok;
 };
 
-__device__ __forceinline__ float to_f32(float v) { return v; }
-__device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
 
 template <typename VT>
 __global__ void __launch_bounds__(kPipeThreads) mix_pipe_kernel(MixArgs m) {
@@ -1244,6 +1294,8 @@ struct mpkg_plan {
   const void *graph_key = nullptr;
   bool graph_ok = false;
   float *d_fb = nullptr;  // staging of mpkg_exec_batch_host
+  mpkg_plan *inner = nullptr;  // mixed form: the wavefront layout it runs on
+  void *mix_sval = nullptr;    // mixed form: sliced FP32 / BF16 values
   // pdmpk buffers (b_vall, b_in_*, b_out_*, b_cm_* shared with the above)
   long *d_row_init = nullptr;
   std::vector<long> pd_row_off;  // per batch: range of rows
@@ -1816,6 +1868,7 @@ const char *mpkg_last_error(void) { return last_error(); }
 int mpkg_version(void) { return 1; }
 
 void mpkg_plan_destroy(mpkg_plan *p) {
+  if (p && p->inner) mpkg_plan_destroy(p->inner);
   if (p && p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
   if (p && p->graph) cudaGraphDestroy(p->graph);
   if (!p) return;
@@ -2127,8 +2180,29 @@ int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out) {
   return kOk;
 }
 
+}  // extern "C"
+
+namespace {
+int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
+                   int occ_value_type, mpkg_plan **out);
+const void *mix_wave_kernel_ptr(int value_type, bool rel);
+}  // namespace
+
+extern "C" {
+
 int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
                    mpkg_plan **out) {
+  return plan_wave_impl(n, ptr, col, val, nlevel, arith, -1, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+// occ_value_type >= 0: size the grid for the mixed-precision kernel of that
+// value type instead of the plan's own kernel
+int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
+                   int occ_value_type, mpkg_plan **out) {
   clear_error();
   if (!out) return fail(kEInval, "out is null");
   *out = nullptr;
@@ -2146,7 +2220,9 @@ int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int
     p->wave_rel = rel;
   }
   int grid = 0;
-  if (!rc) rc = wave_occupancy(p, (const void *)wave_kernel_ptr(p), &grid);
+  if (!rc)
+    rc = wave_occupancy(p, occ_value_type >= 0 ? mix_wave_kernel_ptr(occ_value_type, p->wave_rel)
+                                               : (const void *)wave_kernel_ptr(p), &grid);
   if (!rc) {
     const long nnz = ptr[n];
     const int nslice = (n + 31) / 32;
@@ -2254,6 +2330,10 @@ int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int
   *out = p;
   return kOk;
 }
+
+}  // namespace
+
+extern "C" {
 
 namespace {
 
@@ -2528,6 +2608,60 @@ int mpkg_pdmpk_prep(int n, const int *ptr, const int *col, const double *val, in
   return kOk;
 }
 
+}  // extern "C"
+
+namespace {
+
+const void *mix_wave_kernel_ptr(int value_type, bool rel) {
+  if (value_type == MPKG_VALUE_F32)
+    return rel ? (const void *)wave_mix_kernel<float, true> : (const void *)wave_mix_kernel<float, false>;
+  return rel ? (const void *)wave_mix_kernel<__nv_bfloat16, true> : (const void *)wave_mix_kernel<__nv_bfloat16, false>;
+}
+
+int mixed_wave_setup(mpkg_plan *p, int n, const int *ptr, const int *col, const double *val, int nlevel,
+                     int value_type) {
+  mpkg_plan *w = nullptr;
+  int rc = plan_wave_impl(n, ptr, col, val, nlevel, MPKG_ARITH_FMA, -1, &w);
+  if (rc) return rc;
+  p->inner = w;
+  int per_sm = 0, nsm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_wave_kernel_ptr(value_type, w->wave_rel), 256, 0));
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+  if ((long)per_sm * nsm < w->wave_grid) return fail(kERange, "mixed wavefront kernel cannot cover the grid");
+  const int nslice = (n + 31) / 32;
+  std::vector<long> soff(nslice + 1, 0);
+  for (int sl = 0; sl < nslice; sl++) {
+    int wd = 0;
+    for (int i = sl * 32; i < std::min(n, sl * 32 + 32); i++) wd = std::max(wd, ptr[i + 1] - ptr[i]);
+    soff[sl + 1] = soff[sl] + 32L * wd;
+  }
+  auto fill = [&](auto conv, auto *vec) {
+    vec->assign(soff[nslice], conv(0.0));
+    for (int i = 0; i < n; i++) {
+      const long e0 = soff[i / 32] + (i % 32);
+      for (int t = 0; t < ptr[i + 1] - ptr[i]; t++) (*vec)[e0 + 32L * t] = conv(val[ptr[i] + t]);
+    }
+  };
+  if (value_type == MPKG_VALUE_F32) {
+    std::vector<float> sv;
+    fill([](double v) { return (float)v; }, &sv);
+    float *d = nullptr;
+    if ((rc = dev_copy(p, &d, sv.data(), sv.size()))) return rc;
+    p->mix_sval = d;
+  } else {
+    std::vector<__nv_bfloat16> sv;
+    fill([](double v) { return __double2bfloat16(v); }, &sv);
+    __nv_bfloat16 *d = nullptr;
+    if ((rc = dev_copy(p, &d, sv.data(), sv.size()))) return rc;
+    p->mix_sval = d;
+  }
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
 int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, int nlevel, int value_type,
                     mpkg_plan **out) {
   clear_error();
@@ -2642,6 +2776,12 @@ int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, in
         rc = fail(kERange, "matrix bandwidth too large for the mixed pipeline");
     }
   }
+  // the wavefront schedule (preferred): its layout from an FP64 wave plan,
+  // plus the values in the sliced order and the storage type
+  if (!rc && mixed_wave_setup(p, n, ptr, col, val, nlevel, value_type) != kOk) {
+    if (p->inner) { mpkg_plan_destroy(p->inner); p->inner = nullptr; }
+    clear_error();  // keep the chunk pipeline
+  }
   if (rc) { mpkg_plan_destroy(p); return rc; }
   *out = p;
   return kOk;
@@ -2662,6 +2802,32 @@ int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream) {
   if (p->epoch >= (1u << 30)) {
     CUDA_TRY(cudaMemsetAsync(p->mix.counts, 0, sizeof(unsigned) * (size_t)(p->nlevel + 1) * p->mix.nchunk, st));
     p->epoch = 1;
+  }
+  if (p->inner) {  // wavefront schedule
+    WaveArgs &w = p->inner->wave;
+    const unsigned step = (unsigned)p->nlevel + 1;
+    if (w.base == 0 || w.base > (1u << 30)) {
+      CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(unsigned int) * (size_t)w.nblk, st));
+      w.base = 1;
+    } else {
+      w.base += step;
+    }
+    WaveArgs a = w;
+    a.err = p->d_err;
+    float scale = p->mix.scale;
+    if (p->mix_vt == MPKG_VALUE_F32) {
+      const float *sv = static_cast<const float *>(p->mix_sval);
+      void *args[] = {&a, (void *)&sv, (void *)&d_vv, &scale};
+      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_F32, p->inner->wave_rel), dim3(w.nblk),
+                                           dim3(256), args, 0, st));
+    } else {
+      const __nv_bfloat16 *sv = static_cast<const __nv_bfloat16 *>(p->mix_sval);
+      void *args[] = {&a, (void *)&sv, (void *)&d_vv, &scale};
+      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_BF16, p->inner->wave_rel), dim3(w.nblk),
+                                           dim3(256), args, 0, st));
+    }
+    p->launches = 1;
+    return kOk;
   }
   CUDA_TRY(cudaMemsetAsync(p->mix.ticket, 0, sizeof(unsigned), st));
   MixArgs m = p->mix;
@@ -2724,6 +2890,9 @@ int mpkg_sync(mpkg_plan *p, void *stream) {
       cudaMemset(p->pipe.counts, 0, sizeof(unsigned int) * (size_t)(p->nlevel + 1) * p->pipe.ngroups);
       p->epoch = 0;
     }
+    if (p->exec == MPKG_EXEC_WAVE) p->wave.base = 0;  // flags restart from zero on the next call
+    if (p->inner) p->inner->wave.base = 0;
+    if (p->exec == MPKG_EXEC_BATCH) p->batch.base = 0;
     if (err == kErrTimeout) return fail(kETimeout, "a device-side wait exceeded its spin limit");
     return fail(kERange, "device-side bounds check failed");
   }
