@@ -380,8 +380,11 @@ def main():
     ap.add_argument("--arith", default="df64", choices=["fma", "separate", "df64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="time only the selected executor")
+    ap.add_argument("--sections", default="variants,mixed,batched,sstep",
+                    help="comma list of the extra sections to run (variants, mixed, batched, sstep; 'none')")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    sections = set() if args.no_variants else {t.strip() for t in args.sections.split(",")} - {"none", ""}
 
     world, rank, local = dist_setup(args)
     a, part, x = workload()
@@ -462,7 +465,7 @@ def main():
 
     # the other executors on the same workload, for the record
     variants = {}
-    if not args.no_variants:
+    if "variants" in sections:
         runs = [(ex, ar, None) for ex, ar in (("spmv", "fma"), ("wave", "fma"), ("wave", "df64"), ("pipe", "fma"),
                                               ("pipe", "df64"), ("tiles", "fma"), ("tiles", "df64"))]
         runs += [("spmv", "fma", "valued"), ("wave", "fma", "valued"), ("wave", "df64", "valued")]
@@ -499,15 +502,15 @@ def main():
     same = bool(np.array_equal(exact, hnp))
 
     mixed = {}
-    if not args.no_variants:  # the mixed form runs the valued operator; its FP64 reference:
+    if "mixed" in sections:  # the mixed form runs the valued operator; its FP64 reference:
         vp = M.Plan.spmv(a, k, arith=M.ARITH_FMA)
         exact_val = np.zeros((k + 1) * n)
         exact_val[:n] = x
         vp.exec_host(exact_val)
         vp.close()
         mixed = bench_mixed(M, torch, a, x, k, exact_val, args, flush, stream)
-    batched = {} if args.no_variants else bench_batch(M, torch, args, flush, stream)
-    sstep = {} if args.no_variants else bench_sstep(M)
+    batched = bench_batch(M, torch, args, flush, stream) if "batched" in sections else {}
+    sstep = bench_sstep(M) if "sstep" in sections else {}
 
     peak, peak_kind = peaks()
     B = algorithmic_bytes(n, nnz, k, valued=False)

@@ -129,6 +129,10 @@ int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val,
  * each level. */
 int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
                    mpkg_plan **out);
+/* The same with at most ctas_per_sm resident CTAs per SM (fewer, larger row
+ * ranges; the default is the kernel's occupancy). */
+int mpkg_plan_wave_ctas(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
+                        int ctas_per_sm, mpkg_plan **out);
 
 /* Batched block-vector form (no counterpart in the reference; the
  * batching pattern of the task): nmat independent matrices (host CSR

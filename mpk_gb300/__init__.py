@@ -78,6 +78,7 @@ def _declare(L):
         "mpkg_plan_pipe": (I, [I, P, P, P, I, I, I, pp]),
         "mpkg_plan_spmv": (I, [I, P, P, P, I, I, pp]),
         "mpkg_plan_wave": (I, [I, P, P, P, I, I, pp]),
+        "mpkg_plan_wave_ctas": (I, [I, P, P, P, I, I, I, pp]),
         "mpkg_plan_batch": (I, [I, P, P, P, P, I, I, I, pp]),
         "mpkg_cg": (I, [I, P, P, P, P, P, D, I, C.POINTER(CgInfo)]),
         "mpkg_sstep_cg": (I, [I, P, P, P, P, P, I, P, D, D, I, C.POINTER(CgInfo)]),
@@ -467,8 +468,12 @@ class Plan:
         _check(lib().mpkg_exec_mixed_device(self._h, C.c_void_p(d_vv_ptr), C.c_void_p(stream or None)))
 
     @classmethod
-    def wave(cls, a: Csr, nlevel, arith=ARITH_FMA):
-        """Wavefront executor: one persistent launch, neighbour-only waits."""
+    def wave(cls, a: Csr, nlevel, arith=ARITH_FMA, ctas_per_sm=0):
+        """Wavefront executor: one persistent launch, neighbour-only waits
+        (ctas_per_sm > 0 caps the resident CTAs per SM)."""
+        if ctas_per_sm:
+            return cls._make(lib().mpkg_plan_wave_ctas, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, arith,
+                             ctas_per_sm, a=a, nlevel=nlevel)
         return cls._make(lib().mpkg_plan_wave, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, arith,
                          a=a, nlevel=nlevel)
 

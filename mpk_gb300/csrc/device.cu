@@ -804,6 +804,8 @@ struct WaveArgs {
   const float2 *lut2;          // ... and its double-float split
   double *vv;
   float2 *ring;                // 2 * n: double-float copies of levels l-1 and l
+  int stage_rel_bytes;         // > 0: the CTA's int16 offsets and lengths are staged in shared memory
+                               // once per call (offsets first, this many bytes, then the lengths)
   const int *row_lo;           // nblk + 1
   const int *dep_lo, *dep_hi;  // per CTA: CTAs it reads from or that read from it
   unsigned int *flags;         // per CTA: last level published
@@ -835,6 +837,29 @@ __device__ __forceinline__ void wave_publish(const WaveArgs &a, int b, unsigned 
   }
 }
 
+// Copies the CTA's slab of int16 offsets (whole slices, 64-byte aligned) and
+// its rows' lengths into shared memory; the CTA owns the same rows at every
+// level, so this happens once per call.
+__device__ __forceinline__ void wave_stage(const WaveArgs &a, int r0, int r1, unsigned char *smem) {
+  if (r0 >= r1) return;
+  const long e_lo = a.sell_off[r0 >> 5], e_hi = a.sell_off[(r1 + 31) >> 5];
+  const int4 *g = reinterpret_cast<const int4 *>(a.srel + e_lo);
+  int4 *d = reinterpret_cast<int4 *>(smem);
+  const long nvec = (e_hi - e_lo) / 8;  // slices hold 32*w entries: a multiple of 8 shorts
+  for (long v = threadIdx.x; v < nvec; v += blockDim.x) d[v] = __ldg(g + v);
+  unsigned char *sl = smem + a.stage_rel_bytes;  // staged rows are at most 255 long
+  for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) sl[i - r0] = (unsigned char)__ldg(a.len + i);
+}
+
+// An int16 offset from the staged slab (shared memory: plain load) or
+// from global memory (read-only path).  __ldg must never see a shared
+// address.
+template <bool STAGE>
+__device__ __forceinline__ int ld_off(const short *p) {
+  if (STAGE) return (int)*p;
+  return (int)__ldg(p);
+}
+
 template <bool REL>
 __device__ __forceinline__ int wave_col(const WaveArgs &a, long e, int i) {
   return REL ? i + (int)__ldg(a.srel + e) : __ldg(a.scol + e);
@@ -844,14 +869,19 @@ __device__ __forceinline__ int wave_col(const WaveArgs &a, long e, int i) {
 // A warp computes one 32-row slice; CTA row ranges start on slices.  The
 // previous level is read from vv: every address of it is fresh in this
 // launch, so L1 holds no stale copy.
-template <int ARITH, bool VALUED, bool REL>
+template <int ARITH, bool VALUED, bool REL, bool STAGE>
 __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
+  extern __shared__ __align__(16) unsigned char wave_smem[];
   __shared__ int s_abort;
   __shared__ double s_lut[256];
   if (threadIdx.x == 0) s_abort = 0;
   if (!VALUED) s_lut[threadIdx.x] = a.lut[threadIdx.x];
-  __syncthreads();
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
+  if (STAGE) wave_stage(a, r0, r1, wave_smem);
+  __syncthreads();
+  const long e_lo = STAGE && r0 < r1 ? a.sell_off[r0 >> 5] : 0;
+  const short *s_rel = reinterpret_cast<const short *>(wave_smem);
+  const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int l = 1; l <= a.nlevel; l++) {
     if (l > 1 && !wave_wait(a, b, a.base + (unsigned)(l - 1), &s_abort)) return;
@@ -860,10 +890,10 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
     for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
       const int i = (sl << 5) + lane;
       if (i >= r1) continue;
-      const int len = __ldg(a.len + i);
+      const int len = STAGE ? s_len[i - r0] : __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
       const double cf = VALUED ? 0.0 : (len < 256 ? s_lut[len] : __ldg(a.rdeg + i));
-      const short *cr = a.srel + e0;
+      const short *cr = STAGE ? s_rel + (e0 - e_lo) : a.srel + e0;
       const int *cc = a.scol + e0;
       const double *cv = a.sval + e0;
       const double *xb = src + i;
@@ -874,7 +904,7 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
 #pragma unroll
         for (int u = 0; u < 8; u++) {
           if (u < len) {
-            x[u] = REL ? xb[__ldg(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
+            x[u] = REL ? xb[ld_off<STAGE>(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
             v[u] = VALUED ? __ldg(cv + 32 * u) : cf;
           }
         }
@@ -885,7 +915,7 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
       }
       for (; t < len; t++)
         s = row_term<ARITH>(s, VALUED ? __ldg(cv + 32L * t) : cf,
-                            REL ? xb[__ldg(cr + 32L * t)] : src[__ldg(cc + 32L * t)]);
+                            REL ? xb[ld_off<STAGE>(cr + 32L * t)] : src[__ldg(cc + 32L * t)]);
       __stcs(dst + i, s);
     }
     wave_publish(a, b, a.base + (unsigned)l);
@@ -899,14 +929,19 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
 // after every CTA that reads its rows has finished the level before, which
 // the symmetric dependency ranges guarantee.  Level 0 splits the CTA's
 // own rows of x.
-template <bool VALUED, bool REL>
+template <bool VALUED, bool REL, bool STAGE>
 __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
+  extern __shared__ __align__(16) unsigned char wave_smem[];
   __shared__ int s_abort;
   __shared__ float2 s_lut[256];
   if (threadIdx.x == 0) s_abort = 0;
   if (!VALUED) s_lut[threadIdx.x] = a.lut2[threadIdx.x];
-  __syncthreads();
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
+  if (STAGE) wave_stage(a, r0, r1, wave_smem);
+  __syncthreads();
+  const long e_lo = STAGE && r0 < r1 ? a.sell_off[r0 >> 5] : 0;
+  const short *s_rel = reinterpret_cast<const short *>(wave_smem);
+  const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) a.ring[i] = df_split(a.vv[i]);
   wave_publish(a, b, a.base);
@@ -918,9 +953,9 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
     for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
       const int i = (sl << 5) + lane;
       if (i >= r1) continue;
-      const int len = __ldg(a.len + i);
+      const int len = STAGE ? s_len[i - r0] : __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
-      const short *cr = a.srel + e0;
+      const short *cr = STAGE ? s_rel + (e0 - e_lo) : a.srel + e0;
       const int *cc = a.scol + e0;
       // per-lane bases: slot t of this row is 32*t elements further, an
       // immediate offset of the load
@@ -932,7 +967,7 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
         float2 x[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
-          if (u < len) x[u] = REL ? xb[__ldg(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
+          if (u < len) x[u] = REL ? xb[ld_off<STAGE>(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
         }
 #pragma unroll
         for (int u = 0; u < 8; u++) {
@@ -944,7 +979,7 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
         t = len;
       }
       for (; t < len; t++) {
-        const float2 x = REL ? xb[__ldg(cr + 32L * t)] : src[__ldg(cc + 32L * t)];
+        const float2 x = REL ? xb[ld_off<STAGE>(cr + 32L * t)] : src[__ldg(cc + 32L * t)];
         if (VALUED) df_mac(cv[32L * t], x, sh, sl_);
         else df_acc(x, sh, sl_);
       }
@@ -1283,6 +1318,7 @@ struct mpkg_plan {
   WaveArgs wave{};
   int wave_grid = 0;
   bool wave_rel = false;
+  int wave_stage_len_bytes = 0;
   // batched block-vector form
   BatchArgs batch{};
   int batch_lpr = 0, batch_vw = 0, batch_nmat = 0;
@@ -1512,17 +1548,24 @@ int wave_occupancy(mpkg_plan *p, K kernel, int *grid) {
 }
 
 void *wave_kernel_ptr(const mpkg_plan *p) {
-  const bool rel = p->wave_rel;
-#define MPKG_WK(REL)                                                                                        \
-  if (p->arith == MPKG_ARITH_DF64)                                                                          \
-    return p->valued ? (void *)wave_df_kernel<true, REL> : (void *)wave_df_kernel<false, REL>;             \
-  if (p->arith == MPKG_ARITH_SEPARATE)                                                                      \
-    return p->valued ? (void *)wave_kernel<MPKG_ARITH_SEPARATE, true, REL>                                  \
-                     : (void *)wave_kernel<MPKG_ARITH_SEPARATE, false, REL>;                                \
-  return p->valued ? (void *)wave_kernel<MPKG_ARITH_FMA, true, REL> : (void *)wave_kernel<MPKG_ARITH_FMA, false, REL>;
-  if (rel) { MPKG_WK(true) }
-  MPKG_WK(false)
+  const bool rel = p->wave_rel, stage = p->wave.stage_rel_bytes > 0;
+#define MPKG_WK(REL, ST)                                                                                      \
+  if (p->arith == MPKG_ARITH_DF64)                                                                            \
+    return p->valued ? (void *)wave_df_kernel<true, REL, ST> : (void *)wave_df_kernel<false, REL, ST>;       \
+  if (p->arith == MPKG_ARITH_SEPARATE)                                                                        \
+    return p->valued ? (void *)wave_kernel<MPKG_ARITH_SEPARATE, true, REL, ST>                                \
+                     : (void *)wave_kernel<MPKG_ARITH_SEPARATE, false, REL, ST>;                              \
+  return p->valued ? (void *)wave_kernel<MPKG_ARITH_FMA, true, REL, ST>                                       \
+                   : (void *)wave_kernel<MPKG_ARITH_FMA, false, REL, ST>;
+  if (rel && stage) { MPKG_WK(true, true) }
+  if (rel) { MPKG_WK(true, false) }
+  MPKG_WK(false, false)
 #undef MPKG_WK
+}
+
+// Dynamic shared memory of a wave launch (the staged slab).
+size_t wave_dyn_smem(const mpkg_plan *p) {
+  return p->wave.stage_rel_bytes > 0 ? (size_t)p->wave.stage_rel_bytes + p->wave_stage_len_bytes : 0;
 }
 
 int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st) {
@@ -1537,7 +1580,7 @@ int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st) {
   WaveArgs a = w;
   a.vv = d_vv;
   void *args[] = {&a};
-  CUDA_TRY(cudaLaunchCooperativeKernel(wave_kernel_ptr(p), dim3(w.nblk), dim3(256), args, 0, st));
+  CUDA_TRY(cudaLaunchCooperativeKernel(wave_kernel_ptr(p), dim3(w.nblk), dim3(256), args, wave_dyn_smem(p), st));
   return kOk;
 }
 
@@ -2183,6 +2226,7 @@ int mpkg_plan_bufs(const char *dir, int npart, int arith, mpkg_plan **out) {
 }  // extern "C"
 
 namespace {
+thread_local int g_wave_ctas_per_sm = 0;  // mpkg_plan_wave_ctas: cap on resident CTAs per SM (0: occupancy)
 int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
                    int occ_value_type, mpkg_plan **out);
 const void *mix_wave_kernel_ptr(int value_type, bool rel);
@@ -2193,6 +2237,15 @@ extern "C" {
 int mpkg_plan_wave(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
                    mpkg_plan **out) {
   return plan_wave_impl(n, ptr, col, val, nlevel, arith, -1, out);
+}
+
+int mpkg_plan_wave_ctas(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
+                        int ctas_per_sm, mpkg_plan **out) {
+  if (ctas_per_sm <= 0 || ctas_per_sm > 32) return fail(kEInval, "ctas_per_sm must be in [1, 32]");
+  g_wave_ctas_per_sm = ctas_per_sm;
+  const int rc = plan_wave_impl(n, ptr, col, val, nlevel, arith, -1, out);
+  g_wave_ctas_per_sm = 0;
+  return rc;
 }
 
 }  // extern "C"
@@ -2223,19 +2276,63 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
   if (!rc)
     rc = wave_occupancy(p, occ_value_type >= 0 ? mix_wave_kernel_ptr(occ_value_type, p->wave_rel)
                                                : (const void *)wave_kernel_ptr(p), &grid);
+  if (!rc && g_wave_ctas_per_sm > 0) {
+    int nsm = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+    grid = std::min(grid, g_wave_ctas_per_sm * nsm);
+  }
   if (!rc) {
     const long nnz = ptr[n];
     const int nslice = (n + 31) / 32;
     grid = (int)std::max<long>(1, std::min<long>(grid, nslice));
     // contiguous row ranges of (nearly) equal nonzeros, starting on slices
-    std::vector<int> lo(grid + 1, 0);
-    for (int b = 1; b < grid; b++) {
-      const long target = nnz * b / grid;
-      int r = (int)(std::lower_bound(ptr, ptr + n + 1, (int)target) - ptr);
-      r = std::min(n, (r + 16) / 32 * 32);
-      lo[b] = std::max(r, lo[b - 1]);
+    auto ranges = [&](int g) {
+      std::vector<int> r(g + 1, 0);
+      for (int b = 1; b < g; b++) {
+        const long target = nnz * b / g;
+        int q = (int)(std::lower_bound(ptr, ptr + n + 1, (int)target) - ptr);
+        q = std::min(n, (q + 16) / 32 * 32);
+        r[b] = std::max(q, r[b - 1]);
+      }
+      r[g] = n;
+      return r;
+    };
+    std::vector<int> lo = ranges(grid);
+    // stage each CTA's int16 offsets and uint8 lengths in shared memory when
+    // the slabs fit next to the kernel's own shared memory at this occupancy
+    int maxlen = 0;
+    for (int i = 0; i < n; i++) maxlen = std::max(maxlen, ptr[i + 1] - ptr[i]);
+    if (p->wave_rel && occ_value_type < 0 && maxlen <= 255) {
+      std::vector<long> sw(nslice + 1, 0);  // slice offsets in entries
+      for (int sl = 0; sl < nslice; sl++) {
+        int wd = 0;
+        for (int i = sl * 32; i < std::min(n, sl * 32 + 32); i++) wd = std::max(wd, ptr[i + 1] - ptr[i]);
+        sw[sl + 1] = sw[sl] + 32L * wd;
+      }
+      long relb = 0, lenb = 0;
+      for (int b = 0; b < grid; b++) {
+        if (lo[b] >= lo[b + 1]) continue;
+        relb = std::max(relb, 2 * (sw[(lo[b + 1] + 31) / 32] - sw[lo[b] / 32]));
+        lenb = std::max<long>(lenb, lo[b + 1] - lo[b]);
+      }
+      relb = (relb + 15) / 16 * 16;
+      lenb = (lenb + 15) / 16 * 16;
+      int nsm = 0, per_sm = 0;
+      CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+      p->wave.stage_rel_bytes = (int)relb;
+      p->wave_stage_len_bytes = (int)lenb;
+      const void *k = wave_kernel_ptr(p);
+      bool ok = relb + lenb <= 200 * 1024 &&
+                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(relb + lenb)) ==
+                    cudaSuccess &&
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, (size_t)(relb + lenb)) == cudaSuccess &&
+                (long)per_sm * nsm >= grid;
+      if (!ok) {
+        cudaGetLastError();
+        p->wave.stage_rel_bytes = 0;
+        p->wave_stage_len_bytes = 0;
+      }
     }
-    lo[grid] = n;
     // sliced ELL copy of the matrix
     std::vector<long> soff(nslice + 1, 0);
     std::vector<unsigned short> len(n);

@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const f
     pa = a;
     pb = a + t;
   }
-  double acc = 0.0;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (long r0 = (long)blockIdx.x * kGramRows; r0 < n; r0 += (long)gridDim.x * kGramRows) {
     __syncthreads();
     for (int e = threadIdx.x; e < ncol * kGramRows; e += blockDim.x) {
@@ -172,12 +172,17 @@ __global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const f
       tile[c][rr] = r0 + rr < n ? y[(size_t)c * n + r0 + rr] : 0.f;
     }
     __syncthreads();
-    if ((int)threadIdx.x < npair) {
-#pragma unroll 8
-      for (int rr = 0; rr < kGramRows; rr++) acc = fma((double)tile[pa][rr], (double)tile[pb][rr], acc);
+    if ((int)threadIdx.x < npair) {  // four independent partial sums per thread
+#pragma unroll 4
+      for (int rr = 0; rr < kGramRows; rr += 4) {
+        acc[0] = fma((double)tile[pa][rr], (double)tile[pb][rr], acc[0]);
+        acc[1] = fma((double)tile[pa][rr + 1], (double)tile[pb][rr + 1], acc[1]);
+        acc[2] = fma((double)tile[pa][rr + 2], (double)tile[pb][rr + 2], acc[2]);
+        acc[3] = fma((double)tile[pa][rr + 3], (double)tile[pb][rr + 3], acc[3]);
+      }
     }
   }
-  if ((int)threadIdx.x < npair) part[(size_t)blockIdx.x * npair + threadIdx.x] = acc;
+  if ((int)threadIdx.x < npair) part[(size_t)blockIdx.x * npair + threadIdx.x] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
 }
 
 __global__ void gram_reduce_kernel(int nblk, int ncol, const double *__restrict__ part, double *__restrict__ g) {
@@ -192,63 +197,59 @@ __global__ void gram_reduce_kernel(int nblk, int ncol, const double *__restrict_
   }
 }
 
-// The s inner CG steps in coefficient space (FP64, one warp): p = Y ph,
-// r = Y rh, A Y = Y B on the columns in use.  Outputs xh, ph (and rh).
-// Returns through flag[0] = 1 when a breakdown (non-positive curvature or
-// residual) stopped the inner loop early; flag[1] = steps taken.
+// The s inner CG steps in coefficient space (FP64, one warp; lane c holds
+// coefficient c, m = 2s+1 <= 32): p = Y ph, r = Y rh, A Y = Y B on the
+// columns in use.  Outputs xh, ph (and rh).  flag[0] = 1 when a breakdown
+// (non-positive curvature or residual) stopped the inner loop early;
+// flag[1] = steps taken.
 __global__ void coeff_kernel(int s, const double *__restrict__ g, const double *__restrict__ theta,
                              const double *__restrict__ sigma, double pnorm, double rnorm, double *__restrict__ xh,
                              double *__restrict__ ph, double *__restrict__ rh, int *__restrict__ flag) {
-  if (threadIdx.x != 0) return;
-  const int m = 2 * s + 1;
-  double p[kMaxCols], r[kMaxCols], x[kMaxCols], bp[kMaxCols], gv[kMaxCols];
-  for (int c = 0; c < m; c++) { p[c] = 0.0; r[c] = 0.0; x[c] = 0.0; }
-  p[0] = pnorm;
-  r[s + 1] = rnorm;
-  auto apply_b = [&](const double *v, double *out) {
-    for (int c = 0; c < m; c++) out[c] = 0.0;
-    for (int j = 0; j < s; j++) {  // P block columns 0..s-1
-      out[j] += theta[j] * v[j];
-      out[j + 1] += sigma[j] * v[j];
-    }
-    for (int j = 0; j + 1 < s; j++) {  // R block columns s+1 .. 2s-1
-      const int c = s + 1 + j;
-      out[c] += theta[j] * v[c];
-      out[c + 1] += sigma[j] * v[c];
-    }
+  const int m = 2 * s + 1, c = threadIdx.x;
+  const bool on = c < m;
+  double p = 0.0, r = 0.0, x = 0.0;
+  if (c == 0) p = pnorm;
+  if (c == s + 1) r = rnorm;
+  // B v: column j of the P block (j < s) maps to theta_j e_j + sigma_j e_(j+1),
+  // the R block likewise up to its second-to-last column
+  auto apply_b = [&](double v) {
+    const double vm1 = __shfl_up_sync(0xffffffffu, v, 1);
+    double out = 0.0;
+    if (c < s) out += theta[c] * v;
+    if (c >= 1 && c <= s) out += sigma[c - 1] * vm1;
+    if (c >= s + 1 && c < 2 * s) out += theta[c - s - 1] * v;
+    if (c >= s + 2 && c <= 2 * s) out += sigma[c - s - 2] * vm1;
+    return on ? out : 0.0;
   };
-  auto gdot = [&](const double *u, const double *v) {
-    double t = 0.0;
-    for (int a = 0; a < m; a++) {
-      double w = 0.0;
-      for (int b = 0; b < m; b++) w += g[a * m + b] * v[b];
-      t += u[a] * w;
+  // u^T G v, v distributed over the lanes
+  auto gdot = [&](double u, double v) {
+    double w = 0.0;
+    for (int b = 0; b < m; b++) {
+      const double vb = __shfl_sync(0xffffffffu, v, b);
+      if (on) w = fma(g[c * m + b], vb, w);
     }
+    double t = on ? u * w : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     return t;
   };
   int steps = 0, brk = 0;
   double rr = gdot(r, r);
   for (int j = 0; j < s; j++) {
-    apply_b(p, bp);
+    const double bp = apply_b(p);
     const double pap = gdot(p, bp);
     if (!(pap > 0.0) || !(rr > 0.0)) { brk = 1; break; }
     const double alpha = rr / pap;
-    for (int c = 0; c < m; c++) {
-      x[c] += alpha * p[c];
-      gv[c] = r[c] - alpha * bp[c];
-    }
-    const double rr2 = gdot(gv, gv);
+    x += alpha * p;
+    const double rn = r - alpha * bp;
+    const double rr2 = gdot(rn, rn);
     const double beta = rr2 / rr;
-    for (int c = 0; c < m; c++) {
-      r[c] = gv[c];
-      p[c] = gv[c] + beta * p[c];
-    }
+    r = rn;
+    p = rn + beta * p;
     rr = rr2;
     steps++;
   }
-  for (int c = 0; c < m; c++) { xh[c] = x[c]; ph[c] = p[c]; rh[c] = r[c]; }
-  flag[0] = brk;
-  flag[1] = steps;
+  if (on) { xh[c] = x; ph[c] = p; rh[c] = r; }
+  if (c == 0) { flag[0] = brk; flag[1] = steps; }
 }
 
 // x += Y xh, p = Y ph (FP64 accumulation of the FP32 basis)
