@@ -795,7 +795,10 @@ struct WaveArgs {
   const long *sell_off;        // nslice + 1
   const unsigned short *len;   // entries per row
   const int *scol;             // column of each slot (int32 form) ...
-  const short *srel;           // ... or col - row (int16 form)
+  const short *srel;           // ... or col - row (int16 form), pattern-compressed: a slice whose 32
+                               // rows share one offset list stores it once (runi = 1, padded to 8)
+  const long *rel_off;         // nslice + 1: start of each slice in srel
+  const unsigned char *runi;   // per slice: 1 = shared offset list
   const double *sval;          // value of each slot (valued) ...
   const float2 *sval2;         // ... or its double-float split
   const double *rdeg;          // 1/deg per row (1/deg operator) ...
@@ -805,7 +808,9 @@ struct WaveArgs {
   double *vv;
   float2 *ring;                // 2 * n: double-float copies of levels l-1 and l
   int stage_rel_bytes;         // > 0: the CTA's int16 offsets and lengths are staged in shared memory
-                               // once per call (offsets first, this many bytes, then the lengths)
+                               // once per call (offsets first, this many bytes, then the lengths,
+  int stage_len_bytes;         // this many bytes, then per slice its start (int) and flag (byte),
+  int stage_slices;            // room for this many slices)
   const int *row_lo;           // nblk + 1
   const int *dep_lo, *dep_hi;  // per CTA: CTAs it reads from or that read from it
   unsigned int *flags;         // per CTA: last level published
@@ -842,13 +847,21 @@ __device__ __forceinline__ void wave_publish(const WaveArgs &a, int b, unsigned 
 // level, so this happens once per call.
 __device__ __forceinline__ void wave_stage(const WaveArgs &a, int r0, int r1, unsigned char *smem) {
   if (r0 >= r1) return;
-  const long e_lo = a.sell_off[r0 >> 5], e_hi = a.sell_off[(r1 + 31) >> 5];
+  const long e_lo = a.rel_off[r0 >> 5], e_hi = a.rel_off[(r1 + 31) >> 5];
   const int4 *g = reinterpret_cast<const int4 *>(a.srel + e_lo);
   int4 *d = reinterpret_cast<int4 *>(smem);
-  const long nvec = (e_hi - e_lo) / 8;  // slices hold 32*w entries: a multiple of 8 shorts
+  const long nvec = (e_hi - e_lo) / 8;  // every slice holds a multiple of 8 offsets
   for (long v = threadIdx.x; v < nvec; v += blockDim.x) d[v] = __ldg(g + v);
   unsigned char *sl = smem + a.stage_rel_bytes;  // staged rows are at most 255 long
   for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) sl[i - r0] = (unsigned char)__ldg(a.len + i);
+  // per slice of the range: start in the slab (relative) and the shared-list flag
+  const int s0 = r0 >> 5, ns = ((r1 + 31) >> 5) - s0;
+  int *srs = reinterpret_cast<int *>(smem + a.stage_rel_bytes + a.stage_len_bytes);
+  unsigned char *sus = reinterpret_cast<unsigned char *>(srs + a.stage_slices);
+  for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+    srs[k] = (int)(a.rel_off[s0 + k] - e_lo);
+    sus[k] = a.runi[s0 + k];
+  }
 }
 
 // An int16 offset from the staged slab (shared memory: plain load) or
@@ -865,11 +878,90 @@ __device__ __forceinline__ int wave_col(const WaveArgs &a, long e, int i) {
   return REL ? i + (int)__ldg(a.srel + e) : __ldg(a.scol + e);
 }
 
+// One row's sum over its entries (CSR order): the row's int16 offsets are
+// RS apart (32: per-lane layout, a constant after inlining; 1: a slice's
+// shared list), values and int32 columns 32 apart.  Up to 8 (12 for FP32) entries have all their
+// loads in flight together.
+template <int ARITH, bool VALUED, bool REL, bool STAGE>
+__device__ __forceinline__ double fp_row(int len, int RS, double cf, const short *cr, const int *cc,
+                                         const double *cv, const double *xb, const double *src) {
+  double s = 0.0;
+  int t = 0;
+  if (len <= 8) {
+    double x[8], v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      if (u < len) {
+        x[u] = REL ? xb[ld_off<STAGE>(cr + RS * u)] : src[__ldg(cc + 32 * u)];
+        v[u] = VALUED ? __ldg(cv + 32 * u) : cf;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (u < len) s = row_term<ARITH>(s, v[u], x[u]);
+    t = len;
+  }
+  for (; t < len; t++)
+    s = row_term<ARITH>(s, VALUED ? __ldg(cv + 32L * t) : cf,
+                        REL ? xb[ld_off<STAGE>(cr + RS * t)] : src[__ldg(cc + 32L * t)]);
+  return s;
+}
+
+template <bool VALUED, bool REL, bool STAGE>
+__device__ __forceinline__ void df_row(int len, int RS, const short *cr, const int *cc, const float2 *cv,
+                                       const float2 *xb, const float2 *src, float &sh, float &sl_) {
+  int t = 0;
+  if (len <= 8) {
+    float2 x[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      if (u < len) x[u] = REL ? xb[ld_off<STAGE>(cr + RS * u)] : src[__ldg(cc + 32 * u)];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      if (u < len) {
+        if (VALUED) df_mac(cv[32 * u], x[u], sh, sl_);
+        else df_acc(x[u], sh, sl_);
+      }
+    }
+    t = len;
+  }
+  for (; t < len; t++) {
+    const float2 x = REL ? xb[ld_off<STAGE>(cr + RS * t)] : src[__ldg(cc + 32L * t)];
+    if (VALUED) df_mac(cv[32L * t], x, sh, sl_);
+    else df_acc(x, sh, sl_);
+  }
+}
+
+template <typename VT, bool REL>
+__device__ __forceinline__ float mix_row(int len, int RS, const short *cr, const int *cc, const VT *cv,
+                                         const float *xb, const float *src) {
+  float s = 0.f;
+  int t = 0;
+  if (len <= 12) {
+    float x[12], v[12];
+#pragma unroll
+    for (int u = 0; u < 12; u++) {
+      if (u < len) {
+        x[u] = REL ? xb[__ldg(cr + RS * u)] : src[__ldg(cc + 32 * u)];
+        v[u] = to_f32(cv[32 * u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 12; u++)
+      if (u < len) s = __fmaf_rn(v[u], x[u], s);
+    t = len;
+  }
+  for (; t < len; t++)
+    s = __fmaf_rn(to_f32(cv[32L * t]), REL ? xb[__ldg(cr + RS * t)] : src[__ldg(cc + 32L * t)], s);
+  return s;
+}
+
 // FP64 rows (fma or separate multiply/add, CSR order as the reference).
 // A warp computes one 32-row slice; CTA row ranges start on slices.  The
 // previous level is read from vv: every address of it is fresh in this
 // launch, so L1 holds no stale copy.
-template <int ARITH, bool VALUED, bool REL, bool STAGE>
+template <int ARITH, bool VALUED, bool REL, bool STAGE, bool UNI>
 __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
   extern __shared__ __align__(16) unsigned char wave_smem[];
   __shared__ int s_abort;
@@ -879,7 +971,7 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
   if (STAGE) wave_stage(a, r0, r1, wave_smem);
   __syncthreads();
-  const long e_lo = STAGE && r0 < r1 ? a.sell_off[r0 >> 5] : 0;
+  const long e_lo = STAGE && r0 < r1 ? a.rel_off[r0 >> 5] : 0;
   const short *s_rel = reinterpret_cast<const short *>(wave_smem);
   const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -893,29 +985,16 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
       const int len = STAGE ? s_len[i - r0] : __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
       const double cf = VALUED ? 0.0 : (len < 256 ? s_lut[len] : __ldg(a.rdeg + i));
-      const short *cr = STAGE ? s_rel + (e0 - e_lo) : a.srel + e0;
+      const int *s_srs = reinterpret_cast<const int *>(wave_smem + a.stage_rel_bytes + a.stage_len_bytes);
+      const unsigned char *s_sus = reinterpret_cast<const unsigned char *>(s_srs + a.stage_slices);
+      const int k_sl = sl - (r0 >> 5);
+      const bool uni = UNI && REL && (STAGE ? s_sus[k_sl] != 0 : __ldg(a.runi + sl) != 0);
+      const short *cr = (STAGE ? s_rel + s_srs[k_sl] : a.srel + (REL ? __ldg(a.rel_off + sl) : 0)) + (uni ? 0 : lane);
       const int *cc = a.scol + e0;
       const double *cv = a.sval + e0;
       const double *xb = src + i;
-      double s = 0.0;
-      int t = 0;
-      if (len <= 8) {  // all column loads, then all gathers, in flight together
-        double x[8], v[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-          if (u < len) {
-            x[u] = REL ? xb[ld_off<STAGE>(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
-            v[u] = VALUED ? __ldg(cv + 32 * u) : cf;
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-          if (u < len) s = row_term<ARITH>(s, v[u], x[u]);
-        t = len;
-      }
-      for (; t < len; t++)
-        s = row_term<ARITH>(s, VALUED ? __ldg(cv + 32L * t) : cf,
-                            REL ? xb[ld_off<STAGE>(cr + 32L * t)] : src[__ldg(cc + 32L * t)]);
+      // the stride is the constant 32 unless the plan compresses offsets
+      const double s = fp_row<ARITH, VALUED, REL, STAGE>(len, UNI ? (uni ? 1 : 32) : 32, cf, cr, cc, cv, xb, src);
       __stcs(dst + i, s);
     }
     wave_publish(a, b, a.base + (unsigned)l);
@@ -929,7 +1008,7 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
 // after every CTA that reads its rows has finished the level before, which
 // the symmetric dependency ranges guarantee.  Level 0 splits the CTA's
 // own rows of x.
-template <bool VALUED, bool REL, bool STAGE>
+template <bool VALUED, bool REL, bool STAGE, bool UNI>
 __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
   extern __shared__ __align__(16) unsigned char wave_smem[];
   __shared__ int s_abort;
@@ -939,7 +1018,7 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
   if (STAGE) wave_stage(a, r0, r1, wave_smem);
   __syncthreads();
-  const long e_lo = STAGE && r0 < r1 ? a.sell_off[r0 >> 5] : 0;
+  const long e_lo = STAGE && r0 < r1 ? a.rel_off[r0 >> 5] : 0;
   const short *s_rel = reinterpret_cast<const short *>(wave_smem);
   const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -955,34 +1034,19 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
       if (i >= r1) continue;
       const int len = STAGE ? s_len[i - r0] : __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
-      const short *cr = STAGE ? s_rel + (e0 - e_lo) : a.srel + e0;
+      const int *s_srs = reinterpret_cast<const int *>(wave_smem + a.stage_rel_bytes + a.stage_len_bytes);
+      const unsigned char *s_sus = reinterpret_cast<const unsigned char *>(s_srs + a.stage_slices);
+      const int k_sl = sl - (r0 >> 5);
+      const bool uni = UNI && REL && (STAGE ? s_sus[k_sl] != 0 : __ldg(a.runi + sl) != 0);
+      const short *cr = (STAGE ? s_rel + s_srs[k_sl] : a.srel + (REL ? __ldg(a.rel_off + sl) : 0)) + (uni ? 0 : lane);
+      // per-lane bases: slot t of this row is 32*t elements further (the
+      // offsets of a shared-list slice: t further), an immediate offset
       const int *cc = a.scol + e0;
-      // per-lane bases: slot t of this row is 32*t elements further, an
-      // immediate offset of the load
       const float2 *cv = a.sval2 + e0;
       const float2 *xb = src + i;
       float sh = 0.f, sl_ = 0.f;
-      int t = 0;
-      if (len <= 8) {  // all column loads, then all gathers, in flight together
-        float2 x[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-          if (u < len) x[u] = REL ? xb[ld_off<STAGE>(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
-        }
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-          if (u < len) {
-            if (VALUED) df_mac(cv[32 * u], x[u], sh, sl_);
-            else df_acc(x[u], sh, sl_);
-          }
-        }
-        t = len;
-      }
-      for (; t < len; t++) {
-        const float2 x = REL ? xb[ld_off<STAGE>(cr + 32L * t)] : src[__ldg(cc + 32L * t)];
-        if (VALUED) df_mac(cv[32L * t], x, sh, sl_);
-        else df_acc(x, sh, sl_);
-      }
+      // the stride is the constant 32 unless the plan compresses offsets
+      df_row<VALUED, REL, STAGE>(len, UNI ? (uni ? 1 : 32) : 32, cr, cc, cv, xb, src, sh, sl_);
       float2 v = df_norm(sh, sl_);
       if (!VALUED) v = df_scale(len < 256 ? s_lut[len] : a.rdeg2[i], v);
       sdst[i] = v;
@@ -997,7 +1061,7 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
 // scaled by the exact power of two `scale` (the same arithmetic as
 // mix_pipe_kernel, so both give identical bits).  Levels live at fresh
 // addresses of the FP32 vv.
-template <typename VT, bool REL>
+template <typename VT, bool REL, bool UNI>
 __global__ void __launch_bounds__(256) wave_mix_kernel(WaveArgs a, const VT *__restrict__ sv, float *vf, float scale) {
   __shared__ int s_abort;
   if (threadIdx.x == 0) s_abort = 0;
@@ -1013,28 +1077,14 @@ __global__ void __launch_bounds__(256) wave_mix_kernel(WaveArgs a, const VT *__r
       if (i >= r1) continue;
       const int len = __ldg(a.len + i);
       const long e0 = __ldg(a.sell_off + sl) + lane;
-      const short *cr = a.srel + e0;
+      const bool uni = UNI && REL && __ldg(a.runi + sl);
+      const short *cr = a.srel + (REL ? __ldg(a.rel_off + sl) : 0) + (uni ? 0 : lane);
       const int *cc = a.scol + e0;
       const VT *cv = sv + e0;
       const float *xb = src + i;
-      float s = 0.f;
-      int t = 0;
-      if (len <= 12) {  // all loads in flight together (12 covers 9- and 7-point stencils)
-        float x[12], v[12];
-#pragma unroll
-        for (int u = 0; u < 12; u++) {
-          if (u < len) {
-            x[u] = REL ? xb[__ldg(cr + 32 * u)] : src[__ldg(cc + 32 * u)];
-            v[u] = to_f32(cv[32 * u]);
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 12; u++)
-          if (u < len) s = __fmaf_rn(v[u], x[u], s);
-        t = len;
-      }
-      for (; t < len; t++)
-        s = __fmaf_rn(to_f32(cv[32L * t]), REL ? xb[__ldg(cr + 32L * t)] : src[__ldg(cc + 32L * t)], s);
+      // one loop for both offset layouts (a runtime stride keeps the
+      // registers of a single copy of the 12-wide body)
+      const float s = mix_row<VT, REL>(len, UNI && uni ? 1 : 32, cr, cc, cv, xb, src);
       __stcs(dst + i, s * scale);
     }
     wave_publish(a, b, a.base + (unsigned)l);
@@ -1318,7 +1368,7 @@ struct mpkg_plan {
   WaveArgs wave{};
   int wave_grid = 0;
   bool wave_rel = false;
-  int wave_stage_len_bytes = 0;
+  bool wave_uni = false;  // pattern-compressed offsets (plans with matrix values)
   // batched block-vector form
   BatchArgs batch{};
   int batch_lpr = 0, batch_vw = 0, batch_nmat = 0;
@@ -1548,24 +1598,27 @@ int wave_occupancy(mpkg_plan *p, K kernel, int *grid) {
 }
 
 void *wave_kernel_ptr(const mpkg_plan *p) {
-  const bool rel = p->wave_rel, stage = p->wave.stage_rel_bytes > 0;
-#define MPKG_WK(REL, ST)                                                                                      \
+  const bool rel = p->wave_rel, stage = p->wave.stage_rel_bytes > 0, uni = p->wave_uni;
+#define MPKG_WK(REL, ST, UN)                                                                                  \
   if (p->arith == MPKG_ARITH_DF64)                                                                            \
-    return p->valued ? (void *)wave_df_kernel<true, REL, ST> : (void *)wave_df_kernel<false, REL, ST>;       \
+    return p->valued ? (void *)wave_df_kernel<true, REL, ST, UN> : (void *)wave_df_kernel<false, REL, ST, UN>; \
   if (p->arith == MPKG_ARITH_SEPARATE)                                                                        \
-    return p->valued ? (void *)wave_kernel<MPKG_ARITH_SEPARATE, true, REL, ST>                                \
-                     : (void *)wave_kernel<MPKG_ARITH_SEPARATE, false, REL, ST>;                              \
-  return p->valued ? (void *)wave_kernel<MPKG_ARITH_FMA, true, REL, ST>                                       \
-                   : (void *)wave_kernel<MPKG_ARITH_FMA, false, REL, ST>;
-  if (rel && stage) { MPKG_WK(true, true) }
-  if (rel) { MPKG_WK(true, false) }
-  MPKG_WK(false, false)
+    return p->valued ? (void *)wave_kernel<MPKG_ARITH_SEPARATE, true, REL, ST, UN>                            \
+                     : (void *)wave_kernel<MPKG_ARITH_SEPARATE, false, REL, ST, UN>;                          \
+  return p->valued ? (void *)wave_kernel<MPKG_ARITH_FMA, true, REL, ST, UN>                                   \
+                   : (void *)wave_kernel<MPKG_ARITH_FMA, false, REL, ST, UN>;
+  if (rel && stage && uni) { MPKG_WK(true, true, true) }
+  if (rel && stage) { MPKG_WK(true, true, false) }
+  if (rel && uni) { MPKG_WK(true, false, true) }
+  if (rel) { MPKG_WK(true, false, false) }
+  MPKG_WK(false, false, false)
 #undef MPKG_WK
 }
 
 // Dynamic shared memory of a wave launch (the staged slab).
 size_t wave_dyn_smem(const mpkg_plan *p) {
-  return p->wave.stage_rel_bytes > 0 ? (size_t)p->wave.stage_rel_bytes + p->wave_stage_len_bytes : 0;
+  const WaveArgs &w = p->wave;
+  return w.stage_rel_bytes > 0 ? (size_t)w.stage_rel_bytes + w.stage_len_bytes + 5L * w.stage_slices : 0;
 }
 
 int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st) {
@@ -2229,7 +2282,7 @@ namespace {
 thread_local int g_wave_ctas_per_sm = 0;  // mpkg_plan_wave_ctas: cap on resident CTAs per SM (0: occupancy)
 int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
                    int occ_value_type, mpkg_plan **out);
-const void *mix_wave_kernel_ptr(int value_type, bool rel);
+const void *mix_wave_kernel_ptr(int value_type, bool rel, bool uni);
 }  // namespace
 
 extern "C" {
@@ -2271,10 +2324,13 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
         if (col[q] - i < -32768 || col[q] - i > 32767) { rel = false; break; }
     }
     p->wave_rel = rel;
+    // shared offset lists pay where values dominate the bytes; the pattern
+    // operator keeps the per-lane layout (fewer instructions per entry)
+    p->wave_uni = rel && val != nullptr;
   }
   int grid = 0;
   if (!rc)
-    rc = wave_occupancy(p, occ_value_type >= 0 ? mix_wave_kernel_ptr(occ_value_type, p->wave_rel)
+    rc = wave_occupancy(p, occ_value_type >= 0 ? mix_wave_kernel_ptr(occ_value_type, p->wave_rel, p->wave_uni)
                                                : (const void *)wave_kernel_ptr(p), &grid);
   if (!rc && g_wave_ctas_per_sm > 0) {
     int nsm = 0;
@@ -2298,59 +2354,76 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
       return r;
     };
     std::vector<int> lo = ranges(grid);
+    // sliced ELL copy of the matrix: values (and int32 columns) 32 x width
+    // per slice; int16 offsets pattern-compressed (one list per slice whose
+    // rows share it)
+    std::vector<long> soff(nslice + 1, 0), roff(nslice + 1, 0);
+    std::vector<unsigned char> runi(nslice, 0);
+    std::vector<unsigned short> len(n);
+    for (int sl = 0; sl < nslice; sl++) {
+      const int i0 = sl * 32, i1 = std::min(n, sl * 32 + 32);
+      int w = 0;
+      for (int i = i0; i < i1; i++) w = std::max(w, ptr[i + 1] - ptr[i]);
+      soff[sl + 1] = soff[sl] + 32L * w;
+      bool uni = p->wave_uni && i1 - i0 == 32;
+      for (int i = i0 + 1; i < i1 && uni; i++) {
+        if (ptr[i + 1] - ptr[i] != ptr[i0 + 1] - ptr[i0]) { uni = false; break; }
+        for (int t = 0; t < ptr[i + 1] - ptr[i]; t++)
+          if (col[ptr[i] + t] - i != col[ptr[i0] + t] - i0) { uni = false; break; }
+      }
+      runi[sl] = uni ? 1 : 0;
+      roff[sl + 1] = roff[sl] + (uni ? (w + 7) / 8 * 8 : 32L * w);
+    }
+    std::vector<int> scol(p->wave_rel ? 0 : soff[nslice], 0);
+    std::vector<short> srel(p->wave_rel ? roff[nslice] : 0, 0);
+    std::vector<double> sval(val ? soff[nslice] : 0, 0.0);
+    for (int i = 0; i < n; i++) {
+      len[i] = (unsigned short)(ptr[i + 1] - ptr[i]);
+      const int sl = i / 32;
+      const long e0 = soff[sl] + (i % 32);
+      for (int t = 0; t < len[i]; t++) {
+        if (p->wave_rel) {
+          if (runi[sl]) srel[roff[sl] + t] = (short)(col[ptr[i] + t] - i);
+          else srel[roff[sl] + 32L * t + (i % 32)] = (short)(col[ptr[i] + t] - i);
+        } else {
+          scol[e0 + 32L * t] = col[ptr[i] + t];
+        }
+        if (val) sval[e0 + 32L * t] = val[ptr[i] + t];
+      }
+    }
     // stage each CTA's int16 offsets and uint8 lengths in shared memory when
     // the slabs fit next to the kernel's own shared memory at this occupancy
     int maxlen = 0;
     for (int i = 0; i < n; i++) maxlen = std::max(maxlen, ptr[i + 1] - ptr[i]);
     if (p->wave_rel && occ_value_type < 0 && maxlen <= 255) {
-      std::vector<long> sw(nslice + 1, 0);  // slice offsets in entries
-      for (int sl = 0; sl < nslice; sl++) {
-        int wd = 0;
-        for (int i = sl * 32; i < std::min(n, sl * 32 + 32); i++) wd = std::max(wd, ptr[i + 1] - ptr[i]);
-        sw[sl + 1] = sw[sl] + 32L * wd;
-      }
       long relb = 0, lenb = 0;
       for (int b = 0; b < grid; b++) {
         if (lo[b] >= lo[b + 1]) continue;
-        relb = std::max(relb, 2 * (sw[(lo[b + 1] + 31) / 32] - sw[lo[b] / 32]));
+        relb = std::max(relb, 2 * (roff[(lo[b + 1] + 31) / 32] - roff[lo[b] / 32]));
         lenb = std::max<long>(lenb, lo[b + 1] - lo[b]);
       }
       relb = (relb + 15) / 16 * 16;
       lenb = (lenb + 15) / 16 * 16;
+      long nsl = 0;
+      for (int b = 0; b < grid; b++)
+        if (lo[b] < lo[b + 1]) nsl = std::max<long>(nsl, (lo[b + 1] + 31) / 32 - lo[b] / 32);
+      nsl = (nsl + 15) / 16 * 16;
       int nsm = 0, per_sm = 0;
       CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
       p->wave.stage_rel_bytes = (int)relb;
-      p->wave_stage_len_bytes = (int)lenb;
+      p->wave.stage_len_bytes = (int)lenb;
+      p->wave.stage_slices = (int)nsl;
+      const size_t dyn = wave_dyn_smem(p);
       const void *k = wave_kernel_ptr(p);
-      bool ok = relb + lenb <= 200 * 1024 &&
-                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(relb + lenb)) ==
-                    cudaSuccess &&
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, (size_t)(relb + lenb)) == cudaSuccess &&
+      bool ok = dyn <= 200 * 1024 &&
+                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) == cudaSuccess &&
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, dyn) == cudaSuccess &&
                 (long)per_sm * nsm >= grid;
       if (!ok) {
         cudaGetLastError();
         p->wave.stage_rel_bytes = 0;
-        p->wave_stage_len_bytes = 0;
-      }
-    }
-    // sliced ELL copy of the matrix
-    std::vector<long> soff(nslice + 1, 0);
-    std::vector<unsigned short> len(n);
-    for (int sl = 0; sl < nslice; sl++) {
-      int w = 0;
-      for (int i = sl * 32; i < std::min(n, sl * 32 + 32); i++) w = std::max(w, ptr[i + 1] - ptr[i]);
-      soff[sl + 1] = soff[sl] + 32L * w;
-    }
-    std::vector<int> scol(p->wave_rel ? 0 : soff[nslice], 0);
-    std::vector<short> srel(p->wave_rel ? soff[nslice] : 0, 0);
-    std::vector<double> sval(val ? soff[nslice] : 0, 0.0);
-    for (int i = 0; i < n; i++) {
-      len[i] = (unsigned short)(ptr[i + 1] - ptr[i]);
-      const long e0 = soff[i / 32] + (i % 32);
-      for (int t = 0; t < len[i]; t++) {
-        if (p->wave_rel) srel[e0 + 32L * t] = (short)(col[ptr[i] + t] - i);
-        else scol[e0 + 32L * t] = col[ptr[i] + t];
-        if (val) sval[e0 + 32L * t] = val[ptr[i] + t];
+        p->wave.stage_len_bytes = 0;
+        p->wave.stage_slices = 0;
       }
     }
     // CTA owning column c: the last b' with lo[b'] <= c (empty ranges skipped)
@@ -2388,6 +2461,8 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
     if (!rc) rc = dev_copy(p, (unsigned short **)&w.len, len.data(), len.size());
     if (!rc && !scol.empty()) rc = dev_copy(p, (int **)&w.scol, scol.data(), scol.size());
     if (!rc && !srel.empty()) rc = dev_copy(p, (short **)&w.srel, srel.data(), srel.size());
+    if (!rc && p->wave_rel) rc = dev_copy(p, (long **)&w.rel_off, roff.data(), roff.size());
+    if (!rc && p->wave_rel) rc = dev_copy(p, (unsigned char **)&w.runi, runi.data(), runi.size());
     if (!rc && val) rc = dev_copy(p, (double **)&w.sval, sval.data(), sval.size());
     if (!rc) rc = dev_copy(p, (double **)&w.lut, lut.data(), lut.size());
     if (!rc && arith == MPKG_ARITH_DF64) {
@@ -2709,10 +2784,14 @@ int mpkg_pdmpk_prep(int n, const int *ptr, const int *col, const double *val, in
 
 namespace {
 
-const void *mix_wave_kernel_ptr(int value_type, bool rel) {
-  if (value_type == MPKG_VALUE_F32)
-    return rel ? (const void *)wave_mix_kernel<float, true> : (const void *)wave_mix_kernel<float, false>;
-  return rel ? (const void *)wave_mix_kernel<__nv_bfloat16, true> : (const void *)wave_mix_kernel<__nv_bfloat16, false>;
+const void *mix_wave_kernel_ptr(int value_type, bool rel, bool uni) {
+  if (value_type == MPKG_VALUE_F32) {
+    if (rel && uni) return (const void *)wave_mix_kernel<float, true, true>;
+    return rel ? (const void *)wave_mix_kernel<float, true, false> : (const void *)wave_mix_kernel<float, false, false>;
+  }
+  if (rel && uni) return (const void *)wave_mix_kernel<__nv_bfloat16, true, true>;
+  return rel ? (const void *)wave_mix_kernel<__nv_bfloat16, true, false>
+             : (const void *)wave_mix_kernel<__nv_bfloat16, false, false>;
 }
 
 int mixed_wave_setup(mpkg_plan *p, int n, const int *ptr, const int *col, const double *val, int nlevel,
@@ -2722,7 +2801,7 @@ int mixed_wave_setup(mpkg_plan *p, int n, const int *ptr, const int *col, const 
   if (rc) return rc;
   p->inner = w;
   int per_sm = 0, nsm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_wave_kernel_ptr(value_type, w->wave_rel), 256, 0));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_wave_kernel_ptr(value_type, w->wave_rel, w->wave_uni), 256, 0));
   CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
   if ((long)per_sm * nsm < w->wave_grid) return fail(kERange, "mixed wavefront kernel cannot cover the grid");
   const int nslice = (n + 31) / 32;
@@ -2915,12 +2994,12 @@ int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream) {
     if (p->mix_vt == MPKG_VALUE_F32) {
       const float *sv = static_cast<const float *>(p->mix_sval);
       void *args[] = {&a, (void *)&sv, (void *)&d_vv, &scale};
-      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_F32, p->inner->wave_rel), dim3(w.nblk),
+      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_F32, p->inner->wave_rel, p->inner->wave_uni), dim3(w.nblk),
                                            dim3(256), args, 0, st));
     } else {
       const __nv_bfloat16 *sv = static_cast<const __nv_bfloat16 *>(p->mix_sval);
       void *args[] = {&a, (void *)&sv, (void *)&d_vv, &scale};
-      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_BF16, p->inner->wave_rel), dim3(w.nblk),
+      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_BF16, p->inner->wave_rel, p->inner->wave_uni), dim3(w.nblk),
                                            dim3(256), args, 0, st));
     }
     p->launches = 1;
@@ -2960,6 +3039,10 @@ int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info) {
                    : p->exec == MPKG_EXEC_BUFS ? 2 + 2 * p->nphase + 1
                    : p->exec == MPKG_EXEC_PDMPK ? 2 + 2 * p->nphase : 1;
   if (p->exec == MPKG_EXEC_WAVE) info->pipe_grid = p->wave_grid;
+  if (p->exec == MPKG_EXEC_MIXED && p->inner) {  // the wavefront schedule (pipe_chunk 0)
+    info->pipe_chunk = 0;
+    info->pipe_grid = p->inner->wave_grid;
+  }
   info->tiles_in_smem = p->tiles_smem ? 1 : 0;
   info->max_tile_slots = p->max_tile_slots;
   info->pipe_chunk = p->pipe.chunk;

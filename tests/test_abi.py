@@ -76,7 +76,10 @@ def test_plan_argument_errors():
     assert e.value.code == M.ERANGE
 
 
-@pytest.mark.skipif(not O.ref_available() or not os.path.isdir("/root/reference/mpk2"),
+REF_SRC = os.path.join(ROOT, "oracle", "_ref", "src")  # the reference sources staged by oracle/Makefile
+
+
+@pytest.mark.skipif(not O.ref_available() or not os.path.exists(os.path.join(REF_SRC, "comp.c")),
                     reason="reference sources not present")
 @pytest.mark.parametrize("tool", ["comp", "skirt"])
 def test_reference_tools_relink_against_library(tool):
@@ -90,7 +93,7 @@ def test_reference_tools_relink_against_library(tool):
         open(shim, "w").write('#include "mpk2_compat.h"\n')
         exe = os.path.join(d, tool)
         subprocess.run(["gcc", "-O2", "-w", "-I", d, "-I", os.path.join(ROOT, "include"),
-                        f"/root/reference/mpk2/{tool}.c", "-o", exe, M.LIB_PATH,
+                        os.path.join(REF_SRC, f"{tool}.c"), "-o", exe, M.LIB_PATH,
                         "-Wl,-rpath," + os.path.dirname(M.LIB_PATH)], check=True)
         g = os.path.join(d, "g0")
         a.write_metis(g, ne=(a.nnz + a.n) // 2)
@@ -106,7 +109,7 @@ def test_reference_tools_relink_against_library(tool):
             assert open(os.path.join(d, "mine"), "rb").read() == open(os.path.join(d, "ref"), "rb").read()
 
 
-@pytest.mark.skipif(not O.ref_available() or not os.path.isdir("/root/reference/mpk2"),
+@pytest.mark.skipif(not O.ref_available() or not os.path.exists(os.path.join(REF_SRC, "mpi2_mpkwrtbufs.c")),
                     reason="reference sources not present")
 def test_reference_mpi2_prep_relinks_against_library(monkeypatch):
     """The reference's own mpi2_mpkwrtbufs.c main, compiled against
@@ -122,7 +125,7 @@ def test_reference_mpi2_prep_relinks_against_library(monkeypatch):
             open(os.path.join(d, hdr), "w").write('#include "mpk2_compat.h"\n')
         exe = os.path.join(d, "wrtbufs")
         subprocess.run(["gcc", "-O2", "-w", "-I", d, "-I", os.path.join(ROOT, "include"), "-I",
-                        os.path.join(ROOT, "oracle", "refshim"), "/root/reference/mpk2/mpi2_mpkwrtbufs.c", "-o", exe,
+                        os.path.join(ROOT, "oracle", "refshim"), os.path.join(REF_SRC, "mpi2_mpkwrtbufs.c"), "-o", exe,
                         M.LIB_PATH, "-Wl,-rpath," + os.path.dirname(M.LIB_PATH)], check=True)
         from test_prep import _case_dir
         _case_dir(name, g, a, d)

@@ -56,3 +56,14 @@ def test_mixed_scaling_keeps_basis_bounded(gpu):
     v, e, _ = run_mixed(a, 12, M.VALUE_F32, x)
     raw = v / (2.0 ** (e * np.arange(13)))[:, None]
     assert np.all(np.abs(raw) <= 1.0 + 1e-6)
+
+
+def test_mixed_runs_on_wavefront_schedule(gpu):
+    """The mixed form runs on the wavefront schedule when its kernel fits
+    the wavefront grid (plan info reports pipe_chunk 0)."""
+    for a in (M.Csr.laplacian(64, 64, 16, diag=6.0, off=-1.0),
+              M.Csr.diffusion(256, 256, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=3)):
+        for vt in (M.VALUE_F32, M.VALUE_BF16):
+            plan = M.Plan.mixed(a, 6, vt)
+            assert plan.info()["pipe_chunk"] == 0
+            plan.close()
