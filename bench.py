@@ -377,7 +377,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--exec", default="wave", choices=["pipe", "wave", "tiles", "spmv", "tasks"])
-    ap.add_argument("--arith", default="df64", choices=["fma", "separate", "df64"])
+    ap.add_argument("--arith", default="df64", choices=["fma", "separate", "df64", "fixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="time only the selected executor")
     ap.add_argument("--sections", default="variants,mixed,batched,sstep",
@@ -419,7 +419,8 @@ def main():
     import torch
     import mpk_gb300 as M
     torch.cuda.set_device(local)
-    arith = {"fma": M.ARITH_FMA, "separate": M.ARITH_SEPARATE, "df64": M.ARITH_DF64}[args.arith]
+    ARITHS = {"fma": M.ARITH_FMA, "separate": M.ARITH_SEPARATE, "df64": M.ARITH_DF64, "fixed": M.ARITH_FIXED}
+    arith = ARITHS[args.arith]
     g = a.pattern()  # the 1/deg operator of the reference's exec_mpk
 
     def mk(ex, ar, mat=None):
@@ -466,14 +467,15 @@ def main():
     # the other executors on the same workload, for the record
     variants = {}
     if "variants" in sections:
-        runs = [(ex, ar, None) for ex, ar in (("spmv", "fma"), ("wave", "fma"), ("wave", "df64"), ("pipe", "fma"),
+        runs = [(ex, ar, None) for ex, ar in (("spmv", "fma"), ("wave", "fma"), ("wave", "df64"), ("wave", "fixed"),
+                                              ("pipe", "fma"),
                                               ("pipe", "df64"), ("tiles", "fma"), ("tiles", "df64"))]
         runs += [("spmv", "fma", "valued"), ("wave", "fma", "valued"), ("wave", "df64", "valued")]
         ref_val = None
         for ex, ar, op in runs:
             if ex == args.exec and ar == args.arith and op is None:
                 continue
-            vp = mk(ex, {"fma": M.ARITH_FMA, "df64": M.ARITH_DF64}[ar], a if op else None)
+            vp = mk(ex, ARITHS[ar], a if op else None)
             d2 = torch.zeros_like(d_vv)
             d2[:n] = d_vv[:n]
             t = statistics.mean(time_device(vp, d2, min(args.steps, 50), args.warmup, flush, stream))
@@ -519,6 +521,8 @@ def main():
              "spmv": "spmv_level_kernel"}[args.exec]
     if args.arith == "df64":
         kname = {"pipe": "flow_df_kernel", "wave": "wave_df_kernel", "tiles": "tiles_df_kernel"}.get(args.exec, kname)
+    if args.arith == "fixed":
+        kname = "wave_fix_kernel"
     traffic = profile_traffic(kname)
     rows = info["rows_computed"]
     fp64_tflops = 2.0 * nnz * k * (rows / (n * k)) / (ms * 1e-3) / 1e12
@@ -527,7 +531,7 @@ def main():
     line = {"metric": "MPK powers/sec (FP64, k*n output rows per second)", "value": value,
             "unit": "Grow-powers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"df64": "df64", "fma": "f64", "separate": "f64"}[args.arith], "data": "synthetic",
+            "dtype": {"df64": "df64", "fma": "f64", "separate": "f64", "fixed": "i64"}[args.arith], "data": "synthetic",
             "rel_err_max_vs_fp64": headline_err, "tolerance": 1e-13,
             "config": dict(cfg, executor=args.exec, arith=args.arith,
                            l2="flushed before every call (256 MiB write); per-call CUDA events",

@@ -52,6 +52,11 @@ extern "C" {
 #define MPKG_ARITH_DF64 2     /* double-float (FP32 pair) arithmetic on the
                                  FP32 pipes, FP64 storage; about 2^-46
                                  relative error per operation */
+#define MPKG_ARITH_FIXED 3    /* 64-bit fixed point (1/deg operator, wavefront
+                                 executor only): exact integer row sums at one
+                                 scale 2^S per call, S = 62 - ceil(log2(longest
+                                 row)) - e with max|x| < 2^e; error about 2^-S
+                                 relative to max|x| per level; FP64 storage */
 
 /* Executors. */
 #define MPKG_EXEC_TASKS 0 /* reference task lists, one CTA per (phase,part) */

@@ -19,7 +19,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libmpk_gb300.so")
 
 OK, EINVAL, EIO, EFORMAT, ESTRUCT, ECUDA, ETIMEOUT, ENOMEM, ERANGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
-ARITH_FMA, ARITH_SEPARATE, ARITH_DF64 = 0, 1, 2
+ARITH_FMA, ARITH_SEPARATE, ARITH_DF64, ARITH_FIXED = 0, 1, 2, 3
 EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS, EXEC_MIXED, EXEC_PDMPK, EXEC_WAVE, EXEC_BATCH = \
     0, 1, 2, 3, 4, 5, 6, 7, 8
 PD_PART_BLOCKSHIFT, PD_PART_BFS = 0, 1

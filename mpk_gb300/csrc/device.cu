@@ -815,6 +815,10 @@ struct WaveArgs {
   const int *dep_lo, *dep_hi;  // per CTA: CTAs it reads from or that read from it
   unsigned int *flags;         // per CTA: last level published
   int *err;
+  // fixed-point form (1/deg operator): the ring holds int64 values v * 2^S
+  const unsigned long long *fix_mul;  // 256: ceil(2^64 / d), d >= 2
+  unsigned long long *fix_word;       // per call: (base << 32) | largest biased exponent of |x|
+  int fix_dbits;                      // ceil(log2(longest row))
 };
 
 __device__ __forceinline__ bool wave_wait(const WaveArgs &a, int b, unsigned int want, int *s_abort) {
@@ -1053,6 +1057,140 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
       __stcs(dst + i, df_to_double(v));
     }
     wave_publish(a, b, a.base + (unsigned)l);
+  }
+}
+
+// 64-bit fixed-point rows for the 1/deg operator.  The operator averages
+// (|A^l x| <= max|x| entrywise), so one scale 2^S fixed per call keeps every
+// level exact to 2^-S: S = 62 - ceil(log2(longest row)) - e, max|x| < 2^e,
+// which leaves room for the row sums.  A row is then an exact int64 sum of
+// its neighbours, one division by its length (reciprocal multiply, within
+// one unit) and one conversion to FP64.  The error against FP64 is about
+// 2^-S relative to max|x| per level.  Phase A agrees on e across the grid
+// (all CTAs are resident), phase B converts x, then levels 1..k follow
+// the wavefront rule.  Tags of a call: base (e published), base + 1 (x
+// converted), base + 1 + l (level l).
+__device__ __forceinline__ long long fix_div(long long s, int d, unsigned long long m) {
+  if (d <= 1) return s;
+  const unsigned long long t = (unsigned long long)(s < 0 ? -s : s) + (unsigned long long)(d >> 1);
+  const long long q = (long long)__umul64hi(t, m);
+  return s < 0 ? -q : q;
+}
+
+// q * 2^-S rounded to nearest-even in integer arithmetic (the FP64 pipe's
+// conversions are scarce on this part).  |q| < 2^63 and q * 2^-S stays a
+// normal double for every S the kernel uses (S <= 1022, |q| >= 1).
+__device__ __forceinline__ double fix_to_double(long long q, int S) {
+  if (q == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)q & 0x8000000000000000ull;
+  const unsigned long long m = q < 0 ? 0ull - (unsigned long long)q : (unsigned long long)q;
+  const int lz = __clzll((long long)m);
+  const unsigned long long t = m << lz;  // leading one at bit 63
+  unsigned long long mant = t >> 11;     // 53 bits, implicit one at bit 52
+  const unsigned int rem = (unsigned int)(t & 0x7FFu);
+  mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+  // the implicit one adds 1 to the exponent field (a carry to 2^53 adds one more)
+  return __longlong_as_double((long long)(sgn | (((unsigned long long)(1022 + 63 - lz - S) << 52) + mant)));
+}
+
+// x * 2^S rounded to the nearest integer, ties to even, in integer
+// arithmetic.  |x| * 2^S < 2^62 for every x of the call (S is chosen so).
+__device__ __forceinline__ long long double_to_fix(double x, int S) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (e ? 0x10000000000000ull : 0ull);
+  const int sh = (e ? e - 1075 : -1074) + S;  // x * 2^S = m * 2^sh
+  unsigned long long q;
+  if (sh >= 0) {
+    q = m << sh;
+  } else if (sh < -54) {
+    q = 0;  // below 1/2
+  } else {
+    const int r = -sh;
+    q = m >> r;
+    const unsigned long long rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+    q += (rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull;
+  }
+  return (long long)(b >> 63 ? 0ull - q : q);
+}
+
+template <bool STAGE>
+__global__ void __launch_bounds__(256, 5) wave_fix_kernel(WaveArgs a) {
+  extern __shared__ __align__(16) unsigned char wave_smem[];
+  __shared__ int s_abort, s_emax;
+  __shared__ unsigned long long s_mul[256];
+  if (threadIdx.x == 0) { s_abort = 0; s_emax = 0; }
+  s_mul[threadIdx.x] = a.fix_mul[threadIdx.x];
+  const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
+  if (STAGE) wave_stage(a, r0, r1, wave_smem);
+  __syncthreads();
+  const long e_lo = STAGE && r0 < r1 ? a.rel_off[r0 >> 5] : 0;
+  const short *s_rel = reinterpret_cast<const short *>(wave_smem);
+  const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long *ring = reinterpret_cast<long long *>(a.ring);
+  // phase A: the largest exponent of |x| over the grid
+  int e = 0;
+  for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x)
+    e = max(e, (int)(((unsigned long long)__double_as_longlong(a.vv[i]) >> 52) & 0x7FF));
+  e = (int)__reduce_max_sync(0xFFFFFFFFu, (unsigned)e);
+  if ((threadIdx.x & 31) == 0) atomicMax(&s_emax, e);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicMax(a.fix_word, ((unsigned long long)a.base << 32) | (unsigned)s_emax);
+  wave_publish(a, b, a.base);
+  for (int c = (int)threadIdx.x; c < a.nblk; c += blockDim.x) {  // every CTA has contributed
+    long spins = 0;
+    while (ld_acquire(a.flags + c) < a.base + a.stall) {
+      if (++spins > kSpinLimit || *((volatile int *)a.err)) {
+        atomicCAS(a.err, 0, kErrTimeout);
+        s_abort = 1;
+        break;
+      }
+      __nanosleep(spins < 16 ? 32 : 256);
+    }
+  }
+  __syncthreads();
+  if (s_abort) return;
+  // one read of the grid maximum per CTA (the acquire loads above order it
+  // after every CTA's atomicMax), broadcast through shared memory
+  if (threadIdx.x == 0) s_emax = (int)(atomicOr(a.fix_word, 0ull) & 0xFFFFFFFFull);
+  __syncthreads();
+  const int emax = s_emax - 1022;  // max|x| < 2^emax
+  const int S = min(62 - a.fix_dbits - emax, 1022);
+  // phase B: x in fixed point
+  for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) ring[i] = double_to_fix(a.vv[i], S);
+  wave_publish(a, b, a.base + 1);
+  for (int l = 1; l <= a.nlevel; l++) {
+    if (!wave_wait(a, b, a.base + (unsigned)l, &s_abort)) return;
+    const long long *src = ring + (size_t)((l - 1) & 1) * a.n;
+    long long *sdst = ring + (size_t)(l & 1) * a.n;
+    double *dst = a.vv + (size_t)l * a.n;
+    for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
+      const int i = (sl << 5) + lane;
+      if (i >= r1) continue;
+      const int len = STAGE ? s_len[i - r0] : __ldg(a.len + i);
+      const int *s_srs = reinterpret_cast<const int *>(wave_smem + a.stage_rel_bytes + a.stage_len_bytes);
+      const int k_sl = sl - (r0 >> 5);
+      const short *cr = (STAGE ? s_rel + s_srs[k_sl] : a.srel + __ldg(a.rel_off + sl)) + lane;
+      const long long *xb = src + i;
+      long long sum = 0;
+      int t = 0;
+      if (len <= 8) {
+        long long x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+          if (u < len) x[u] = xb[ld_off<STAGE>(cr + 32 * u)];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+          if (u < len) sum += x[u];
+        t = len;
+      }
+      for (; t < len; t++) sum += xb[ld_off<STAGE>(cr + 32L * t)];
+      const long long q = fix_div(sum, len, s_mul[len & 255]);
+      sdst[i] = q;
+      __stcs(dst + i, fix_to_double(q, S));
+    }
+    wave_publish(a, b, a.base + 1 + (unsigned)l);
   }
 }
 
@@ -1416,6 +1554,7 @@ int dev_alloc(mpkg_plan *p, T **dst, size_t count) {
 int check_csr(int n, const int *ptr, const int *col) {
   if (n <= 0 || !ptr || !col) return fail(kEInval, "empty matrix or null arrays");
   if (ptr[0] != 0) return fail(kEInval, "ptr[0] must be 0");
+  if (ptr[n] <= 0) return fail(kEInval, "the matrix has no entries");
   for (int i = 0; i < n; i++)
     if (ptr[i + 1] < ptr[i]) return fail(kEInval, "ptr must be non-decreasing");
   for (long j = 0; j < ptr[n]; j++)
@@ -1424,11 +1563,14 @@ int check_csr(int n, const int *ptr, const int *col) {
 }
 
 int plan_common(mpkg_plan *p, int n, const int *ptr, const int *col, const double *val,
-                int nlevel, int arith) {
+                int nlevel, int arith, bool allow_fixed = false) {
   int rc = check_csr(n, ptr, col);
   if (rc) return rc;
   if (nlevel <= 0 || nlevel > 31) return fail(kEInval, "nlevel must be in [1, 31]");
-  if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE && arith != MPKG_ARITH_DF64)
+  if (arith == MPKG_ARITH_FIXED && !(allow_fixed && val == nullptr))
+    return fail(kEInval, "fixed-point arithmetic runs the 1/deg operator on the wavefront executor only");
+  if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE && arith != MPKG_ARITH_DF64 &&
+      arith != MPKG_ARITH_FIXED)
     return fail(kEInval, "unknown arith mode");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
@@ -1445,7 +1587,10 @@ int plan_common(mpkg_plan *p, int n, const int *ptr, const int *col, const doubl
     if ((rc = dev_copy(p, &p->d_coef, val, (size_t)p->nnz))) return rc;
   } else {
     std::vector<double> rdeg(n);
-    for (int i = 0; i < n; i++) rdeg[i] = 1.0 / (ptr[i + 1] - ptr[i]);  // as mpk2/mpkexec.c:28
+    // as mpk2/mpkexec.c:28; an empty row sums no terms (0 in the reference),
+    // so its unused coefficient is 0 rather than 1/0 (a row-sum-then-scale
+    // kernel would otherwise form 0 * inf)
+    for (int i = 0; i < n; i++) rdeg[i] = ptr[i + 1] > ptr[i] ? 1.0 / (ptr[i + 1] - ptr[i]) : 0.0;
     if ((rc = dev_copy(p, &p->d_coef, rdeg.data(), (size_t)n))) return rc;
   }
   if (arith == MPKG_ARITH_DF64) {
@@ -1599,6 +1744,7 @@ int wave_occupancy(mpkg_plan *p, K kernel, int *grid) {
 
 void *wave_kernel_ptr(const mpkg_plan *p) {
   const bool rel = p->wave_rel, stage = p->wave.stage_rel_bytes > 0, uni = p->wave_uni;
+  if (p->arith == MPKG_ARITH_FIXED) return stage ? (void *)wave_fix_kernel<true> : (void *)wave_fix_kernel<false>;
 #define MPKG_WK(REL, ST, UN)                                                                                  \
   if (p->arith == MPKG_ARITH_DF64)                                                                            \
     return p->valued ? (void *)wave_df_kernel<true, REL, ST, UN> : (void *)wave_df_kernel<false, REL, ST, UN>; \
@@ -1623,9 +1769,10 @@ size_t wave_dyn_smem(const mpkg_plan *p) {
 
 int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st) {
   WaveArgs &w = p->wave;
-  const unsigned step = (unsigned)p->nlevel + 1;
+  const unsigned step = (unsigned)p->nlevel + (p->arith == MPKG_ARITH_FIXED ? 2 : 1);
   if (w.base == 0 || w.base > (1u << 30)) {  // first call, or the flags would wrap: start over
     CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(unsigned int) * (size_t)w.nblk, st));
+    if (w.fix_word) CUDA_TRY(cudaMemsetAsync(w.fix_word, 0, sizeof(unsigned long long), st));
     w.base = 1;
   } else {
     w.base += step;
@@ -2315,7 +2462,15 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
   mpkg_plan *p = new_plan();
   if (!p) return fail(kENoMem, "plan allocation failed");
   p->exec = MPKG_EXEC_WAVE;
-  int rc = plan_common(p, n, ptr, col, val, nlevel, arith);
+  int rc = plan_common(p, n, ptr, col, val, nlevel, arith, true);
+  if (!rc && arith == MPKG_ARITH_FIXED) {
+    int maxlen = 0;
+    for (int i = 0; i < n; i++) maxlen = std::max(maxlen, ptr[i + 1] - ptr[i]);
+    if (maxlen > 255) rc = fail(kERange, "fixed-point form: rows are limited to 255 entries");
+    int dbits = 0;
+    while ((1 << dbits) < maxlen) dbits++;
+    p->wave.fix_dbits = dbits;
+  }
   if (!rc) {
     bool rel = true;
     for (int i = 0; i < n && rel; i++) {
@@ -2324,6 +2479,8 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
         if (col[q] - i < -32768 || col[q] - i > 32767) { rel = false; break; }
     }
     p->wave_rel = rel;
+    if (!rc && arith == MPKG_ARITH_FIXED && !rel)
+      rc = fail(kERange, "fixed-point form: every |column - row| must be below 32768");
     // shared offset lists pay where values dominate the bytes; the pattern
     // operator keeps the per-lane layout (fewer instructions per entry)
     p->wave_uni = rel && val != nullptr;
@@ -2485,12 +2642,20 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
       }
       w.sval2 = sv2;
     }
-    const bool df = arith == MPKG_ARITH_DF64;
+    const bool df = arith == MPKG_ARITH_DF64 || arith == MPKG_ARITH_FIXED;  // ring of two slots
     if (!rc) rc = dev_copy(p, &d_lo, lo.data(), lo.size());
     if (!rc) rc = dev_copy(p, &d_dlo, (df ? slo : dlo).data(), dlo.size());
     if (!rc) rc = dev_copy(p, &d_dhi, (df ? shi : dhi).data(), dhi.size());
     if (!rc) rc = dev_alloc(p, &w.flags, (size_t)grid);
     if (!rc && df) rc = dev_alloc(p, &w.ring, (size_t)2 * n);
+    if (!rc && arith == MPKG_ARITH_FIXED) {
+      std::vector<unsigned long long> mul(256, 0);
+      for (int d = 2; d < 256; d++) mul[d] = ~0ull / (unsigned long long)d + 1;  // ceil(2^64 / d)
+      rc = dev_copy(p, (unsigned long long **)&w.fix_mul, mul.data(), mul.size());
+      if (!rc) rc = dev_alloc(p, &w.fix_word, 1);
+      if (!rc && cudaMemset(w.fix_word, 0, sizeof(unsigned long long)) != cudaSuccess)
+        rc = fail(kECuda, "memset failed");
+    }
     w.row_lo = d_lo; w.dep_lo = d_dlo; w.dep_hi = d_dhi;
     long reach = 0;
     for (int b = 0; b < grid; b++)

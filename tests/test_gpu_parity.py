@@ -221,3 +221,47 @@ def test_rank_buffers_on_gpu_bitwise(name, gpu):
         vv = _run(plan, g["x"], n, nlevel)
         want = O.bufs_exec([os.path.join(d, f"rank{r}.bufs") for r in range(P)], g["x"], nlevel, O.MODE_FMA)
         assert vv.tobytes() == want.tobytes()
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_fixed_point_wave_within_fp64_tolerance(name, gpu):
+    """64-bit fixed-point rows (1/deg operator) stay within the FP64
+    tolerance of the reference's exec_mpk_xd results."""
+    g = load_golden(name)
+    a = golden_matrix(name).pattern()
+    n, nlevel = int(g["n"]), int(g["nlevel"])
+    want = O.mpk(a.ptr, a.col, None, g["x"], nlevel, O.MODE_FMA)
+    vv = _run(M.Plan.wave(a, nlevel, arith=M.ARITH_FIXED), g["x"], n, nlevel)
+    assert vv[:n].tobytes() == g["x"].tobytes()
+    errs = _rel_errors(vv, want, n, nlevel)
+    assert max(errs) <= TOL, errs
+
+
+def test_fixed_point_full_size_and_known_answers(config2, gpu):
+    a, part, x, _ = config2
+    g = a.pattern()
+    want = O.mpk(g.ptr, g.col, None, x, 8, O.MODE_FMA)
+    plan = M.Plan.wave(g, 8, arith=M.ARITH_FIXED)
+    errs = _rel_errors(_run(plan, x, a.n, 8), want, a.n, 8)
+    assert max(errs) <= TOL, errs
+    ones = _run(plan, np.ones(a.n), a.n, 8)  # the 1/deg operator's fixed point, exactly
+    assert np.all(ones == 1.0)
+    big = _run(plan, 1e6 * x, a.n, 8)  # the scale follows max|x|
+    assert max(_rel_errors(big, 1e6 * want, a.n, 8)) <= TOL
+    with pytest.raises(M.MpkError):  # the valued operator has no fixed-point form
+        M.Plan.wave(a, 8, arith=M.ARITH_FIXED)
+
+
+def test_fixed_point_wait_times_out_and_recovers(gpu):
+    a = M.Csr.laplacian(64, 64, 4).pattern()
+    x = M.uniform(5, a.n)
+    plan = M.Plan.wave(a, 4, arith=M.ARITH_FIXED)
+    plan.debug_stall(100)
+    vv = np.zeros(5 * a.n)
+    vv[:a.n] = x
+    with pytest.raises(M.MpkError) as e:
+        plan.exec_host(vv)
+    assert e.value.code == M.ETIMEOUT
+    plan.debug_stall(0)
+    want = O.mpk(a.ptr, a.col, None, x, 4, O.MODE_FMA)
+    assert max(_rel_errors(_run(plan, x, a.n, 4), want, a.n, 4)) <= TOL
