@@ -290,7 +290,10 @@ int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info);
 
 /* Execute with host memory: vv holds (nlevel+1)*n doubles, x in vv[0..n);
  * levels 1..nlevel are written back.  The host->device copy of x and the
- * device->host copy of the levels are part of the call. */
+ * device->host copy of the levels are part of the call.  When vv is
+ * page-locked (cudaHostAlloc / cudaHostRegister) and the plan is a
+ * wavefront plan in double-float or fixed point, the kernel reads x and
+ * writes the levels through the host mapping while it computes. */
 int mpkg_exec_host(mpkg_plan *p, double *vv);
 
 /* Execute on device memory: d_vv as above, on `stream` (a cudaStream_t,

@@ -3248,6 +3248,20 @@ int mpkg_exec_host(mpkg_plan *p, double *vv) {
   clear_error();
   if (!p || !vv) return fail(kEInval, "null plan or vv");
   const long total = (long)p->n * (p->nlevel + 1);
+  // Page-locked vv on a wavefront plan whose levels travel in the device
+  // ring (double-float, fixed point): the kernel reads x and writes every
+  // level straight through the host mapping, so the host<->device traffic
+  // overlaps the computation instead of following it.  The FP64 forms
+  // read their levels back and keep the copies below.
+  if (p->exec == MPKG_EXEC_WAVE && (p->arith == MPKG_ARITH_DF64 || p->arith == MPKG_ARITH_FIXED)) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, vv) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+      int rc = plan_launch(p, static_cast<double *>(at.devicePointer), p->stream);
+      if (rc) return rc;
+      return mpkg_sync(p, p->stream);
+    }
+    cudaGetLastError();  // pageable memory: the copies below
+  }
   if (!p->d_vv) {
     CUDA_TRY(cudaMalloc(&p->d_vv, sizeof(double) * total));
   }

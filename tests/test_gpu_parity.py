@@ -265,3 +265,28 @@ def test_fixed_point_wait_times_out_and_recovers(gpu):
     plan.debug_stall(0)
     want = O.mpk(a.ptr, a.col, None, x, 4, O.MODE_FMA)
     assert max(_rel_errors(_run(plan, x, a.n, 4), want, a.n, 4)) <= TOL
+
+
+@pytest.mark.parametrize("arith", [M.ARITH_DF64, M.ARITH_FIXED])
+def test_host_mapped_execution_matches_device(arith, gpu):
+    """Page-locked host vv runs the ring forms through the host mapping;
+    pageable vv goes through the copies; both give the device path's bits."""
+    import torch
+    a = M.Csr.laplacian(64, 64, 16).pattern()
+    k = 6
+    x = M.uniform(21, a.n)
+    plan = M.Plan.wave(a, k, arith=arith)
+    d = torch.zeros((k + 1) * a.n, dtype=torch.float64, device="cuda")
+    d[:a.n] = torch.from_numpy(x).cuda()
+    torch.cuda.synchronize()
+    plan.exec_device(d.data_ptr())
+    plan.sync()
+    want = d.cpu().numpy()
+    pinned = torch.zeros((k + 1) * a.n, dtype=torch.float64).pin_memory()
+    pinned[:a.n] = torch.from_numpy(x)
+    got_pinned = plan.exec_host(pinned.numpy())
+    got_pageable = _run(plan, x, a.n, k)
+    plan.close()
+    assert got_pinned.tobytes() == want.tobytes()
+    assert got_pageable.tobytes() == want.tobytes()
+    assert np.array_equal(got_pinned[:a.n], x)  # x is read, not written
