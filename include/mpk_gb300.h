@@ -369,6 +369,29 @@ int mpkg_tasks(int n, const int *ptr, const int *col, int npart, int nlevel, int
                const int *parts, const int *levels, int check, long *off, long **idx,
                long *count);
 
+/* PA1 tile metadata of mpkg_plan_pa1 (EXEC_TILES): for every part, the
+ * vertices within nlevel arcs (the reference's skirt distance,
+ * mpk2/lib.c:584-615, with radius nlevel so that the tile holds its level-0
+ * halo) sorted by (distance, vertex), and the sliced-ELL local structure
+ * of the rows computed at level 1.  on_gpu != 0 builds it on the current
+ * GPU (one persistent CTA per SM, balls up to 32768 vertices; beyond that,
+ * and for every error, the host build runs and built_on_gpu reports 0).
+ * The arrays are malloc'd; release them with mpkg_tiles_free. */
+typedef struct {
+  int npart, nlevel, max_slots, built_on_gpu;
+  long total_rows, nslots, nslices, nell;
+  long *slot_off;         /* npart + 1: first slot of each tile */
+  int *shell;             /* npart * (nlevel + 1): vertices within distance d */
+  int *slot_vert;         /* nslots: vertex of each slot */
+  long *slice_off;        /* npart + 1: first slice of each tile */
+  long *ell_off;          /* nslices + 1: first entry of each slice */
+  uint16_t *ell_col;      /* nell: local slot per entry, 32 rows per slice, 0xFFFF = padding */
+  uint8_t *ell_width;     /* nslices */
+} mpkg_tiles_t;
+int mpkg_tile_prep(int n, const int *ptr, const int *col, const int *part, int npart, int nlevel,
+                   int on_gpu, mpkg_tiles_t *out);
+void mpkg_tiles_free(mpkg_tiles_t *t);
+
 /* The MPI-2 prep of every rank at once (what mpi2_mpkwrtbufs does rank by
  * rank, mpk2/mpi2_mpkwrtbufs.c:41-60): reads `dir` (ghead_npart_nlevel_
  * nphase with loop.g0, g<ph>.part.<npart>, l<ph>, s<nphase>, and

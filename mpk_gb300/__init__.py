@@ -49,6 +49,14 @@ def lib():
     return _lib
 
 
+class TilesT(C.Structure):
+    _fields_ = [("npart", C.c_int), ("nlevel", C.c_int), ("max_slots", C.c_int), ("built_on_gpu", C.c_int),
+                ("total_rows", C.c_long), ("nslots", C.c_long), ("nslices", C.c_long), ("nell", C.c_long),
+                ("slot_off", C.c_void_p), ("shell", C.c_void_p), ("slot_vert", C.c_void_p),
+                ("slice_off", C.c_void_p), ("ell_off", C.c_void_p), ("ell_col", C.c_void_p),
+                ("ell_width", C.c_void_p)]
+
+
 class BatchInfo(C.Structure):
     _fields_ = [("nmat", C.c_int), ("nrhs", C.c_int), ("nlevel", C.c_int), ("rows", C.c_long), ("nnz", C.c_long),
                 ("lanes_per_row", C.c_int), ("vector_width", C.c_int), ("group_bytes", C.c_long),
@@ -116,6 +124,8 @@ def _declare(L):
         "mpkg_level_weights": (I, [I, P, P, P, P, P]),
         "mpkg_skirt_write": (I, [C.c_char_p, I, P, P, P, I, P, I]),
         "mpkg_tasks": (I, [I, P, P, I, I, I, P, P, I, P, pp, C.POINTER(Lg)]),
+        "mpkg_tile_prep": (I, [I, P, P, P, I, I, I, C.POINTER(TilesT)]),
+        "mpkg_tiles_free": (None, [C.POINTER(TilesT)]),
         "mpkg_partition_rcb": (I, [I, P, I, I, P]),
         "mpkg_partition_bfs": (I, [I, P, P, I, P]),
         "mpkg_gen_stencil": (I, [C.c_char_p, I, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
@@ -392,6 +402,33 @@ def tasks(a: Csr, npart, nlevel, parts, levels_=None, check=True):
     _check(lib().mpkg_tasks(a.n, _ptr(a.ptr), _ptr(a.col), npart, nlevel, nphase, _ptr(parts),
                             _ptr(lv), 1 if check else 0, _ptr(off), C.byref(ip), C.byref(cnt)))
     return off, _take(ip, cnt.value, np.int64)
+
+
+def tile_prep(a: Csr, part, npart, nlevel, on_gpu=True):
+    """PA1 tile metadata (the balls of every part sorted by (distance,
+    vertex) and the tiles' sliced-ELL local structure), built on the GPU
+    (on_gpu) or on the host; a dict of numpy arrays plus 'built_on_gpu'."""
+    part = _i32(part)
+    t = TilesT()
+    _check(lib().mpkg_tile_prep(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(part), npart, nlevel, 1 if on_gpu else 0,
+                                C.byref(t)))
+    try:
+        def arr(ptr, count, dt):
+            if count == 0:
+                return np.zeros(0, dtype=dt)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                         shape=(count,)).copy()
+        out = {"slot_off": arr(t.slot_off, npart + 1, np.int64),
+               "shell": arr(t.shell, npart * (nlevel + 1), np.int32).reshape(npart, nlevel + 1),
+               "slot_vert": arr(t.slot_vert, t.nslots, np.int32),
+               "slice_off": arr(t.slice_off, npart + 1, np.int64),
+               "ell_off": arr(t.ell_off, t.nslices + 1, np.int64),
+               "ell_col": arr(t.ell_col, t.nell, np.uint16),
+               "ell_width": arr(t.ell_width, t.nslices, np.uint8),
+               "max_slots": t.max_slots, "total_rows": t.total_rows, "built_on_gpu": bool(t.built_on_gpu)}
+    finally:
+        lib().mpkg_tiles_free(C.byref(t))
+    return out
 
 
 # ---------------------------------------------------------------- plans

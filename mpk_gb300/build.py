@@ -11,7 +11,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpk_gb300.so")
 
 HOST_SOURCES = ["graph.cc", "partition.cc", "prep.cc", "bufs.cc", "pdmpk.cc", "api.cc"]
-CUDA_SOURCES = ["device.cu", "sstep.cu", "mlp.cu"]
+CUDA_SOURCES = ["device.cu", "sstep.cu", "mlp.cu", "prep_gpu.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -2169,7 +2169,8 @@ int mpkg_plan_pa1(int n, const int *ptr, const int *col, const double *val, cons
     return mpkg_plan_tasks(n, ptr, col, val, npart, nlevel, 0, tl.off.data(), tl.idx.data(), arith, out);
   }
   TilePlan tp;
-  if ((rc = build_tile_plan(g, pv, npart, nlevel, &tp))) return rc;
+  bool prep_on_gpu = false;
+  if ((rc = build_tile_plan_gpu(g, pv, npart, nlevel, &tp, &prep_on_gpu))) return rc;
   mpkg_plan *p = new_plan();
   if (!p) return fail(kENoMem, "plan allocation failed");
   rc = plan_common(p, n, ptr, col, val, nlevel, arith);

@@ -151,6 +151,11 @@ struct TilePlan {
 };
 int build_tile_plan(const Csr &g, const std::vector<int> &part, int npart, int nlevel,
                     TilePlan *tp);
+// The same plan built on the current GPU (prep_gpu.cu); falls back to
+// build_tile_plan for balls beyond its capacity and for every error case.
+// *on_gpu tells which ran.
+int build_tile_plan_gpu(const Csr &g, const std::vector<int> &part, int npart, int nlevel,
+                        TilePlan *tp, bool *on_gpu);
 
 // ---- level pipeline plans (prep.cc) ---------------------------------------
 // Zero-redundancy pipeline: rows in chunks of `chunk` consecutive ids;

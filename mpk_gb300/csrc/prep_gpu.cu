@@ -1,0 +1,408 @@
+// PA1 tile metadata built on the GPU: the distance-bounded ball of every
+// part (the vertices within nlevel arcs of the part, following the
+// reference's skirt distance, mpk2/lib.c:584-615), sorted by (distance,
+// vertex), and the tiles' sliced-ELL local structure.  The result is the
+// same TilePlan that build_tile_plan (prep.cc) computes on the host, byte
+// for byte; the host build stays the fallback for balls beyond the GPU
+// path's capacity and for every error case, so errors keep their codes and
+// messages.
+//
+// Layout: one persistent CTA per SM.  Each CTA owns an n-entry mark array
+// (distance during the search, slot index while the local structure is
+// built, -1 otherwise) that it restores after every part, so one memset per
+// call prepares all parts.  A part's ball (at most kBallCap vertices) is
+// gathered level by level into its own row of a [npart][kBallCap] array and
+// sorted in shared memory as 32-bit keys (distance << 27 | vertex).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
+#include <numeric>
+#include <vector>
+
+#include "../../include/mpk_gb300.h"
+#include "host.h"
+
+namespace mpkg {
+namespace {
+
+constexpr int kBallCap = 32768;             // vertices per ball (keys sorted in 128 KB of shared memory)
+constexpr int kSliceCap = kBallCap / 32;    // slices of 32 rows per ball
+constexpr int kThreads = 1024;
+constexpr int kVertBits = 27;               // vertex field of a sort key
+constexpr long kMaxBallBytes = 8L << 30;    // the [npart][kBallCap] array
+
+#define PG_TRY(x)                                                                  \
+  do {                                                                             \
+    cudaError_t e_ = (x);                                                          \
+    if (e_ != cudaSuccess) return fail(kECuda, std::string("prep: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct BallArgs {
+  int n, npart, nlevel;
+  const int *ptr;                 // CSR rows (degrees)
+  const long *trptr;              // transpose: the rows that read vertex u
+  const int *tridx;
+  const int *mptr, *mvert;        // members of each part, ascending
+  int *mark;                      // gridDim.x * n, -1 when idle
+  int *ball;                      // npart * kBallCap
+  int *bsize;                     // ball size; -1 beyond capacity, -2 empty part
+  int *shell;                     // npart * (nlevel + 1): vertices within distance d
+  unsigned char *width;           // npart * kSliceCap: slice widths (255 caps)
+  long long *ell;                 // npart: sum of 32 * width; -1 when a row is longer than 255
+};
+
+__global__ void __launch_bounds__(kThreads, 1) ball_kernel(BallArgs a) {
+  extern __shared__ unsigned int keys[];  // kBallCap
+  __shared__ int s_cnt, s_over, s_wide;
+  __shared__ unsigned long long s_ell;
+  int *mark = a.mark + (size_t)blockIdx.x * a.n;
+  for (int p = blockIdx.x; p < a.npart; p += gridDim.x) {
+    int *list = a.ball + (size_t)p * kBallCap;
+    const int m0 = a.mptr[p + 1] - a.mptr[p];
+    if (m0 == 0 || m0 > kBallCap) {
+      if (threadIdx.x == 0) a.bsize[p] = m0 == 0 ? -2 : -1;
+      continue;
+    }
+    if (threadIdx.x == 0) { s_cnt = m0; s_over = 0; s_wide = 0; s_ell = 0; }
+    for (int t = threadIdx.x; t < m0; t += blockDim.x) {
+      const int v = a.mvert[a.mptr[p] + t];
+      mark[v] = 0;
+      list[t] = v;
+    }
+    __syncthreads();
+    int *shell = a.shell + (size_t)p * (a.nlevel + 1);
+    int lo = 0, hi = m0;
+    for (int d = 0; d < a.nlevel; d++) {
+      if (threadIdx.x == 0) shell[d] = hi;
+      for (int q = lo + (int)threadIdx.x; q < hi; q += blockDim.x) {
+        const int u = list[q];
+        for (long t = a.trptr[u]; t < a.trptr[u + 1]; t++) {
+          const int i = a.tridx[t];
+          if (mark[i] < 0 && atomicCAS(&mark[i], -1, d + 1) == -1) {
+            const int pos = atomicAdd(&s_cnt, 1);
+            if (pos < kBallCap) {
+              list[pos] = i;
+            } else {  // beyond capacity: leave the mark as it was
+              mark[i] = -1;
+              s_over = 1;
+            }
+          }
+        }
+      }
+      __syncthreads();
+      lo = hi;
+      hi = min(s_cnt, kBallCap);
+      const int over = s_over;
+      __syncthreads();
+      if (over) break;
+    }
+    if (s_over) {
+      for (int q = threadIdx.x; q < hi; q += blockDim.x) mark[list[q]] = -1;
+      if (threadIdx.x == 0) a.bsize[p] = -1;
+      __syncthreads();
+      continue;
+    }
+    const int m = hi;
+    if (threadIdx.x == 0) shell[a.nlevel] = m;
+    // sort by (distance, vertex)
+    int p2 = 2;
+    while (p2 < m) p2 <<= 1;
+    for (int q = threadIdx.x; q < p2; q += blockDim.x)
+      keys[q] = q < m ? ((unsigned)mark[list[q]] << kVertBits) | (unsigned)list[q] : 0xFFFFFFFFu;
+    __syncthreads();
+    for (int k2 = 2; k2 <= p2; k2 <<= 1)
+      for (int j = k2 >> 1; j > 0; j >>= 1) {
+        for (int q = threadIdx.x; q < p2; q += blockDim.x) {
+          const int r = q ^ j;
+          if (r > q) {
+            const unsigned x0 = keys[q], x1 = keys[r];
+            if ((x0 > x1) == ((q & k2) == 0)) {
+              keys[q] = x1;
+              keys[r] = x0;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+      const int v = (int)(keys[q] & ((1u << kVertBits) - 1));
+      list[q] = v;
+      mark[v] = -1;
+    }
+    __syncthreads();
+    // widths of the slices of the rows computed at level 1 (distance <= nlevel - 1)
+    const int nrows = shell[a.nlevel - 1];
+    unsigned char *wd = a.width + (size_t)p * kSliceCap;
+    for (int s = threadIdx.x; s * 32 < nrows; s += blockDim.x) {
+      int w = 0;
+      for (int r = s * 32; r < min(nrows, s * 32 + 32); r++) {
+        const int v = list[r];
+        w = max(w, a.ptr[v + 1] - a.ptr[v]);
+      }
+      if (w > 255) s_wide = 1;
+      wd[s] = (unsigned char)min(w, 255);
+      atomicAdd(&s_ell, 32ull * (unsigned)w);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      a.bsize[p] = m;
+      a.ell[p] = s_wide ? -1 : (long long)s_ell;
+    }
+    __syncthreads();
+  }
+}
+
+struct EllArgs {
+  int n, npart, nlevel;
+  const int *ptr, *col;
+  const int *ball, *bsize, *shell;
+  const long *slot_off, *slice_off, *ell_off;
+  int *mark;
+  int *slot_vert;
+  unsigned short *ell_col;   // prefilled with 0xFFFF (padding)
+  int *err;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) ell_kernel(EllArgs a) {
+  int *mark = a.mark + (size_t)blockIdx.x * a.n;
+  for (int p = blockIdx.x; p < a.npart; p += gridDim.x) {
+    const int *list = a.ball + (size_t)p * kBallCap;
+    const int m = a.bsize[p];
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+      mark[list[q]] = q;
+      a.slot_vert[a.slot_off[p] + q] = list[q];
+    }
+    __syncthreads();
+    const int nrows = a.shell[(size_t)p * (a.nlevel + 1) + a.nlevel - 1];
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+      const int v = list[r];
+      const long base = a.ell_off[a.slice_off[p] + r / 32] + (r & 31);
+      for (int j = a.ptr[v], t = 0; j < a.ptr[v + 1]; j++, t++) {
+        const int c = mark[a.col[j]];
+        if (c < 0) atomicExch(a.err, 1);
+        else a.ell_col[base + 32L * t] = (unsigned short)c;
+      }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < m; q += blockDim.x) mark[list[q]] = -1;
+    __syncthreads();
+  }
+}
+
+// Device buffers released on every exit path.
+struct DevBufs {
+  std::vector<void *> ptrs;
+  ~DevBufs() {
+    for (void *q : ptrs) cudaFree(q);
+  }
+  template <typename T>
+  int alloc(T **out, size_t count) {
+    *out = nullptr;
+    PG_TRY(cudaMalloc((void **)out, sizeof(T) * std::max<size_t>(count, 1)));
+    ptrs.push_back(*out);
+    return kOk;
+  }
+  template <typename T>
+  int upload(T **out, const T *src, size_t count) {
+    int rc = alloc(out, count);
+    if (rc) return rc;
+    if (count) PG_TRY(cudaMemcpy(*out, src, sizeof(T) * count, cudaMemcpyHostToDevice));
+    return kOk;
+  }
+};
+
+}  // namespace
+
+int build_tile_plan_gpu(const Csr &g, const std::vector<int> &part, int npart, int nlevel, TilePlan *tp,
+                        bool *on_gpu) {
+  *on_gpu = false;
+  const int n = g.n;
+  if ((int)part.size() != n) return fail(kEInval, "partition size != n");
+  for (int q : part) if (q < 0 || q >= npart) return fail(kERange, "part id out of range");
+  if (n >= (1 << kVertBits) || nlevel < 1 || nlevel > 31 || (long)npart * kBallCap * 4 > kMaxBallBytes)
+    return build_tile_plan(g, part, npart, nlevel, tp);
+  int dev = 0, nsm = 0;
+  PG_TRY(cudaGetDevice(&dev));
+  PG_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  // one CTA per SM, fewer when the mark arrays would pass 4 GB
+  const long per_cta = 4L * n;
+  const int grid = (int)std::max(1L, std::min<long>(std::min(nsm, npart), (4L << 30) / std::max(per_cta, 1L)));
+  // members (ascending) and the transpose, on the host: O(n + nnz)
+  std::vector<int> mptr(npart + 1, 0), mvert(n);
+  for (int v = 0; v < n; v++) mptr[part[v] + 1]++;
+  for (int p = 0; p < npart; p++) mptr[p + 1] += mptr[p];
+  {
+    std::vector<int> fill(mptr.begin(), mptr.end() - 1);
+    for (int v = 0; v < n; v++) mvert[fill[part[v]]++] = v;
+  }
+  std::vector<long> trptr(n + 1, 0);
+  std::vector<int> tridx(g.nnz());
+  for (long j = 0; j < g.nnz(); j++) trptr[g.col[j] + 1]++;
+  for (int i = 0; i < n; i++) trptr[i + 1] += trptr[i];
+  {
+    std::vector<long> fill(trptr.begin(), trptr.end() - 1);
+    for (int i = 0; i < n; i++)
+      for (int j = g.ptr[i]; j < g.ptr[i + 1]; j++) tridx[fill[g.col[j]]++] = i;
+  }
+  DevBufs db;
+  int rc;
+  BallArgs ba;
+  std::memset(&ba, 0, sizeof(ba));
+  ba.n = n; ba.npart = npart; ba.nlevel = nlevel;
+  int *d_ptr, *d_col, *d_tridx, *d_mptr, *d_mvert, *d_mark, *d_ball, *d_bsize, *d_shell;
+  long *d_trptr;
+  unsigned char *d_width;
+  long long *d_ell;
+  if ((rc = db.upload(&d_ptr, g.ptr.data(), g.ptr.size()))) return rc;
+  if ((rc = db.upload(&d_col, g.col.data(), g.col.size()))) return rc;
+  if ((rc = db.upload(&d_trptr, trptr.data(), trptr.size()))) return rc;
+  if ((rc = db.upload(&d_tridx, tridx.data(), tridx.size()))) return rc;
+  if ((rc = db.upload(&d_mptr, mptr.data(), mptr.size()))) return rc;
+  if ((rc = db.upload(&d_mvert, mvert.data(), mvert.size()))) return rc;
+  if ((rc = db.alloc(&d_mark, (size_t)grid * n))) return rc;
+  PG_TRY(cudaMemset(d_mark, 0xFF, sizeof(int) * (size_t)grid * n));
+  if ((rc = db.alloc(&d_ball, (size_t)npart * kBallCap))) return rc;
+  if ((rc = db.alloc(&d_bsize, npart))) return rc;
+  if ((rc = db.alloc(&d_shell, (size_t)npart * (nlevel + 1)))) return rc;
+  if ((rc = db.alloc(&d_width, (size_t)npart * kSliceCap))) return rc;
+  if ((rc = db.alloc(&d_ell, npart))) return rc;
+  ba.ptr = d_ptr; ba.trptr = d_trptr; ba.tridx = d_tridx; ba.mptr = d_mptr; ba.mvert = d_mvert;
+  ba.mark = d_mark; ba.ball = d_ball; ba.bsize = d_bsize; ba.shell = d_shell; ba.width = d_width; ba.ell = d_ell;
+  const size_t smem = sizeof(unsigned int) * kBallCap;
+  PG_TRY(cudaFuncSetAttribute(ball_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ball_kernel<<<grid, kThreads, smem>>>(ba);
+  PG_TRY(cudaGetLastError());
+  std::vector<int> bsize(npart);
+  std::vector<long long> ell(npart);
+  std::vector<int> shell((size_t)npart * (nlevel + 1));
+  std::vector<unsigned char> width((size_t)npart * kSliceCap);
+  PG_TRY(cudaMemcpy(bsize.data(), d_bsize, sizeof(int) * npart, cudaMemcpyDeviceToHost));
+  PG_TRY(cudaMemcpy(ell.data(), d_ell, sizeof(long long) * npart, cudaMemcpyDeviceToHost));
+  PG_TRY(cudaMemcpy(shell.data(), d_shell, sizeof(int) * shell.size(), cudaMemcpyDeviceToHost));
+  PG_TRY(cudaMemcpy(width.data(), d_width, width.size(), cudaMemcpyDeviceToHost));
+  // empty parts, balls beyond capacity, rows beyond 255 entries: the host
+  // build decides (and reports the first error in part order)
+  for (int p = 0; p < npart; p++)
+    if (bsize[p] < 0 || ell[p] < 0) return build_tile_plan(g, part, npart, nlevel, tp);
+  tp->n = n; tp->npart = npart; tp->nlevel = nlevel;
+  tp->order.resize(npart);
+  std::iota(tp->order.begin(), tp->order.end(), 0);
+  tp->shell = shell;
+  tp->slot_off.assign(npart + 1, 0);
+  tp->slice_off.assign(npart + 1, 0);
+  tp->ell_off.assign(1, 0);
+  tp->ell_width.clear();
+  tp->max_slots = 0;
+  tp->total_rows = 0;
+  for (int p = 0; p < npart; p++) {
+    const int *sh = &shell[(size_t)p * (nlevel + 1)];
+    tp->slot_off[p + 1] = tp->slot_off[p] + bsize[p];
+    tp->max_slots = std::max(tp->max_slots, bsize[p]);
+    for (int l = 1; l <= nlevel; l++) tp->total_rows += sh[nlevel - l];
+    const int nsl = (sh[nlevel - 1] + 31) / 32;
+    tp->slice_off[p + 1] = tp->slice_off[p] + nsl;
+    for (int s = 0; s < nsl; s++) {
+      const unsigned char w = width[(size_t)p * kSliceCap + s];
+      tp->ell_width.push_back(w);
+      tp->ell_off.push_back(tp->ell_off.back() + 32L * w);
+    }
+  }
+  const long nslots = tp->slot_off[npart], nell = tp->ell_off.back();
+  long *d_slot_off, *d_slice_off, *d_ell_off;
+  int *d_slot_vert, *d_err;
+  unsigned short *d_ell_col;
+  if ((rc = db.upload(&d_slot_off, tp->slot_off.data(), tp->slot_off.size()))) return rc;
+  if ((rc = db.upload(&d_slice_off, tp->slice_off.data(), tp->slice_off.size()))) return rc;
+  if ((rc = db.upload(&d_ell_off, tp->ell_off.data(), tp->ell_off.size()))) return rc;
+  if ((rc = db.alloc(&d_slot_vert, nslots))) return rc;
+  if ((rc = db.alloc(&d_ell_col, nell))) return rc;
+  if ((rc = db.alloc(&d_err, 1))) return rc;
+  PG_TRY(cudaMemset(d_ell_col, 0xFF, sizeof(unsigned short) * std::max<long>(nell, 1)));
+  PG_TRY(cudaMemset(d_err, 0, sizeof(int)));
+  EllArgs ea;
+  ea.n = n; ea.npart = npart; ea.nlevel = nlevel;
+  ea.ptr = d_ptr; ea.col = d_col; ea.ball = d_ball; ea.bsize = d_bsize; ea.shell = d_shell;
+  ea.slot_off = d_slot_off; ea.slice_off = d_slice_off; ea.ell_off = d_ell_off;
+  ea.mark = d_mark; ea.slot_vert = d_slot_vert; ea.ell_col = d_ell_col; ea.err = d_err;
+  ell_kernel<<<grid, kThreads>>>(ea);
+  PG_TRY(cudaGetLastError());
+  int err = 0;
+  PG_TRY(cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return build_tile_plan(g, part, npart, nlevel, tp);  // a column outside its tile's halo
+  tp->slot_vert.resize(nslots);
+  tp->ell_col.resize(nell);
+  if (nslots) PG_TRY(cudaMemcpy(tp->slot_vert.data(), d_slot_vert, sizeof(int) * nslots, cudaMemcpyDeviceToHost));
+  if (nell) PG_TRY(cudaMemcpy(tp->ell_col.data(), d_ell_col, sizeof(unsigned short) * nell, cudaMemcpyDeviceToHost));
+  *on_gpu = true;
+  return kOk;
+}
+
+}  // namespace mpkg
+
+extern "C" {
+
+int mpkg_tile_prep(int n, const int *ptr, const int *col, const int *part, int npart, int nlevel, int on_gpu,
+                   mpkg_tiles_t *out) {
+  using namespace mpkg;
+  clear_error();
+  if (!out || !part || npart <= 0 || nlevel <= 0) return fail(kEInval, "bad argument");
+  std::memset(out, 0, sizeof(*out));
+  if (n <= 0 || !ptr || !col || ptr[0] != 0) return fail(kEInval, "bad CSR");
+  for (int i = 0; i < n; i++)
+    if (ptr[i + 1] < ptr[i]) return fail(kEInval, "ptr must be non-decreasing");
+  for (long j = 0; j < ptr[n]; j++)
+    if (col[j] < 0 || col[j] >= n) return fail(kERange, "column index out of range");
+  Csr g;
+  g.n = n;
+  g.ptr.assign(ptr, ptr + n + 1);
+  g.col.assign(col, col + ptr[n]);
+  std::vector<int> pv(part, part + n);
+  TilePlan tp;
+  bool gpu = false;
+  int rc = on_gpu ? build_tile_plan_gpu(g, pv, npart, nlevel, &tp, &gpu) : build_tile_plan(g, pv, npart, nlevel, &tp);
+  if (rc) return rc;
+  auto dup = [](const auto &v) {
+    using T = typename std::decay_t<decltype(v)>::value_type;
+    T *q = (T *)std::malloc(sizeof(T) * std::max<size_t>(v.size(), 1));
+    if (q && !v.empty()) std::memcpy(q, v.data(), sizeof(T) * v.size());
+    return q;
+  };
+  out->npart = npart;
+  out->nlevel = nlevel;
+  out->max_slots = tp.max_slots;
+  out->total_rows = tp.total_rows;
+  out->nslots = (long)tp.slot_vert.size();
+  out->nslices = (long)tp.ell_width.size();
+  out->nell = (long)tp.ell_col.size();
+  out->built_on_gpu = gpu ? 1 : 0;
+  out->slot_off = dup(tp.slot_off);
+  out->shell = dup(tp.shell);
+  out->slot_vert = dup(tp.slot_vert);
+  out->slice_off = dup(tp.slice_off);
+  out->ell_off = dup(tp.ell_off);
+  out->ell_col = dup(tp.ell_col);
+  out->ell_width = dup(tp.ell_width);
+  if (!out->slot_off || !out->shell || !out->slot_vert || !out->slice_off || !out->ell_off || !out->ell_col ||
+      !out->ell_width) {
+    mpkg_tiles_free(out);
+    return fail(kENoMem, "allocation failed");
+  }
+  return kOk;
+}
+
+void mpkg_tiles_free(mpkg_tiles_t *t) {
+  if (!t) return;
+  std::free(t->slot_off);
+  std::free(t->shell);
+  std::free(t->slot_vert);
+  std::free(t->slice_off);
+  std::free(t->ell_off);
+  std::free(t->ell_col);
+  std::free(t->ell_width);
+  std::memset(t, 0, sizeof(*t));
+}
+
+}  // extern "C"
