@@ -338,6 +338,26 @@ def bench_batch(M, torch, args, flush, stream):
             "gpu_launches_per_step": 1}
 
 
+def bench_prep(M, a, part):
+    """PA1 tile metadata of the headline workload (2048 RCB parts, k=8):
+    the GPU build next to the host build (same bytes)."""
+    g = a.pattern()
+    out = {"workload": "128^3 7-point, 2048 RCB parts, k=8: balls within k arcs, sorted, sliced-ELL local slots"}
+    M.tile_prep(g, part, NPART, K_LEVELS, on_gpu=True)  # warm-up (kernel load)
+    t0 = time.perf_counter()
+    dev = M.tile_prep(g, part, NPART, K_LEVELS, on_gpu=True)
+    out["gpu_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    host = M.tile_prep(g, part, NPART, K_LEVELS, on_gpu=False)
+    out["host_s"] = time.perf_counter() - t0
+    out["built_on_gpu"] = dev["built_on_gpu"]
+    out["identical"] = all(np.array_equal(dev[k], host[k]) for k in
+                           ("slot_off", "shell", "slot_vert", "slice_off", "ell_off", "ell_col", "ell_width"))
+    out["slots"] = int(len(host["slot_vert"]))
+    out["local_columns"] = int(len(host["ell_col"]))
+    return out
+
+
 def bench_sstep(M):
     """s-step CG (s=8) on the 96^3 7-point variable-coefficient diffusion
     matrix (log-normal sigma=1), b ~ U[-1,1], tol 1e-8: monomial,
@@ -380,8 +400,8 @@ def main():
     ap.add_argument("--arith", default="df64", choices=["fma", "separate", "df64", "fixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="time only the selected executor")
-    ap.add_argument("--sections", default="variants,mixed,batched,sstep",
-                    help="comma list of the extra sections to run (variants, mixed, batched, sstep; 'none')")
+    ap.add_argument("--sections", default="variants,mixed,batched,sstep,prep",
+                    help="comma list of the extra sections to run (variants, mixed, batched, sstep, prep; 'none')")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     sections = set() if args.no_variants else {t.strip() for t in args.sections.split(",")} - {"none", ""}
@@ -513,6 +533,7 @@ def main():
         mixed = bench_mixed(M, torch, a, x, k, exact_val, args, flush, stream)
     batched = bench_batch(M, torch, args, flush, stream) if "batched" in sections else {}
     sstep = bench_sstep(M) if "sstep" in sections else {}
+    prep = bench_prep(M, a, part) if "prep" in sections else {}
 
     peak, peak_kind = peaks()
     B = algorithmic_bytes(n, nnz, k, valued=False)
@@ -546,7 +567,7 @@ def main():
                                   "caps plain FP64 at ~195 us for this workload, so the headline runs the rows in "
                                   "double-float on the FP32 pipes (FP64 storage, error vs FP64 stated)"},
             "k_spmv_ms": base_ms, "speedup_vs_k_spmv": (base_ms / ms) if base_ms else None,
-            "variants": variants, "mixed": mixed, "batched": batched, "sstep": sstep,
+            "variants": variants, "mixed": mixed, "batched": batched, "sstep": sstep, "prep": prep,
             "gpu_launches": info["launches"] * args.steps,
             "clocks": clk.summary(), "wall_s_timed_region": wall, "host_device_agree": same,
             "plan": {kk: info[kk] for kk in ("rows_computed", "device_bytes", "pipe_reach", "pipe_grid",

@@ -392,6 +392,13 @@ int mpkg_tile_prep(int n, const int *ptr, const int *col, const int *part, int n
                    int on_gpu, mpkg_tiles_t *out);
 void mpkg_tiles_free(mpkg_tiles_t *t);
 
+/* PA1 task lists (what mpkg_tasks returns for nphase = 0, without the
+ * dependency checks): off has npart+1 entries, idx is allocated
+ * (mpkg_free).  on_gpu != 0 builds the skirts and lists on the current GPU
+ * (same fallback as mpkg_tile_prep; *built_on_gpu tells which ran). */
+int mpkg_pa1_tasks(int n, const int *ptr, const int *col, const int *part, int npart, int nlevel,
+                   int on_gpu, long *off, long **idx, long *count, int *built_on_gpu);
+
 /* The MPI-2 prep of every rank at once (what mpi2_mpkwrtbufs does rank by
  * rank, mpk2/mpi2_mpkwrtbufs.c:41-60): reads `dir` (ghead_npart_nlevel_
  * nphase with loop.g0, g<ph>.part.<npart>, l<ph>, s<nphase>, and

@@ -126,6 +126,7 @@ def _declare(L):
         "mpkg_tasks": (I, [I, P, P, I, I, I, P, P, I, P, pp, C.POINTER(Lg)]),
         "mpkg_tile_prep": (I, [I, P, P, P, I, I, I, C.POINTER(TilesT)]),
         "mpkg_tiles_free": (None, [C.POINTER(TilesT)]),
+        "mpkg_pa1_tasks": (I, [I, P, P, P, I, I, I, P, pp, C.POINTER(Lg), C.POINTER(I)]),
         "mpkg_partition_rcb": (I, [I, P, I, I, P]),
         "mpkg_partition_bfs": (I, [I, P, P, I, P]),
         "mpkg_gen_stencil": (I, [C.c_char_p, I, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
@@ -429,6 +430,17 @@ def tile_prep(a: Csr, part, npart, nlevel, on_gpu=True):
     finally:
         lib().mpkg_tiles_free(C.byref(t))
     return out
+
+
+def pa1_tasks(a: Csr, part, npart, nlevel, on_gpu=True):
+    """PA1 task lists (nphase = 0) built on the GPU or the host ->
+    (off, idx, built_on_gpu)."""
+    part = _i32(part)
+    off = np.empty(npart + 1, dtype=np.int64)
+    ip, cnt, on = C.c_void_p(), C.c_long(), C.c_int()
+    _check(lib().mpkg_pa1_tasks(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(part), npart, nlevel, 1 if on_gpu else 0,
+                                _ptr(off), C.byref(ip), C.byref(cnt), C.byref(on)))
+    return off, _take(ip, cnt.value, np.int64), bool(on.value)
 
 
 # ---------------------------------------------------------------- plans

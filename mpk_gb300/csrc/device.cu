@@ -2162,10 +2162,9 @@ int mpkg_plan_pa1(int n, const int *ptr, const int *col, const double *val, cons
   std::vector<int> pv(part, part + n);
   for (int q : pv) if (q < 0 || q >= npart) return fail(kERange, "part id out of range");
   if (exec == MPKG_EXEC_TASKS) {
-    std::vector<PartSkirt> sk;
-    if ((rc = comp_skirts(g, pv, npart, nullptr, nlevel, &sk))) return rc;
     TaskLists tl;
-    if ((rc = build_tasks(g, npart, nlevel, 0, {pv}, {}, sk, false, &tl))) return rc;
+    bool tasks_on_gpu = false;
+    if ((rc = build_pa1_tasks_gpu(g, pv, npart, nlevel, &tl, &tasks_on_gpu))) return rc;
     return mpkg_plan_tasks(n, ptr, col, val, npart, nlevel, 0, tl.off.data(), tl.idx.data(), arith, out);
   }
   TilePlan tp;

@@ -156,6 +156,10 @@ int build_tile_plan(const Csr &g, const std::vector<int> &part, int npart, int n
 // *on_gpu tells which ran.
 int build_tile_plan_gpu(const Csr &g, const std::vector<int> &part, int npart, int nlevel,
                         TilePlan *tp, bool *on_gpu);
+// PA1 task lists (nphase = 0: comp_skirts + build_tasks without the
+// dependency checks) built on the current GPU, with the same fallback.
+int build_pa1_tasks_gpu(const Csr &g, const std::vector<int> &part, int npart, int nlevel,
+                        TaskLists *tl, bool *on_gpu);
 
 // ---- level pipeline plans (prep.cc) ---------------------------------------
 // Zero-redundancy pipeline: rows in chunks of `chunk` consecutive ids;

@@ -1,18 +1,21 @@
-// PA1 tile metadata built on the GPU: the distance-bounded ball of every
-// part (the vertices within nlevel arcs of the part, following the
-// reference's skirt distance, mpk2/lib.c:584-615), sorted by (distance,
-// vertex), and the tiles' sliced-ELL local structure.  The result is the
-// same TilePlan that build_tile_plan (prep.cc) computes on the host, byte
-// for byte; the host build stays the fallback for balls beyond the GPU
-// path's capacity and for every error case, so errors keep their codes and
-// messages.
+// PA1 prep on the GPU.  For every part, the distance-bounded ball (the
+// vertices within r arcs of the part under the reference's skirt distance,
+// mpk2/lib.c:584-615: row i is one arc from every column it reads), then
+//  * tiles (r = nlevel): the ball sorted by (distance, vertex) and the
+//    tiles' sliced-ELL local structure -- the TilePlan of build_tile_plan;
+//  * task lists (r = nlevel - 1): the ball sorted by vertex (the skirt of
+//    comp_skirts) and the level-major task lists of build_tasks
+//    (mpk2/mpkprep.c:185-233 for nphase = 0).
+// Results equal the host builds (prep.cc) byte for byte; the host builds
+// stay the fallback for balls beyond the GPU path's capacity and for every
+// error case, so errors keep their codes and messages.
 //
 // Layout: one persistent CTA per SM.  Each CTA owns an n-entry mark array
 // (distance during the search, slot index while the local structure is
 // built, -1 otherwise) that it restores after every part, so one memset per
 // call prepares all parts.  A part's ball (at most kBallCap vertices) is
 // gathered level by level into its own row of a [npart][kBallCap] array and
-// sorted in shared memory as 32-bit keys (distance << 27 | vertex).
+// sorted in shared memory as 32-bit keys.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,6 +35,7 @@ constexpr int kBallCap = 32768;             // vertices per ball (keys sorted in
 constexpr int kSliceCap = kBallCap / 32;    // slices of 32 rows per ball
 constexpr int kThreads = 1024;
 constexpr int kVertBits = 27;               // vertex field of a sort key
+constexpr int kDistBits = 5;                // distance field of a (vertex, distance) key
 constexpr long kMaxBallBytes = 8L << 30;    // the [npart][kBallCap] array
 
 #define PG_TRY(x)                                                                  \
@@ -41,19 +45,20 @@ constexpr long kMaxBallBytes = 8L << 30;    // the [npart][kBallCap] array
   } while (0)
 
 struct BallArgs {
-  int n, npart, nlevel;
+  int n, npart, nlevel, radius;
   const int *ptr;                 // CSR rows (degrees)
   const long *trptr;              // transpose: the rows that read vertex u
   const int *tridx;
   const int *mptr, *mvert;        // members of each part, ascending
   int *mark;                      // gridDim.x * n, -1 when idle
-  int *ball;                      // npart * kBallCap
+  int *ball;                      // npart * kBallCap: vertices (tiles) or (vertex, distance) keys
   int *bsize;                     // ball size; -1 beyond capacity, -2 empty part
-  int *shell;                     // npart * (nlevel + 1): vertices within distance d
+  int *shell;                     // npart * (nlevel + 1): vertices within distance d <= radius
   unsigned char *width;           // npart * kSliceCap: slice widths (255 caps)
   long long *ell;                 // npart: sum of 32 * width; -1 when a row is longer than 255
 };
 
+template <bool TILES>
 __global__ void __launch_bounds__(kThreads, 1) ball_kernel(BallArgs a) {
   extern __shared__ unsigned int keys[];  // kBallCap
   __shared__ int s_cnt, s_over, s_wide;
@@ -64,6 +69,7 @@ __global__ void __launch_bounds__(kThreads, 1) ball_kernel(BallArgs a) {
     const int m0 = a.mptr[p + 1] - a.mptr[p];
     if (m0 == 0 || m0 > kBallCap) {
       if (threadIdx.x == 0) a.bsize[p] = m0 == 0 ? -2 : -1;
+      for (int d = threadIdx.x; d <= a.nlevel; d += blockDim.x) a.shell[(size_t)p * (a.nlevel + 1) + d] = 0;
       continue;
     }
     if (threadIdx.x == 0) { s_cnt = m0; s_over = 0; s_wide = 0; s_ell = 0; }
@@ -75,7 +81,7 @@ __global__ void __launch_bounds__(kThreads, 1) ball_kernel(BallArgs a) {
     __syncthreads();
     int *shell = a.shell + (size_t)p * (a.nlevel + 1);
     int lo = 0, hi = m0;
-    for (int d = 0; d < a.nlevel; d++) {
+    for (int d = 0; d < a.radius; d++) {
       if (threadIdx.x == 0) shell[d] = hi;
       for (int q = lo + (int)threadIdx.x; q < hi; q += blockDim.x) {
         const int u = list[q];
@@ -106,12 +112,18 @@ __global__ void __launch_bounds__(kThreads, 1) ball_kernel(BallArgs a) {
       continue;
     }
     const int m = hi;
-    if (threadIdx.x == 0) shell[a.nlevel] = m;
-    // sort by (distance, vertex)
+    if (threadIdx.x == 0) shell[a.radius] = m;
+    // sort by (distance, vertex) for tiles, by vertex for task lists
     int p2 = 2;
     while (p2 < m) p2 <<= 1;
-    for (int q = threadIdx.x; q < p2; q += blockDim.x)
-      keys[q] = q < m ? ((unsigned)mark[list[q]] << kVertBits) | (unsigned)list[q] : 0xFFFFFFFFu;
+    for (int q = threadIdx.x; q < p2; q += blockDim.x) {
+      unsigned key = 0xFFFFFFFFu;
+      if (q < m) {
+        const unsigned v = (unsigned)list[q], d = (unsigned)mark[v];
+        key = TILES ? (d << kVertBits) | v : (v << kDistBits) | d;
+      }
+      keys[q] = key;
+    }
     __syncthreads();
     for (int k2 = 2; k2 <= p2; k2 <<= 1)
       for (int j = k2 >> 1; j > 0; j >>= 1) {
@@ -128,11 +140,19 @@ __global__ void __launch_bounds__(kThreads, 1) ball_kernel(BallArgs a) {
         __syncthreads();
       }
     for (int q = threadIdx.x; q < m; q += blockDim.x) {
-      const int v = (int)(keys[q] & ((1u << kVertBits) - 1));
-      list[q] = v;
+      const int v = TILES ? (int)(keys[q] & ((1u << kVertBits) - 1)) : (int)(keys[q] >> kDistBits);
+      list[q] = TILES ? v : (int)keys[q];
       mark[v] = -1;
     }
     __syncthreads();
+    if (!TILES) {
+      if (threadIdx.x == 0) {
+        a.bsize[p] = m;
+        a.ell[p] = 0;
+      }
+      __syncthreads();
+      continue;
+    }
     // widths of the slices of the rows computed at level 1 (distance <= nlevel - 1)
     const int nrows = shell[a.nlevel - 1];
     unsigned char *wd = a.width + (size_t)p * kSliceCap;
@@ -192,6 +212,54 @@ __global__ void __launch_bounds__(kThreads, 1) ell_kernel(EllArgs a) {
   }
 }
 
+// Level-major task lists of every part from its vertex-sorted skirt: level
+// l takes the skirt vertices at distance <= nlevel - l, in vertex order
+// (an order-keeping compaction per level: per-thread runs, block scan).
+struct TaskArgs {
+  int n, npart, nlevel;
+  const int *ball, *bsize;
+  const long *off;
+  long *idx;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) task_kernel(TaskArgs a) {
+  __shared__ int s_warp[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int p = blockIdx.x; p < a.npart; p += gridDim.x) {
+    const unsigned *keys = reinterpret_cast<const unsigned *>(a.ball + (size_t)p * kBallCap);
+    const int m = max(a.bsize[p], 0);
+    const int per = (m + blockDim.x - 1) / blockDim.x;
+    const int q0 = min(m, (int)threadIdx.x * per), q1 = min(m, q0 + per);
+    long base = a.off[p];
+    for (int l = 1; l <= a.nlevel; l++) {
+      const unsigned dmax = (unsigned)(a.nlevel - l);
+      int c = 0;
+      for (int q = q0; q < q1; q++) c += (keys[q] & ((1u << kDistBits) - 1)) <= dmax;
+      int x = c;  // inclusive scan within the warp
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) s_warp[warp] = x;
+      __syncthreads();
+      if (warp == 0) {
+        int w = s_warp[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+          if (lane >= o) w += y;
+        }
+        s_warp[lane] = w;
+      }
+      __syncthreads();
+      long r = base + (x - c) + (warp ? s_warp[warp - 1] : 0);
+      for (int q = q0; q < q1; q++)
+        if ((keys[q] & ((1u << kDistBits) - 1)) <= dmax) a.idx[r++] = (long)l * a.n + (long)(keys[q] >> kDistBits);
+      base += s_warp[kThreads / 32 - 1];
+      __syncthreads();
+    }
+  }
+}
+
 // Device buffers released on every exit path.
 struct DevBufs {
   std::vector<void *> ptrs;
@@ -214,75 +282,154 @@ struct DevBufs {
   }
 };
 
+// The ball search of every part on the GPU: inputs uploaded once, results
+// (sizes, shells, slice widths) copied back.
+struct BallRun {
+  DevBufs db;
+  int n = 0, npart = 0, nlevel = 0, grid = 0;
+  int *d_ptr = nullptr, *d_col = nullptr, *d_mark = nullptr, *d_ball = nullptr, *d_bsize = nullptr,
+      *d_shell = nullptr;
+  unsigned char *d_width = nullptr;
+  long long *d_ell = nullptr;
+  std::vector<int> bsize, shell;
+  std::vector<long long> ell;
+  std::vector<unsigned char> width;
+
+  // false: the GPU path does not apply (sizes beyond its limits)
+  static bool fits(int n, int npart, int nlevel) {
+    return n < (1 << kVertBits) - 1 && nlevel >= 1 && nlevel <= 31 && (long)npart * kBallCap * 4 <= kMaxBallBytes;
+  }
+
+  int run(const Csr &g, const std::vector<int> &part, int npart_, int nlevel_, int radius, bool tiles) {
+    n = g.n; npart = npart_; nlevel = nlevel_;
+    int dev = 0, nsm = 0;
+    PG_TRY(cudaGetDevice(&dev));
+    PG_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    // one CTA per SM, fewer when the mark arrays would pass 4 GB
+    const long per_cta = 4L * n;
+    grid = (int)std::max(1L, std::min<long>(std::min(nsm, npart), (4L << 30) / std::max(per_cta, 1L)));
+    // members (ascending) and the transpose, on the host: O(n + nnz)
+    std::vector<int> mptr(npart + 1, 0), mvert(n);
+    for (int v = 0; v < n; v++) mptr[part[v] + 1]++;
+    for (int p = 0; p < npart; p++) mptr[p + 1] += mptr[p];
+    {
+      std::vector<int> fill(mptr.begin(), mptr.end() - 1);
+      for (int v = 0; v < n; v++) mvert[fill[part[v]]++] = v;
+    }
+    std::vector<long> trptr(n + 1, 0);
+    std::vector<int> tridx(g.nnz());
+    for (long j = 0; j < g.nnz(); j++) trptr[g.col[j] + 1]++;
+    for (int i = 0; i < n; i++) trptr[i + 1] += trptr[i];
+    {
+      std::vector<long> fill(trptr.begin(), trptr.end() - 1);
+      for (int i = 0; i < n; i++)
+        for (int j = g.ptr[i]; j < g.ptr[i + 1]; j++) tridx[fill[g.col[j]]++] = i;
+    }
+    int rc;
+    int *d_tridx, *d_mptr, *d_mvert;
+    long *d_trptr;
+    if ((rc = db.upload(&d_ptr, g.ptr.data(), g.ptr.size()))) return rc;
+    if ((rc = db.upload(&d_col, g.col.data(), g.col.size()))) return rc;
+    if ((rc = db.upload(&d_trptr, trptr.data(), trptr.size()))) return rc;
+    if ((rc = db.upload(&d_tridx, tridx.data(), tridx.size()))) return rc;
+    if ((rc = db.upload(&d_mptr, mptr.data(), mptr.size()))) return rc;
+    if ((rc = db.upload(&d_mvert, mvert.data(), mvert.size()))) return rc;
+    if ((rc = db.alloc(&d_mark, (size_t)grid * n))) return rc;
+    PG_TRY(cudaMemset(d_mark, 0xFF, sizeof(int) * (size_t)grid * n));
+    if ((rc = db.alloc(&d_ball, (size_t)npart * kBallCap))) return rc;
+    if ((rc = db.alloc(&d_bsize, npart))) return rc;
+    if ((rc = db.alloc(&d_shell, (size_t)npart * (nlevel + 1)))) return rc;
+    if ((rc = db.alloc(&d_width, tiles ? (size_t)npart * kSliceCap : 1))) return rc;
+    if ((rc = db.alloc(&d_ell, npart))) return rc;
+    BallArgs ba;
+    std::memset(&ba, 0, sizeof(ba));
+    ba.n = n; ba.npart = npart; ba.nlevel = nlevel; ba.radius = radius;
+    ba.ptr = d_ptr; ba.trptr = d_trptr; ba.tridx = d_tridx; ba.mptr = d_mptr; ba.mvert = d_mvert;
+    ba.mark = d_mark; ba.ball = d_ball; ba.bsize = d_bsize; ba.shell = d_shell; ba.width = d_width; ba.ell = d_ell;
+    const size_t smem = sizeof(unsigned int) * kBallCap;
+    if (tiles) {
+      PG_TRY(cudaFuncSetAttribute(ball_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      ball_kernel<true><<<grid, kThreads, smem>>>(ba);
+    } else {
+      PG_TRY(cudaFuncSetAttribute(ball_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      ball_kernel<false><<<grid, kThreads, smem>>>(ba);
+    }
+    PG_TRY(cudaGetLastError());
+    bsize.resize(npart);
+    ell.resize(npart);
+    shell.resize((size_t)npart * (nlevel + 1));
+    PG_TRY(cudaMemcpy(bsize.data(), d_bsize, sizeof(int) * npart, cudaMemcpyDeviceToHost));
+    PG_TRY(cudaMemcpy(ell.data(), d_ell, sizeof(long long) * npart, cudaMemcpyDeviceToHost));
+    PG_TRY(cudaMemcpy(shell.data(), d_shell, sizeof(int) * shell.size(), cudaMemcpyDeviceToHost));
+    if (tiles) {
+      width.resize((size_t)npart * kSliceCap);
+      PG_TRY(cudaMemcpy(width.data(), d_width, width.size(), cudaMemcpyDeviceToHost));
+    }
+    return kOk;
+  }
+};
+
+int check_part(int n, const std::vector<int> &part, int npart) {
+  if ((int)part.size() != n) return fail(kEInval, "partition size != n");
+  for (int q : part) if (q < 0 || q >= npart) return fail(kERange, "part id out of range");
+  return kOk;
+}
+
+int host_pa1_tasks(const Csr &g, const std::vector<int> &part, int npart, int nlevel, TaskLists *tl) {
+  std::vector<PartSkirt> sk;
+  int rc = comp_skirts(g, part, npart, nullptr, nlevel, &sk);
+  if (rc) return rc;
+  return build_tasks(g, npart, nlevel, 0, {part}, {}, sk, false, tl);
+}
+
 }  // namespace
+
+int build_pa1_tasks_gpu(const Csr &g, const std::vector<int> &part, int npart, int nlevel, TaskLists *tl,
+                        bool *on_gpu) {
+  *on_gpu = false;
+  const int n = g.n;
+  int rc = check_part(n, part, npart);
+  if (rc) return rc;
+  if (!BallRun::fits(n, npart, nlevel)) return host_pa1_tasks(g, part, npart, nlevel, tl);
+  BallRun br;
+  if ((rc = br.run(g, part, npart, nlevel, nlevel - 1, false))) return rc;
+  for (int p = 0; p < npart; p++)
+    if (br.bsize[p] == -1) return host_pa1_tasks(g, part, npart, nlevel, tl);  // beyond capacity
+  tl->n = n; tl->npart = npart; tl->nlevel = nlevel; tl->nphase = 0;
+  tl->off.assign((size_t)npart + 1, 0);
+  for (int p = 0; p < npart; p++) {
+    const int *sh = &br.shell[(size_t)p * (nlevel + 1)];
+    long c = 0;
+    for (int l = 1; l <= nlevel; l++) c += sh[nlevel - l];
+    tl->off[p + 1] = tl->off[p] + c;
+  }
+  const long total = tl->off[npart];
+  long *d_off, *d_idx;
+  if ((rc = br.db.upload(&d_off, tl->off.data(), tl->off.size()))) return rc;
+  if ((rc = br.db.alloc(&d_idx, total))) return rc;
+  TaskArgs ta;
+  ta.n = n; ta.npart = npart; ta.nlevel = nlevel;
+  ta.ball = br.d_ball; ta.bsize = br.d_bsize; ta.off = d_off; ta.idx = d_idx;
+  task_kernel<<<br.grid, kThreads>>>(ta);
+  PG_TRY(cudaGetLastError());
+  tl->idx.resize(total);
+  if (total) PG_TRY(cudaMemcpy(tl->idx.data(), d_idx, sizeof(long) * total, cudaMemcpyDeviceToHost));
+  *on_gpu = true;
+  return kOk;
+}
 
 int build_tile_plan_gpu(const Csr &g, const std::vector<int> &part, int npart, int nlevel, TilePlan *tp,
                         bool *on_gpu) {
   *on_gpu = false;
   const int n = g.n;
-  if ((int)part.size() != n) return fail(kEInval, "partition size != n");
-  for (int q : part) if (q < 0 || q >= npart) return fail(kERange, "part id out of range");
-  if (n >= (1 << kVertBits) || nlevel < 1 || nlevel > 31 || (long)npart * kBallCap * 4 > kMaxBallBytes)
-    return build_tile_plan(g, part, npart, nlevel, tp);
-  int dev = 0, nsm = 0;
-  PG_TRY(cudaGetDevice(&dev));
-  PG_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  // one CTA per SM, fewer when the mark arrays would pass 4 GB
-  const long per_cta = 4L * n;
-  const int grid = (int)std::max(1L, std::min<long>(std::min(nsm, npart), (4L << 30) / std::max(per_cta, 1L)));
-  // members (ascending) and the transpose, on the host: O(n + nnz)
-  std::vector<int> mptr(npart + 1, 0), mvert(n);
-  for (int v = 0; v < n; v++) mptr[part[v] + 1]++;
-  for (int p = 0; p < npart; p++) mptr[p + 1] += mptr[p];
-  {
-    std::vector<int> fill(mptr.begin(), mptr.end() - 1);
-    for (int v = 0; v < n; v++) mvert[fill[part[v]]++] = v;
-  }
-  std::vector<long> trptr(n + 1, 0);
-  std::vector<int> tridx(g.nnz());
-  for (long j = 0; j < g.nnz(); j++) trptr[g.col[j] + 1]++;
-  for (int i = 0; i < n; i++) trptr[i + 1] += trptr[i];
-  {
-    std::vector<long> fill(trptr.begin(), trptr.end() - 1);
-    for (int i = 0; i < n; i++)
-      for (int j = g.ptr[i]; j < g.ptr[i + 1]; j++) tridx[fill[g.col[j]]++] = i;
-  }
-  DevBufs db;
-  int rc;
-  BallArgs ba;
-  std::memset(&ba, 0, sizeof(ba));
-  ba.n = n; ba.npart = npart; ba.nlevel = nlevel;
-  int *d_ptr, *d_col, *d_tridx, *d_mptr, *d_mvert, *d_mark, *d_ball, *d_bsize, *d_shell;
-  long *d_trptr;
-  unsigned char *d_width;
-  long long *d_ell;
-  if ((rc = db.upload(&d_ptr, g.ptr.data(), g.ptr.size()))) return rc;
-  if ((rc = db.upload(&d_col, g.col.data(), g.col.size()))) return rc;
-  if ((rc = db.upload(&d_trptr, trptr.data(), trptr.size()))) return rc;
-  if ((rc = db.upload(&d_tridx, tridx.data(), tridx.size()))) return rc;
-  if ((rc = db.upload(&d_mptr, mptr.data(), mptr.size()))) return rc;
-  if ((rc = db.upload(&d_mvert, mvert.data(), mvert.size()))) return rc;
-  if ((rc = db.alloc(&d_mark, (size_t)grid * n))) return rc;
-  PG_TRY(cudaMemset(d_mark, 0xFF, sizeof(int) * (size_t)grid * n));
-  if ((rc = db.alloc(&d_ball, (size_t)npart * kBallCap))) return rc;
-  if ((rc = db.alloc(&d_bsize, npart))) return rc;
-  if ((rc = db.alloc(&d_shell, (size_t)npart * (nlevel + 1)))) return rc;
-  if ((rc = db.alloc(&d_width, (size_t)npart * kSliceCap))) return rc;
-  if ((rc = db.alloc(&d_ell, npart))) return rc;
-  ba.ptr = d_ptr; ba.trptr = d_trptr; ba.tridx = d_tridx; ba.mptr = d_mptr; ba.mvert = d_mvert;
-  ba.mark = d_mark; ba.ball = d_ball; ba.bsize = d_bsize; ba.shell = d_shell; ba.width = d_width; ba.ell = d_ell;
-  const size_t smem = sizeof(unsigned int) * kBallCap;
-  PG_TRY(cudaFuncSetAttribute(ball_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  ball_kernel<<<grid, kThreads, smem>>>(ba);
-  PG_TRY(cudaGetLastError());
-  std::vector<int> bsize(npart);
-  std::vector<long long> ell(npart);
-  std::vector<int> shell((size_t)npart * (nlevel + 1));
-  std::vector<unsigned char> width((size_t)npart * kSliceCap);
-  PG_TRY(cudaMemcpy(bsize.data(), d_bsize, sizeof(int) * npart, cudaMemcpyDeviceToHost));
-  PG_TRY(cudaMemcpy(ell.data(), d_ell, sizeof(long long) * npart, cudaMemcpyDeviceToHost));
-  PG_TRY(cudaMemcpy(shell.data(), d_shell, sizeof(int) * shell.size(), cudaMemcpyDeviceToHost));
-  PG_TRY(cudaMemcpy(width.data(), d_width, width.size(), cudaMemcpyDeviceToHost));
+  int rc = check_part(n, part, npart);
+  if (rc) return rc;
+  if (!BallRun::fits(n, npart, nlevel)) return build_tile_plan(g, part, npart, nlevel, tp);
+  BallRun br;
+  if ((rc = br.run(g, part, npart, nlevel, nlevel, true))) return rc;
+  const std::vector<int> &bsize = br.bsize, &shell = br.shell;
+  const std::vector<long long> &ell = br.ell;
+  const std::vector<unsigned char> &width = br.width;
   // empty parts, balls beyond capacity, rows beyond 255 entries: the host
   // build decides (and reports the first error in part order)
   for (int p = 0; p < npart; p++)
@@ -311,6 +458,10 @@ int build_tile_plan_gpu(const Csr &g, const std::vector<int> &part, int npart, i
     }
   }
   const long nslots = tp->slot_off[npart], nell = tp->ell_off.back();
+  DevBufs &db = br.db;
+  const int grid = br.grid;
+  int *d_ptr = br.d_ptr, *d_col = br.d_col, *d_ball = br.d_ball, *d_bsize = br.d_bsize, *d_shell = br.d_shell,
+      *d_mark = br.d_mark;
   long *d_slot_off, *d_slice_off, *d_ell_off;
   int *d_slot_vert, *d_err;
   unsigned short *d_ell_col;
@@ -338,6 +489,13 @@ int build_tile_plan_gpu(const Csr &g, const std::vector<int> &part, int npart, i
   if (nell) PG_TRY(cudaMemcpy(tp->ell_col.data(), d_ell_col, sizeof(unsigned short) * nell, cudaMemcpyDeviceToHost));
   *on_gpu = true;
   return kOk;
+}
+
+// The host build of the same lists (comp_skirts + build_tasks, nphase = 0).
+int check_part_host(const Csr &g, const std::vector<int> &part, int npart, int nlevel, TaskLists *tl) {
+  int rc = check_part(g.n, part, npart);
+  if (rc) return rc;
+  return host_pa1_tasks(g, part, npart, nlevel, tl);
 }
 
 }  // namespace mpkg
@@ -390,6 +548,37 @@ int mpkg_tile_prep(int n, const int *ptr, const int *col, const int *part, int n
     mpkg_tiles_free(out);
     return fail(kENoMem, "allocation failed");
   }
+  return kOk;
+}
+
+int mpkg_pa1_tasks(int n, const int *ptr, const int *col, const int *part, int npart, int nlevel, int on_gpu,
+                   long *off, long **idx, long *count, int *built_on_gpu) {
+  using namespace mpkg;
+  clear_error();
+  if (!part || !off || !idx || !count || npart <= 0 || nlevel <= 0) return fail(kEInval, "bad argument");
+  *idx = nullptr;
+  *count = 0;
+  if (built_on_gpu) *built_on_gpu = 0;
+  if (n <= 0 || !ptr || !col || ptr[0] != 0) return fail(kEInval, "bad CSR");
+  for (int i = 0; i < n; i++)
+    if (ptr[i + 1] < ptr[i]) return fail(kEInval, "ptr must be non-decreasing");
+  for (long j = 0; j < ptr[n]; j++)
+    if (col[j] < 0 || col[j] >= n) return fail(kERange, "column index out of range");
+  Csr g;
+  g.n = n;
+  g.ptr.assign(ptr, ptr + n + 1);
+  g.col.assign(col, col + ptr[n]);
+  std::vector<int> pv(part, part + n);
+  TaskLists tl;
+  bool gpu = false;
+  int rc = on_gpu ? build_pa1_tasks_gpu(g, pv, npart, nlevel, &tl, &gpu) : check_part_host(g, pv, npart, nlevel, &tl);
+  if (rc) return rc;
+  std::copy(tl.off.begin(), tl.off.end(), off);
+  *idx = (long *)std::malloc(sizeof(long) * std::max<size_t>(tl.idx.size(), 1));
+  if (!*idx) return fail(kENoMem, "allocation failed");
+  if (!tl.idx.empty()) std::memcpy(*idx, tl.idx.data(), sizeof(long) * tl.idx.size());
+  *count = (long)tl.idx.size();
+  if (built_on_gpu) *built_on_gpu = gpu ? 1 : 0;
   return kOk;
 }
 

@@ -1,6 +1,7 @@
-"""PA1 tile metadata (mpkg_tile_prep): the host build against a plain
-Python restatement of its definition (CPU), and the GPU build byte for
-byte against the host build (GPU).  A tile of part p holds the vertices
+"""PA1 prep on the GPU.  Tile metadata (mpkg_tile_prep): the host build
+against a plain Python restatement of its definition (CPU), and the GPU
+build byte for byte against the host build (GPU); task lists
+(mpkg_pa1_tasks): the GPU build against the host build.  A tile of part p holds the vertices
 within nlevel arcs of p under the reference's skirt distance
 (mpk2/lib.c:584-615: row i is one arc from every column it reads), sorted
 by (distance, vertex); the rows within nlevel-1 arcs are computed at level
@@ -149,3 +150,37 @@ def test_gpu_tile_prep_errors_as_host(gpu):
             M.tile_prep(b, pt, 4, 3, on_gpu=True)
         assert e1.value.code == e2.value.code == code
         assert str(e1.value) == str(e2.value)
+
+
+def test_host_pa1_tasks_equal_mpkg_tasks():
+    a0 = M.Csr.laplacian(16, 16, 4)
+    a = a0.pattern()
+    part = M.partition_rcb(a0.coords, 12)
+    off, idx, on = M.pa1_tasks(a, part, 12, 5, on_gpu=False)
+    off2, idx2 = M.tasks(a, 12, 5, part, check=False)
+    assert not on
+    assert np.array_equal(off, off2) and np.array_equal(idx, idx2)
+
+
+@pytest.mark.gpu
+def test_gpu_pa1_tasks_identical_to_host(gpu):
+    cases = _cases()
+    a0 = M.Csr.laplacian(24, 24)
+    part = M.partition_rcb(a0.coords, 6)
+    cases.append(("empty_part", a0.pattern(), np.where(part == 5, 4, part), 6, 4))  # part 5 has no vertices
+    cases.append(("one_level", a0.pattern(), part, 6, 1))
+    for name, a, pt, npart, nlevel in cases:
+        off, idx, on = M.pa1_tasks(a, pt, npart, nlevel, on_gpu=False)
+        goff, gidx, gon = M.pa1_tasks(a, pt, npart, nlevel, on_gpu=True)
+        assert gon and not on, name
+        assert np.array_equal(goff, off) and np.array_equal(gidx, idx), name
+
+
+@pytest.mark.gpu
+def test_gpu_pa1_tasks_fall_back_beyond_capacity(gpu):
+    a0 = M.Csr.laplacian(64, 64, 16)
+    part = M.partition_rcb(a0.coords, 2)
+    off, idx, on = M.pa1_tasks(a0.pattern(), part, 2, 3, on_gpu=True)
+    assert not on
+    off2, idx2, _ = M.pa1_tasks(a0.pattern(), part, 2, 3, on_gpu=False)
+    assert np.array_equal(off, off2) and np.array_equal(idx, idx2)
