@@ -148,11 +148,24 @@ __global__ void basis_step_kernel(int n, const int *__restrict__ ptr, const int 
   }
 }
 
-// Gram matrix G = Y^T Y in FP64 (products of FP32 values are exact in
-// FP64).  A CTA stages a tile of rows of all columns in shared memory;
-// thread t accumulates pair t of the upper triangle; per-CTA partials are
-// summed in a fixed order by gram_reduce_kernel.
+// Gram matrix G = Y^T Y of the FP32 basis, on the FP32 pipes: each product
+// a*b of two FP32 values is split exactly into p + e (p = a*b rounded,
+// e = fma(a, b, -p)) and summed in double-float (a two-sum on the high
+// parts, the errors and low parts added), about 2^-46 relative to the sum
+// of |products| -- FP64's own rounding (2^-53 per add) is not needed for
+// the coefficient solve, and GB300's FP64 pipe runs at 1/64 of FP32.
+// A CTA stages a tile of rows of all columns in shared memory; thread t
+// accumulates pair t of the upper triangle with four independent sums;
+// per-CTA partials (FP64) are summed in a fixed order by gram_reduce_kernel.
 constexpr int kGramRows = 64;
+__device__ __forceinline__ void gram_acc(float a, float b, float &sh, float &sl) {
+  const float p = __fmul_rn(a, b), e = __fmaf_rn(a, b, -p);
+  const float t = __fadd_rn(sh, p), bp = __fadd_rn(t, -sh);
+  const float err = __fadd_rn(__fadd_rn(sh, -__fadd_rn(t, -bp)), __fadd_rn(p, -bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
 __global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const float *__restrict__ y,
                                                         double *__restrict__ part) {
   __shared__ float tile[kMaxCols][kGramRows];
@@ -164,7 +177,7 @@ __global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const f
     pa = a;
     pb = a + t;
   }
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  float h[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
   for (long r0 = (long)blockIdx.x * kGramRows; r0 < n; r0 += (long)gridDim.x * kGramRows) {
     __syncthreads();
     for (int e = threadIdx.x; e < ncol * kGramRows; e += blockDim.x) {
@@ -175,21 +188,31 @@ __global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const f
     if ((int)threadIdx.x < npair) {  // four independent partial sums per thread
 #pragma unroll 4
       for (int rr = 0; rr < kGramRows; rr += 4) {
-        acc[0] = fma((double)tile[pa][rr], (double)tile[pb][rr], acc[0]);
-        acc[1] = fma((double)tile[pa][rr + 1], (double)tile[pb][rr + 1], acc[1]);
-        acc[2] = fma((double)tile[pa][rr + 2], (double)tile[pb][rr + 2], acc[2]);
-        acc[3] = fma((double)tile[pa][rr + 3], (double)tile[pb][rr + 3], acc[3]);
+        gram_acc(tile[pa][rr], tile[pb][rr], h[0], lo[0]);
+        gram_acc(tile[pa][rr + 1], tile[pb][rr + 1], h[1], lo[1]);
+        gram_acc(tile[pa][rr + 2], tile[pb][rr + 2], h[2], lo[2]);
+        gram_acc(tile[pa][rr + 3], tile[pb][rr + 3], h[3], lo[3]);
       }
     }
   }
-  if ((int)threadIdx.x < npair) part[(size_t)blockIdx.x * npair + threadIdx.x] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  if ((int)threadIdx.x < npair) {
+    double s = 0.0;
+    for (int k = 0; k < 4; k++) s += (double)h[k] + (double)lo[k];
+    part[(size_t)blockIdx.x * npair + threadIdx.x] = s;
+  }
 }
 
+// One warp per pair: lane j sums partials j, j+32, ... in order, then a
+// fixed butterfly combines the lanes (the same bits on every run).
 __global__ void gram_reduce_kernel(int nblk, int ncol, const double *__restrict__ part, double *__restrict__ g) {
   const int npair = ncol * (ncol + 1) / 2;
-  for (int t = threadIdx.x; t < npair; t += blockDim.x) {
-    double s = 0.0;
-    for (int b = 0; b < nblk; b++) s += part[(size_t)b * npair + t];
+  const int lane = threadIdx.x & 31;
+  const int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (t >= npair) return;
+  double s = 0.0;
+  for (int b = lane; b < nblk; b += 32) s += part[(size_t)b * npair + t];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+  if (lane == 0) {
     int a = 0, u = t;
     while (u >= ncol - a) { u -= ncol - a; a++; }
     g[a * ncol + a + u] = s;
@@ -252,21 +275,50 @@ __global__ void coeff_kernel(int s, const double *__restrict__ g, const double *
   if (c == 0) { flag[0] = brk; flag[1] = steps; }
 }
 
-// x += Y xh, p = Y ph (FP64 accumulation of the FP32 basis)
+// x += Y xh and p = Y ph: the coefficient (FP64) times basis (FP32)
+// products and their sums in double-float on the FP32 pipes (each
+// coefficient split into two floats; products exact up to the low part's
+// rounding, about 2^-46 relative), then one FP64 add into x per row.
+__device__ __forceinline__ double ss_widen(float f) {  // exact float -> double in integer arithmetic
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xFF;
+  const unsigned int sgn = u & 0x80000000u;
+  const unsigned int bias = e == 0xFF ? (1792u << 20) : (896u << 20);
+  const unsigned int hi = e == 0 ? sgn : (sgn | (((u >> 3) & 0x0FFFFFFFu) + bias));
+  const unsigned int lo = e == 0 ? 0u : (u << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ void ss_mac(float ch, float cl, float v, float &sh, float &sl) {
+  const float p = __fmul_rn(ch, v);
+  float e = __fmaf_rn(ch, v, -p);
+  e = __fmaf_rn(cl, v, e);
+  const float t = __fadd_rn(sh, p), bp = __fadd_rn(t, -sh);
+  const float err = __fadd_rn(__fadd_rn(sh, -__fadd_rn(t, -bp)), __fadd_rn(p, -bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
 __global__ void combine_kernel(int n, int m, const float *__restrict__ y, const double *__restrict__ xh,
                                const double *__restrict__ ph, double *__restrict__ x, double *__restrict__ p) {
-  __shared__ double cx[kMaxCols], cp[kMaxCols];
-  if ((int)threadIdx.x < m) { cx[threadIdx.x] = xh[threadIdx.x]; cp[threadIdx.x] = ph[threadIdx.x]; }
+  __shared__ float cxh[kMaxCols], cxl[kMaxCols], cph[kMaxCols], cpl[kMaxCols];
+  if ((int)threadIdx.x < m) {
+    const double a = xh[threadIdx.x], b = ph[threadIdx.x];
+    cxh[threadIdx.x] = __double2float_rn(a);
+    cxl[threadIdx.x] = __double2float_rn(a - (double)cxh[threadIdx.x]);
+    cph[threadIdx.x] = __double2float_rn(b);
+    cpl[threadIdx.x] = __double2float_rn(b - (double)cph[threadIdx.x]);
+  }
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double sx = x[i], sp = 0.0;
+    float xs = 0.f, xl = 0.f, ps = 0.f, pl = 0.f;
     for (int c = 0; c < m; c++) {
-      const double v = (double)y[(size_t)c * n + i];
-      sx = fma(cx[c], v, sx);
-      sp = fma(cp[c], v, sp);
+      const float v = y[(size_t)c * n + i];
+      ss_mac(cxh[c], cxl[c], v, xs, xl);
+      ss_mac(cph[c], cpl[c], v, ps, pl);
     }
-    x[i] = sx;
-    p[i] = sp;
+    x[i] += ss_widen(xs) + ss_widen(xl);
+    p[i] = ss_widen(ps) + ss_widen(pl);
   }
 }
 
@@ -358,6 +410,16 @@ struct DevBuf {
   ~DevBuf() { cudaFree(p); }
   int alloc(size_t n) {
     SS_TRY(cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)));
+    return kOk;
+  }
+};
+
+// Page-locked host bytes (int-addressed), released on scope exit.
+struct HostBuf {
+  int *p = nullptr;
+  ~HostBuf() { cudaFreeHost(p); }
+  int alloc(size_t bytes) {
+    SS_TRY(cudaMallocHost((void **)&p, bytes));
     return kOk;
   }
 };
@@ -587,7 +649,10 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
   DevBuf<double> dx, db, dr, dp, part, gpart, dg, dth, dsg, dxh, dph, drh;
   DevBuf<float> y;
   DevBuf<int> dflag;
-  if ((rc = dx.alloc(n)) || (rc = db.alloc(n)) || (rc = dr.alloc(n)) || (rc = dp.alloc(n)) || (rc = part.alloc(nb)) ||
+  HostBuf hbuf;  // page-locked: flags (8 ints), then 2 * nb partial sums
+  if ((rc = hbuf.alloc(8 * sizeof(int) + 2 * sizeof(double) * (size_t)nb))) return rc;
+  if ((rc = dx.alloc(n)) || (rc = db.alloc(n)) || (rc = dr.alloc(n)) || (rc = dp.alloc(n)) ||
+      (rc = part.alloc(2 * (size_t)nb)) ||
       (rc = gpart.alloc((size_t)gblk * npair)) || (rc = dg.alloc(m * m)) || (rc = dth.alloc(s)) ||
       (rc = dsg.alloc(s)) || (rc = dxh.alloc(m)) || (rc = dph.alloc(m)) || (rc = drh.alloc(m)) ||
       (rc = y.alloc((size_t)m * n)) || (rc = dflag.alloc(2)))
@@ -621,14 +686,28 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
                                           (float)(1.0 / sg[j]));
     }
     gram_kernel<<<gblk, kThreads>>>(n, m, Y, gpart.p);
-    gram_reduce_kernel<<<1, kThreads>>>(gblk, m, gpart.p, dg.p);
+    gram_reduce_kernel<<<(npair * 32 + kThreads - 1) / kThreads, kThreads>>>(gblk, m, gpart.p, dg.p);
     coeff_kernel<<<1, 32>>>(s, dg.p, dth.p, dsg.p, pn, rn, dxh.p, dph.p, drh.p, dflag.p);
     combine_kernel<<<nb, kThreads>>>(n, m, Y, dxh.p, dph.p, dx.p, dp.p);
+    // true residual (FP64) and |p|^2, then one round trip for the flags,
+    // both sets of partial sums and (with info) the Gram matrix
+    resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+    axpy_norm_kernel<<<nb, kThreads>>>(n, 0.0, dp.p, dp.p, part.p + nb);
     SS_TRY(cudaGetLastError());
+    SS_TRY(cudaMemcpyAsync(hbuf.p, dflag.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, 0));
+    SS_TRY(cudaMemcpyAsync(hbuf.p + 8, part.p, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, 0));
+    if (info) SS_TRY(cudaMemcpyAsync(hg.data(), dg.p, sizeof(double) * m * m, cudaMemcpyDeviceToHost, 0));
+    SS_TRY(cudaStreamSynchronize(0));
     int flag[2];
-    SS_TRY(cudaMemcpy(flag, dflag.p, sizeof flag, cudaMemcpyDeviceToHost));
+    std::memcpy(flag, hbuf.p, sizeof flag);
+    {
+      const double *hp = reinterpret_cast<const double *>(hbuf.p + 8);
+      rr = 0.0;
+      for (int k = 0; k < nb; k++) rr += hp[k];
+      pp = 0.0;
+      for (int k = 0; k < nb; k++) pp += hp[nb + k];
+    }
     if (info) {  // condition number of the P block (the s-step polynomial basis) from its Gram eigenvalues
-      SS_TRY(cudaMemcpy(hg.data(), dg.p, sizeof(double) * m * m, cudaMemcpyDeviceToHost));
       const int mp = s + 1;
       std::vector<double> A((size_t)mp * mp);
       for (int r2 = 0; r2 < mp; r2++)
@@ -669,11 +748,6 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
     breakdowns += flag[0];
     steps += flag[1];
     outer++;
-    // true residual (FP64) and |p|^2
-    resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
-    if ((rc = sum_parts(part.p, nb, &rr))) return rc;
-    axpy_norm_kernel<<<nb, kThreads>>>(n, 0.0, dp.p, dp.p, part.p);
-    if ((rc = sum_parts(part.p, nb, &pp))) return rc;
     if (flag[1] == 0 || !(pp > 0.0)) {  // no progress possible with this basis: restart from r
       SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
       pp = rr;
