@@ -406,6 +406,21 @@ int mpkg_pa1_tasks(int n, const int *ptr, const int *col, const int *part, int n
  * rank, byte-compatible with the reference's files. */
 int mpkg_bufs_prepare(const char *dir);
 
+/* The counts of the reference's work_count tool (mpk2/work_count.c:13-149)
+ * for a prepared MPI-2 directory (ghead_npart_nlevel_nphase with loop.g0
+ * and rank<r>.bufs): doubles communicated (received minus kept on the
+ * rank), ops (row lengths of every rank's local CSR), minops (nlevel *
+ * nnz), nvert (n * nlevel), and *redundant = the (rank, phase, index)
+ * entries both received and computed on the rank (the reference prints
+ * one line for each; 0 for a correct prep; may be NULL). */
+int mpkg_work_count(const char *dir, long *comm, long *ops, long *minops, long *nvert, long *redundant);
+
+/* The label assignment of the MPI-2 and pdmpk preps (mpk2/lapjv.c:366
+ * lapjv(sums, npart, perm)): perm maximises sum_j sums[perm[j]*npart + j]
+ * over permutations, with the reference's tie-breaking (Jonker-Volgenant
+ * steps in the published order). */
+int mpkg_lapjv(const int *sums, int npart, int *perm);
+
 /* Partitioners (METIS is not available): recursive coordinate bisection
  * (coords: dim ints per vertex) and breadth-first recursive bisection. */
 int mpkg_partition_rcb(int n, const int *coords, int dim, int npart, int *part);

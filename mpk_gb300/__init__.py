@@ -127,6 +127,9 @@ def _declare(L):
         "mpkg_tile_prep": (I, [I, P, P, P, I, I, I, C.POINTER(TilesT)]),
         "mpkg_tiles_free": (None, [C.POINTER(TilesT)]),
         "mpkg_pa1_tasks": (I, [I, P, P, P, I, I, I, P, pp, C.POINTER(Lg), C.POINTER(I)]),
+        "mpkg_work_count": (I, [C.c_char_p, C.POINTER(Lg), C.POINTER(Lg), C.POINTER(Lg), C.POINTER(Lg),
+                                C.POINTER(Lg)]),
+        "mpkg_lapjv": (I, [P, I, P]),
         "mpkg_partition_rcb": (I, [I, P, I, I, P]),
         "mpkg_partition_bfs": (I, [I, P, P, I, P]),
         "mpkg_gen_stencil": (I, [C.c_char_p, I, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
@@ -441,6 +444,25 @@ def pa1_tasks(a: Csr, part, npart, nlevel, on_gpu=True):
     _check(lib().mpkg_pa1_tasks(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(part), npart, nlevel, 1 if on_gpu else 0,
                                 _ptr(off), C.byref(ip), C.byref(cnt), C.byref(on)))
     return off, _take(ip, cnt.value, np.int64), bool(on.value)
+
+
+def work_count(dirname):
+    """The reference work_count's counts for a prepared MPI-2 directory
+    (mpk2/work_count.c): dict comm, ops, minops, nvert, redundant."""
+    v = [C.c_long() for _ in range(5)]
+    _check(lib().mpkg_work_count(dirname.encode(), *[C.byref(x) for x in v]))
+    return dict(zip(("comm", "ops", "minops", "nvert", "redundant"), (x.value for x in v)))
+
+
+def lapjv(sums):
+    """The preps' label assignment (mpk2/lapjv.c:366): perm maximising
+    sum_j sums[perm[j], j]."""
+    s = np.ascontiguousarray(sums, dtype=np.int32)
+    npart = s.shape[0]
+    assert s.shape == (npart, npart)
+    perm = np.empty(npart, dtype=np.int32)
+    _check(lib().mpkg_lapjv(_ptr(s), npart, _ptr(perm)))
+    return perm
 
 
 # ---------------------------------------------------------------- plans

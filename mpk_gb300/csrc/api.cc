@@ -1058,3 +1058,90 @@ int mpkg_bufs_prepare(const char *dir) {
 }
 
 }  // extern "C"
+
+// ==========================================================================
+// Verification counts (mpk2/work_count.c) and the label assignment
+// (mpk2/lapjv.c:366 lapjv)
+// ==========================================================================
+extern "C" {
+
+int mpkg_work_count(const char *dir, long *comm, long *ops, long *minops, long *nvert, long *redundant) {
+  clear_error();
+  if (!dir || !comm || !ops || !minops || !nvert) return fail(kEInval, "null argument");
+  int npart, nlevel, nphase;
+  if (!parse_dir(dir, &npart, &nlevel, &nphase)) {
+    dir_name_error(const_cast<char *>(dir));
+    return kEFormat;
+  }
+  crs0_t *g = read_matrix(const_cast<char *>(dir));
+  if (!g) return kEIo;
+  const int n = g->n;
+  const long nnz = g->ptr[n];
+  del_crs(g);
+  std::vector<RankBuffers> bufs(npart);
+  for (int r = 0; r < npart; r++) {
+    int rc = read_rank_buffers(std::string(dir) + "/rank" + std::to_string(r) + ".bufs", &bufs[r]);
+    if (rc) return rc;
+    if (bufs[r].n != n || bufs[r].npart != npart || bufs[r].nlevel != nlevel || bufs[r].nphase != nphase)
+      return fail(kEFormat, "rank " + std::to_string(r) + ": buffer header does not match " + dir);
+  }
+  int rc = check_rank_buffers(bufs);
+  if (rc) return rc;
+  // count_comm: received doubles minus those a rank keeps for itself
+  long c = 0, o = 0, red = 0;
+  for (int ph = 0; ph <= nphase; ph++)
+    for (int p = 0; p < npart; p++) {
+      const RankBuffers &b = bufs[p];
+      const long self = (long)npart * ph + p;
+      if (b.sendcounts[self] != b.recvcounts[self]) return fail(kEFormat, "send/receive counts differ");
+      c += b.rcount[ph] - b.recvcounts[self];
+    }
+  // count_ops: the row lengths of every rank's local CSR, all phases
+  for (int ph = 0; ph <= nphase; ph++)
+    for (int p = 0; p < npart; p++) {
+      const RankBuffers &b = bufs[p];
+      const long *mp = b.mptr_buf.data() + b.mptr_offsets[ph];
+      for (int t = 0; t < b.mcount[ph]; t++) o += mp[t + 1] - mp[t];
+    }
+  // redundancy: an index received in some phase that the rank also
+  // computes (received once and computed once: the reference's tmp == 3)
+  const long size = (long)n * (nlevel + 1);
+  std::vector<unsigned char> computed(size), got(size);
+  for (int p = 0; p < npart; p++) {
+    const RankBuffers &b = bufs[p];
+    std::fill(computed.begin(), computed.end(), 0);
+    for (int ph = 0; ph <= nphase; ph++)
+      for (int mi = 0; mi < b.mcount[ph]; mi++) {
+        const long e = b.idx_buf[b.mbuf_offsets[ph] + mi];
+        if (e < 0 || e >= size) return fail(kEFormat, "buffer index out of range");
+        if (computed[e] < 255) computed[e]++;
+      }
+    for (int ph = 0; ph <= nphase; ph++) {
+      std::fill(got.begin(), got.end(), 0);
+      for (int ri = 0; ri < b.rcount[ph]; ri++) {
+        const long e = b.idx_buf[b.rbuf_offsets[ph] + ri];
+        if (e < 0 || e >= size) return fail(kEFormat, "buffer index out of range");
+        if (got[e] < 255) got[e]++;
+      }
+      for (long e = 0; e < size; e++) red += got[e] == 1 && computed[e] == 1;
+    }
+  }
+  *comm = c;
+  *ops = o;
+  *minops = (long)nlevel * nnz;
+  *nvert = (long)n * nlevel;
+  if (redundant) *redundant = red;
+  return kOk;
+}
+
+int mpkg_lapjv(const int *sums, int npart, int *perm) {
+  clear_error();
+  if (!sums || !perm || npart <= 0) return fail(kEInval, "bad argument");
+  std::vector<long> s(sums, sums + (long)npart * npart);
+  std::vector<int> pv;
+  assign_max_trace(s, npart, &pv);
+  std::copy(pv.begin(), pv.end(), perm);
+  return kOk;
+}
+
+}  // extern "C"

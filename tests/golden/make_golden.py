@@ -11,6 +11,7 @@ scripts drive them (mpk2/driver.c, mpk2/mpktest.c, mpk2/verify_val.c):
   exec_mpk / vexec_mpk      -> vv for a seeded x (1/deg and valued operator)
   verify_val                -> gold_result.bin (x = 1, valued operator)
   pdmpk prep (apps/prep.cc) -> per-rank buf.bin / results.bin (pdmpk.npz)
+  lapjv, work_count         -> lapjv.npz, work_count.json (verification tools)
 
 Inputs (graphs, partitions, x) come from the product's generators and
 partitioners; METIS is not available, so partitions are recursive
@@ -19,10 +20,12 @@ fixture.  The reference binaries here are x86-64 gcc -O2 builds, which do
 not contract a*b+c, so every floating-point fixture is in the oracle's
 "separate" arithmetic mode.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py                # everything
+    python tests/golden/make_golden.py verification   # lapjv + work_count only
 """
 import ctypes as C
 import hashlib
+import json
 import os
 import shutil
 import subprocess
@@ -193,17 +196,72 @@ def make_pdmpk(tmp):
     return out
 
 
+def make_verification(tmp):
+    """Known answers of the reference's verification tools:
+    * lapjv.npz: lapjv (mpk2/lapjv.c:366) permutations on seeded square
+      matrices, half of them with many ties (entries in {0, 1, 2});
+    * work_count.json: mpk2/work_count's summary (communication, ops,
+      minops, nvert) and its redundancy lines for every golden case that
+      carries rank buffers, run on a directory rebuilt from the fixture."""
+    R = O.ref()
+    R.lapjv.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(20191129)
+    sizes, sums, perms = [], [], []
+    for n in (2, 3, 4, 5, 6, 8, 12, 16):
+        for t in range(40):
+            s = np.ascontiguousarray(rng.integers(0, 3 if t % 2 else 10000, (n, n)), dtype=np.int32)
+            p = np.zeros(n, dtype=np.int32)
+            R.lapjv(s.ctypes.data, n, p.ctypes.data)
+            sizes.append(n)
+            sums.append(s.ravel())
+            perms.append(p)
+    np.savez_compressed(os.path.join(HERE, "lapjv.npz"), sizes=np.array(sizes, dtype=np.int32),
+                        sums=np.concatenate(sums), perms=np.concatenate(perms))
+    counts = {}
+    for case in CASES:
+        g = np.load(os.path.join(HERE, case["name"] + ".npz"))
+        if "bufs0" not in g:
+            continue
+        a = loop_matrix(case)
+        name, npart, nphase = case["name"], case["npart"], case["nphase"]
+        d = os.path.join(tmp, name)
+        os.makedirs(d)
+        a.write_metis(os.path.join(d, "loop.g0"), ne=(a.nnz + a.n) // 2)
+        for r in range(npart):
+            g[f"bufs{r}"].tofile(os.path.join(d, f"rank{r}.bufs"))
+        for ph in range(max(nphase, 1)):
+            np.savetxt(os.path.join(d, f"g{ph}.part.{npart}"), g["parts"][ph], fmt="%d")
+        for ph in range(nphase):
+            np.savetxt(os.path.join(d, f"l{ph}"), g["levels"][ph], fmt="%d")
+        g["skirt"].tofile(os.path.join(d, f"s{nphase}"))
+        a.write_values(os.path.join(tmp, name.split("_")[0] + ".loop.val"))
+        out = subprocess.run([O.ref_tool("work_count"), name], cwd=tmp, check=True, capture_output=True, text=True)
+        with open(os.path.join(tmp, f"summary-{name}.log")) as f:
+            f.readline()
+            comm, ops, minops, nvert = (int(v) for v in f.readline().split())
+        counts[name] = dict(comm=comm, ops=ops, minops=minops, nvert=nvert,
+                            redundant=out.stdout.count("!!!Redundancy"))
+    with open(os.path.join(HERE, "work_count.json"), "w") as f:
+        json.dump(counts, f, indent=1)
+        f.write("\n")
+    return counts
+
+
 def main():
     O.build()
     if not O.ref_available():
         sys.exit("reference sources not available: cannot regenerate golden fixtures")
     tmp = tempfile.mkdtemp()
     try:
+        if sys.argv[1:] == ["verification"]:  # only the verification-tool answers
+            print(make_verification(tmp))
+            return
         for case in CASES:
             out = make(case, tmp)
             print(case["name"], "n", out["n"], "tasks", len(out["idx"]))
         out = make_pdmpk(tmp)
         print("pdmpk", len(out), "arrays")
+        print(make_verification(tempfile.mkdtemp(dir=tmp)))
     finally:
         shutil.rmtree(tmp)
 
