@@ -12,6 +12,7 @@ scripts drive them (mpk2/driver.c, mpk2/mpktest.c, mpk2/verify_val.c):
   verify_val                -> gold_result.bin (x = 1, valued operator)
   pdmpk prep (apps/prep.cc) -> per-rank buf.bin / results.bin (pdmpk.npz)
   lapjv, work_count         -> lapjv.npz, work_count.json (verification tools)
+  pdmpk prep, CTest shapes  -> pdmpk_ctest.json (hashes of every rank's files)
 
 Inputs (graphs, partitions, x) come from the product's generators and
 partitioners; METIS is not available, so partitions are recursive
@@ -22,6 +23,7 @@ not contract a*b+c, so every floating-point fixture is in the oracle's
 
     python tests/golden/make_golden.py                # everything
     python tests/golden/make_golden.py verification   # lapjv + work_count only
+    python tests/golden/make_golden.py ctest          # pdmpk CTest shapes only
 """
 import ctypes as C
 import hashlib
@@ -196,6 +198,35 @@ def make_pdmpk(tmp):
     return out
 
 
+# The reference's CTest shapes (tests/CMakeLists.txt:3-42): gen2 meshes
+# written as pattern Matrix Market files (1/deg values), mirror 5, weight 3.
+PD_CTEST = [("m5p", 4, 4, 4)] + [(t, size, P, L) for t in ("m5p", "m9p") for size in (10, 100)
+                                 for P in (4, 8) for L in (10, 20)]
+
+
+def make_pdmpk_ctest(tmp):
+    """sha256 of the reference prep's per-rank buf.bin / results.bin for
+    every CTest shape (pdmpk_ctest.json)."""
+    d = os.path.join(tmp, "ctest")
+    os.makedirs(d)
+    out = {}
+    for t, size, P, L in PD_CTEST:
+        m = f"{t}{size}"
+        M.Csr.stencil(t, size).write_mtx(os.path.join(d, m + ".mtx"), pattern=True)
+        run([O.ref_tool("pdmpk_prep"), "--matrix", m + ".mtx", "--npart", str(P), "--nlevel", str(L),
+             "--mirror", "5", "--weight", "3", "--keepfiles"], cwd=d)
+        ranks = []
+        for r in range(P):
+            stem = os.path.join(d, f"{m}.mtx-np{P}-nl{L}-mm5-wm3-r{r}-ref-oracle")
+            ranks.append([hashlib.sha256(open(stem + ext, "rb").read()).hexdigest()
+                          for ext in (".buf.bin", ".results.bin")])
+        out[f"{m}_{P}_{L}"] = ranks
+    with open(os.path.join(HERE, "pdmpk_ctest.json"), "w") as f:
+        json.dump(out, f, indent=1)
+        f.write("\n")
+    return out
+
+
 def make_verification(tmp):
     """Known answers of the reference's verification tools:
     * lapjv.npz: lapjv (mpk2/lapjv.c:366) permutations on seeded square
@@ -256,12 +287,16 @@ def main():
         if sys.argv[1:] == ["verification"]:  # only the verification-tool answers
             print(make_verification(tmp))
             return
+        if sys.argv[1:] == ["ctest"]:  # only the pdmpk CTest shapes
+            print(len(make_pdmpk_ctest(tmp)), "pdmpk CTest shapes")
+            return
         for case in CASES:
             out = make(case, tmp)
             print(case["name"], "n", out["n"], "tasks", len(out["idx"]))
         out = make_pdmpk(tmp)
         print("pdmpk", len(out), "arrays")
         print(make_verification(tempfile.mkdtemp(dir=tmp)))
+        print(len(make_pdmpk_ctest(tmp)), "pdmpk CTest shapes")
     finally:
         shutil.rmtree(tmp)
 

@@ -61,3 +61,27 @@ def fields(data):
         o += 8 + c * size
     assert o == len(data)
     return out
+
+
+def ctest():
+    """The reference's CTest shapes with the sha256 of every rank's
+    (buf.bin, results.bin) from the reference prep: {"m9p100_8_20": [...]}."""
+    import json
+    with open(os.path.join(GOLDEN, "pdmpk_ctest.json")) as f:
+        return json.load(f)
+
+
+def ctest_prep(key, d):
+    """The product's prep of one CTest shape (pattern MTX of the gen2 mesh,
+    mirror 5, weight 3); returns (matrix, buf paths, results paths)."""
+    import mpk_gb300 as M
+    m, P, L = key.split("_")
+    P, L = int(P), int(L)
+    t, size = m[:3], int(m[3:])
+    path = os.path.join(d, m + ".mtx")
+    M.Csr.stencil(t, size).write_mtx(path, pattern=True)
+    a = M.Csr.read_mtx(path)
+    bp = [os.path.join(d, f"{key}-r{r}.buf.bin") for r in range(P)]
+    rp = [os.path.join(d, f"{key}-r{r}.results.bin") for r in range(P)]
+    M.pdmpk_prep(a, P, L, bp, rp, mirror=5, weight=3)
+    return a, bp, rp

@@ -69,3 +69,24 @@ def test_pdmpk_device_path(tmp_path, gpu):
     plan.sync()
     got = vv[L * a.n:].cpu().numpy()
     assert got.tobytes() == O.pd_exec(bp, rp, x, O.MODE_SEPARATE).tobytes()
+
+
+@pytest.mark.parametrize("key", sorted(PC.ctest()))
+def test_pdmpk_ctest_shapes_on_gpu(key, tmp_path, gpu):
+    """Every CTest shape (tests/CMakeLists.txt:3-42) prepared by the product
+    runs on one GPU bit for bit as the oracle's all-rank AsyncExec, and
+    passes the reference's check (apps/check.cc:83: cos^2 against the
+    chain within 1e-9)."""
+    a, bp, rp = PC.ctest_prep(key, str(tmp_path))
+    L = int(key.split("_")[2])
+    x = M.uniform(17, a.n)
+    plan = M.Plan.pdmpk(bp, rp, arith=M.ARITH_FMA)
+    vv = np.zeros((L + 1) * a.n)
+    vv[:a.n] = x
+    plan.exec_host(vv)
+    plan.close()
+    got = vv[L * a.n:]
+    assert got.tobytes() == O.pd_exec(bp, rp, x, O.MODE_FMA).tobytes()
+    gold = O.mpk(a.ptr, a.col, a.val, x, L, O.MODE_FMA)[L * a.n:]
+    cos2 = float(np.dot(got, gold)) ** 2 / (float(np.dot(got, got)) * float(np.dot(gold, gold)))
+    assert abs(cos2 - 1.0) < 1e-9

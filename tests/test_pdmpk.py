@@ -96,3 +96,18 @@ def test_malformed_buffers_are_rejected(tmp_path):
     with pytest.raises(M.MpkError) as e:  # missing rank file
         M.pdmpk_info(bp[:1] + [str(tmp_path / "nope")] + bp[2:], rp)
     assert e.value.code == M.EIO
+
+
+CTEST = PC.ctest()
+
+
+@pytest.mark.parametrize("key", sorted(CTEST))
+def test_prep_ctest_shapes_byte_identical(key, tmp_path):
+    """The reference's CTest shapes (tests/CMakeLists.txt:3-42: m5p/m9p
+    meshes of size 10 and 100, 4 and 8 parts, 10 and 20 levels, mirror 5,
+    weight 3, plus m5p4): the product's prep writes the reference prep's
+    files, byte for byte (compared by sha256)."""
+    import hashlib
+    a, bp, rp = PC.ctest_prep(key, str(tmp_path))
+    got = [[hashlib.sha256(open(p, "rb").read()).hexdigest() for p in (b, r)] for b, r in zip(bp, rp)]
+    assert got == CTEST[key]
