@@ -812,7 +812,9 @@ struct WaveArgs {
   int stage_len_bytes;         // this many bytes, then per slice its start (int) and flag (byte),
   int stage_slices;            // room for this many slices)
   const int *row_lo;           // nblk + 1
-  const int *dep_lo, *dep_hi;  // per CTA: CTAs it reads from or that read from it
+  const int *dep_ptr;          // nblk + 1: CTA b waits for dep_idx[dep_ptr[b] .. dep_ptr[b+1]):
+  const int *dep_idx;          // the other CTAs owning columns of its rows (and, for the ring
+                               // forms, those reading its rows)
   unsigned int *flags;         // per CTA: last level published
   int *err;
   // fixed-point form (1/deg operator): the ring holds int64 values v * 2^S
@@ -822,8 +824,9 @@ struct WaveArgs {
 };
 
 __device__ __forceinline__ bool wave_wait(const WaveArgs &a, int b, unsigned int want, int *s_abort) {
-  const int lo = a.dep_lo[b], hi = a.dep_hi[b];
-  for (int c = lo + (int)threadIdx.x; c <= hi; c += blockDim.x) {
+  const int lo = a.dep_ptr[b], hi = a.dep_ptr[b + 1];
+  for (int k = lo + (int)threadIdx.x; k < hi; k += blockDim.x) {
+    const int c = a.dep_idx[k];
     long spins = 0;
     while (ld_acquire(a.flags + c) < want + a.stall) {
       if (++spins > kSpinLimit || *((volatile int *)a.err)) {
@@ -2585,27 +2588,37 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
     }
     // CTA owning column c: the last b' with lo[b'] <= c (empty ranges skipped)
     auto owner = [&](int c) { return (int)(std::upper_bound(lo.begin(), lo.end() - 1, c) - lo.begin()) - 1; };
-    std::vector<int> dlo(grid), dhi(grid);
-    for (int b = 0; b < grid; b++) {
-      int cmin = INT32_MAX, cmax = -1;
-      for (long q = ptr[lo[b]]; q < ptr[lo[b + 1]]; q++) {
-        cmin = std::min(cmin, col[q]);
-        cmax = std::max(cmax, col[q]);
-      }
-      dlo[b] = dhi[b] = b;
-      if (cmax >= 0) {
-        dlo[b] = std::min(b, owner(cmin));
-        dhi[b] = std::max(b, owner(cmax));
-      }
+    // the exact set of other CTAs whose rows CTA b reads (a CTA's own rows
+    // of the previous level are ordered by its barrier)
+    std::vector<std::vector<int>> reads(grid);
+    {
+      std::vector<int> seen(grid, -1);
+      for (int b = 0; b < grid; b++)
+        for (long q = ptr[lo[b]]; q < ptr[lo[b + 1]]; q++) {
+          const int c = col[q];
+          if (c >= lo[b] && c < lo[b + 1]) continue;
+          const int o = owner(c);
+          if (seen[o] != b) { seen[o] = b; reads[b].push_back(o); }
+        }
     }
-    // symmetric closure: also wait for the CTAs that read this one's rows
-    // (the double-float ring reuses a slot two levels later)
-    std::vector<int> slo(dlo), shi(dhi);
-    for (int c = 0; c < grid; c++)
-      for (int b = dlo[c]; b <= dhi[c]; b++) {
-        slo[b] = std::min(slo[b], c);
-        shi[b] = std::max(shi[b], c);
+    const bool ring = arith == MPKG_ARITH_DF64 || arith == MPKG_ARITH_FIXED;
+    std::vector<std::vector<int>> waits(reads);
+    if (ring)  // symmetric closure: a ring slot is reused two levels later, so
+               // also wait for the CTAs that read this one's rows
+      for (int c = 0; c < grid; c++)
+        for (int b : reads[c]) waits[b].push_back(c);
+    std::vector<int> dptr(grid + 1, 0), didx;
+    long reach = 0;
+    for (int b = 0; b < grid; b++) {
+      std::sort(waits[b].begin(), waits[b].end());
+      waits[b].erase(std::unique(waits[b].begin(), waits[b].end()), waits[b].end());
+      for (int c : waits[b]) {
+        didx.push_back(c);
+        reach = std::max<long>(reach, std::abs(c - b));
       }
+      dptr[b + 1] = (int)didx.size();
+    }
+    if (didx.empty()) didx.push_back(0);
     p->wave_grid = grid;
     p->pipe_grid = grid;
     WaveArgs &w = p->wave;
@@ -2642,12 +2655,11 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
       }
       w.sval2 = sv2;
     }
-    const bool df = arith == MPKG_ARITH_DF64 || arith == MPKG_ARITH_FIXED;  // ring of two slots
     if (!rc) rc = dev_copy(p, &d_lo, lo.data(), lo.size());
-    if (!rc) rc = dev_copy(p, &d_dlo, (df ? slo : dlo).data(), dlo.size());
-    if (!rc) rc = dev_copy(p, &d_dhi, (df ? shi : dhi).data(), dhi.size());
+    if (!rc) rc = dev_copy(p, &d_dlo, dptr.data(), dptr.size());
+    if (!rc) rc = dev_copy(p, &d_dhi, didx.data(), didx.size());
     if (!rc) rc = dev_alloc(p, &w.flags, (size_t)grid);
-    if (!rc && df) rc = dev_alloc(p, &w.ring, (size_t)2 * n);
+    if (!rc && ring) rc = dev_alloc(p, &w.ring, (size_t)2 * n);
     if (!rc && arith == MPKG_ARITH_FIXED) {
       std::vector<unsigned long long> mul(256, 0);
       for (int d = 2; d < 256; d++) mul[d] = ~0ull / (unsigned long long)d + 1;  // ceil(2^64 / d)
@@ -2656,10 +2668,7 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
       if (!rc && cudaMemset(w.fix_word, 0, sizeof(unsigned long long)) != cudaSuccess)
         rc = fail(kECuda, "memset failed");
     }
-    w.row_lo = d_lo; w.dep_lo = d_dlo; w.dep_hi = d_dhi;
-    long reach = 0;
-    for (int b = 0; b < grid; b++)
-      reach = std::max<long>(reach, std::max(b - (df ? slo : dlo)[b], (df ? shi : dhi)[b] - b));
+    w.row_lo = d_lo; w.dep_ptr = d_dlo; w.dep_idx = d_dhi;
     p->pipe_reach = (int)reach;
     p->rows_computed = (long)n * nlevel;
   }
