@@ -1203,7 +1203,7 @@ __global__ void __launch_bounds__(256, 5) wave_fix_kernel(WaveArgs a) {
 // mix_pipe_kernel, so both give identical bits).  Levels live at fresh
 // addresses of the FP32 vv.
 template <typename VT, bool REL, bool UNI>
-__global__ void __launch_bounds__(256) wave_mix_kernel(WaveArgs a, const VT *__restrict__ sv, float *vf, float scale) {
+__global__ void __launch_bounds__(256, 5) wave_mix_kernel(WaveArgs a, const VT *__restrict__ sv, float *vf, float scale) {
   __shared__ int s_abort;
   if (threadIdx.x == 0) s_abort = 0;
   __syncthreads();
@@ -2971,7 +2971,7 @@ const void *mix_wave_kernel_ptr(int value_type, bool rel, bool uni) {
 int mixed_wave_setup(mpkg_plan *p, int n, const int *ptr, const int *col, const double *val, int nlevel,
                      int value_type) {
   mpkg_plan *w = nullptr;
-  int rc = plan_wave_impl(n, ptr, col, val, nlevel, MPKG_ARITH_FMA, -1, &w);
+  int rc = plan_wave_impl(n, ptr, col, val, nlevel, MPKG_ARITH_FMA, value_type, &w);
   if (rc) return rc;
   p->inner = w;
   int per_sm = 0, nsm = 0;
