@@ -775,11 +775,13 @@ __global__ void __launch_bounds__(256) bufs_phase_kernel(int list_base, const lo
 // Wavefront executor: one persistent (cooperative) launch; CTA b owns the
 // contiguous rows [row_lo[b], row_lo[b+1]) (equal nonzeros) at every level
 // and computes level l as soon as the CTAs owning the columns those rows
-// read (dep_lo[b]..dep_hi[b]) have published level l-1.  No grid-wide
-// barrier and no redundant rows; the matrix slices stay in L2 across
-// levels.  Every level is written to a fresh address range (vv, and in
-// double-float mode one float2 shadow level per level), so L1 never holds
-// a stale copy of data another SM produced during the launch.
+// read (the plan's exact list dep_idx[dep_ptr[b] ..)) have published level
+// l-1.  No grid-wide barrier and no redundant rows; the matrix slices stay
+// in L2 across levels.  FP64 levels are written to fresh addresses of vv;
+// the double-float and fixed-point forms carry levels in a two-slot ring,
+// reused two levels later only after the CTAs reading this CTA's rows have
+// moved on (their flags are in the list too), and read after an acquire
+// of the writers' flags, so L1 never serves a stale line.
 // ------------------------------------------------------------------------
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
@@ -1251,7 +1253,8 @@ struct BatchArgs {
   const float *val;
   float *vb;                   // (nlevel + 1) * N * nrhs, level 0 = input
   const int *row_lo;           // ngroup * (nblk + 1)
-  const int *dep_lo, *dep_hi;  // ngroup * nblk
+  const int *dep_ptr;          // ngroup * nblk + 1: CTA b of group g waits for
+  const int *dep_idx;          // dep_idx[dep_ptr[g*nblk+b] ..), the other CTAs owning its columns
   unsigned int *flags;
   int *err;
 };
@@ -1294,10 +1297,11 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
   for (int g = 0; g < a.ngroup; g++) {
     const int r0 = a.row_lo[(size_t)g * (a.nblk + 1) + b], r1 = a.row_lo[(size_t)g * (a.nblk + 1) + b + 1];
     const unsigned tag = a.base + (unsigned)g * (unsigned)(a.nlevel + 1);
-    const int dlo = a.dep_lo[(size_t)g * a.nblk + b], dhi = a.dep_hi[(size_t)g * a.nblk + b];
+    const int dlo = a.dep_ptr[(size_t)g * a.nblk + b], dhi = a.dep_ptr[(size_t)g * a.nblk + b + 1];
     for (int l = 1; l <= a.nlevel; l++) {
       if (l > 1) {  // the CTAs owning this range's columns have published level l-1 of group g
-        for (int c = dlo + (int)threadIdx.x; c <= dhi; c += blockDim.x) {
+        for (int k = dlo + (int)threadIdx.x; k < dhi; k += blockDim.x) {
+          const int c = a.dep_idx[k];
           long spins = 0;
           while (ld_acquire(a.flags + c) < tag + (unsigned)(l - 1) + a.stall) {
             if (++spins > kSpinLimit || *((volatile int *)a.err)) {
@@ -1811,7 +1815,7 @@ struct BatchHost {
 // levels of vectors); per group, CTA row ranges of equal nonzeros and the
 // CTAs owning each range's columns.
 void batch_layout(const BatchHost &h, int nrhs, long budget, int grid, std::vector<int> *row_lo,
-                  std::vector<int> *dlo, std::vector<int> *dhi, int *ngroup) {
+                  std::vector<int> *dptr, std::vector<int> *didx, int *ngroup) {
   const int nmat = (int)h.mat_row0.size() - 1;
   std::vector<long> g0(1, 0);
   long bytes = 0;
@@ -1827,8 +1831,9 @@ void batch_layout(const BatchHost &h, int nrhs, long budget, int grid, std::vect
   g0.push_back(h.N);
   *ngroup = (int)g0.size() - 1;
   row_lo->assign((size_t)*ngroup * (grid + 1), 0);
-  dlo->assign((size_t)*ngroup * grid, 0);
-  dhi->assign((size_t)*ngroup * grid, 0);
+  dptr->assign((size_t)*ngroup * grid + 1, 0);
+  didx->clear();
+  std::vector<int> seen(grid, -1);
   for (int g = 0; g < *ngroup; g++) {
     int *lo = row_lo->data() + (size_t)g * (grid + 1);
     const long a = g0[g], z = g0[g + 1];
@@ -1840,18 +1845,23 @@ void batch_layout(const BatchHost &h, int nrhs, long budget, int grid, std::vect
       lo[b] = std::max(std::min(r, (int)z), lo[b - 1]);
     }
     lo[grid] = (int)z;
+    // the exact set of other CTAs whose rows CTA b reads (its own rows of
+    // the previous level are ordered by its barrier)
     for (int b = 0; b < grid; b++) {
-      int cmin = INT32_MAX, cmax = -1;
+      const size_t u = (size_t)g * grid + b;
+      const size_t first = didx->size();
       for (long q = h.ptr[lo[b]]; q < h.ptr[lo[b + 1]]; q++) {
-        cmin = std::min(cmin, h.col[q]);
-        cmax = std::max(cmax, h.col[q]);
+        const int c = h.col[q];
+        if (c >= lo[b] && c < lo[b + 1]) continue;
+        const int o = (int)(std::upper_bound(lo, lo + grid, c) - lo) - 1;  // last CTA starting at or before c
+        if (seen[o] != (int)u) { seen[o] = (int)u; didx->push_back(o); }
       }
-      int &L = (*dlo)[(size_t)g * grid + b], &H = (*dhi)[(size_t)g * grid + b];
-      if (cmax < 0) { L = H = b; continue; }
-      L = (int)(std::upper_bound(lo, lo + grid, cmin) - lo) - 1;
-      H = (int)(std::upper_bound(lo, lo + grid, cmax) - lo) - 1;
+      std::sort(didx->begin() + first, didx->end());
+      (*dptr)[u + 1] = (int)didx->size();
     }
+    std::fill(seen.begin(), seen.end(), -1);
   }
+  if (didx->empty()) didx->push_back(0);
 }
 
 int batch_launch_raw(mpkg_plan *p, float *d_vb, cudaStream_t st, bool capture) {
@@ -2697,7 +2707,7 @@ int batch_configure(mpkg_plan *p, const BatchHost &h, int lpr, int vw, long budg
   if (!rc) rc = dev_copy(p, &d_dhi, dhi.data(), dhi.size());
   if (!rc) rc = dev_alloc(p, &d_flags, (size_t)grid);
   if (rc) return rc;
-  a.row_lo = d_lo; a.dep_lo = d_dlo; a.dep_hi = d_dhi; a.flags = d_flags;
+  a.row_lo = d_lo; a.dep_ptr = d_dlo; a.dep_idx = d_dhi; a.flags = d_flags;
   a.nblk = grid; a.ngroup = ngroup; a.base = 0;
   p->batch_lpr = lpr; p->batch_vw = vw; p->batch_group_bytes = budget;
   p->pipe_grid = grid;
