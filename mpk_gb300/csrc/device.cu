@@ -980,7 +980,6 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
   if (STAGE) wave_stage(a, r0, r1, wave_smem);
   __syncthreads();
-  const long e_lo = STAGE && r0 < r1 ? a.rel_off[r0 >> 5] : 0;
   const short *s_rel = reinterpret_cast<const short *>(wave_smem);
   const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -1027,7 +1026,6 @@ __global__ void __launch_bounds__(256, 5) wave_df_kernel(WaveArgs a) {
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
   if (STAGE) wave_stage(a, r0, r1, wave_smem);
   __syncthreads();
-  const long e_lo = STAGE && r0 < r1 ? a.rel_off[r0 >> 5] : 0;
   const short *s_rel = reinterpret_cast<const short *>(wave_smem);
   const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -1129,7 +1127,6 @@ __global__ void __launch_bounds__(256, 5) wave_fix_kernel(WaveArgs a) {
   const int b = blockIdx.x, r0 = a.row_lo[b], r1 = a.row_lo[b + 1];
   if (STAGE) wave_stage(a, r0, r1, wave_smem);
   __syncthreads();
-  const long e_lo = STAGE && r0 < r1 ? a.rel_off[r0 >> 5] : 0;
   const short *s_rel = reinterpret_cast<const short *>(wave_smem);
   const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -1452,11 +1449,6 @@ __global__ void __launch_bounds__(kPipeThreads) mix_pipe_kernel(MixArgs m) {
       pipe_publish(a, c, l);
     }
   }
-}
-
-__global__ void copy_kernel(const double *__restrict__ src, double *__restrict__ dst, long n) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    dst[i] = src[i];
 }
 
 }  // namespace
