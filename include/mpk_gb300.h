@@ -308,7 +308,8 @@ int mpkg_sync(mpkg_plan *p, void *stream);
 void mpkg_plan_destroy(mpkg_plan *p);
 
 /* Test hook for failure detection: makes every later dependency wait of a
- * pipeline plan wait for `extra_levels` levels more than exist, so the
+ * pipeline, wavefront, mixed-wavefront or batched plan wait for
+ * `extra_levels` levels more than exist, so the
  * bounded waits give up (about a second) and mpkg_sync returns
  * MPKG_ETIMEOUT with the context still usable; 0 restores normal waits. */
 int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels);

@@ -3195,10 +3195,21 @@ int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream) {
 }
 
 int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels) {
-  if (!p || (p->exec != MPKG_EXEC_PIPE && p->exec != MPKG_EXEC_WAVE) || extra_levels < 0 || extra_levels > 1000)
-    return fail(kEInval, "stall hook needs a pipeline or wavefront plan and 0 <= extra <= 1000");
+  const bool mixed_wave = p && p->exec == MPKG_EXEC_MIXED && p->inner;
+  if (!p || (p->exec != MPKG_EXEC_PIPE && p->exec != MPKG_EXEC_WAVE && p->exec != MPKG_EXEC_BATCH && !mixed_wave) ||
+      extra_levels < 0 || extra_levels > 1000)
+    return fail(kEInval,
+                "stall hook needs a pipeline, wavefront, mixed-wavefront or batched plan and 0 <= extra <= 1000");
   p->pipe.stall = (uint32_t)extra_levels;
   p->wave.stall = (uint32_t)extra_levels;
+  if (mixed_wave) p->inner->wave.stall = (uint32_t)extra_levels;
+  if (p->exec == MPKG_EXEC_BATCH) {  // the replayed graph holds the launch's arguments: capture again
+    p->batch.stall = (uint32_t)extra_levels;
+    if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    p->graph_ok = false;
+    p->graph_key = nullptr;
+  }
   return kOk;
 }
 

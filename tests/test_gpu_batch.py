@@ -79,3 +79,22 @@ def test_batch_graph_replay_device(small_batch, gpu):
         plan.sync()
     assert plan.batch_info()["graph"] == 1
     assert d.cpu().numpy().tobytes() == _oracle(mats, X, k).tobytes()
+
+
+def test_batch_wait_times_out_and_recovers(small_batch, gpu):
+    """The batched form's bounded waits give up on a flag that is never set
+    (ETIMEOUT) and the same plan, its graph captured again, then runs bit
+    for bit."""
+    mats, k = small_batch, 6
+    X = _inputs(mats, 16, 9)
+    plan = M.Plan.batch(mats, 16, k, tune=False)
+    plan.debug_stall(100)
+    vb = np.zeros((k + 1,) + X.shape, dtype=np.float32)
+    vb[0] = X
+    with pytest.raises(M.MpkError) as e:
+        plan.exec_batch_host(vb)
+    assert e.value.code == M.ETIMEOUT
+    plan.debug_stall(0)
+    vb[1:] = 0
+    plan.exec_batch_host(vb)
+    assert vb.tobytes() == _oracle(mats, X, k).tobytes()

@@ -67,3 +67,26 @@ def test_mixed_runs_on_wavefront_schedule(gpu):
             plan = M.Plan.mixed(a, 6, vt)
             assert plan.info()["pipe_chunk"] == 0
             plan.close()
+
+
+def test_mixed_wait_times_out_and_recovers(gpu):
+    """The mixed wavefront's bounded waits give up on a flag that is never
+    set (ETIMEOUT, context usable) and the same plan then runs correctly."""
+    a = M.Csr.laplacian(48, 40, 32, diag=6.0, off=-1.0)
+    x = M.uniform(5, a.n)
+    plan = M.Plan.mixed(a, 6, M.VALUE_F32)
+    assert plan.info()["pipe_chunk"] == 0  # the wavefront schedule
+    plan.debug_stall(100)
+    import torch
+    d = torch.zeros(7 * a.n, dtype=torch.float32, device="cuda")
+    d[:a.n] = torch.from_numpy(x.astype(np.float32)).cuda()
+    torch.cuda.synchronize()
+    plan.exec_mixed_device(d.data_ptr())
+    with pytest.raises(M.MpkError) as e:
+        plan.sync()
+    assert e.value.code == M.ETIMEOUT
+    plan.debug_stall(0)
+    plan.close()
+    v, e_, _ = run_mixed(a, 6, M.VALUE_F32, x)
+    want = O.mpk(a.ptr, a.col, a.val, x, 6, O.MODE_FMA)
+    assert max(rel_errors(v, want, a.n, 6)) <= MIXED_TOL
