@@ -168,7 +168,9 @@ __device__ __forceinline__ void gram_acc(float a, float b, float &sh, float &sl)
 
 __global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const float *__restrict__ y,
                                                         double *__restrict__ part) {
-  __shared__ float tile[kMaxCols][kGramRows];
+  // one padding word per column: the threads of a warp read up to 17
+  // different columns at the same row, which would otherwise share a bank
+  __shared__ float tile[kMaxCols][kGramRows + 1];
   const int npair = ncol * (ncol + 1) / 2;
   int pa = 0, pb = 0;
   {
