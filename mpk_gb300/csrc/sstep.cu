@@ -122,8 +122,39 @@ __global__ void axpby_kernel(int n, double a, const double *__restrict__ x, doub
 
 // Column c of the basis Y (column-major, n floats each).  P block: columns
 // 0..s, R block: columns s+1..2s.  Start columns: p / |p| and r / |r|.
-__global__ void basis_start_kernel(int n, const double *__restrict__ p, double ip, const double *__restrict__ r,
-                                   double ir, float *__restrict__ y0, float *__restrict__ yr) {
+// The scalars of an outer iteration, in device memory so that the whole
+// iteration replays as one graph: [0] |p|, [1] |r|, [2] 1/|p|, [3] 1/|r|,
+// [4] r.r, [5] p.p.
+constexpr int kScalars = 6;
+
+// r.r and p.p from the per-CTA partial sums (one warp: lane j sums
+// partials j, j+32, ... in order, then a fixed butterfly, so the same bits
+// on every run), and the norms that scale the next basis.
+__global__ void norms_kernel(int nb, const double *__restrict__ part, double *__restrict__ sc) {
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  double rr = 0.0, pp = 0.0;
+  for (int k = lane; k < nb; k += 32) {
+    rr += part[k];
+    pp += part[nb + k];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    rr += __shfl_xor_sync(0xFFFFFFFFu, rr, o);
+    pp += __shfl_xor_sync(0xFFFFFFFFu, pp, o);
+  }
+  if (lane != 0) return;
+  const double pn = sqrt(pp), rn = sqrt(rr);
+  sc[0] = pn;
+  sc[1] = rn;
+  sc[2] = 1.0 / pn;
+  sc[3] = 1.0 / rn;
+  sc[4] = rr;
+  sc[5] = pp;
+}
+
+__global__ void basis_start_kernel(int n, const double *__restrict__ p, const double *__restrict__ r,
+                                   const double *__restrict__ sc, float *__restrict__ y0, float *__restrict__ yr) {
+  const double ip = sc[2], ir = sc[3];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     y0[i] = (float)(p[i] * ip);
     yr[i] = (float)(r[i] * ir);
@@ -228,8 +259,9 @@ __global__ void gram_reduce_kernel(int nblk, int ncol, const double *__restrict_
 // (non-positive curvature or residual) stopped the inner loop early;
 // flag[1] = steps taken.
 __global__ void coeff_kernel(int s, const double *__restrict__ g, const double *__restrict__ theta,
-                             const double *__restrict__ sigma, double pnorm, double rnorm, double *__restrict__ xh,
+                             const double *__restrict__ sigma, const double *__restrict__ sc, double *__restrict__ xh,
                              double *__restrict__ ph, double *__restrict__ rh, int *__restrict__ flag) {
+  const double pnorm = sc[0], rnorm = sc[1];
   const int m = 2 * s + 1, c = threadIdx.x;
   const bool on = c < m;
   double p = 0.0, r = 0.0, x = 0.0;
@@ -413,6 +445,18 @@ struct DevBuf {
   int alloc(size_t n) {
     SS_TRY(cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)));
     return kOk;
+  }
+};
+
+// A captured graph, its instance and its stream, released on scope exit.
+struct GraphRun {
+  cudaStream_t st = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~GraphRun() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (st) cudaStreamDestroy(st);
   }
 };
 
@@ -651,8 +695,11 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
   DevBuf<double> dx, db, dr, dp, part, gpart, dg, dth, dsg, dxh, dph, drh;
   DevBuf<float> y;
   DevBuf<int> dflag;
-  HostBuf hbuf;  // page-locked: flags (8 ints), then 2 * nb partial sums
-  if ((rc = hbuf.alloc(8 * sizeof(int) + 2 * sizeof(double) * (size_t)nb))) return rc;
+  HostBuf hbuf;  // page-locked: flags (8 ints), r.r and p.p, the Gram matrix, staged scalars
+  const size_t hb_sc = 8 * sizeof(int), hb_g = hb_sc + 2 * sizeof(double), hb_up = hb_g + sizeof(double) * m * m;
+  if ((rc = hbuf.alloc(hb_up + sizeof(double) * kScalars))) return rc;
+  DevBuf<double> dsc;
+  if ((rc = dsc.alloc(kScalars))) return rc;
   if ((rc = dx.alloc(n)) || (rc = db.alloc(n)) || (rc = dr.alloc(n)) || (rc = dp.alloc(n)) ||
       (rc = part.alloc(2 * (size_t)nb)) ||
       (rc = gpart.alloc((size_t)gblk * npair)) || (rc = dg.alloc(m * m)) || (rc = dth.alloc(s)) ||
@@ -673,41 +720,61 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
   if ((rc = sum_parts(part.p, nb, &rr))) return rc;
   SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
   double pp = rr;
+  // One outer iteration as a graph, captured once and replayed: basis,
+  // Gram, coefficient steps, update, true residual, scalars for the next
+  // iteration, and one copy back of the flags, r.r, p.p (and the Gram
+  // matrix for the condition number).
+  GraphRun gr;
+  SS_TRY(cudaStreamCreateWithFlags(&gr.st, cudaStreamNonBlocking));
+  auto upload_scalars = [&]() -> int {  // host values of the norms, e.g. after a restart
+    double *h = reinterpret_cast<double *>(reinterpret_cast<char *>(hbuf.p) + hb_up);
+    const double pn = std::sqrt(pp), rn = std::sqrt(rr);
+    h[0] = pn; h[1] = rn; h[2] = 1.0 / pn; h[3] = 1.0 / rn; h[4] = rr; h[5] = pp;
+    SS_TRY(cudaMemcpyAsync(dsc.p, h, sizeof(double) * kScalars, cudaMemcpyHostToDevice, gr.st));
+    return kOk;
+  };
+  if ((rc = upload_scalars())) return rc;
+  {
+    float *Y = y.p;
+    cudaStream_t cs = gr.st;
+    SS_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    basis_start_kernel<<<nb, kThreads, 0, cs>>>(n, dp.p, dr.p, dsc.p, Y, Y + (size_t)(s + 1) * n);
+    for (int j = 0; j < s; j++) {
+      const bool rstep = j + 1 < s;
+      basis_step_kernel<<<nb, kThreads, 0, cs>>>(n, a.ptr, a.col, a.valf, Y + (size_t)j * n, Y + (size_t)(j + 1) * n,
+                                                 rstep ? Y + (size_t)(s + 1 + j) * n : nullptr,
+                                                 rstep ? Y + (size_t)(s + 2 + j) * n : nullptr, (float)th[j],
+                                                 (float)(1.0 / sg[j]));
+    }
+    gram_kernel<<<gblk, kThreads, 0, cs>>>(n, m, Y, gpart.p);
+    gram_reduce_kernel<<<(npair * 32 + kThreads - 1) / kThreads, kThreads, 0, cs>>>(gblk, m, gpart.p, dg.p);
+    coeff_kernel<<<1, 32, 0, cs>>>(s, dg.p, dth.p, dsg.p, dsc.p, dxh.p, dph.p, drh.p, dflag.p);
+    combine_kernel<<<nb, kThreads, 0, cs>>>(n, m, Y, dxh.p, dph.p, dx.p, dp.p);
+    resid_kernel<<<nb, kThreads, 0, cs>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+    axpy_norm_kernel<<<nb, kThreads, 0, cs>>>(n, 0.0, dp.p, dp.p, part.p + nb);
+    norms_kernel<<<1, 32, 0, cs>>>(nb, part.p, dsc.p);
+    cudaMemcpyAsync(hbuf.p, dflag.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, cs);
+    cudaMemcpyAsync(reinterpret_cast<char *>(hbuf.p) + hb_sc, dsc.p + 4, sizeof(double) * 2, cudaMemcpyDeviceToHost,
+                    cs);
+    if (info)
+      cudaMemcpyAsync(reinterpret_cast<char *>(hbuf.p) + hb_g, dg.p, sizeof(double) * m * m, cudaMemcpyDeviceToHost,
+                      cs);
+    SS_TRY(cudaStreamEndCapture(cs, &gr.graph));
+    SS_TRY(cudaGraphInstantiate(&gr.exec, gr.graph, 0));
+  }
   int outer = 0, steps = 0, breakdowns = 0;
   double cond_max = 0.0;
   std::vector<double> hg(m * m);
   while (outer < max_outer && std::sqrt(rr) > tol * bnorm) {
-    const double pn = std::sqrt(pp), rn = std::sqrt(rr);
-    float *Y = y.p;
-    basis_start_kernel<<<nb, kThreads>>>(n, dp.p, 1.0 / pn, dr.p, 1.0 / rn, Y, Y + (size_t)(s + 1) * n);
-    for (int j = 0; j < s; j++) {
-      const bool rstep = j + 1 < s;
-      basis_step_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.valf, Y + (size_t)j * n, Y + (size_t)(j + 1) * n,
-                                          rstep ? Y + (size_t)(s + 1 + j) * n : nullptr,
-                                          rstep ? Y + (size_t)(s + 2 + j) * n : nullptr, (float)th[j],
-                                          (float)(1.0 / sg[j]));
-    }
-    gram_kernel<<<gblk, kThreads>>>(n, m, Y, gpart.p);
-    gram_reduce_kernel<<<(npair * 32 + kThreads - 1) / kThreads, kThreads>>>(gblk, m, gpart.p, dg.p);
-    coeff_kernel<<<1, 32>>>(s, dg.p, dth.p, dsg.p, pn, rn, dxh.p, dph.p, drh.p, dflag.p);
-    combine_kernel<<<nb, kThreads>>>(n, m, Y, dxh.p, dph.p, dx.p, dp.p);
-    // true residual (FP64) and |p|^2, then one round trip for the flags,
-    // both sets of partial sums and (with info) the Gram matrix
-    resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
-    axpy_norm_kernel<<<nb, kThreads>>>(n, 0.0, dp.p, dp.p, part.p + nb);
-    SS_TRY(cudaGetLastError());
-    SS_TRY(cudaMemcpyAsync(hbuf.p, dflag.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, 0));
-    SS_TRY(cudaMemcpyAsync(hbuf.p + 8, part.p, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, 0));
-    if (info) SS_TRY(cudaMemcpyAsync(hg.data(), dg.p, sizeof(double) * m * m, cudaMemcpyDeviceToHost, 0));
-    SS_TRY(cudaStreamSynchronize(0));
+    SS_TRY(cudaGraphLaunch(gr.exec, gr.st));
+    SS_TRY(cudaStreamSynchronize(gr.st));
     int flag[2];
     std::memcpy(flag, hbuf.p, sizeof flag);
     {
-      const double *hp = reinterpret_cast<const double *>(hbuf.p + 8);
-      rr = 0.0;
-      for (int k = 0; k < nb; k++) rr += hp[k];
-      pp = 0.0;
-      for (int k = 0; k < nb; k++) pp += hp[nb + k];
+      const double *hs = reinterpret_cast<const double *>(reinterpret_cast<char *>(hbuf.p) + hb_sc);
+      rr = hs[0];
+      pp = hs[1];
+      if (info) std::memcpy(hg.data(), reinterpret_cast<char *>(hbuf.p) + hb_g, sizeof(double) * m * m);
     }
     if (info) {  // condition number of the P block (the s-step polynomial basis) from its Gram eigenvalues
       const int mp = s + 1;
@@ -751,11 +818,13 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
     steps += flag[1];
     outer++;
     if (flag[1] == 0 || !(pp > 0.0)) {  // no progress possible with this basis: restart from r
-      SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+      SS_TRY(cudaMemcpyAsync(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, gr.st));
       pp = rr;
+      if ((rc = upload_scalars())) return rc;
       if (flag[1] == 0) break;
     }
   }
+  SS_TRY(cudaStreamSynchronize(gr.st));
   SS_TRY(cudaMemcpy(x, dx.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (info) {
     std::memset(info, 0, sizeof *info);
