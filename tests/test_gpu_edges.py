@@ -176,3 +176,49 @@ def test_matrix_without_entries_is_rejected(gpu):
         with pytest.raises(M.MpkError) as e:
             mk()
         assert e.value.code == M.EINVAL
+
+
+def _random_csr(n, seed, unsorted, dups, far):
+    """Random rows of 0..12 entries; columns near the row (or anywhere with
+    `far`), optionally unsorted within rows and with repeated columns."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for i in range(n):
+        k = int(rng.integers(0, 13))
+        if far:
+            c = rng.integers(0, n, size=k)
+        else:
+            c = np.clip(i + rng.integers(-300, 301, size=k), 0, n - 1)
+        if dups and k > 1:
+            c[-1] = c[0]
+        if not unsorted:
+            c = np.sort(c)
+        rows.append(c.astype(np.int32))
+    ptr = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+    return M.Csr(ptr, np.concatenate(rows).astype(np.int32), M.uniform(seed + 1, int(ptr[-1])))
+
+
+@pytest.mark.parametrize("unsorted,dups,far", [(False, False, False), (True, False, False), (True, True, False),
+                                               (False, False, True)])
+def test_random_structures_bitwise(unsorted, dups, far, gpu):
+    """Random sparse rows (empty rows included), columns in any order and
+    repeated: the rows are summed in the stored order, as the reference
+    does, so every executor matches the oracle bit for bit (valued and
+    1/deg operators)."""
+    a = _random_csr(20000, 31, unsorted, dups, far)
+    k = 5
+    x = M.uniform(32, a.n)
+    for op in (a, a.pattern()):
+        want = O.mpk(op.ptr, op.col, op.val, x, k, O.MODE_FMA)
+        for ex, mk in (("spmv", lambda: M.Plan.spmv(op, k)), ("wave", lambda: M.Plan.wave(op, k)),
+                       ("pipe", lambda: M.Plan.pipe(op, k))):
+            try:
+                plan = mk()
+            except M.MpkError as e:  # the pipeline's chunk window cannot span columns anywhere
+                assert ex == "pipe" and far and e.code == M.ERANGE, (ex, str(e))
+                continue
+            got = _run(plan, x, a.n, k)
+            bad = np.flatnonzero(got.view(np.int64) != want.view(np.int64))
+            assert bad.size == 0, f"{ex}: {bad.size} words differ"
+        got = _run(M.Plan.wave(op, k, arith=M.ARITH_DF64), x, a.n, k)
+        assert _relerr(got, want, a.n, k) <= TOL
