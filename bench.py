@@ -387,6 +387,9 @@ def bench_sstep(M):
     _, out["learned_shifts"] = M.sstep_cg(a, b, 8, shifts=sh)
     out["learned_shifts"]["shift_ms"] = pred_ms
     out["learned_shifts"]["model"] = src
+    # the same solve with the Gram matrix summed in double-float on the FP32 pipes
+    _, out["learned_shifts_df64_gram"] = M.sstep_cg(a, b, 8, shifts=sh, gram=M.GRAM_DF64)
+    out["gram"] = "FP64 FMAs over the exact FP64 products of the FP32 basis (df64: double-float sums)"
     return out
 
 

@@ -188,6 +188,15 @@ typedef struct {
  * count).  x: initial guess in, solution out. */
 int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const double *b, double *x, double tol,
             int max_iter, mpkg_cg_info_t *info);
+/* Accumulation of the s-step Gram matrix for the calling thread's later
+ * mpkg_sstep_cg calls: MPKG_GRAM_FP64 (default; FP64 FMAs over the exact
+ * FP64 products of the FP32 basis) or MPKG_GRAM_DF64 (the same products
+ * split exactly and summed in double-float on the FP32 pipes, about
+ * 2^-46 relative to the sum of |products|; faster on GB300). */
+#define MPKG_GRAM_FP64 0
+#define MPKG_GRAM_DF64 1
+int mpkg_sstep_gram(int mode);
+
 /* s-step CG (s <= 10): Newton basis rho_(j+1) = (A - shifts[j]) rho_j /
  * scale (shifts NULL: monomial basis), 2s+1 FP32 basis vectors per outer
  * iteration, FP64 Gram + coefficient solve, FP64 residual replacement. */

@@ -130,6 +130,7 @@ def _declare(L):
         "mpkg_work_count": (I, [C.c_char_p, C.POINTER(Lg), C.POINTER(Lg), C.POINTER(Lg), C.POINTER(Lg),
                                 C.POINTER(Lg)]),
         "mpkg_lapjv": (I, [P, I, P]),
+        "mpkg_sstep_gram": (I, [I]),
         "mpkg_partition_rcb": (I, [I, P, I, I, P]),
         "mpkg_partition_bfs": (I, [I, P, P, I, P]),
         "mpkg_gen_stencil": (I, [C.c_char_p, I, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
@@ -644,9 +645,14 @@ def cg(a: Csr, b, x0=None, tol=1e-8, max_iter=10000):
     return x, _info_dict(inf)
 
 
-def sstep_cg(a: Csr, b, s=8, shifts=None, scale=None, x0=None, tol=1e-8, max_outer=2000):
+GRAM_FP64, GRAM_DF64 = 0, 1
+
+
+def sstep_cg(a: Csr, b, s=8, shifts=None, scale=None, x0=None, tol=1e-8, max_outer=2000, gram=GRAM_FP64):
     """s-step CG with an FP32 Newton basis (shifts None: monomial) scaled
-    by `scale` per step (default: the Gershgorin upper bound / 2)."""
+    by `scale` per step (default: the Gershgorin upper bound / 2); the
+    Gram matrix in FP64 (GRAM_FP64) or double-float (GRAM_DF64)."""
+    _check(lib().mpkg_sstep_gram(gram))
     x = np.zeros(a.n) if x0 is None else np.array(x0, dtype=np.float64)
     b = _f64(b)
     if scale is None:

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mpk_gb300.h"
@@ -179,16 +180,18 @@ __global__ void basis_step_kernel(int n, const int *__restrict__ ptr, const int 
   }
 }
 
-// Gram matrix G = Y^T Y of the FP32 basis, on the FP32 pipes: each product
-// a*b of two FP32 values is split exactly into p + e (p = a*b rounded,
-// e = fma(a, b, -p)) and summed in double-float (a two-sum on the high
-// parts, the errors and low parts added), about 2^-46 relative to the sum
-// of |products| -- FP64's own rounding (2^-53 per add) is not needed for
-// the coefficient solve, and GB300's FP64 pipe runs at 1/64 of FP32.
+// Gram matrix G = Y^T Y of the FP32 basis.  Every product a*b of two FP32
+// values is exact in FP64 (48-bit mantissa).  F64: the products are
+// summed with FP64 FMAs (the FP64 Gram of the s-step method).  !F64: each
+// product is split exactly into p + e (p = a*b rounded, e = fma(a, b, -p))
+// and summed in double-float on the FP32 pipes (a two-sum on the high
+// parts, errors and low parts added; about 2^-46 relative to the sum of
+// |products|), for GB300 whose FP64 pipe runs at 1/64 of FP32.
 // A CTA stages a tile of rows of all columns in shared memory; thread t
 // accumulates pair t of the upper triangle with four independent sums;
 // per-CTA partials (FP64) are summed in a fixed order by gram_reduce_kernel.
 constexpr int kGramRows = 64;
+thread_local bool g_gram_f64 = true;  // mpkg_sstep_gram: FP64 (default) or double-float Gram
 __device__ __forceinline__ void gram_acc(float a, float b, float &sh, float &sl) {
   const float p = __fmul_rn(a, b), e = __fmaf_rn(a, b, -p);
   const float t = __fadd_rn(sh, p), bp = __fadd_rn(t, -sh);
@@ -197,11 +200,15 @@ __device__ __forceinline__ void gram_acc(float a, float b, float &sh, float &sl)
   sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
 
+template <bool F64>
 __global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const float *__restrict__ y,
                                                         double *__restrict__ part) {
   // one padding word per column: the threads of a warp read up to 17
-  // different columns at the same row, which would otherwise share a bank
-  __shared__ float tile[kMaxCols][kGramRows + 1];
+  // different columns at the same row, which would otherwise share a bank.
+  // F64 stages the values already widened, so that each is converted once
+  // per tile rather than once per pair (the conversion shares the FP64 pipe)
+  using Stage = typename std::conditional<F64, double, float>::type;
+  __shared__ Stage tile[kMaxCols][kGramRows + 1];
   const int npair = ncol * (ncol + 1) / 2;
   int pa = 0, pb = 0;
   {
@@ -211,26 +218,28 @@ __global__ void __launch_bounds__(kThreads) gram_kernel(int n, int ncol, const f
     pb = a + t;
   }
   float h[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (long r0 = (long)blockIdx.x * kGramRows; r0 < n; r0 += (long)gridDim.x * kGramRows) {
     __syncthreads();
     for (int e = threadIdx.x; e < ncol * kGramRows; e += blockDim.x) {
       const int c = e / kGramRows, rr = e % kGramRows;
-      tile[c][rr] = r0 + rr < n ? y[(size_t)c * n + r0 + rr] : 0.f;
+      tile[c][rr] = (Stage)(r0 + rr < n ? y[(size_t)c * n + r0 + rr] : 0.f);
     }
     __syncthreads();
     if ((int)threadIdx.x < npair) {  // four independent partial sums per thread
 #pragma unroll 4
       for (int rr = 0; rr < kGramRows; rr += 4) {
-        gram_acc(tile[pa][rr], tile[pb][rr], h[0], lo[0]);
-        gram_acc(tile[pa][rr + 1], tile[pb][rr + 1], h[1], lo[1]);
-        gram_acc(tile[pa][rr + 2], tile[pb][rr + 2], h[2], lo[2]);
-        gram_acc(tile[pa][rr + 3], tile[pb][rr + 3], h[3], lo[3]);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if (F64) acc[u] = fma((double)tile[pa][rr + u], (double)tile[pb][rr + u], acc[u]);
+          else gram_acc((float)tile[pa][rr + u], (float)tile[pb][rr + u], h[u], lo[u]);
+        }
       }
     }
   }
   if ((int)threadIdx.x < npair) {
     double s = 0.0;
-    for (int k = 0; k < 4; k++) s += (double)h[k] + (double)lo[k];
+    for (int k = 0; k < 4; k++) s += F64 ? acc[k] : (double)h[k] + (double)lo[k];
     part[(size_t)blockIdx.x * npair + threadIdx.x] = s;
   }
 }
@@ -681,6 +690,13 @@ int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const doub
   return kOk;
 }
 
+int mpkg_sstep_gram(int mode) {
+  clear_error();
+  if (mode != MPKG_GRAM_FP64 && mode != MPKG_GRAM_DF64) return fail(kEInval, "unknown Gram mode");
+  g_gram_f64 = mode == MPKG_GRAM_FP64;
+  return kOk;
+}
+
 int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, const double *b, double *x, int s,
                   const double *shifts, double scale, double tol, int max_outer, mpkg_cg_info_t *info) {
   clear_error();
@@ -746,7 +762,8 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
                                                  rstep ? Y + (size_t)(s + 2 + j) * n : nullptr, (float)th[j],
                                                  (float)(1.0 / sg[j]));
     }
-    gram_kernel<<<gblk, kThreads, 0, cs>>>(n, m, Y, gpart.p);
+    if (g_gram_f64) gram_kernel<true><<<gblk, kThreads, 0, cs>>>(n, m, Y, gpart.p);
+    else gram_kernel<false><<<gblk, kThreads, 0, cs>>>(n, m, Y, gpart.p);
     gram_reduce_kernel<<<(npair * 32 + kThreads - 1) / kThreads, kThreads, 0, cs>>>(gblk, m, gpart.p, dg.p);
     coeff_kernel<<<1, 32, 0, cs>>>(s, dg.p, dth.p, dsg.p, dsc.p, dxh.p, dph.p, drh.p, dflag.p);
     combine_kernel<<<nb, kThreads, 0, cs>>>(n, m, Y, dxh.p, dph.p, dx.p, dp.p);

@@ -74,3 +74,19 @@ def test_sstep_cg_bases(dims, trained_mlp, gpu):
     assert lrn["iterations"] <= mono["iterations"]
     assert lrn["iterations"] <= 1.2 * lan["iterations"]
     assert np.linalg.norm(x_l - x_cg) / np.linalg.norm(x_cg) < 1e-6
+
+
+def test_sstep_gram_modes_agree(gpu):
+    """The FP64 Gram (default) and the double-float Gram take the same
+    outer iterations on a diffusion problem and give solutions and basis
+    condition numbers that agree far below the solve's tolerance."""
+    a = M.Csr.diffusion(64, 64, 8, sigma=1.0, seed=5)
+    b = M.uniform(9, a.n)
+    sh = S.from_lanczos(a, 8)
+    x64, i64 = M.sstep_cg(a, b, 8, shifts=sh, gram=M.GRAM_FP64)
+    xdf, idf = M.sstep_cg(a, b, 8, shifts=sh, gram=M.GRAM_DF64)
+    for inf in (i64, idf):
+        assert inf["converged"] and inf["relres"] <= 1e-8
+    assert abs(i64["iterations"] - idf["iterations"]) <= 1
+    assert np.linalg.norm(x64 - xdf) / np.linalg.norm(x64) < 1e-7
+    assert abs(i64["basis_cond"] - idf["basis_cond"]) <= 1e-6 * i64["basis_cond"]

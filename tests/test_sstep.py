@@ -40,3 +40,12 @@ def test_mlp_oracle_gradient_finite_differences():
         lp = mlp_ref.gradient(p + e, X, T, nin, w, nout)[1]
         lm = mlp_ref.gradient(p - e, X, T, nin, w, nout)[1]
         assert abs((lp - lm) / (2 * eps) - g[k]) < 1e-6
+
+
+def test_sstep_gram_mode_is_checked():
+    """The Gram mode is a host setting: known modes are accepted, others
+    are refused with EINVAL before any GPU work."""
+    lib = M.lib()
+    assert lib.mpkg_sstep_gram(M.GRAM_DF64) == 0
+    assert lib.mpkg_sstep_gram(M.GRAM_FP64) == 0
+    assert lib.mpkg_sstep_gram(7) == M.EINVAL
