@@ -390,6 +390,11 @@ def bench_sstep(M):
     # the same solve with the Gram matrix summed in double-float on the FP32 pipes
     _, out["learned_shifts_df64_gram"] = M.sstep_cg(a, b, 8, shifts=sh, gram=M.GRAM_DF64)
     out["gram"] = "FP64 FMAs over the exact FP64 products of the FP32 basis (df64: double-float sums)"
+    # the same solve with the outer loop driven from the host (one graph
+    # launch and synchronisation per outer iteration)
+    _, out["learned_shifts_host_loop"] = M.sstep_cg(a, b, 8, shifts=sh, loop=M.SSTEP_HOST_LOOP)
+    out["loop"] = ("device-side: the whole solve is one graph launch (conditional WHILE node); "
+                   "loop_ms = the iterations alone, ms = the whole call incl. matrix upload and setup")
     return out
 
 

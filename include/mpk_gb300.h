@@ -182,6 +182,9 @@ typedef struct {
   double basis_cond;/* largest condition number of the s+1 vectors
                        p, rho_1(A) p, ..., rho_s(A) p over the outer iterations */
   double ms;        /* wall time of the call */
+  double loop_ms;   /* wall time of the iterations alone (no upload or setup) */
+  int loop_launches;/* graph launches of the s-step outer loop: 1 with the
+                       device-side loop, one per outer iteration on the host */
 } mpkg_cg_info_t;
 
 /* Standard FP64 conjugate gradients on the GPU (the reference iteration
@@ -196,6 +199,15 @@ int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const doub
 #define MPKG_GRAM_FP64 0
 #define MPKG_GRAM_DF64 1
 int mpkg_sstep_gram(int mode);
+/* Where the calling thread's later mpkg_sstep_cg calls run their outer
+ * loop: MPKG_SSTEP_DEVICE_LOOP (default; the whole solve is one CUDA graph
+ * launch, a conditional WHILE node deciding on the device after each
+ * iteration; falls back to the host loop where the runtime lacks it) or
+ * MPKG_SSTEP_HOST_LOOP (one graph launch and one host synchronisation per
+ * outer iteration).  Both give the same bits. */
+#define MPKG_SSTEP_DEVICE_LOOP 0
+#define MPKG_SSTEP_HOST_LOOP 1
+int mpkg_sstep_loop(int mode);
 
 /* s-step CG (s <= 10): Newton basis rho_(j+1) = (A - shifts[j]) rho_j /
  * scale (shifts NULL: monomial basis), 2s+1 FP32 basis vectors per outer

@@ -66,7 +66,8 @@ class BatchInfo(C.Structure):
 
 class CgInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("mpk_steps", C.c_int), ("converged", C.c_int), ("breakdowns", C.c_int),
-                ("relres", C.c_double), ("basis_cond", C.c_double), ("ms", C.c_double)]
+                ("relres", C.c_double), ("basis_cond", C.c_double), ("ms", C.c_double),
+                ("loop_ms", C.c_double), ("loop_launches", C.c_int)]
 
 
 class PlanInfo(C.Structure):
@@ -131,6 +132,7 @@ def _declare(L):
                                 C.POINTER(Lg)]),
         "mpkg_lapjv": (I, [P, I, P]),
         "mpkg_sstep_gram": (I, [I]),
+        "mpkg_sstep_loop": (I, [I]),
         "mpkg_partition_rcb": (I, [I, P, I, I, P]),
         "mpkg_partition_bfs": (I, [I, P, P, I, P]),
         "mpkg_gen_stencil": (I, [C.c_char_p, I, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
@@ -646,13 +648,18 @@ def cg(a: Csr, b, x0=None, tol=1e-8, max_iter=10000):
 
 
 GRAM_FP64, GRAM_DF64 = 0, 1
+SSTEP_DEVICE_LOOP, SSTEP_HOST_LOOP = 0, 1
 
 
-def sstep_cg(a: Csr, b, s=8, shifts=None, scale=None, x0=None, tol=1e-8, max_outer=2000, gram=GRAM_FP64):
+def sstep_cg(a: Csr, b, s=8, shifts=None, scale=None, x0=None, tol=1e-8, max_outer=2000, gram=GRAM_FP64,
+             loop=SSTEP_DEVICE_LOOP):
     """s-step CG with an FP32 Newton basis (shifts None: monomial) scaled
     by `scale` per step (default: the Gershgorin upper bound / 2); the
-    Gram matrix in FP64 (GRAM_FP64) or double-float (GRAM_DF64)."""
+    Gram matrix in FP64 (GRAM_FP64) or double-float (GRAM_DF64); the
+    outer loop decided on the device (one graph launch per solve) or on
+    the host (one launch and synchronisation per outer iteration)."""
     _check(lib().mpkg_sstep_gram(gram))
+    _check(lib().mpkg_sstep_loop(loop))
     x = np.zeros(a.n) if x0 is None else np.array(x0, dtype=np.float64)
     b = _f64(b)
     if scale is None:

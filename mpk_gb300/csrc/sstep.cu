@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -153,6 +154,49 @@ __global__ void norms_kernel(int nb, const double *__restrict__ part, double *__
   sc[5] = pp;
 }
 
+// The whole solve as one graph: a conditional WHILE node whose body is
+// one outer iteration, ended by decide_kernel (one warp), which counts the
+// iteration, records the P block of the Gram matrix for the host's
+// condition number (a ring in page-locked memory, with a progress count),
+// asks for a restart when p.p is not positive, and sets the loop
+// condition: more iterations allowed, progress made, |r| above tol |b|.
+// The count of iterations bounds the loop by max_outer.
+struct LoopState {
+  int outer, steps, breakdowns, restart;
+};
+constexpr int kCondRing = 512;
+
+__global__ void restart_kernel(int n, const LoopState *__restrict__ st, const double *__restrict__ r,
+                               double *__restrict__ p, double *__restrict__ sc) {
+  if (!st->restart) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = r[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {  // |p| = |r|, p.p = r.r
+    sc[0] = sc[1];
+    sc[2] = sc[3];
+    sc[5] = sc[4];
+  }
+}
+
+__global__ void decide_kernel(int s, int m, const int *__restrict__ flag, const double *__restrict__ sc,
+                              const double *__restrict__ g, int max_outer, double rtol, LoopState *st, double *ring,
+                              int *progress, cudaGraphConditionalHandle loop) {
+  const int lane = threadIdx.x, mp = s + 1, o = st->outer;
+  double *slot = ring + (size_t)(o % kCondRing) * mp * mp;
+  for (int k = lane; k < mp * mp; k += 32) slot[k] = g[(k / mp) * m + k % mp];
+  __threadfence_system();
+  __syncwarp();
+  if (lane != 0) return;
+  const int steps = flag[1];
+  st->outer = o + 1;
+  st->steps += steps;
+  st->breakdowns += flag[0];
+  st->restart = steps > 0 && !(sc[5] > 0.0);
+  const bool more = o + 1 < max_outer && steps > 0 && sqrt(sc[4]) > rtol;
+  __threadfence_system();
+  *(volatile int *)progress = o + 1;
+  cudaGraphSetConditional(loop, more ? 1u : 0u);
+}
+
 __global__ void basis_start_kernel(int n, const double *__restrict__ p, const double *__restrict__ r,
                                    const double *__restrict__ sc, float *__restrict__ y0, float *__restrict__ yr) {
   const double ip = sc[2], ir = sc[3];
@@ -192,6 +236,7 @@ __global__ void basis_step_kernel(int n, const int *__restrict__ ptr, const int 
 // per-CTA partials (FP64) are summed in a fixed order by gram_reduce_kernel.
 constexpr int kGramRows = 64;
 thread_local bool g_gram_f64 = true;  // mpkg_sstep_gram: FP64 (default) or double-float Gram
+thread_local bool g_device_loop = true;  // mpkg_sstep_loop: device-side (default) or host-side outer loop
 __device__ __forceinline__ void gram_acc(float a, float b, float &sh, float &sl) {
   const float p = __fmul_rn(a, b), e = __fmaf_rn(a, b, -p);
   const float t = __fadd_rn(sh, p), bp = __fadd_rn(t, -sh);
@@ -287,14 +332,19 @@ __global__ void coeff_kernel(int s, const double *__restrict__ g, const double *
     if (c >= s + 2 && c <= 2 * s) out += sigma[c - s - 2] * vm1;
     return on ? out : 0.0;
   };
-  // u^T G v, v distributed over the lanes
+  // lane c keeps row c of G in registers for the s steps
+  double grow[kMaxCols];
+#pragma unroll
+  for (int b = 0; b < kMaxCols; b++) grow[b] = on && b < m ? g[c * m + b] : 0.0;
+  // u^T G v, v distributed over the lanes; three independent partial sums
+  // per row (the FP64 FMA latency bounds this one-warp kernel)
   auto gdot = [&](double u, double v) {
-    double w = 0.0;
-    for (int b = 0; b < m; b++) {
-      const double vb = __shfl_sync(0xffffffffu, v, b);
-      if (on) w = fma(g[c * m + b], vb, w);
+    double w[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int b = 0; b < kMaxCols; b++) {
+      if (b < m) w[b % 3] = fma(grow[b], __shfl_sync(0xffffffffu, v, b), w[b % 3]);
     }
-    double t = on ? u * w : 0.0;
+    double t = on ? u * ((w[0] + w[1]) + w[2]) : 0.0;
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     return t;
   };
@@ -468,6 +518,72 @@ struct GraphRun {
     if (st) cudaStreamDestroy(st);
   }
 };
+
+// Page-locked, device-mapped ring of P-block Gram matrices and the
+// progress count written by decide_kernel.
+struct LoopHost {
+  void *base = nullptr;
+  double *ring = nullptr, *d_ring = nullptr;
+  int *progress = nullptr, *d_progress = nullptr;
+  ~LoopHost() {
+    if (base) cudaFreeHost(base);
+  }
+  bool alloc(size_t ring_doubles) {
+    const size_t bytes = sizeof(double) * ring_doubles + 64;
+    void *d = nullptr;
+    if (cudaHostAlloc(&base, bytes, cudaHostAllocMapped) != cudaSuccess) {
+      base = nullptr;
+      cudaGetLastError();
+      return false;
+    }
+    std::memset(base, 0, bytes);
+    if (cudaHostGetDevicePointer(&d, base, 0) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    ring = static_cast<double *>(base);
+    progress = reinterpret_cast<int *>(static_cast<char *>(base) + sizeof(double) * ring_doubles);
+    d_ring = static_cast<double *>(d);
+    d_progress = reinterpret_cast<int *>(static_cast<char *>(d) + sizeof(double) * ring_doubles);
+    return true;
+  }
+};
+
+// A graph holding one conditional WHILE node whose body `body(stream,
+// handle)` issues by stream capture.  False (and no graph) when the
+// runtime refuses any step; the caller then loops on the host.
+template <typename F>
+bool build_device_loop(GraphRun &gr, F &&body) {
+  cudaGraph_t g = nullptr, out = nullptr;
+  cudaGraphConditionalHandle h;
+  cudaGraphNode_t node;
+  cudaGraphNodeParams np = {};
+  bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+            cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
+  if (ok) {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+  }
+  if (ok) ok = cudaStreamBeginCaptureToGraph(gr.st, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    body(gr.st, h);
+    ok = cudaStreamEndCapture(gr.st, &out) == cudaSuccess;
+  }
+  if (ok) ok = cudaGraphInstantiate(&gr.exec, g, 0) == cudaSuccess;
+  if (!ok) {
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+    gr.exec = nullptr;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return false;
+  }
+  gr.graph = g;
+  return true;
+}
 
 // Page-locked host bytes (int-addressed), released on scope exit.
 struct HostBuf {
@@ -660,6 +776,7 @@ int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const doub
   if ((rc = sum_parts(part.p, nb, &rr))) return rc;
   SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
   int it = 0;
+  const auto t_loop = std::chrono::steady_clock::now();
   while (it < max_iter && std::sqrt(rr) > tol * bnorm) {
     spmv64_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dp.p, dq.p, nullptr, 0.0, part.p);
     double pq;
@@ -674,6 +791,7 @@ int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const doub
     rr = rr2;
     it++;
   }
+  const auto t_loop_end = std::chrono::steady_clock::now();
   // true residual
   resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
   double rt;
@@ -686,6 +804,7 @@ int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const doub
     info->relres = std::sqrt(rt) / bnorm;
     info->converged = info->relres <= tol;
     info->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    info->loop_ms = std::chrono::duration<double, std::milli>(t_loop_end - t_loop).count();
   }
   return kOk;
 }
@@ -694,6 +813,13 @@ int mpkg_sstep_gram(int mode) {
   clear_error();
   if (mode != MPKG_GRAM_FP64 && mode != MPKG_GRAM_DF64) return fail(kEInval, "unknown Gram mode");
   g_gram_f64 = mode == MPKG_GRAM_FP64;
+  return kOk;
+}
+
+int mpkg_sstep_loop(int mode) {
+  clear_error();
+  if (mode != MPKG_SSTEP_DEVICE_LOOP && mode != MPKG_SSTEP_HOST_LOOP) return fail(kEInval, "unknown loop mode");
+  g_device_loop = mode == MPKG_SSTEP_DEVICE_LOOP;
   return kOk;
 }
 
@@ -736,10 +862,6 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
   if ((rc = sum_parts(part.p, nb, &rr))) return rc;
   SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
   double pp = rr;
-  // One outer iteration as a graph, captured once and replayed: basis,
-  // Gram, coefficient steps, update, true residual, scalars for the next
-  // iteration, and one copy back of the flags, r.r, p.p (and the Gram
-  // matrix for the condition number).
   GraphRun gr;
   SS_TRY(cudaStreamCreateWithFlags(&gr.st, cudaStreamNonBlocking));
   auto upload_scalars = [&]() -> int {  // host values of the norms, e.g. after a restart
@@ -750,10 +872,10 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
     return kOk;
   };
   if ((rc = upload_scalars())) return rc;
-  {
+  // one outer iteration: basis, Gram, coefficient steps, update, true
+  // residual, scalars for the next iteration
+  auto iteration = [&](cudaStream_t cs) {
     float *Y = y.p;
-    cudaStream_t cs = gr.st;
-    SS_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     basis_start_kernel<<<nb, kThreads, 0, cs>>>(n, dp.p, dr.p, dsc.p, Y, Y + (size_t)(s + 1) * n);
     for (int j = 0; j < s; j++) {
       const bool rstep = j + 1 < s;
@@ -770,81 +892,146 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
     resid_kernel<<<nb, kThreads, 0, cs>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
     axpy_norm_kernel<<<nb, kThreads, 0, cs>>>(n, 0.0, dp.p, dp.p, part.p + nb);
     norms_kernel<<<1, 32, 0, cs>>>(nb, part.p, dsc.p);
+  };
+  int outer = 0, steps = 0, breakdowns = 0;
+  double cond_max = 0.0;
+  // condition number of the P block (the s-step polynomial basis, (s+1)^2
+  // row-major) from its Gram eigenvalues, computed on the host while the
+  // GPU runs the following iterations
+  auto basis_cond = [&](const double *blk) {
+    const int m = s + 1;  // Jacobi sweeps on the leading (s+1) x (s+1) block
+    std::vector<double> A(blk, blk + (size_t)m * m);
+    for (int sweep = 0; sweep < 60; sweep++) {
+      double off = 0.0;
+      for (int p2 = 0; p2 < m; p2++)
+        for (int q2 = p2 + 1; q2 < m; q2++) off += A[p2 * m + q2] * A[p2 * m + q2];
+      if (off < 1e-30) break;
+      for (int p2 = 0; p2 < m; p2++)
+        for (int q2 = p2 + 1; q2 < m; q2++) {
+          const double apq = A[p2 * m + q2];
+          if (std::fabs(apq) < 1e-300) continue;
+          const double tau = (A[q2 * m + q2] - A[p2 * m + p2]) / (2.0 * apq);
+          const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+          const double c = 1.0 / std::sqrt(1.0 + t * t), sn = t * c;
+          for (int k = 0; k < m; k++) {
+            const double akp = A[k * m + p2], akq = A[k * m + q2];
+            A[k * m + p2] = c * akp - sn * akq;
+            A[k * m + q2] = sn * akp + c * akq;
+          }
+          for (int k = 0; k < m; k++) {
+            const double apk = A[p2 * m + k], aqk = A[q2 * m + k];
+            A[p2 * m + k] = c * apk - sn * aqk;
+            A[q2 * m + k] = sn * apk + c * aqk;
+          }
+        }
+    }
+    double emin = 1e300, emax = 0.0;
+    for (int k = 0; k < m; k++) {
+      emin = std::min(emin, A[k * m + k]);
+      emax = std::max(emax, A[k * m + k]);
+    }
+    const double cnd = emin > 0 ? std::sqrt(emax / emin) : 1e300;
+    cond_max = std::max(cond_max, cnd);
+  };
+  const int mp2 = (s + 1) * (s + 1);
+  const double rtol = tol * bnorm;
+  int launches = 0;
+  auto t_loop = std::chrono::steady_clock::now(), t_loop_end = t_loop;
+  // Device-side loop (a conditional WHILE node), when the runtime offers it
+  DevBuf<int> dstate;
+  LoopHost lh;
+  bool device_loop = g_device_loop && lh.alloc((size_t)kCondRing * mp2);
+  if (device_loop && (rc = dstate.alloc(sizeof(LoopState) / sizeof(int)))) return rc;
+  if (device_loop) {
+    SS_TRY(cudaMemsetAsync(dstate.p, 0, sizeof(LoopState), gr.st));
+    device_loop = build_device_loop(gr, [&](cudaStream_t cs, cudaGraphConditionalHandle h) {
+      restart_kernel<<<nb, kThreads, 0, cs>>>(n, reinterpret_cast<const LoopState *>(dstate.p), dr.p, dp.p, dsc.p);
+      iteration(cs);
+      decide_kernel<<<1, 32, 0, cs>>>(s, m, dflag.p, dsc.p, dg.p, max_outer, rtol,
+                                       reinterpret_cast<LoopState *>(dstate.p), lh.d_ring, lh.d_progress, h);
+    });
+  }
+  if (device_loop) {
+    if (std::sqrt(rr) > rtol) {
+      t_loop = std::chrono::steady_clock::now();
+      SS_TRY(cudaGraphLaunch(gr.exec, gr.st));
+      launches = 1;
+      int seen = 0;
+      std::vector<double> blk(mp2);
+      for (;;) {  // condition numbers of the iterations done so far, while the loop runs
+        const cudaError_t q = cudaStreamQuery(gr.st);
+        const int avail = __atomic_load_n(lh.progress, __ATOMIC_ACQUIRE);
+        for (; seen < avail; seen++) {
+          if (avail - seen > kCondRing) continue;  // overwritten before it was read
+          std::memcpy(blk.data(), lh.ring + (size_t)(seen % kCondRing) * mp2, sizeof(double) * mp2);
+          // the slot is rewritten by iteration seen + kCondRing: use the copy
+          // only if that iteration had not reached its decision yet
+          const int now = __atomic_load_n(lh.progress, __ATOMIC_ACQUIRE);
+          if (info && now - seen < kCondRing) basis_cond(blk.data());
+        }
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) SS_TRY(q);
+        std::this_thread::yield();
+      }
+      LoopState hs;
+      double sc[kScalars];
+      SS_TRY(cudaMemcpy(&hs, dstate.p, sizeof hs, cudaMemcpyDeviceToHost));
+      SS_TRY(cudaMemcpy(sc, dsc.p, sizeof sc, cudaMemcpyDeviceToHost));
+      outer = hs.outer;
+      steps = hs.steps;
+      breakdowns = hs.breakdowns;
+      rr = sc[4];
+      t_loop_end = std::chrono::steady_clock::now();
+    }
+  } else {
+    // host loop: the iteration as a graph replayed per outer iteration,
+    // with one copy back of the flags, r.r, p.p and the Gram matrix
+    cudaStream_t cs = gr.st;
+    SS_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    iteration(cs);
     cudaMemcpyAsync(hbuf.p, dflag.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, cs);
     cudaMemcpyAsync(reinterpret_cast<char *>(hbuf.p) + hb_sc, dsc.p + 4, sizeof(double) * 2, cudaMemcpyDeviceToHost,
                     cs);
-    if (info)
-      cudaMemcpyAsync(reinterpret_cast<char *>(hbuf.p) + hb_g, dg.p, sizeof(double) * m * m, cudaMemcpyDeviceToHost,
-                      cs);
+    cudaMemcpyAsync(reinterpret_cast<char *>(hbuf.p) + hb_g, dg.p, sizeof(double) * m * m, cudaMemcpyDeviceToHost, cs);
     SS_TRY(cudaStreamEndCapture(cs, &gr.graph));
     SS_TRY(cudaGraphInstantiate(&gr.exec, gr.graph, 0));
-  }
-  int outer = 0, steps = 0, breakdowns = 0;
-  double cond_max = 0.0;
-  std::vector<double> hg(m * m);
-  while (outer < max_outer && std::sqrt(rr) > tol * bnorm) {
-    SS_TRY(cudaGraphLaunch(gr.exec, gr.st));
-    SS_TRY(cudaStreamSynchronize(gr.st));
-    int flag[2];
-    std::memcpy(flag, hbuf.p, sizeof flag);
-    {
+    std::vector<double> blk(mp2);
+    bool cond_pending = false;
+    t_loop = std::chrono::steady_clock::now();
+    while (outer < max_outer && std::sqrt(rr) > rtol) {
+      SS_TRY(cudaGraphLaunch(gr.exec, gr.st));
+      launches++;
+      if (cond_pending && info) basis_cond(blk.data());
+      cond_pending = false;
+      SS_TRY(cudaStreamSynchronize(gr.st));
+      int flag[2];
+      std::memcpy(flag, hbuf.p, sizeof flag);
       const double *hs = reinterpret_cast<const double *>(reinterpret_cast<char *>(hbuf.p) + hb_sc);
       rr = hs[0];
       pp = hs[1];
-      if (info) std::memcpy(hg.data(), reinterpret_cast<char *>(hbuf.p) + hb_g, sizeof(double) * m * m);
-    }
-    if (info) {  // condition number of the P block (the s-step polynomial basis) from its Gram eigenvalues
-      const int mp = s + 1;
-      std::vector<double> A((size_t)mp * mp);
-      for (int r2 = 0; r2 < mp; r2++)
-        for (int c2 = 0; c2 < mp; c2++) A[r2 * mp + c2] = hg[r2 * m + c2];
-      const int m = mp;  // Jacobi sweeps on the leading (s+1) x (s+1) block
-      for (int sweep = 0; sweep < 60; sweep++) {
-        double off = 0.0;
-        for (int p2 = 0; p2 < m; p2++)
-          for (int q2 = p2 + 1; q2 < m; q2++) off += A[p2 * m + q2] * A[p2 * m + q2];
-        if (off < 1e-30) break;
-        for (int p2 = 0; p2 < m; p2++)
-          for (int q2 = p2 + 1; q2 < m; q2++) {
-            const double apq = A[p2 * m + q2];
-            if (std::fabs(apq) < 1e-300) continue;
-            const double tau = (A[q2 * m + q2] - A[p2 * m + p2]) / (2.0 * apq);
-            const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
-            const double c = 1.0 / std::sqrt(1.0 + t * t), sn = t * c;
-            for (int k = 0; k < m; k++) {
-              const double akp = A[k * m + p2], akq = A[k * m + q2];
-              A[k * m + p2] = c * akp - sn * akq;
-              A[k * m + q2] = sn * akp + c * akq;
-            }
-            for (int k = 0; k < m; k++) {
-              const double apk = A[p2 * m + k], aqk = A[q2 * m + k];
-              A[p2 * m + k] = c * apk - sn * aqk;
-              A[q2 * m + k] = sn * apk + c * aqk;
-            }
-          }
+      const double *hg = reinterpret_cast<const double *>(reinterpret_cast<char *>(hbuf.p) + hb_g);
+      for (int k = 0; k < mp2; k++) blk[k] = hg[(k / (s + 1)) * m + k % (s + 1)];
+      cond_pending = true;
+      breakdowns += flag[0];
+      steps += flag[1];
+      outer++;
+      if (flag[1] == 0 || !(pp > 0.0)) {  // no progress possible with this basis: restart from r
+        SS_TRY(cudaMemcpyAsync(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, gr.st));
+        pp = rr;
+        if ((rc = upload_scalars())) return rc;
+        if (flag[1] == 0) break;
       }
-      double emin = 1e300, emax = 0.0;
-      for (int k = 0; k < m; k++) {
-        emin = std::min(emin, A[k * m + k]);
-        emax = std::max(emax, A[k * m + k]);
-      }
-      const double cnd = emin > 0 ? std::sqrt(emax / emin) : 1e300;
-      cond_max = std::max(cond_max, cnd);
     }
-    breakdowns += flag[0];
-    steps += flag[1];
-    outer++;
-    if (flag[1] == 0 || !(pp > 0.0)) {  // no progress possible with this basis: restart from r
-      SS_TRY(cudaMemcpyAsync(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, gr.st));
-      pp = rr;
-      if ((rc = upload_scalars())) return rc;
-      if (flag[1] == 0) break;
-    }
+    if (cond_pending && info) basis_cond(blk.data());
+    SS_TRY(cudaStreamSynchronize(gr.st));
+    t_loop_end = std::chrono::steady_clock::now();
   }
   SS_TRY(cudaStreamSynchronize(gr.st));
   SS_TRY(cudaMemcpy(x, dx.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (info) {
     std::memset(info, 0, sizeof *info);
+    info->loop_ms = std::chrono::duration<double, std::milli>(t_loop_end - t_loop).count();
+    info->loop_launches = launches;
     info->iterations = outer;
     info->mpk_steps = steps;
     info->relres = std::sqrt(rr) / bnorm;

@@ -92,3 +92,23 @@ def test_sstep_gram_modes_agree(gpu):
     assert abs(i64["iterations"] - idf["iterations"]) <= 1
     assert np.linalg.norm(x64 - xdf) / np.linalg.norm(x64) < 1e-7
     assert 0.5 < i64["basis_cond"] / idf["basis_cond"] < 2.0
+
+
+@pytest.mark.parametrize("gram", [M.GRAM_FP64, M.GRAM_DF64])
+def test_sstep_device_loop_equals_host_loop(gram, gpu):
+    """The solve as one graph with a device-side WHILE node gives the
+    bits, iteration counts and basis condition number of the host-driven
+    loop (the same kernels in the same order), including a run cut short
+    by max_outer."""
+    a = M.Csr.diffusion(48, 48, 16, sigma=1.0, seed=8)
+    b = M.uniform(4, a.n)
+    sh = S.from_lanczos(a, 8)
+    for max_outer in (2000, 3):
+        xd, idev = M.sstep_cg(a, b, 8, shifts=sh, gram=gram, max_outer=max_outer, loop=M.SSTEP_DEVICE_LOOP)
+        xh, ihost = M.sstep_cg(a, b, 8, shifts=sh, gram=gram, max_outer=max_outer, loop=M.SSTEP_HOST_LOOP)
+        assert xd.tobytes() == xh.tobytes()
+        for key in ("iterations", "mpk_steps", "breakdowns", "converged", "relres", "basis_cond"):
+            assert idev[key] == ihost[key], key
+        assert idev["loop_launches"] == 1  # the device-side loop ran
+        assert ihost["loop_launches"] == ihost["iterations"]
+    assert idev["iterations"] == 3 and not idev["converged"]

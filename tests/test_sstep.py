@@ -49,3 +49,10 @@ def test_sstep_gram_mode_is_checked():
     assert lib.mpkg_sstep_gram(M.GRAM_DF64) == 0
     assert lib.mpkg_sstep_gram(M.GRAM_FP64) == 0
     assert lib.mpkg_sstep_gram(7) == M.EINVAL
+
+
+def test_sstep_loop_mode_is_checked():
+    lib = M.lib()
+    assert lib.mpkg_sstep_loop(M.SSTEP_HOST_LOOP) == 0
+    assert lib.mpkg_sstep_loop(M.SSTEP_DEVICE_LOOP) == 0
+    assert lib.mpkg_sstep_loop(2) == M.EINVAL
