@@ -50,17 +50,45 @@ int check_csr(int n, const int *ptr, const int *col) {
 
 int blocks_for(long n) { return (int)std::max<long>(1, std::min<long>((n + kThreads - 1) / kThreads, 1216)); }
 
+// ---- sliced matrix layout ---------------------------------------------------
+// Rows in slices of 32; entry t of row i at off[i/32] + 32 t + i%32, so a
+// warp's loads of the same slot are coalesced.  Each row keeps CSR order,
+// so every row sum below has the bits of the CSR loop.
+struct Sell {
+  const long *off;   // nslice + 1
+  const int *len;    // per row
+  const int *col;
+  const double *val;
+  const float *valf; // FP32 copy (s-step basis), or null
+};
+
+__global__ void sell_fill_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                                 const double *__restrict__ val, const long *__restrict__ off, int *__restrict__ len,
+                                 int *__restrict__ scol, double *__restrict__ sval, float *__restrict__ svalf) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int q0 = ptr[i], l = ptr[i + 1] - q0;
+    const long e0 = off[i >> 5] + (i & 31);
+    len[i] = l;
+    for (int t = 0; t < l; t++) {
+      scol[e0 + 32L * t] = col[q0 + t];
+      sval[e0 + 32L * t] = val[q0 + t];
+      if (svalf) svalf[e0 + 32L * t] = __double2float_rn(val[q0 + t]);
+    }
+  }
+}
+
 // ---- FP64 vector kernels -------------------------------------------------
 
 // r = b - A x, and per-CTA partial sums of r.r (deterministic reduction).
-__global__ void resid_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
-                             const double *__restrict__ val, const double *__restrict__ x,
-                             const double *__restrict__ b, double *__restrict__ r, double *__restrict__ part) {
+__global__ void resid_kernel(int n, Sell a, const double *__restrict__ x, const double *__restrict__ b,
+                             double *__restrict__ r, double *__restrict__ part) {
   __shared__ double red[kThreads];
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int q = ptr[i]; q < ptr[i + 1]; q++) s = fma(val[q], x[col[q]], s);
+    const long e0 = a.off[i >> 5] + (i & 31);
+    const int l = a.len[i];
+    for (int t = 0; t < l; t++) s = fma(a.val[e0 + 32L * t], x[a.col[e0 + 32L * t]], s);
     const double ri = b[i] - s;
     r[i] = ri;
     acc = fma(ri, ri, acc);
@@ -75,14 +103,15 @@ __global__ void resid_kernel(int n, const int *__restrict__ ptr, const int *__re
 }
 
 // y = A x (FP64), optionally y -= beta * z; partial sums of y.x
-__global__ void spmv64_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
-                              const double *__restrict__ val, const double *__restrict__ x, double *__restrict__ y,
+__global__ void spmv64_kernel(int n, Sell a, const double *__restrict__ x, double *__restrict__ y,
                               const double *__restrict__ z, double beta, double *__restrict__ part) {
   __shared__ double red[kThreads];
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int q = ptr[i]; q < ptr[i + 1]; q++) s = fma(val[q], x[col[q]], s);
+    const long e0 = a.off[i >> 5] + (i & 31);
+    const int l = a.len[i];
+    for (int t = 0; t < l; t++) s = fma(a.val[e0 + 32L * t], x[a.col[e0 + 32L * t]], s);
     if (z) s = fma(-beta, z[i], s);
     y[i] = s;
     acc = fma(s, x[i], acc);
@@ -208,14 +237,15 @@ __global__ void basis_start_kernel(int n, const double *__restrict__ p, const do
 
 // One Newton step of both blocks: out = (A in - theta in) / sigma, FP32
 // values and accumulation in CSR order; the R block stops one step early.
-__global__ void basis_step_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
-                                  const float *__restrict__ val, const float *__restrict__ pin, float *__restrict__ pout,
+__global__ void basis_step_kernel(int n, Sell a, const float *__restrict__ pin, float *__restrict__ pout,
                                   const float *__restrict__ rin, float *__restrict__ rout, float theta, float rsigma) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float sp = 0.f, sr = 0.f;
-    for (int q = ptr[i]; q < ptr[i + 1]; q++) {
-      const int c = col[q];
-      const float v = val[q];
+    const long e0 = a.off[i >> 5] + (i & 31);
+    const int l = a.len[i];
+    for (int t = 0; t < l; t++) {
+      const int c = a.col[e0 + 32L * t];
+      const float v = a.valf[e0 + 32L * t];
       sp = __fmaf_rn(v, pin[c], sp);
       if (rout) sr = __fmaf_rn(v, rin[c], sr);
     }
@@ -473,10 +503,15 @@ struct DevCsr {
   long nnz = 0;
   int *ptr = nullptr, *col = nullptr;
   double *val = nullptr;
-  float *valf = nullptr;
+  long *soff = nullptr;
+  int *slen = nullptr, *scol = nullptr;
+  double *sval = nullptr;
+  float *svalf = nullptr;
   ~DevCsr() {
-    cudaFree(ptr); cudaFree(col); cudaFree(val); cudaFree(valf);
+    cudaFree(ptr); cudaFree(col); cudaFree(val);
+    cudaFree(soff); cudaFree(slen); cudaFree(scol); cudaFree(sval); cudaFree(svalf);
   }
+  Sell sell() const { return Sell{soff, slen, scol, sval, svalf}; }
   int upload(int n_, const int *p, const int *c, const double *v, bool f32) {
     int rc = check_csr(n_, p, c);
     if (rc) return rc;
@@ -488,11 +523,23 @@ struct DevCsr {
     SS_TRY(cudaMemcpy(ptr, p, sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
     SS_TRY(cudaMemcpy(col, c, sizeof(int) * nnz, cudaMemcpyHostToDevice));
     SS_TRY(cudaMemcpy(val, v, sizeof(double) * nnz, cudaMemcpyHostToDevice));
-    if (f32) {
-      std::vector<float> vf(v, v + nnz);
-      SS_TRY(cudaMalloc(&valf, sizeof(float) * std::max<long>(nnz, 1)));
-      SS_TRY(cudaMemcpy(valf, vf.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice));
+    // the sliced copy, filled on the device from the CSR arrays
+    const int nsl = (n + 31) / 32;
+    std::vector<long> so(nsl + 1, 0);
+    for (int sl = 0; sl < nsl; sl++) {
+      int w = 0;
+      for (int i = sl * 32; i < std::min(n, sl * 32 + 32); i++) w = std::max(w, p[i + 1] - p[i]);
+      so[sl + 1] = so[sl] + 32L * w;
     }
+    const size_t ne = (size_t)std::max<long>(so[nsl], 1);
+    SS_TRY(cudaMalloc(&soff, sizeof(long) * (nsl + 1)));
+    SS_TRY(cudaMalloc(&slen, sizeof(int) * n));
+    SS_TRY(cudaMalloc(&scol, sizeof(int) * ne));
+    SS_TRY(cudaMalloc(&sval, sizeof(double) * ne));
+    if (f32) SS_TRY(cudaMalloc(&svalf, sizeof(float) * ne));
+    SS_TRY(cudaMemcpy(soff, so.data(), sizeof(long) * (nsl + 1), cudaMemcpyHostToDevice));
+    sell_fill_kernel<<<blocks_for(n), kThreads>>>(n, ptr, col, val, soff, slen, scol, sval, svalf);
+    SS_TRY(cudaGetLastError());
     return kOk;
   }
 };
@@ -725,7 +772,7 @@ int mpkg_lanczos(int n, const int *ptr, const int *col, const double *val, int m
   int steps = 0;
   for (int j = 0; j < m; j++) {
     // w = A v_j - beta_j v_(j-1);  alpha_j = w . v_j
-    spmv64_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, vc, w.p, j ? vp : nullptr, bprev, part.p);
+    spmv64_kernel<<<nb, kThreads>>>(n, a.sell(), vc, w.p, j ? vp : nullptr, bprev, part.p);
     SS_TRY(cudaGetLastError());
     double al;
     if ((rc = sum_parts(part.p, nb, &al))) return rc;
@@ -771,14 +818,14 @@ int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const doub
   double bb = 0.0;
   for (int i = 0; i < n; i++) bb += b[i] * b[i];
   const double bnorm = std::sqrt(bb);
-  resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+  resid_kernel<<<nb, kThreads>>>(n, a.sell(), dx.p, db.p, dr.p, part.p);
   double rr;
   if ((rc = sum_parts(part.p, nb, &rr))) return rc;
   SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
   int it = 0;
   const auto t_loop = std::chrono::steady_clock::now();
   while (it < max_iter && std::sqrt(rr) > tol * bnorm) {
-    spmv64_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dp.p, dq.p, nullptr, 0.0, part.p);
+    spmv64_kernel<<<nb, kThreads>>>(n, a.sell(), dp.p, dq.p, nullptr, 0.0, part.p);
     double pq;
     if ((rc = sum_parts(part.p, nb, &pq))) return rc;
     if (!(pq > 0.0)) break;
@@ -793,7 +840,7 @@ int mpkg_cg(int n, const int *ptr, const int *col, const double *val, const doub
   }
   const auto t_loop_end = std::chrono::steady_clock::now();
   // true residual
-  resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+  resid_kernel<<<nb, kThreads>>>(n, a.sell(), dx.p, db.p, dr.p, part.p);
   double rt;
   if ((rc = sum_parts(part.p, nb, &rt))) return rc;
   SS_TRY(cudaMemcpy(x, dx.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
@@ -857,7 +904,7 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
   double bb = 0.0;
   for (int i = 0; i < n; i++) bb += b[i] * b[i];
   const double bnorm = std::sqrt(bb);
-  resid_kernel<<<nb, kThreads>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+  resid_kernel<<<nb, kThreads>>>(n, a.sell(), dx.p, db.p, dr.p, part.p);
   double rr;
   if ((rc = sum_parts(part.p, nb, &rr))) return rc;
   SS_TRY(cudaMemcpy(dp.p, dr.p, sizeof(double) * n, cudaMemcpyDeviceToDevice));
@@ -879,7 +926,7 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
     basis_start_kernel<<<nb, kThreads, 0, cs>>>(n, dp.p, dr.p, dsc.p, Y, Y + (size_t)(s + 1) * n);
     for (int j = 0; j < s; j++) {
       const bool rstep = j + 1 < s;
-      basis_step_kernel<<<nb, kThreads, 0, cs>>>(n, a.ptr, a.col, a.valf, Y + (size_t)j * n, Y + (size_t)(j + 1) * n,
+      basis_step_kernel<<<nb, kThreads, 0, cs>>>(n, a.sell(), Y + (size_t)j * n, Y + (size_t)(j + 1) * n,
                                                  rstep ? Y + (size_t)(s + 1 + j) * n : nullptr,
                                                  rstep ? Y + (size_t)(s + 2 + j) * n : nullptr, (float)th[j],
                                                  (float)(1.0 / sg[j]));
@@ -889,7 +936,7 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
     gram_reduce_kernel<<<(npair * 32 + kThreads - 1) / kThreads, kThreads, 0, cs>>>(gblk, m, gpart.p, dg.p);
     coeff_kernel<<<1, 32, 0, cs>>>(s, dg.p, dth.p, dsg.p, dsc.p, dxh.p, dph.p, drh.p, dflag.p);
     combine_kernel<<<nb, kThreads, 0, cs>>>(n, m, Y, dxh.p, dph.p, dx.p, dp.p);
-    resid_kernel<<<nb, kThreads, 0, cs>>>(n, a.ptr, a.col, a.val, dx.p, db.p, dr.p, part.p);
+    resid_kernel<<<nb, kThreads, 0, cs>>>(n, a.sell(), dx.p, db.p, dr.p, part.p);
     axpy_norm_kernel<<<nb, kThreads, 0, cs>>>(n, 0.0, dp.p, dp.p, part.p + nb);
     norms_kernel<<<1, 32, 0, cs>>>(nb, part.p, dsc.p);
   };
