@@ -798,9 +798,10 @@ struct WaveArgs {
   const unsigned short *len;   // entries per row
   const int *scol;             // column of each slot (int32 form) ...
   const short *srel;           // ... or col - row (int16 form), pattern-compressed: a slice whose 32
-                               // rows share one offset list stores it once (runi = 1, padded to 8)
+                               // rows share one offset list stores it once (runi != 0, padded to 8)
   const long *rel_off;         // nslice + 1: start of each slice in srel
-  const unsigned char *runi;   // per slice: 1 = shared offset list
+  const unsigned char *runi;   // per slice: 0 = per-lane offsets; else a shared offset list, and
+                               // 1 + the rows' common length (255: read the lengths)
   const double *sval;          // value of each slot (valued) ...
   const float2 *sval2;         // ... or its double-float split
   const double *rdeg;          // 1/deg per row (1/deg operator) ...
@@ -823,6 +824,9 @@ struct WaveArgs {
   const unsigned long long *fix_mul;  // 256: ceil(2^64 / d), d >= 2
   unsigned long long *fix_word;       // per call: (base << 32) | largest biased exponent of |x|
   int fix_dbits;                      // ceil(log2(longest row))
+  // mixed form: the values are larger than L2, so they are loaded
+  // evict-first (they would only push the level vectors out of L2)
+  int stream_vals;
 };
 
 __device__ __forceinline__ bool wave_wait(const WaveArgs &a, int b, unsigned int want, int *s_abort) {
@@ -942,7 +946,13 @@ __device__ __forceinline__ void df_row(int len, int RS, const short *cr, const i
   }
 }
 
-template <typename VT, bool REL>
+template <bool STREAM, typename VT>
+__device__ __forceinline__ VT ld_val(const VT *p) {
+  if (STREAM) return __ldcs(p);
+  return __ldg(p);
+}
+
+template <typename VT, bool REL, bool STREAM>
 __device__ __forceinline__ float mix_row(int len, int RS, const short *cr, const int *cc, const VT *cv,
                                          const float *xb, const float *src) {
   float s = 0.f;
@@ -953,7 +963,7 @@ __device__ __forceinline__ float mix_row(int len, int RS, const short *cr, const
     for (int u = 0; u < 12; u++) {
       if (u < len) {
         x[u] = REL ? xb[__ldg(cr + RS * u)] : src[__ldg(cc + 32 * u)];
-        v[u] = to_f32(cv[32 * u]);
+        v[u] = to_f32(ld_val<STREAM>(cv + 32 * u));
       }
     }
 #pragma unroll
@@ -962,7 +972,7 @@ __device__ __forceinline__ float mix_row(int len, int RS, const short *cr, const
     t = len;
   }
   for (; t < len; t++)
-    s = __fmaf_rn(to_f32(cv[32L * t]), REL ? xb[__ldg(cr + RS * t)] : src[__ldg(cc + 32L * t)], s);
+    s = __fmaf_rn(to_f32(ld_val<STREAM>(cv + 32L * t)), REL ? xb[__ldg(cr + RS * t)] : src[__ldg(cc + 32L * t)], s);
   return s;
 }
 
@@ -1201,7 +1211,7 @@ __global__ void __launch_bounds__(256, 5) wave_fix_kernel(WaveArgs a) {
 // scaled by the exact power of two `scale` (the same arithmetic as
 // mix_pipe_kernel, so both give identical bits).  Levels live at fresh
 // addresses of the FP32 vv.
-template <typename VT, bool REL, bool UNI>
+template <typename VT, bool REL, bool UNI, bool STREAM>
 __global__ void __launch_bounds__(256, 5) wave_mix_kernel(WaveArgs a, const VT *__restrict__ sv, float *vf, float scale) {
   __shared__ int s_abort;
   if (threadIdx.x == 0) s_abort = 0;
@@ -1215,16 +1225,27 @@ __global__ void __launch_bounds__(256, 5) wave_mix_kernel(WaveArgs a, const VT *
     for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
       const int i = (sl << 5) + lane;
       if (i >= r1) continue;
-      const int len = __ldg(a.len + i);
+      // a shared-list slice carries its rows' common length in runi: the
+      // streaming build takes it from there (less HBM traffic, but the
+      // other slices' length loads wait for runi); the other loads both
+      int len;
+      bool uni;
+      if (STREAM) {
+        const int ru = UNI && REL ? __ldg(a.runi + sl) : 0;
+        uni = ru != 0;
+        len = ru != 0 && ru != 255 ? ru - 1 : __ldg(a.len + i);
+      } else {
+        len = __ldg(a.len + i);
+        uni = UNI && REL && __ldg(a.runi + sl);
+      }
       const long e0 = __ldg(a.sell_off + sl) + lane;
-      const bool uni = UNI && REL && __ldg(a.runi + sl);
       const short *cr = a.srel + (REL ? __ldg(a.rel_off + sl) : 0) + (uni ? 0 : lane);
       const int *cc = a.scol + e0;
       const VT *cv = sv + e0;
       const float *xb = src + i;
       // one loop for both offset layouts (a runtime stride keeps the
       // registers of a single copy of the 12-wide body)
-      const float s = mix_row<VT, REL>(len, UNI && uni ? 1 : 32, cr, cc, cv, xb, src);
+      const float s = mix_row<VT, REL, STREAM>(len, UNI && uni ? 1 : 32, cr, cc, cv, xb, src);
       __stcs(dst + i, s * scale);
     }
     wave_publish(a, b, a.base + (unsigned)l);
@@ -2434,7 +2455,7 @@ namespace {
 thread_local int g_wave_ctas_per_sm = 0;  // mpkg_plan_wave_ctas: cap on resident CTAs per SM (0: occupancy)
 int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int nlevel, int arith,
                    int occ_value_type, mpkg_plan **out);
-const void *mix_wave_kernel_ptr(int value_type, bool rel, bool uni);
+const void *mix_wave_kernel_ptr(int value_type, bool rel, bool uni, bool stream);
 }  // namespace
 
 extern "C" {
@@ -2492,7 +2513,7 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
   }
   int grid = 0;
   if (!rc)
-    rc = wave_occupancy(p, occ_value_type >= 0 ? mix_wave_kernel_ptr(occ_value_type, p->wave_rel, p->wave_uni)
+    rc = wave_occupancy(p, occ_value_type >= 0 ? mix_wave_kernel_ptr(occ_value_type, p->wave_rel, p->wave_uni, false)
                                                : (const void *)wave_kernel_ptr(p), &grid);
   if (!rc && g_wave_ctas_per_sm > 0) {
     int nsm = 0;
@@ -2533,7 +2554,7 @@ int plan_wave_impl(int n, const int *ptr, const int *col, const double *val, int
         for (int t = 0; t < ptr[i + 1] - ptr[i]; t++)
           if (col[ptr[i] + t] - i != col[ptr[i0] + t] - i0) { uni = false; break; }
       }
-      runi[sl] = uni ? 1 : 0;
+      runi[sl] = uni ? (unsigned char)std::min(w + 1, 255) : 0;
       roff[sl + 1] = roff[sl] + (uni ? (w + 7) / 8 * 8 : 32L * w);
     }
     std::vector<int> scol(p->wave_rel ? 0 : soff[nslice], 0);
@@ -2960,14 +2981,20 @@ int mpkg_pdmpk_prep(int n, const int *ptr, const int *col, const double *val, in
 
 namespace {
 
-const void *mix_wave_kernel_ptr(int value_type, bool rel, bool uni) {
+template <bool STREAM>
+const void *mix_wave_kernel_for(int value_type, bool rel, bool uni) {
   if (value_type == MPKG_VALUE_F32) {
-    if (rel && uni) return (const void *)wave_mix_kernel<float, true, true>;
-    return rel ? (const void *)wave_mix_kernel<float, true, false> : (const void *)wave_mix_kernel<float, false, false>;
+    if (rel && uni) return (const void *)wave_mix_kernel<float, true, true, STREAM>;
+    return rel ? (const void *)wave_mix_kernel<float, true, false, STREAM>
+               : (const void *)wave_mix_kernel<float, false, false, STREAM>;
   }
-  if (rel && uni) return (const void *)wave_mix_kernel<__nv_bfloat16, true, true>;
-  return rel ? (const void *)wave_mix_kernel<__nv_bfloat16, true, false>
-             : (const void *)wave_mix_kernel<__nv_bfloat16, false, false>;
+  if (rel && uni) return (const void *)wave_mix_kernel<__nv_bfloat16, true, true, STREAM>;
+  return rel ? (const void *)wave_mix_kernel<__nv_bfloat16, true, false, STREAM>
+             : (const void *)wave_mix_kernel<__nv_bfloat16, false, false, STREAM>;
+}
+
+const void *mix_wave_kernel_ptr(int value_type, bool rel, bool uni, bool stream) {
+  return stream ? mix_wave_kernel_for<true>(value_type, rel, uni) : mix_wave_kernel_for<false>(value_type, rel, uni);
 }
 
 int mixed_wave_setup(mpkg_plan *p, int n, const int *ptr, const int *col, const double *val, int nlevel,
@@ -2977,7 +3004,10 @@ int mixed_wave_setup(mpkg_plan *p, int n, const int *ptr, const int *col, const 
   if (rc) return rc;
   p->inner = w;
   int per_sm = 0, nsm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_wave_kernel_ptr(value_type, w->wave_rel, w->wave_uni), 256, 0));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_wave_kernel_ptr(value_type, w->wave_rel, w->wave_uni, false), 256, 0));
+  int per_sm_s = 0;  // the streaming build must cover the grid too
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, mix_wave_kernel_ptr(value_type, w->wave_rel, w->wave_uni, true), 256, 0));
+  per_sm = std::min(per_sm, per_sm_s);
   CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
   if ((long)per_sm * nsm < w->wave_grid) return fail(kERange, "mixed wavefront kernel cannot cover the grid");
   const int nslice = (n + 31) / 32;
@@ -2994,6 +3024,12 @@ int mixed_wave_setup(mpkg_plan *p, int n, const int *ptr, const int *col, const 
       for (int t = 0; t < ptr[i + 1] - ptr[i]; t++) (*vec)[e0 + 32L * t] = conv(val[ptr[i] + t]);
     }
   };
+  {  // values larger than L2: every level streams them from HBM anyway
+    int l2 = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, p->device));
+    const double vbytes = (double)soff[nslice] * (value_type == MPKG_VALUE_F32 ? 4.0 : 2.0);
+    w->wave.stream_vals = vbytes > (double)l2 ? 1 : 0;
+  }
   if (value_type == MPKG_VALUE_F32) {
     std::vector<float> sv;
     fill([](double v) { return (float)v; }, &sv);
@@ -3170,12 +3206,12 @@ int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream) {
     if (p->mix_vt == MPKG_VALUE_F32) {
       const float *sv = static_cast<const float *>(p->mix_sval);
       void *args[] = {&a, (void *)&sv, (void *)&d_vv, &scale};
-      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_F32, p->inner->wave_rel, p->inner->wave_uni), dim3(w.nblk),
+      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_F32, p->inner->wave_rel, p->inner->wave_uni, w.stream_vals != 0), dim3(w.nblk),
                                            dim3(256), args, 0, st));
     } else {
       const __nv_bfloat16 *sv = static_cast<const __nv_bfloat16 *>(p->mix_sval);
       void *args[] = {&a, (void *)&sv, (void *)&d_vv, &scale};
-      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_BF16, p->inner->wave_rel, p->inner->wave_uni), dim3(w.nblk),
+      CUDA_TRY(cudaLaunchCooperativeKernel(mix_wave_kernel_ptr(MPKG_VALUE_BF16, p->inner->wave_rel, p->inner->wave_uni, w.stream_vals != 0), dim3(w.nblk),
                                            dim3(256), args, 0, st));
     }
     p->launches = 1;

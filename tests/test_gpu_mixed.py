@@ -90,3 +90,21 @@ def test_mixed_wait_times_out_and_recovers(gpu):
     v, e_, _ = run_mixed(a, 6, M.VALUE_F32, x)
     want = O.mpk(a.ptr, a.col, a.val, x, 6, O.MODE_FMA)
     assert max(rel_errors(v, want, a.n, 6)) <= MIXED_TOL
+
+
+def test_mixed_values_beyond_l2_bitwise_vs_fp32_oracle(gpu):
+    """2048^2 9-point diffusion: 151 MB of FP32 values, more than L2, so
+    the plan loads them evict-first.  The
+    levels equal the FP32 oracle's bit for bit (FP32 FMA in CSR order on
+    the values scaled by the exact power of two) and stay within 1e-6 of
+    FP64 per power."""
+    a = M.Csr.diffusion(2048, 2048, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=3)
+    k = 8
+    x = M.uniform(4, a.n)
+    v, e, _ = run_mixed(a, k, M.VALUE_F32, x)
+    got = (v / (2.0 ** (e * np.arange(k + 1)))[:, None]).astype(np.float32)
+    sval = a.val.astype(np.float32) * np.float32(2.0 ** -e)
+    want = O.spmm_f32(a.ptr, a.col, sval, x.astype(np.float32)[:, None], k)[:, :, 0]
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    want64 = O.mpk(a.ptr, a.col, a.val, x, k, O.MODE_FMA)
+    assert max(rel_errors(v, want64, a.n, k)) <= MIXED_TOL
