@@ -422,9 +422,14 @@ __device__ __forceinline__ void ss_mac(float ch, float cl, float v, float &sh, f
   sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
 
+// Also the per-CTA partial sums of p.p (same order and tree as
+// axpy_norm_kernel on the same grid, so the same bits).
 __global__ void combine_kernel(int n, int m, const float *__restrict__ y, const double *__restrict__ xh,
-                               const double *__restrict__ ph, double *__restrict__ x, double *__restrict__ p) {
+                               const double *__restrict__ ph, double *__restrict__ x, double *__restrict__ p,
+                               double *__restrict__ part) {
   __shared__ float cxh[kMaxCols], cxl[kMaxCols], cph[kMaxCols], cpl[kMaxCols];
+  __shared__ double red[kThreads];
+  double acc = 0.0;
   if ((int)threadIdx.x < m) {
     const double a = xh[threadIdx.x], b = ph[threadIdx.x];
     cxh[threadIdx.x] = __double2float_rn(a);
@@ -441,8 +446,17 @@ __global__ void combine_kernel(int n, int m, const float *__restrict__ y, const 
       ss_mac(cph[c], cpl[c], v, ps, pl);
     }
     x[i] += ss_widen(xs) + ss_widen(xl);
-    p[i] = ss_widen(ps) + ss_widen(pl);
+    const double pv = ss_widen(ps) + ss_widen(pl);
+    p[i] = pv;
+    acc = fma(pv, pv, acc);
   }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
 // ---- matrix features ---------------------------------------------------------
@@ -935,9 +949,8 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
     else gram_kernel<false><<<gblk, kThreads, 0, cs>>>(n, m, Y, gpart.p);
     gram_reduce_kernel<<<(npair * 32 + kThreads - 1) / kThreads, kThreads, 0, cs>>>(gblk, m, gpart.p, dg.p);
     coeff_kernel<<<1, 32, 0, cs>>>(s, dg.p, dth.p, dsg.p, dsc.p, dxh.p, dph.p, drh.p, dflag.p);
-    combine_kernel<<<nb, kThreads, 0, cs>>>(n, m, Y, dxh.p, dph.p, dx.p, dp.p);
+    combine_kernel<<<nb, kThreads, 0, cs>>>(n, m, Y, dxh.p, dph.p, dx.p, dp.p, part.p + nb);
     resid_kernel<<<nb, kThreads, 0, cs>>>(n, a.sell(), dx.p, db.p, dr.p, part.p);
-    axpy_norm_kernel<<<nb, kThreads, 0, cs>>>(n, 0.0, dp.p, dp.p, part.p + nb);
     norms_kernel<<<1, 32, 0, cs>>>(nb, part.p, dsc.p);
   };
   int outer = 0, steps = 0, breakdowns = 0;
