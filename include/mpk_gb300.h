@@ -344,8 +344,11 @@ int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels);
  * d_vv[0..n); writes levels 1..nlevel.  Its bookkeeping lives in a
  * file-scope device array of about 1.2 MB that every GPU loading this
  * library holds until the process exits; limits: n <= 4096*1024 rows,
- * nlevel <= 16 (larger sizes return MPKG_ERANGE / MPKG_EINVAL).  It calls no
- * allocating routine.  The first call on a device looks up the array's
+ * nlevel <= 16 (larger sizes return MPKG_ERANGE / MPKG_EINVAL).  The CSR is
+ * checked on the device before anything is computed: a column outside
+ * [0, n) returns MPKG_ERANGE, a ptr that decreases or does not start at 0
+ * (or a matrix without entries) MPKG_EINVAL, and vv is then left as it was;
+ * col and val must hold ptr[n] entries.  It calls no allocating routine.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress) with that device current; make that
  * first call before any stream capture.  All calls share the one array and
  * it keeps the last call's contents (each call clears what must start at

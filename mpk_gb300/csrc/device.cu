@@ -3362,9 +3362,10 @@ namespace {
 constexpr int kNoAllocMaxChunks = 16384;  // n <= 16384 * 256 = 4096 * 1024 rows
 constexpr int kNoAllocMaxLevels = 16;
 // word layout: [0] ticket, [1] error, [2] max chunk nnz, [3] reach,
-// [4, 4+C) first dependency chunk, [4+C, 4+2C) last dependency chunk,
-// then (kNoAllocMaxLevels+1) * C completion counters.
-constexpr int kNoAllocHeader = 4;
+// [4] a column outside [0, n) was seen, [5] ptr decreases somewhere or
+// ptr[0] != 0, [6] the matrix has no entries, [7] unused, [8, 8+C) first dependency chunk, [8+C, 8+2C)
+// last dependency chunk, then (kNoAllocMaxLevels+1) * C completion counters.
+constexpr int kNoAllocHeader = 8;
 constexpr long kNoAllocWords =
     kNoAllocHeader + 2L * kNoAllocMaxChunks + (long)(kNoAllocMaxLevels + 1) * kNoAllocMaxChunks;
 
@@ -3390,6 +3391,11 @@ int noalloc_scratch(int dev, unsigned int **out) {
 
 // One CTA per chunk: first and last chunk its rows' columns fall in, its
 // entry count, and the largest chunk distance (atomics into the header).
+// It also validates the caller's CSR, which the host cannot read: a ptr
+// that decreases (or ptr[0] != 0) sets word 5, a column outside [0, n) word
+// 4, and the host launches nothing more when either is set.  Column reads
+// stay inside [0, ptr[n]) even for a malformed ptr (the caller's col holds
+// ptr[n] entries).
 __global__ void noalloc_deps_kernel(int n, int chunk, const int *__restrict__ ptr,
                                     const int *__restrict__ col, unsigned int *scr) {
   __shared__ int s_lo, s_hi;
@@ -3397,19 +3403,32 @@ __global__ void noalloc_deps_kernel(int n, int chunk, const int *__restrict__ pt
   const int r0 = c * chunk, r1 = min(n, r0 + chunk);
   if (threadIdx.x == 0) { s_lo = c; s_hi = c; }
   __syncthreads();
+  bool bad_ptr = (c == 0 && threadIdx.x == 0 && ptr[0] != 0);
+  if (c == 0 && threadIdx.x == 0 && ptr[n] <= 0) atomicExch(scr + 6, 1u);
+  for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) bad_ptr |= ptr[i + 1] < ptr[i];
+  const int nnz = ptr[n];
+  const int j0 = max(ptr[r0], 0), j1 = min(ptr[r1], nnz);
   int lo = c, hi = c;
-  for (int j = ptr[r0] + threadIdx.x; j < ptr[r1]; j += blockDim.x) {
-    const int cc = col[j] / chunk;
+  bool bad_col = false;
+  for (int j = j0 + (int)threadIdx.x; j < j1; j += blockDim.x) {
+    const int cj = col[j];
+    if (cj < 0 || cj >= n) {
+      bad_col = true;
+      continue;
+    }
+    const int cc = cj / chunk;
     lo = min(lo, cc);
     hi = max(hi, cc);
   }
+  if (bad_col) atomicExch(scr + 4, 1u);
+  if (bad_ptr) atomicExch(scr + 5, 1u);
   atomicMin(&s_lo, lo);
   atomicMax(&s_hi, hi);
   __syncthreads();
   if (threadIdx.x == 0) {
     scr[kNoAllocHeader + c] = (unsigned)s_lo;
     scr[kNoAllocHeader + kNoAllocMaxChunks + c] = (unsigned)s_hi;
-    atomicMax(scr + 2, (unsigned)(ptr[r1] - ptr[r0]));
+    atomicMax(scr + 2, (unsigned)max(j1 - j0, 0));
     atomicMax(scr + 3, (unsigned)max(c - s_lo, s_hi - c));
   }
 }
@@ -3438,9 +3457,12 @@ extern "C" int mpkg_pipe_noalloc(int n, const int *d_ptr, const int *d_col, cons
   CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(unsigned int) * (size_t)(nlevel + 1) * nchunk, st));
   noalloc_deps_kernel<<<(unsigned)nchunk, 256, 0, st>>>(n, chunk, d_ptr, d_col, scr);
   CUDA_TRY(cudaGetLastError());
-  unsigned int info[2] = {0, 0};
+  unsigned int info[5] = {0, 0, 0, 0, 0};
   CUDA_TRY(cudaMemcpyAsync(info, scr + 2, sizeof info, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
+  if (info[3]) return fail(kEInval, "mpkg_pipe_noalloc: ptr[0] must be 0 and ptr non-decreasing");
+  if (info[4]) return fail(kEInval, "mpkg_pipe_noalloc: the matrix has no entries");
+  if (info[2]) return fail(kERange, "mpkg_pipe_noalloc: column index out of range");
   const int max_nnz = std::max<int>((int)info[0], 1);
   const long reach = info[1];
   const size_t smem = pipe_smem_size(chunk, max_nnz, true, sizeof(double));
