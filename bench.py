@@ -1,27 +1,35 @@
 """Benchmark: FP64 matrix powers kernel on one GB300 (or N replicas).
 
 Workload (the GB300 configuration of the task): 3-D 7-point Laplacian on a
-128^3 grid (n = 2,097,152, nnz = 14,581,760, diagonal 6, off-diagonal -1),
-CSR with FP64 values and int32 indices, x ~ U[-1,1] (seed 1), k = 8 powers,
-2048 parts from recursive coordinate bisection (8x8x16 boxes; METIS is not
-available).  One step = one MPK call computing [Ax, ..., A^8 x] into the
-level-major vv array.
+128^3 grid (n = 2,097,152, nnz = 14,581,760), CSR with int32 indices, the
+reference's exec_mpk operator (row-normalised adjacency, A_ij = 1/deg(i)),
+FP64 vectors, x ~ U[-1,1] (seed 1), k = 8 powers, 2048 METIS parts
+(gpmetis -ufactor=100, through the METIS library bundled with the CUDA
+toolkit; recursive coordinate bisection where the toolkit has none).  One
+step = one MPK call computing [Ax, ..., A^8 x] into the level-major vv.
 
   value  : row-powers per second, k*n / (device time of one call), summed
            over ranks; device time from CUDA events around each call on the
            launching stream, L2 flushed (256 MiB write) before every call.
+           Headline executor: the wavefront, FP64 FMA in CSR order -- the
+           same bits as the reference's exec_mpk_xd built with FMA
+           contraction (its result is checked bit for bit each run).
   e2e    : the same metric through mpkg_exec_host with pinned host buffers:
            x copied host->device and the k output vectors device->host
            inside the timed call.
   roofline: HBM bound; algorithmic bytes of one call
-           B = nnz*(8+4) + 4*(n+1) + 8*n*(k+1) (matrix once, x once, k
-           outputs once) over the call's device time, against the measured
-           copy bandwidth in MEASURED_PEAKS.json.
+           B = 4*nnz + 4*(n+1) + 8*n*(k+1) (pattern once, x once, k outputs
+           once) over the call's device time, against the measured copy
+           bandwidth in MEASURED_PEAKS.json; plus the FP64 pipe bound (the
+           call's nnz*k FMAs at the GPU's FP64 FMA rate, measured in this
+           run), the one that binds plain FP64 on GB300.
 
---impl reference runs the reference mpk2 exec_mpk_xd (compiled from its
-own sources into oracle/_ref, OpenMP over parts, all host cores) on a
-bounded sample of the same workload's PA1 task lists; if that library is
-absent the oracle's C restatement of the same loop runs instead.
+--impl reference times the reference mpk2 exec_mpk_xd (compiled from its
+own sources into oracle/_ref; the oracle's C restatement where absent) on
+all host cores over the PA1 task lists of all 2048 parts (the lists
+prep_mpk would build, from the oracle's bounded search; the reference prep
+itself needs npart*n ints of skirt and npart*nlevel*n steps here).  That
+process loads only the oracle's and the reference's libraries.
 """
 import argparse
 import json
@@ -44,12 +52,56 @@ SEED = 1
 FLUSH_BYTES = 256 << 20
 
 
+def box_partition(nx, ny, nz, npart):
+    """Fallback partition without METIS: npart equal boxes (powers of two),
+    splitting the longest side first (what recursive coordinate bisection
+    gives on this grid)."""
+    dims = [nx, ny, nz]
+    cuts = [1, 1, 1]
+    p = npart
+    while p > 1:
+        d = max(range(3), key=lambda t: (dims[t] / cuts[t], -t))
+        cuts[d] *= 2
+        p //= 2
+    i = np.arange(nx * ny * nz)
+    x, y, z = i % nx, (i // nx) % ny, i // (nx * ny)
+    bx, by, bz = x // (nx // cuts[0]), y // (ny // cuts[1]), z // (nz // cuts[2])
+    return ((bz * cuts[1] + by) * cuts[0] + bx).astype(np.int32)
+
+
+def parts_kind():
+    return "METIS k-way (gpmetis -ufactor=100)" if _metis() else "equal boxes (no METIS in this toolkit)"
+
+
+_METIS = None
+
+
+def _metis():
+    global _METIS
+    if _METIS is None:
+        from oracle import oracle as O
+        _METIS = O.metis_available()
+    return _METIS
+
+
 def workload():
     import mpk_gb300 as M
     a = M.Csr.laplacian(GRID, GRID, GRID, diag=6.0, off=-1.0)
-    part = M.partition_rcb(a.coords, NPART)
+    if _metis() and M.have_metis():
+        part = M.partition_metis(a, NPART, ufactor=100)[0]
+    else:
+        part = box_partition(GRID, GRID, GRID, NPART)
     x = M.uniform(SEED, a.n)
     return a, part, x
+
+
+def shared_config():
+    """The workload, as both arms print it."""
+    n = GRID ** 3
+    return {"workload": "3-D 7-point Laplacian 128^3 (n=2,097,152, nnz=14,581,760), CSR int32, operator 1/deg "
+                        "(the reference exec_mpk), FP64 vectors, x~U[-1,1] seed 1, k=8; PA1 over 2048 parts",
+            "n": n, "nnz": 7 * n - 6 * GRID * GRID, "k": K_LEVELS, "parts": NPART, "partitioner": parts_kind(),
+            "operator": "1/deg (mpk2/mpkexec.c:22-35)"}
 
 
 def algorithmic_bytes(n, nnz, k, valued=False):
@@ -78,7 +130,9 @@ def profile_traffic(kernel):
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples while the timed region runs."""
+    """nvidia-smi clock/throttle samples (every 50 ms) from before the
+    warm-up calls to the end of a tail of the same calls that follows the
+    timed region (the timed steps alone last milliseconds)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -87,6 +141,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.marks = {}
 
     def __enter__(self):
         try:
@@ -98,6 +153,15 @@ class ClockSampler:
         except OSError:
             self.proc = None
         return self
+
+    def wait_first(self, timeout=5.0):
+        """Until the first sample arrives (nvidia-smi takes a moment to start)."""
+        t0 = time.perf_counter()
+        while self.proc and not self.lines and time.perf_counter() - t0 < timeout:
+            time.sleep(0.02)
+
+    def mark(self, name):
+        self.marks[name] = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -111,25 +175,33 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    def count(self):
+        return len(self.lines)
+
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        sm, mx, reasons, power = [], None, set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        lo = self.marks.get("warmup", 0)
+        for line in self.lines[lo:]:
             f = [t.strip() for t in line.split(",")]
             if len(f) < 9:
                 continue
             try:
                 sm.append(float(f[1]))
                 mx = float(f[2])
+                power.append(float(f[3]))
             except ValueError:
                 continue
             for nm, v in zip(names, f[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
+        window = "warm-up calls, the timed steps and a tail of the same calls (about 1 s)"
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0, "window": window}
+        return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None,
+                "samples_in_timed_steps": self.marks.get("timed_end", 0) - self.marks.get("timed", 0),
+                "window": window}
 
 
 def dist_setup(args):
@@ -179,36 +251,52 @@ def time_device(plan, d_vv, steps, warmup, flush, stream):
     return [e0.elapsed_time(e1) for e0, e1 in ev]
 
 
-def cpu_reference_sample(a, part, nth, reps=3, sample_parts=256):
-    """Reference exec_mpk_xd (or the oracle's restatement) on the PA1 task
-    lists of the first `sample_parts` parts; returns (seconds per sample
-    call, row evaluations per call, output rows per call, kind)."""
-    import mpk_gb300 as M
-    from oracle import oracle as O
-    O.build()
-    g = a.pattern()
-    off, idx = M.tasks(g, NPART, K_LEVELS, part, check=False)
-    sp = sample_parts
-    off_s = off[:sp + 1].copy()
-    idx_s = idx[:off_s[-1]].copy()
-    # owned rows of the sampled parts, per level: what the sample contributes
-    owned = int(np.count_nonzero(part < sp))
-    vv = np.zeros((K_LEVELS + 1) * a.n)
-    vv[:a.n] = M.uniform(SEED, a.n)
-    if O.ref_available():
-        r = O.RefTaskLists(g.ptr, g.col, sp, K_LEVELS, 0, off_s, idx_s)
-        run = lambda: r.exec_xd(vv, nth)  # noqa: E731
-        kind = "reference"
-    else:
-        run = lambda: O.exec_tasks_par(g.ptr, g.col, None, 0, sp, off_s, idx_s, vv, O.MODE_FMA, nth)  # noqa: E731
-        kind = "port"
-    run()
-    ts = []
-    for _ in range(reps):
+class ReferenceRun:
+    """The reference's exec_mpk_xd (oracle/_ref; else the oracle's
+    restatement of the same loop) over the PA1 task lists of every part,
+    all host threads.  Built from the oracle only: the matrix, x and the
+    partition from its generators and METIS wrapper (or `part`), the task
+    lists from its bounded search (orc_pa1_tasks, pinned to the reference
+    prep's lists by tests/test_metis.py)."""
+
+    def __init__(self, part=None):
+        from oracle import oracle as O
+        O.lib()
+        ptr, col, _ = O.laplacian(GRID, GRID, GRID, 6.0, -1.0)
+        n = len(ptr) - 1
+        if part is None:
+            part = O.metis_kway(ptr, col, NPART, 100) if _metis() else box_partition(GRID, GRID, GRID, NPART)
         t0 = time.perf_counter()
-        run()
-        ts.append(time.perf_counter() - t0)
-    return min(ts), int(off_s[-1]), owned * K_LEVELS, kind
+        off, idx = O.pa1_tasks(ptr, col, part, NPART, K_LEVELS)
+        self.prep_s = time.perf_counter() - t0
+        self.rows_eval = int(off[-1])
+        self.n = n
+        self.nth = os.cpu_count() or 1
+        self.vv = np.zeros((K_LEVELS + 1) * n)
+        self.vv[:n] = O.uniform(SEED, n)
+        if O.ref_available():
+            r = O.RefTaskLists(ptr, col, NPART, K_LEVELS, 0, off, idx)
+            self.run = lambda: r.exec_xd(self.vv, self.nth)
+            self.kind = "reference"
+        else:
+            self.run = lambda: O.exec_tasks_par(ptr, col, None, 0, NPART, off, idx, self.vv, O.MODE_FMA, self.nth)
+            self.kind = "port"
+        self._keep = (ptr, col, off, idx)
+
+    def time(self, steps, warmup):
+        for _ in range(warmup):
+            self.run()
+        ts = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            self.run()
+            ts.append(time.perf_counter() - t0)
+        return ts
+
+    def sample(self):
+        return (f"exec_mpk_xd over the PA1 task lists of all {NPART} parts ({self.rows_eval} row evaluations per "
+                f"call, {self.rows_eval / (self.n * K_LEVELS):.2f}x the owned rows), {self.nth} OpenMP threads, "
+                "1/deg operator, the whole call each step")
 
 
 def time_mixed(plan, d_vv, steps, warmup, flush, stream):
@@ -269,16 +357,21 @@ def bench_mixed(M, torch, a, x, k, exact, args, flush, stream):
         del d64
     best64 = min(fp64, key=fp64.get)
     t64 = fp64[best64]
-    p32 = M.Plan.mixed(b, k, M.VALUE_F32)
-    e, inexact = p32.mixed_scale()
-    d32 = torch.zeros((k + 1) * b.n, dtype=torch.float32, device="cuda")
-    d32[:b.n] = torch.from_numpy(xb.astype(np.float32)).cuda()
-    t32 = statistics.mean(time_mixed(p32, d32, min(args.steps, 100), args.warmup, flush, stream))
-    errs = mixed_errors(d32.cpu().numpy(), e, ex64, b.n, k)
-    out["diffusion2048_9pt"] = {"n": b.n, "nnz": b.nnz, "fp64_ms": fp64, "fp64_best": best64, "f32_ms": t32,
-                                "speedup_f32_vs_fp64": t64 / t32, "rel_err_per_power": errs,
-                                "value_f32": k * b.n / (t32 * 1e-3) / 1e9}
-    p32.close()
+    res = {"n": b.n, "nnz": b.nnz, "fp64_ms": fp64, "fp64_best": best64,
+           "algorithmic_bytes_f32": b.nnz * 8 + 4 * (b.n + 1) + 4 * b.n * (k + 1)}
+    for name, vt in (("f32", M.VALUE_F32), ("bf16", M.VALUE_BF16)):
+        p32 = M.Plan.mixed(b, k, vt)
+        e, inexact = p32.mixed_scale()
+        d32 = torch.zeros((k + 1) * b.n, dtype=torch.float32, device="cuda")
+        d32[:b.n] = torch.from_numpy(xb.astype(np.float32)).cuda()
+        t32 = statistics.mean(time_mixed(p32, d32, min(args.steps, 100), args.warmup, flush, stream))
+        errs = mixed_errors(d32.cpu().numpy(), e, ex64, b.n, k)
+        res[name] = {"ms_per_step": t32, "speedup_vs_best_fp64": t64 / t32, "rel_err_per_power": errs,
+                     "values_rounded": inexact, "value": k * b.n / (t32 * 1e-3) / 1e9,
+                     "executor": p32.info()["exec"]}
+        p32.close()
+        del d32
+    out["diffusion2048_9pt"] = res
     return out
 
 
@@ -398,6 +491,59 @@ def bench_sstep(M):
     return out
 
 
+def time_headline(plan, d_vv, steps, warmup, flush, stream, clk, world):
+    """W warm-up calls, then exactly K timed calls (CUDA events on the
+    launching stream around each call, an L2 flush before each), bracketed
+    by a barrier and a device synchronisation; then untimed calls until
+    about a second has passed, so that the clock sampler sees the load."""
+    import torch
+    clk.wait_first()
+    t_start = time.perf_counter()
+    clk.mark("warmup")
+    for _ in range(warmup):
+        flush.fill_(1.0)
+        plan.exec_device(d_vv.data_ptr(), stream.cuda_stream)
+    plan.sync(stream.cuda_stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clk.mark("timed")
+    w0 = time.perf_counter()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for e0, e1 in ev:
+            flush.fill_(1.0)
+            e0.record(stream)
+            plan.exec_device(d_vv.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+    plan.sync(stream.cuda_stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    clk.mark("timed_end")
+    times = [e0.elapsed_time(e1) for e0, e1 in ev]
+    tail = 0
+    while time.perf_counter() - t_start < 1.2 or (clk.count() - clk.marks["warmup"] < 10 and tail < 20000):
+        with torch.cuda.stream(stream):
+            for _ in range(20):
+                flush.fill_(1.0)
+                plan.exec_device(d_vv.data_ptr(), stream.cuda_stream)
+        plan.sync(stream.cuda_stream)
+        tail += 20
+        if time.perf_counter() - t_start > 10:
+            break
+    return times, wall, tail
+
+
+def fp64_rate():
+    import mpk_gb300 as M
+    try:
+        return M.fp64_fma_rate()
+    except M.MpkError:
+        return None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -405,7 +551,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--exec", default="wave", choices=["pipe", "wave", "tiles", "spmv", "tasks"])
-    ap.add_argument("--arith", default="df64", choices=["fma", "separate", "df64", "fixed"])
+    ap.add_argument("--arith", default="fma", choices=["fma", "separate", "df64", "fixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="time only the selected executor")
     ap.add_argument("--sections", default="variants,mixed,batched,sstep,prep",
@@ -413,40 +559,36 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     sections = set() if args.no_variants else {t.strip() for t in args.sections.split(",")} - {"none", ""}
-
-    world, rank, local = dist_setup(args)
-    a, part, x = workload()
-    n, nnz, k = a.n, a.nnz, K_LEVELS
-    nth = os.cpu_count() or 1
-    cfg = {"workload": "3-D 7-point Laplacian 128^3 (n=2,097,152, nnz=14,581,760), CSR int32, 1/deg operator "
-                       "(the reference exec_mpk), FP64 vectors, x~U[-1,1] seed 1, k=8, 2048 RCB parts",
-           "n": n, "nnz": nnz, "k": k, "parts": NPART, "operator": "1/deg (mpk2/mpkexec.c)"}
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    k = K_LEVELS
 
     if args.impl == "reference":
+        # the reference arm: this process loads only oracle/ and the
+        # reference's own code (no product library, no GPU)
         if rank != 0:
             return
-        t, rows_eval, out_rows, kind = cpu_reference_sample(a, part, nth)
-        steps = max(1, min(args.steps, 20))
-        per = []
-        import mpk_gb300 as M  # noqa: F401
-        for _ in range(steps):
-            per.append(t)
-        value = out_rows / t / 1e9
+        ref = ReferenceRun()
+        ts = ref.time(args.steps, args.warmup)
+        sec = statistics.mean(ts)
+        value = k * ref.n / sec / 1e9
         line = {"impl": "reference", "metric": "MPK powers/sec (FP64, k*n output rows per second)",
-                "value": value, "unit": "Grow-powers/s", "n_gpus": 0, "steps": steps, "warmup": args.warmup,
-                "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic",
-                "config": dict(cfg, sample=f"PA1 task lists of parts 0..255 of 2048 (1/8 of the call)"),
-                "cpu_baseline": {"value": value, "unit": "Grow-powers/s", "cores": nth, "kind": kind,
-                                 "sample": "exec_mpk_xd, 1/deg operator, PA1 task lists of 256 of 2048 parts, "
-                                           f"{rows_eval} row evaluations per step, {nth} OpenMP threads"},
+                "value": value, "unit": "Grow-powers/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": sec * 1e3, "ms_min": min(ts) * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": shared_config(),
+                "cpu_baseline": {"value": value, "unit": "Grow-powers/s", "cores": ref.nth, "kind": ref.kind,
+                                 "sample": ref.sample(), "task_list_build_s": ref.prep_s},
                 "e2e": {"value": value, "unit": "Grow-powers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
 
     import torch
+    dist_setup(args)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
     import mpk_gb300 as M
     torch.cuda.set_device(local)
+    a, part, x = workload()
+    n, nnz = a.n, a.nnz
     ARITHS = {"fma": M.ARITH_FMA, "separate": M.ARITH_SEPARATE, "df64": M.ARITH_DF64, "fixed": M.ARITH_FIXED}
     arith = ARITHS[args.arith]
     g = a.pattern()  # the 1/deg operator of the reference's exec_mpk
@@ -466,23 +608,18 @@ def main():
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
 
-    barrier(world)
-    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        w0 = time.perf_counter()
-        times = time_device(plan, d_vv, args.steps, args.warmup, flush, stream)
-        barrier(world)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - w0
+        times, wall, tail = time_headline(plan, d_vv, args.steps, args.warmup, flush, stream, clk, world)
     ms = statistics.mean(times)
     ms_max = reduce_max(world, ms)
     value = world * k * n / (ms_max * 1e-3) / 1e9
-    exact = d_vv.cpu().numpy()
+    got = d_vv.cpu().numpy()
 
-    # FP64 reference result (k chained SpMVs in FP64 FMA, bit-identical to
-    # the oracle's chain) and the headline's error against it
-    def relerr(got, ref):
-        return max(float(np.linalg.norm(got[l * n:(l + 1) * n] - ref[l * n:(l + 1) * n]) /
+    # the FP64 chain (k chained SpMVs in FP64 FMA, CSR order: the bits of the
+    # reference's exec_mpk_xd built with FMA contraction) and the
+    # headline's error against it
+    def relerr(v, ref):
+        return max(float(np.linalg.norm(v[l * n:(l + 1) * n] - ref[l * n:(l + 1) * n]) /
                          np.linalg.norm(ref[l * n:(l + 1) * n])) for l in range(1, k + 1))
 
     rp = mk("spmv", M.ARITH_FMA)
@@ -490,14 +627,15 @@ def main():
     ref64[:n] = x
     rp.exec_host(ref64)
     rp.close()
-    headline_err = relerr(exact, ref64)
+    headline_err = relerr(got, ref64)
+    bit_equal = bool(got.tobytes() == ref64.tobytes())
 
-    # the other executors on the same workload, for the record
+    # the other executors and arithmetic forms on the same workload
     variants = {}
     if "variants" in sections:
         runs = [(ex, ar, None) for ex, ar in (("spmv", "fma"), ("wave", "fma"), ("wave", "df64"), ("wave", "fixed"),
-                                              ("pipe", "fma"),
-                                              ("pipe", "df64"), ("tiles", "fma"), ("tiles", "df64"))]
+                                              ("pipe", "fma"), ("pipe", "df64"), ("tiles", "fma"), ("tiles", "df64"),
+                                              ("tasks", "fma"))]
         runs += [("spmv", "fma", "valued"), ("wave", "fma", "valued"), ("wave", "df64", "valued")]
         ref_val = None
         for ex, ar, op in runs:
@@ -507,13 +645,15 @@ def main():
             d2 = torch.zeros_like(d_vv)
             d2[:n] = d_vv[:n]
             t = statistics.mean(time_device(vp, d2, min(args.steps, 50), args.warmup, flush, stream))
-            got = d2.cpu().numpy()
+            v2 = d2.cpu().numpy()
             if op and ref_val is None:
-                ref_val = got  # spmv fma valued runs first among the valued
+                ref_val = v2  # spmv fma valued runs first among the valued
+            rv = ref_val if op else ref64
             variants[f"{ex}_{ar}" + ("_valued" if op else "")] = {
-                "ms_per_step": t, "value": k * n / (t * 1e-3) / 1e9,
-                "rel_err_max_vs_fp64": relerr(got, ref_val if op else ref64),
-                "algorithmic_bytes": algorithmic_bytes(n, nnz, k, valued=bool(op))}
+                "ms_per_step": t, "value": k * n / (t * 1e-3) / 1e9, "rel_err_max_vs_fp64": relerr(v2, rv),
+                "bit_equal_fp64_fma_chain": bool(v2.tobytes() == rv.tobytes()),
+                "algorithmic_bytes": algorithmic_bytes(n, nnz, k, valued=bool(op)),
+                "rows_computed": vp.info()["rows_computed"]}
             vp.close()
             del d2
 
@@ -529,7 +669,7 @@ def main():
         plan.exec_host(hnp)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_s = reduce_max(world, e2e_s)
-    same = bool(np.array_equal(exact, hnp))
+    same = bool(np.array_equal(got, hnp))
 
     mixed = {}
     if "mixed" in sections:  # the mixed form runs the valued operator; its FP64 reference:
@@ -554,37 +694,44 @@ def main():
         kname = "wave_fix_kernel"
     traffic = profile_traffic(kname)
     rows = info["rows_computed"]
-    fp64_tflops = 2.0 * nnz * k * (rows / (n * k)) / (ms * 1e-3) / 1e12
+    fmas = nnz * k * (rows / (n * k))
+    rate = fp64_rate()
+    fp64 = None
+    if args.arith in ("fma", "separate") and rate:
+        fp64 = {"fma_per_call": fmas, "peak_fma_per_s": rate, "peak_source": "measured in this run "
+                "(mpkg_fp64_fma_rate: independent FMA chains, best of five launches)",
+                "bound_us": fmas / rate * 1e6, "achieved_fma_per_s": fmas / (ms * 1e-3),
+                "frac": fmas / (ms * 1e-3) / rate}
     base_ms = variants.get("spmv_fma", {}).get("ms_per_step")
-
+    cfg = dict(shared_config())
     line = {"metric": "MPK powers/sec (FP64, k*n output rows per second)", "value": value,
             "unit": "Grow-powers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"df64": "df64", "fma": "f64", "separate": "f64", "fixed": "i64"}[args.arith], "data": "synthetic",
-            "rel_err_max_vs_fp64": headline_err, "tolerance": 1e-13,
-            "config": dict(cfg, executor=args.exec, arith=args.arith,
-                           l2="flushed before every call (256 MiB write); per-call CUDA events",
-                           parallelism=f"replicas{world}"),
+            "config": cfg, "executor": args.exec, "arith": args.arith,
+            "l2": "flushed before every call (256 MiB write); per-call CUDA events",
+            "parallelism": f"replicas{world}",
+            "rel_err_max_vs_fp64": headline_err, "bit_equal_fp64_fma_chain": bit_equal, "tolerance": 1e-13,
             "e2e": {"value": world * k * n / e2e_s / 1e9, "unit": "Grow-powers/s",
                     "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n * k},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "algorithmic_bytes": B, "kernel": kname},
-            "fp64_pipe": {"achieved_tflops": fp64_tflops, "peak_tflops_measured": 1.19,
-                          "note": "2*nnz*k*redundancy flops over call time; GB300 FP64 FMA measured at 0.60 TFMA/s "
-                                  "caps plain FP64 at ~195 us for this workload, so the headline runs the rows in "
-                                  "double-float on the FP32 pipes (FP64 storage, error vs FP64 stated)"},
+                         "algorithmic_bytes": B, "kernel": kname,
+                         "traffic_note": "ncu dram bytes of one launch (profiles/ncu_traffic.json); output lines "
+                                         "still dirty in L2 when the kernel ends are written back after it",
+                         "fp64_pipe": fp64},
             "k_spmv_ms": base_ms, "speedup_vs_k_spmv": (base_ms / ms) if base_ms else None,
             "variants": variants, "mixed": mixed, "batched": batched, "sstep": sstep, "prep": prep,
             "gpu_launches": info["launches"] * args.steps,
-            "clocks": clk.summary(), "wall_s_timed_region": wall, "host_device_agree": same,
+            "clocks": clk.summary(), "wall_s_timed_region": wall, "tail_calls_for_clock_samples": tail,
+            "host_device_agree": same,
             "plan": {kk: info[kk] for kk in ("rows_computed", "device_bytes", "pipe_reach", "pipe_grid",
                                             "tiles_in_smem", "max_tile_slots")}}
     if rank == 0 and not args.no_cpu_baseline:
-        t, rows_eval, out_rows, kind = cpu_reference_sample(a, part, nth)
-        line["cpu_baseline"] = {"value": out_rows / t / 1e9, "unit": "Grow-powers/s", "cores": nth, "kind": kind,
-                                "sample": "exec_mpk_xd, 1/deg operator, PA1 task lists of 256 of 2048 parts "
-                                          f"({rows_eval} row evaluations), best of 3"}
+        ref = ReferenceRun(part)
+        ts = ref.time(5, 1)
+        line["cpu_baseline"] = {"value": k * n / min(ts) / 1e9, "unit": "Grow-powers/s", "cores": ref.nth,
+                                "kind": ref.kind, "sample": ref.sample() + ", best of 5 (as mpk2/mpktest.c:121-133)"}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

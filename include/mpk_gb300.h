@@ -78,6 +78,11 @@ extern "C" {
 #define MPKG_PD_PART_BLOCKSHIFT 0 /* contiguous blocks, shifted by half a
                                      block per call */
 #define MPKG_PD_PART_BFS 1        /* breadth-first recursive bisection */
+#define MPKG_PD_PART_METIS 2      /* METIS_PartGraphKway with the reference's
+                                     arguments (pdmpk/pdmpk_buffers.cc:
+                                     183-202): the matrix pattern as is,
+                                     default options; edge weights on the
+                                     re-partitioning calls */
 
 /* Value storage of the mixed-precision form. */
 #define MPKG_VALUE_F32 0
@@ -358,6 +363,12 @@ int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels);
 int mpkg_pipe_noalloc(int n, const int *d_ptr, const int *d_col, const double *d_val,
                       int nlevel, double *d_vv, void *stream);
 
+/* Measurement utility (no counterpart in the reference): the current
+ * GPU's peak FP64 fused multiply-add rate in FMAs per second, from a
+ * kernel of independent FMA chains timed with CUDA events (best of five
+ * launches).  The plain FP64 forms are bound by it on GB300. */
+int mpkg_fp64_fma_rate(double *fma_per_s);
+
 /* Stand-alone k-SpMV on device arrays (no plan). */
 int mpkg_spmv_chain_device(int n, const int *d_ptr, const int *d_col, const double *d_val,
                            int nlevel, double *d_vv, int arith, void *stream);
@@ -446,8 +457,20 @@ int mpkg_work_count(const char *dir, long *comm, long *ops, long *minops, long *
  * steps in the published order). */
 int mpkg_lapjv(const int *sums, int npart, int *perm);
 
-/* Partitioners (METIS is not available): recursive coordinate bisection
- * (coords: dim ints per vertex) and breadth-first recursive bisection. */
+/* METIS k-way partition, as the reference's `gpmetis -ufactor=<ufactor>
+ * graph npart` (mpk2/driver.c:63-66, mpk2/driver.sh:46,63) computes it: the
+ * METIS library bundled with the CUDA toolkit, called on the graph without
+ * its self loops, default options except the imbalance ufactor (<= 0
+ * keeps METIS's default) and 0-based numbering.  vwgt (n) and adjwgt (one
+ * per stored entry, as the weighted graphs level2wcrs writes) may be
+ * NULL; edgecut may be NULL.  Returns MPKG_EINVAL when the library was
+ * built without METIS (mpkg_have_metis() == 0). */
+int mpkg_have_metis(void);
+int mpkg_partition_metis(int n, const int *ptr, const int *col, const int *vwgt, const int *adjwgt, int npart,
+                         int ufactor, int *part, long *edgecut);
+
+/* Project partitioners: recursive coordinate bisection (coords: dim ints
+ * per vertex) and breadth-first recursive bisection. */
 int mpkg_partition_rcb(int n, const int *coords, int dim, int npart, int *part);
 int mpkg_partition_bfs(int n, const int *ptr, const int *col, int npart, int *part);
 

@@ -151,6 +151,12 @@ typedef std::function<int(const Csr &csr, const idx_t *adjwgt, int npart, int ca
 Partitioner BlockShiftPartitioner();
 // Breadth-first recursive bisection of the graph (weights ignored).
 Partitioner BfsPartitioner();
+// METIS_PartGraphKway exactly as the reference calls it
+// (pdmpk/pdmpk_buffers.cc:183-202): the CSR pattern as is (diagonal
+// included), no vertex weights, the edge weights on calls after the first,
+// default options (none on the first call).  Fails when the library was
+// built without METIS.
+Partitioner MetisPartitioner();
 
 // pdmpk/args.h: the prep parameters.
 struct Args {

@@ -22,7 +22,7 @@ OK, EINVAL, EIO, EFORMAT, ESTRUCT, ECUDA, ETIMEOUT, ENOMEM, ERANGE = 0, -1, -2, 
 ARITH_FMA, ARITH_SEPARATE, ARITH_DF64, ARITH_FIXED = 0, 1, 2, 3
 EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS, EXEC_MIXED, EXEC_PDMPK, EXEC_WAVE, EXEC_BATCH = \
     0, 1, 2, 3, 4, 5, 6, 7, 8
-PD_PART_BLOCKSHIFT, PD_PART_BFS = 0, 1
+PD_PART_BLOCKSHIFT, PD_PART_BFS, PD_PART_METIS = 0, 1, 2
 VALUE_F32, VALUE_BF16 = 0, 1
 
 _ERRNAMES = {EINVAL: "EINVAL", EIO: "EIO", EFORMAT: "EFORMAT", ESTRUCT: "ESTRUCT", ECUDA: "ECUDA",
@@ -135,6 +135,8 @@ def _declare(L):
         "mpkg_sstep_loop": (I, [I]),
         "mpkg_partition_rcb": (I, [I, P, I, I, P]),
         "mpkg_partition_bfs": (I, [I, P, P, I, P]),
+        "mpkg_have_metis": (I, []),
+        "mpkg_partition_metis": (I, [I, P, P, P, P, I, I, P, P]),
         "mpkg_gen_stencil": (I, [C.c_char_p, I, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
         "mpkg_gen_laplacian": (I, [I, I, I, D, D, C.POINTER(I), C.POINTER(Lg), pp, pp, pp, pp]),
         "mpkg_uniform": (None, [C.c_uint64, Lg, P]),
@@ -146,6 +148,7 @@ def _declare(L):
         "mpkg_bufs_prepare": (I, [C.c_char_p]),
         "mpkg_last_error": (C.c_char_p, []),
         "mpkg_version": (I, []),
+        "mpkg_fp64_fma_rate": (I, [C.POINTER(D)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -365,6 +368,30 @@ def partition_rcb(coords, npart):
     part = np.empty(n, dtype=np.int32)
     _check(lib().mpkg_partition_rcb(n, _ptr(coords), dim, npart, _ptr(part)))
     return part
+
+
+def fp64_fma_rate():
+    """Peak FP64 FMA rate of the current GPU (FMAs per second)."""
+    r = C.c_double()
+    _check(lib().mpkg_fp64_fma_rate(C.byref(r)))
+    return r.value
+
+
+def have_metis():
+    """True when the library links the CUDA toolkit's METIS."""
+    return bool(lib().mpkg_have_metis())
+
+
+def partition_metis(a: Csr, npart, ufactor=0, vwgt=None, adjwgt=None):
+    """METIS k-way partition as `gpmetis -ufactor=<ufactor>` computes it
+    (mpk2/driver.c:63-66): the graph without self loops, default options
+    otherwise.  Returns (part, edgecut)."""
+    part = np.empty(a.n, dtype=np.int32)
+    vw, ew = _i32(vwgt), _i32(adjwgt)
+    cut = C.c_long()
+    _check(lib().mpkg_partition_metis(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(vw), _ptr(ew), npart, ufactor, _ptr(part),
+                                      C.byref(cut)))
+    return part, cut.value
 
 
 def partition_bfs(a: Csr, npart):

@@ -1,5 +1,8 @@
 """Builds libmpk_gb300.so in-tree: host C++ with g++, kernels with nvcc for
-sm_103a, translation units compiled in parallel, linked with nvcc."""
+sm_103a, translation units compiled in parallel, linked with nvcc.  The
+METIS library bundled with the CUDA toolkit (libmetis_static.a) is linked
+in when present (the reference's partitioner); without it the library
+builds with METIS calls returning an error."""
 import os
 import shutil
 import subprocess
@@ -22,6 +25,19 @@ def _nvcc():
     raise RuntimeError("nvcc not found")
 
 
+def _metis_archive(nvcc):
+    """The toolkit's libmetis_static.a, or None."""
+    root = os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    cands = [os.path.join(root, "lib64", "libmetis_static.a")]
+    tdir = os.path.join(root, "targets")
+    if os.path.isdir(tdir):
+        cands += [os.path.join(tdir, t, "lib", "libmetis_static.a") for t in sorted(os.listdir(tdir))]
+    for c in cands:
+        if os.path.exists(c):
+            return c
+    return None
+
+
 def _newer(target, sources):
     if not os.path.exists(target):
         return True
@@ -32,6 +48,25 @@ def _newer(target, sources):
 def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
+    metis = None if os.environ.get("MPKG_NO_METIS") else _metis_archive(nvcc)
+    try:
+        return _build(nvcc, metis, verbose, force)
+    except RuntimeError:
+        if metis is None:
+            raise
+        # the archive did not link (e.g. not position-independent here):
+        # build without METIS
+        sys.stderr.write("libmpk_gb300: linking METIS failed, building without it\n")
+        return _build(nvcc, None, verbose, True)
+
+
+def _build(nvcc, metis, verbose, force):
+    stamp = os.path.join(BUILD, "metis.stamp")
+    want = metis or "none"
+    if not os.path.exists(stamp) or open(stamp).read() != want:
+        force = True
+        with open(stamp, "w") as f:
+            f.write(want)
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")]
     inc = os.path.join(os.path.dirname(HERE), "include")
     headers += [os.path.join(inc, h) for h in os.listdir(inc) if h.endswith(".h")]
@@ -42,7 +77,7 @@ def build(verbose=False, force=False):
         objs.append(o)
         if force or _newer(o, [s] + headers):
             jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", "-Wno-unused-function",
-                         "-c", s, "-o", o])
+                         *(["-DMPKG_HAVE_METIS"] if metis else []), "-c", s, "-o", o])
     for src in CUDA_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")
@@ -63,7 +98,7 @@ def build(verbose=False, force=False):
     if failed:
         raise RuntimeError("libmpk_gb300 build failed")
     if force or _newer(LIB, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, *([metis, "-Xlinker", "--exclude-libs,libmetis_static.a"] if metis else []), "-lcudart"]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout)

@@ -186,6 +186,22 @@ int mpkg_partition_rcb(int n, const int *coords, int dim, int npart, int *part) 
   return kOk;
 }
 
+int mpkg_have_metis(void) { return have_metis() ? 1 : 0; }
+
+int mpkg_partition_metis(int n, const int *ptr, const int *col, const int *vwgt, const int *adjwgt, int npart,
+                         int ufactor, int *part, long *edgecut) {
+  clear_error();
+  int rc = check_csr_host(n, ptr, col);
+  if (rc) return rc;
+  if (!part) return fail(kEInval, "null argument");
+  Csr g = view_csr(n, ptr, col);
+  std::vector<int> out;
+  rc = partition_metis(g, vwgt, adjwgt, npart, ufactor, &out, edgecut);
+  if (rc) return rc;
+  std::copy(out.begin(), out.end(), part);
+  return kOk;
+}
+
 int mpkg_partition_bfs(int n, const int *ptr, const int *col, int npart, int *part) {
   clear_error();
   int rc = check_csr_host(n, ptr, col);

@@ -2967,6 +2967,7 @@ int mpkg_pdmpk_prep(int n, const int *ptr, const int *col, const double *val, in
   args.weight_update_method = weight_update_method;
   if (partitioner == MPKG_PD_PART_BLOCKSHIFT) args.partitioner = pdmpk_gb300::BlockShiftPartitioner();
   else if (partitioner == MPKG_PD_PART_BFS) args.partitioner = pdmpk_gb300::BfsPartitioner();
+  else if (partitioner == MPKG_PD_PART_METIS) args.partitioner = pdmpk_gb300::MetisPartitioner();
   else return fail(kEInval, "unknown partitioner");
   std::vector<pdmpk_gb300::Buffers> bufs;
   if ((rc = pdmpk_gb300::CommCompPatterns(csr, args, &bufs))) return rc;
@@ -3333,6 +3334,56 @@ int mpkg_exec_host(mpkg_plan *p, double *vv) {
   CUDA_TRY(cudaMemcpyAsync(vv + first, p->d_vv + first, sizeof(double) * (total - first),
                            cudaMemcpyDeviceToHost, st));
   return mpkg_sync(p, st);
+}
+
+}  // extern "C"
+
+// Peak FP64 fused multiply-add rate of the current GPU: every thread runs 8
+// independent FMA chains (a contraction toward b / (1 - a), bounded), so
+// the FP64 pipe, not latency, sets the time.
+__global__ void __launch_bounds__(256) fp64_rate_kernel(double *sink, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int u = 0; u < 8; u++) x[u] = 1e-3 * threadIdx.x + u;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int u = 0; u < 8; u++) x[u] = __fma_rn(x[u], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int u = 0; u < 8; u++) s += x[u];
+  if (s == -1.0) sink[blockIdx.x] = s;  // never true; keeps the chains live
+}
+
+extern "C" {
+
+int mpkg_fp64_fma_rate(double *fma_per_s) {
+  clear_error();
+  if (!fma_per_s) return fail(kEInval, "null argument");
+  int dev = 0, nsm = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = nsm * 8, iters = 4096;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  float best = 0.f;
+  for (int rep = 0; rep < 6; rep++) {
+    CUDA_TRY(cudaEventRecord(e0, st));
+    fp64_rate_kernel<<<grid, 256, 0, st>>>(nullptr, iters, 0.9999999, 1e-3);
+    CUDA_TRY(cudaEventRecord(e1, st));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;  // the first launch warms up
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  *fma_per_s = (double)grid * 256 * 8 * iters / (best * 1e-3);
+  return kOk;
 }
 
 int mpkg_spmv_chain_device(int n, const int *d_ptr, const int *d_col, const double *d_val,

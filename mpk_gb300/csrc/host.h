@@ -84,6 +84,18 @@ int partition_rcb(int n, const std::vector<int> &coords, int dim, int npart,
 // Graph-only recursive bisection: breadth-first growth from a
 // pseudo-peripheral vertex, halves by BFS order.  Works on any graph.
 int partition_bfs(const Csr &g, int npart, std::vector<int> *part);
+// METIS (when the build links it; see partition.cc).  Option slots of the
+// METIS 5.1 layout this library sets.
+constexpr int kMetisNOptions = 40, kMetisOptUfactor = 16, kMetisOptNumbering = 17;
+bool have_metis();
+// METIS_PartGraphKway on the graph exactly as given (options: null or
+// kMetisNOptions values, -1 = METIS's default).
+int metis_kway(int n, const int *ptr, const int *col, const int *vwgt, const int *adjwgt, int npart,
+               const int *options, int *part, long *edgecut);
+// gpmetis -ufactor=<ufactor> on g (self loops dropped; ufactor <= 0: METIS's
+// default imbalance).
+int partition_metis(const Csr &g, const int *vwgt, const int *adjwgt, int npart, int ufactor, std::vector<int> *part,
+                    long *edgecut);
 
 // ---- levels, weights, skirts (prep.cc) ---------------------------------
 // comp_level / update_level (mpk2/lib.c:330-412): level_org == nullptr for

@@ -1,10 +1,14 @@
-// Partition providers.  METIS is not available to this library, so the
-// partition vector comes from a file in gpmetis's output format (the
-// reference's partition contract, mpk2/driver.c:63-66 + mpk2/lib.c:273-284)
-// or from one of two project partitioners: recursive coordinate bisection
-// for grids with known coordinates, and breadth-first recursive bisection
-// for any graph.
+// Partition providers.  The reference partitions with METIS 5.1
+// (mpk2/driver.c:63-66 runs `gpmetis -ufactor=100`; pdmpk/pdmpk_buffers.cc:
+// 183-202 calls METIS_PartGraphKway).  When the CUDA toolkit bundles METIS
+// (libmetis_static.a: 64-bit idx_t, the METIS 5.1 option layout) the
+// library links it and calls it through its public API (metis_kway below).
+// Besides METIS: partition files in gpmetis's output format (the
+// reference's partition contract, mpk2/lib.c:273-284), and two project
+// partitioners, recursive coordinate bisection for grids with known
+// coordinates and breadth-first recursive bisection for any graph.
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <numeric>
@@ -14,7 +18,81 @@
 
 #include "host.h"
 
+#ifdef MPKG_HAVE_METIS
+extern "C" {
+int METIS_SetDefaultOptions(int64_t *options);
+int METIS_PartGraphKway(int64_t *nvtxs, int64_t *ncon, int64_t *xadj, int64_t *adjncy, int64_t *vwgt,
+                        int64_t *vsize, int64_t *adjwgt, int64_t *nparts, void *tpwgts, void *ubvec,
+                        int64_t *options, int64_t *edgecut, int64_t *part);
+}
+#endif
+
 namespace mpkg {
+
+bool have_metis() {
+#ifdef MPKG_HAVE_METIS
+  return true;
+#else
+  return false;
+#endif
+}
+
+int metis_kway(int n, const int *ptr, const int *col, const int *vwgt, const int *adjwgt, int npart,
+               const int *options, int *part, long *edgecut) {
+  if (npart <= 0 || npart > n) return fail(kEInval, "npart must be in [1, n]");
+  if (npart == 1) {
+    std::fill(part, part + n, 0);
+    if (edgecut) *edgecut = 0;
+    return kOk;
+  }
+#ifdef MPKG_HAVE_METIS
+  const long nnz = ptr[n];
+  std::vector<int64_t> xadj(ptr, ptr + n + 1), adj(col, col + nnz), pp(n), vw, ew, opt;
+  if (vwgt) vw.assign(vwgt, vwgt + n);
+  if (adjwgt) ew.assign(adjwgt, adjwgt + nnz);
+  if (options) opt.assign(options, options + kMetisNOptions);
+  int64_t nv = n, ncon = 1, np = npart, cut = 0;
+  const int rc = METIS_PartGraphKway(&nv, &ncon, xadj.data(), adj.data(), vwgt ? vw.data() : nullptr, nullptr,
+                                     adjwgt ? ew.data() : nullptr, &np, nullptr, nullptr,
+                                     options ? opt.data() : nullptr, &cut, pp.data());
+  if (rc != 1) return fail(kEInval, "METIS_PartGraphKway failed (" + std::to_string(rc) + ")");
+  for (int i = 0; i < n; i++) {
+    if (pp[i] < 0 || pp[i] >= npart) return fail(kERange, "METIS returned a part out of range");
+    part[i] = (int)pp[i];
+  }
+  if (edgecut) *edgecut = (long)cut;
+  return kOk;
+#else
+  (void)ptr; (void)col; (void)vwgt; (void)adjwgt; (void)options; (void)edgecut;
+  return fail(kEInval, "this build has no METIS (the CUDA toolkit's libmetis_static.a was not found)");
+#endif
+}
+
+int partition_metis(const Csr &g, const int *vwgt, const int *adjwgt, int npart, int ufactor, std::vector<int> *part,
+                    long *edgecut) {
+  // gpmetis's input: the graph without self loops (the reference's g0 and
+  // weighted gN files hold none), weights kept with their entries
+  Csr h;
+  h.n = g.n;
+  h.ptr.assign(g.n + 1, 0);
+  h.col.reserve(g.col.size());
+  std::vector<int> ew;
+  for (int i = 0; i < g.n; i++) {
+    for (int j = g.ptr[i]; j < g.ptr[i + 1]; j++)
+      if (g.col[j] != i) {
+        h.col.push_back(g.col[j]);
+        if (adjwgt) ew.push_back(adjwgt[j]);
+      }
+    h.ptr[i + 1] = (int)h.col.size();
+  }
+  int opt[kMetisNOptions];
+  std::fill(opt, opt + kMetisNOptions, -1);  // METIS_SetDefaultOptions
+  opt[kMetisOptNumbering] = 0;
+  if (ufactor > 0) opt[kMetisOptUfactor] = ufactor;
+  part->assign(g.n, 0);
+  return metis_kway(h.n, h.ptr.data(), h.col.data(), vwgt, adjwgt ? ew.data() : nullptr, npart, opt, part->data(),
+                    edgecut);
+}
 
 int read_partition(const std::string &path, int n, std::vector<int> *part, int *npart) {
   FILE *f = std::fopen(path.c_str(), "r");

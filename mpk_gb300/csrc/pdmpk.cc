@@ -224,6 +224,18 @@ Partitioner BfsPartitioner() {
   };
 }
 
+Partitioner MetisPartitioner() {
+  return [](const Csr &csr, const idx_t *adjwgt, int npart, int, idx_t *part) {
+    // MetisPartition passes options = NULL; MetisPartitionWithWeights passes
+    // args.opt, METIS_SetDefaultOptions's all -1 unless the command line
+    // changed it (pdmpk/args.cc:24-31)
+    int opt[mpkg::kMetisNOptions];
+    std::fill(opt, opt + mpkg::kMetisNOptions, -1);
+    return mpkg::metis_kway(csr.n, csr.ptr.data(), csr.col.data(), nullptr, adjwgt, npart, adjwgt ? opt : nullptr,
+                            part, nullptr);
+  };
+}
+
 // ---- CommCompPatterns ---------------------------------------------------------
 //
 // The prep walks the levels of every vertex upwards in batches.  A batch

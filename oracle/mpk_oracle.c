@@ -727,3 +727,138 @@ void orc_spmm_f32(int n, const int *ptr, const int *col, const float *val, int n
       }
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* PA1 task lists at sizes where the reference's dense skirt is out of  */
+/* reach (npart*n ints).  Same lists as comp_skirt (mpk2/lib.c:584-615)  */
+/* -> write_skirt/read_skirt (lib.c:617-707, PA1 branch: dist < nlevel)  */
+/* -> prep_mpk's skirt loop (mpk2/mpkprep.c:186-233, prevl = 0): part p  */
+/* computes level l on {i : dist_p(i) <= nlevel - l}, level-major,      */
+/* vertex-ascending.  The distance is restated as a breadth-first       */
+/* search bounded at nlevel - 1: minplus_x lowers row i to 1 + the      */
+/* smallest distance among its columns, so distances spread from a     */
+/* vertex j to every row i holding column j (the transpose's edges).    */
+/* Returns the number of entries (off: npart + 1), ORC_ERANGE when cap  */
+/* is too small (pass cap = 0 and tasks = NULL to count).               */
+/* ------------------------------------------------------------------ */
+static int cmp_int(const void *a, const void *b) {
+  const int x = *(const int *)a, y = *(const int *)b;
+  return (x > y) - (x < y);
+}
+
+long orc_pa1_tasks(int n, const int *ptr, const int *col, const int *part, int npart,
+                   int nlevel, long *off, long *tasks, long cap) {
+  /* transpose: rows holding column j */
+  long nnz = ptr[n];
+  int *tptr = calloc((size_t)n + 1, sizeof(int)), *trow = malloc(sizeof(int) * (nnz ? nnz : 1));
+  int *fill = malloc(sizeof(int) * (size_t)n), *dist = malloc(sizeof(int) * (size_t)n);
+  int *ball = malloc(sizeof(int) * (size_t)n);
+  long *pstart = calloc((size_t)npart + 1, sizeof(long));
+  int *pverts = malloc(sizeof(int) * (size_t)n);
+  if (!tptr || !trow || !fill || !dist || !ball || !pstart || !pverts) {
+    free(tptr); free(trow); free(fill); free(dist); free(ball); free(pstart); free(pverts);
+    return ORC_EIO;
+  }
+  for (long j = 0; j < nnz; j++) tptr[col[j] + 1]++;
+  for (int i = 0; i < n; i++) tptr[i + 1] += tptr[i];
+  memcpy(fill, tptr, sizeof(int) * (size_t)n);
+  for (int i = 0; i < n; i++)
+    for (int j = ptr[i]; j < ptr[i + 1]; j++) trow[fill[col[j]]++] = i;
+  /* vertices of each part, ascending */
+  for (int i = 0; i < n; i++) pstart[part[i] + 1]++;
+  for (int p = 0; p < npart; p++) pstart[p + 1] += pstart[p];
+  {
+    long *pf = malloc(sizeof(long) * (size_t)(npart + 1));
+    memcpy(pf, pstart, sizeof(long) * (size_t)(npart + 1));
+    for (int i = 0; i < n; i++) pverts[pf[part[i]]++] = i;
+    free(pf);
+  }
+  for (int i = 0; i < n; i++) dist[i] = -1;
+  long total = 0;
+  off[0] = 0;
+  for (int p = 0; p < npart; p++) {
+    int nb = 0;
+    for (long q = pstart[p]; q < pstart[p + 1]; q++) {
+      ball[nb++] = pverts[q];
+      dist[pverts[q]] = 0;
+    }
+    int lo = 0;
+    for (int d = 1; d <= nlevel - 1; d++) {
+      const int hi = nb;
+      for (int q = lo; q < hi; q++) {
+        const int j = ball[q];
+        for (int t = tptr[j]; t < tptr[j + 1]; t++) {
+          const int i = trow[t];
+          if (dist[i] < 0) {
+            dist[i] = d;
+            ball[nb++] = i;
+          }
+        }
+      }
+      lo = hi;
+    }
+    /* the ball in vertex order; keep each vertex's distance */
+    int *sorted = malloc(sizeof(int) * (size_t)(nb ? nb : 1));
+    memcpy(sorted, ball, sizeof(int) * (size_t)nb);
+    qsort(sorted, (size_t)nb, sizeof(int), cmp_int);
+    for (int l = 1; l <= nlevel; l++)
+      for (int q = 0; q < nb; q++) {
+        const int i = sorted[q];
+        if (dist[i] <= nlevel - l) {
+          if (tasks) {
+            if (total >= cap) {
+              free(sorted);
+              free(tptr); free(trow); free(fill); free(dist); free(ball); free(pstart); free(pverts);
+              return ORC_ERANGE;
+            }
+            tasks[total] = (long)l * n + i;
+          }
+          total++;
+        }
+      }
+    off[p + 1] = total;
+    for (int q = 0; q < nb; q++) dist[ball[q]] = -1;
+    free(sorted);
+  }
+  free(tptr); free(trow); free(fill); free(dist); free(ball); free(pstart); free(pverts);
+  return total;
+}
+
+/* ------------------------------------------------------------------ */
+/* Workload generators for the CPU arms of the benchmark, so that those */
+/* arms need nothing but the oracle and the reference.  Definitions of  */
+/* this project's own workload (no reference counterpart): the 3-D      */
+/* 7-point Laplacian on nx*ny*nz (x fastest; columns ascending: z-, y-, */
+/* x-, diagonal, x+, y+, z+), and uniform[-1,1] doubles from a          */
+/* splitmix64 stream (2u - 1 with u = (z >> 11) * 2^-53).               */
+/* ------------------------------------------------------------------ */
+long orc_gen_laplacian(int nx, int ny, int nz, double diag, double offd, int *ptr, int *col, double *val) {
+  const long sy = nx, sz = (long)nx * ny, n = sz * nz;
+  long e = 0;
+  ptr[0] = 0;
+  for (long i = 0; i < n; i++) {
+    const long x = i % nx, y = (i / nx) % ny, z = i / sz;
+    const long c[7] = {i - sz, i - sy, i - 1, i, i + 1, i + sy, i + sz};
+    const int ok[7] = {z > 0, y > 0, x > 0, 1, x < nx - 1, y < ny - 1, z < nz - 1};
+    for (int t = 0; t < 7; t++)
+      if (ok[t]) {
+        col[e] = (int)c[t];
+        val[e] = (t == 3) ? diag : offd;
+        e++;
+      }
+    ptr[i + 1] = (int)e;
+  }
+  return e;
+}
+
+void orc_uniform(unsigned long long seed, long n, double *out) {
+  unsigned long long s = seed;
+  for (long i = 0; i < n; i++) {
+    s += 0x9E3779B97F4A7C15ULL;
+    unsigned long long z = s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    out[i] = 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+  }
+}

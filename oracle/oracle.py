@@ -25,7 +25,7 @@ MODE_SEPARATE, MODE_FMA = 0, 1
 
 def build(quiet=True):
     """make liboracle (always) and the reference (when its sources exist)."""
-    out = subprocess.run(["make", "-s", "-C", HERE, "stage", "liboracle", "ref"],
+    out = subprocess.run(["make", "-s", "-C", HERE, "stage", "liboracle", "libmetis", "ref"],
                          stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout)
@@ -184,6 +184,77 @@ def mpk(ptr, col, val, x, nlevel, mode=MODE_FMA):
     vv[:n] = x
     return spmv_chain(np.ascontiguousarray(ptr, dtype=np.int32), np.ascontiguousarray(col, dtype=np.int32),
                       None if val is None else np.ascontiguousarray(val, dtype=np.float64), nlevel, vv, mode)
+
+
+def pa1_tasks(ptr, col, part, npart, nlevel):
+    """PA1 task lists (orc_pa1_tasks: comp_skirt + prep_mpk's skirt loop
+    with a bounded search): (off[npart+1], idx) in the reference layout."""
+    o = lib()
+    o.orc_pa1_tasks.restype = C.c_long
+    o.orc_pa1_tasks.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                C.c_void_p, C.c_long]
+    p = np.ascontiguousarray(ptr, dtype=np.int32)
+    c = np.ascontiguousarray(col, dtype=np.int32)
+    pt = np.ascontiguousarray(part, dtype=np.int32)
+    off = np.zeros(npart + 1, dtype=np.int64)
+    cnt = o.orc_pa1_tasks(len(p) - 1, _p(p), _p(c), _p(pt), npart, nlevel, _p(off), None, 0)
+    if cnt < 0:
+        raise ValueError(f"oracle: orc_pa1_tasks failed ({cnt})")
+    idx = np.zeros(cnt, dtype=np.int64)
+    cnt2 = o.orc_pa1_tasks(len(p) - 1, _p(p), _p(c), _p(pt), npart, nlevel, _p(off), _p(idx), cnt)
+    if cnt2 != cnt:
+        raise ValueError("oracle: orc_pa1_tasks count changed")
+    return off, idx
+
+
+def laplacian(nx, ny, nz, diag, offd):
+    """The 3-D 7-point Laplacian of the workloads (orc_gen_laplacian)."""
+    o = lib()
+    o.orc_gen_laplacian.restype = C.c_long
+    o.orc_gen_laplacian.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]
+    n = nx * ny * nz
+    ptr = np.zeros(n + 1, dtype=np.int32)
+    cap = 7 * n
+    col = np.zeros(cap, dtype=np.int32)
+    val = np.zeros(cap)
+    e = o.orc_gen_laplacian(nx, ny, nz, diag, offd, _p(ptr), _p(col), _p(val))
+    return ptr, col[:e].copy(), val[:e].copy()
+
+
+def uniform(seed, n):
+    """uniform[-1,1] doubles from the workloads' splitmix64 stream."""
+    o = lib()
+    o.orc_uniform.argtypes = [C.c_ulonglong, C.c_long, C.c_void_p]
+    out = np.zeros(n)
+    o.orc_uniform(seed, n, _p(out))
+    return out
+
+
+LIBMETIS = os.path.join(HERE, "_build", "libmetis_oracle.so")
+
+
+def metis_available():
+    return os.path.exists(LIBMETIS)
+
+
+def metis_kway(ptr, col, npart, ufactor=0, vwgt=None, adjwgt=None):
+    """k-way partition by the METIS library bundled with CUDA (the
+    reference's partitioner), as `gpmetis -ufactor=<ufactor>` computes it:
+    the graph without its diagonal, optional vertex and edge weights."""
+    m = C.CDLL(LIBMETIS)
+    m.orc_metis_kway.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                 C.c_void_p, C.c_void_p]
+    p = np.ascontiguousarray(ptr, dtype=np.int32)
+    c = np.ascontiguousarray(col, dtype=np.int32)
+    vw = None if vwgt is None else np.ascontiguousarray(vwgt, dtype=np.int32)
+    ew = None if adjwgt is None else np.ascontiguousarray(adjwgt, dtype=np.int32)
+    part = np.zeros(len(p) - 1, dtype=np.int32)
+    cut = C.c_long()
+    if m.orc_metis_kway(len(p) - 1, _p(p), _p(c), None if vw is None else _p(vw), None if ew is None else _p(ew),
+                        npart, ufactor, _p(part), C.byref(cut)) != 0:
+        raise RuntimeError("METIS_PartGraphKway failed")
+    return part
 
 
 # ---------------------------------------------------------------- reference

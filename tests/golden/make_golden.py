@@ -13,17 +13,26 @@ scripts drive them (mpk2/driver.c, mpk2/mpktest.c, mpk2/verify_val.c):
   pdmpk prep (apps/prep.cc) -> per-rank buf.bin / results.bin (pdmpk.npz)
   lapjv, work_count         -> lapjv.npz, work_count.json (verification tools)
   pdmpk prep, CTest shapes  -> pdmpk_ctest.json (hashes of every rank's files)
+  METIS partitions          -> m9p24_8_4_2m.npz (the mpk2 driver's flow with
+                               METIS at every phase) and pdmpk_metis.json (the
+                               CTest shapes with the reference prep compiled
+                               against METIS)
 
 Inputs (graphs, partitions, x) come from the product's generators and
-partitioners; METIS is not available, so partitions are recursive
-coordinate bisection or breadth-first bisection vectors, stored with the
-fixture.  The reference binaries here are x86-64 gcc -O2 builds, which do
+partitioners, stored with the fixture: recursive coordinate bisection or
+breadth-first bisection vectors, or METIS partitions.  METIS is the library
+bundled with the CUDA toolkit; gpmetis itself is not installed, so the
+driver's `gpmetis -ufactor=100 g<ph> P` calls (mpk2/driver.c:63-66) are
+made through oracle/metis_part.c on the same graph files, and the reference
+pdmpk prep is compiled a second time against METIS
+(oracle/refshim_metis/metis.h).  The reference binaries here are x86-64 gcc -O2 builds, which do
 not contract a*b+c, so every floating-point fixture is in the oracle's
 "separate" arithmetic mode.
 
     python tests/golden/make_golden.py                # everything
     python tests/golden/make_golden.py verification   # lapjv + work_count only
     python tests/golden/make_golden.py ctest          # pdmpk CTest shapes only
+    python tests/golden/make_golden.py metis          # the METIS fixtures only
 """
 import ctypes as C
 import hashlib
@@ -51,12 +60,33 @@ CASES = [
     dict(name="m5p16_4_6_3", grid=(16, 16, 1), npart=4, nlevel=6, nphase=3, part="bfs+rcb+bfs", seed=6),
     dict(name="cube6_8_3_0", grid=("cube", 6), npart=8, nlevel=3, nphase=0, part="bfs", seed=7),
 ]
+# the driver's flow with METIS partitions at every phase (9-point mesh)
+METIS_CASES = [
+    dict(name="m9p24_8_4_2m", grid=("m9p", 24), npart=8, nlevel=4, nphase=2, part="metis", seed=9),
+]
+
+
+def read_weighted_graph(path):
+    """A METIS graph file written by the reference's `comp weight`
+    (header "n m 011": each line a vertex weight, then column/weight
+    pairs): (ptr, col, vwgt, adjwgt), 0-based columns."""
+    with open(path) as f:
+        f.readline()
+        ptr, col, vw, ew = [0], [], [], []
+        for line in f:
+            t = [int(v) for v in line.split()]
+            vw.append(t[0])
+            col += [c - 1 for c in t[1::2]]
+            ew += t[2::2]
+            ptr.append(len(col))
+    return (np.array(ptr, dtype=np.int32), np.array(col, dtype=np.int32), np.array(vw, dtype=np.int32),
+            np.array(ew, dtype=np.int32))
 
 
 def loop_matrix(case):
     """The matrix with diagonal (the .loop.g0/.loop.val pair)."""
-    if case["grid"][0] == "cube":
-        return M.Csr.stencil("cube", case["grid"][1])
+    if isinstance(case["grid"][0], str):
+        return M.Csr.stencil(case["grid"][0], case["grid"][1])
     nx, ny, nz = case["grid"]
     return M.Csr.laplacian(nx, ny, nz, diag=4.0 if nz == 1 else 6.0, off=-1.0)
 
@@ -86,12 +116,17 @@ def make(case, tmp):
     a.write_metis(os.path.join(d, "g0"), ne=(a.nnz + a.n) // 2)
     a.write_metis(os.path.join(d, "loop.g0"), ne=(a.nnz + a.n) // 2)
     a.write_values(os.path.join(tmp, ghead + ".loop.val"))
-    parts = partitions(case, a)
+    metis = case["part"] == "metis"
+    parts = [O.metis_kway(a.ptr, a.col, npart, 100)] if metis else partitions(case, a)
     for ph, p in enumerate(parts):
         np.savetxt(os.path.join(d, f"g{ph}.part.{npart}"), p, fmt="%d")
     comp, skirt = O.ref_tool("comp"), O.ref_tool("skirt")
     levels, weights = [], []
     for ph in range(nphase):
+        if metis and ph > 0:  # gpmetis -ufactor=100 on the weighted graph of the phase
+            gp, gc, vw, ew = read_weighted_graph(f"{d}/g{ph}")
+            parts.append(O.metis_kway(gp, gc, npart, 100, vw, ew))
+            np.savetxt(os.path.join(d, f"g{ph}.part.{npart}"), parts[-1], fmt="%d")
         args = [comp, "level", f"{d}/g0", "x", f"{d}/g{ph}.part.{npart}"]
         if ph > 0:
             args.append(f"{d}/l{ph - 1}")
@@ -227,6 +262,36 @@ def make_pdmpk_ctest(tmp):
     return out
 
 
+def make_pdmpk_metis(tmp):
+    """sha256 of the reference prep's per-rank files for every CTest shape
+    with the reference compiled against METIS (pdmpk_metis.json)."""
+    d = os.path.join(tmp, "ctest_metis")
+    os.makedirs(d)
+    out = {}
+    for t, size, P, L in PD_CTEST:
+        m = f"{t}{size}"
+        M.Csr.stencil(t, size).write_mtx(os.path.join(d, m + ".mtx"), pattern=True)
+        run([O.ref_tool("pdmpk_prep_metis"), "--matrix", m + ".mtx", "--npart", str(P), "--nlevel", str(L),
+             "--mirror", "5", "--weight", "3", "--keepfiles"], cwd=d)
+        ranks = []
+        for r in range(P):
+            stem = os.path.join(d, f"{m}.mtx-np{P}-nl{L}-mm5-wm3-r{r}-ref-oracle")
+            ranks.append([hashlib.sha256(open(stem + ext, "rb").read()).hexdigest()
+                          for ext in (".buf.bin", ".results.bin")])
+        out[f"{m}_{P}_{L}"] = ranks
+    with open(os.path.join(HERE, "pdmpk_metis.json"), "w") as f:
+        json.dump(out, f, indent=1)
+        f.write("\n")
+    return out
+
+
+def make_metis(tmp):
+    for case in METIS_CASES:
+        out = make(case, tmp)
+        print(case["name"], "n", out["n"], "tasks", len(out["idx"]))
+    print(len(make_pdmpk_metis(tmp)), "pdmpk CTest shapes with METIS")
+
+
 def make_verification(tmp):
     """Known answers of the reference's verification tools:
     * lapjv.npz: lapjv (mpk2/lapjv.c:366) permutations on seeded square
@@ -290,6 +355,9 @@ def main():
         if sys.argv[1:] == ["ctest"]:  # only the pdmpk CTest shapes
             print(len(make_pdmpk_ctest(tmp)), "pdmpk CTest shapes")
             return
+        if sys.argv[1:] == ["metis"]:  # only the METIS fixtures
+            make_metis(tmp)
+            return
         for case in CASES:
             out = make(case, tmp)
             print(case["name"], "n", out["n"], "tasks", len(out["idx"]))
@@ -297,6 +365,7 @@ def main():
         print("pdmpk", len(out), "arrays")
         print(make_verification(tempfile.mkdtemp(dir=tmp)))
         print(len(make_pdmpk_ctest(tmp)), "pdmpk CTest shapes")
+        make_metis(tmp)
     finally:
         shutil.rmtree(tmp)
 
