@@ -304,6 +304,18 @@ int mpkg_pdmpk_prep(int n, const int *ptr, const int *col, const double *val, in
  * (nlevel-1) x the matrix's dependency reach, else MPKG_ERANGE). */
 int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, int nlevel, int value_type,
                     mpkg_plan **out);
+/* The same mixed-precision form on PA1 tiles, for matrices larger than L2
+ * (the PA1 diamond schedule of mpk2/mpkprep.c:186-233, temporal blocking):
+ * every part plus the vertices within nlevel arcs of it is one tile; a
+ * persistent CTA gathers the tile's level-0 halo into shared memory, loads
+ * its rows' local columns and values once into registers, and computes all
+ * nlevel levels on chip (skirt rows recomputed, no inter-CTA waits),
+ * writing the part's own rows of each level.  The tile metadata is built on
+ * the GPU (mpkg_tile_prep).  Same scaling, storage and bits as
+ * mpkg_plan_mixed; executed with mpkg_exec_mixed_device.  MPKG_ERANGE when
+ * a tile's two FP32 level vectors exceed shared memory (use more parts). */
+int mpkg_plan_mixed_tiles(int n, const int *ptr, const int *col, const double *val, const int *part, int npart,
+                          int nlevel, int value_type, mpkg_plan **out);
 /* e of the plan's scaling and the number of values the storage type
  * cannot represent exactly (0 means lossless, e.g. BF16 on stencils). */
 int mpkg_mixed_scale(const mpkg_plan *p, int *exponent, long *inexact_values);

@@ -143,6 +143,7 @@ def _declare(L):
         "mpkg_gen_diffusion": (I, [I, I, I, D, D, D, D, D, C.c_uint64, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
         "mpkg_gen_banded": (I, [Lg, I, I, I, C.c_uint64, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
         "mpkg_plan_mixed": (I, [I, P, P, P, I, I, pp]),
+        "mpkg_plan_mixed_tiles": (I, [I, P, P, P, P, I, I, I, pp]),
         "mpkg_mixed_scale": (I, [P, C.POINTER(I), C.POINTER(Lg)]),
         "mpkg_exec_mixed_device": (I, [P, P, P]),
         "mpkg_bufs_prepare": (I, [C.c_char_p]),
@@ -558,6 +559,15 @@ class Plan:
         per level (A^l x = 2^(l e) v_l)."""
         return cls._make(lib().mpkg_plan_mixed, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), nlevel, value_type,
                          a=a, nlevel=nlevel)
+
+    @classmethod
+    def mixed_tiles(cls, a: Csr, part, npart, nlevel, value_type=VALUE_F32):
+        """Mixed-precision form on PA1 tiles (temporal blocking: each part
+        plus its nlevel-deep skirt computes every level on chip, its
+        matrix rows read once per call); same bits as Plan.mixed."""
+        part = _i32(part)
+        return cls._make(lib().mpkg_plan_mixed_tiles, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), _ptr(part),
+                         npart, nlevel, value_type, a=a, nlevel=nlevel)
 
     def mixed_scale(self):
         """(e, number of values the storage type rounds)."""

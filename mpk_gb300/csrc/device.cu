@@ -827,6 +827,10 @@ struct WaveArgs {
   // mixed form: the values are larger than L2, so they are loaded
   // evict-first (they would only push the level vectors out of L2)
   int stream_vals;
+  // FP64 forms, host execution on page-locked vv: the caller's vv through
+  // its host mapping (x read from it, every level written to it as well as
+  // to the device copy the next level reads); null otherwise
+  double *hv;
 };
 
 __device__ __forceinline__ bool wave_wait(const WaveArgs &a, int b, unsigned int want, int *s_abort) {
@@ -993,10 +997,15 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
   const short *s_rel = reinterpret_cast<const short *>(wave_smem);
   const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (a.hv) {  // x from the host mapping into the device copy, own rows
+    for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) a.vv[i] = a.hv[i];
+    wave_publish(a, b, a.base);
+  }
   for (int l = 1; l <= a.nlevel; l++) {
-    if (l > 1 && !wave_wait(a, b, a.base + (unsigned)(l - 1), &s_abort)) return;
+    if ((l > 1 || a.hv) && !wave_wait(a, b, a.base + (unsigned)(l - 1), &s_abort)) return;
     const double *src = a.vv + (size_t)(l - 1) * a.n;
     double *dst = a.vv + (size_t)l * a.n;
+    double *hdst = a.hv ? a.hv + (size_t)l * a.n : nullptr;
     for (int sl = (r0 >> 5) + warp; r0 < r1 && (sl << 5) < r1; sl += nw) {
       const int i = (sl << 5) + lane;
       if (i >= r1) continue;
@@ -1014,6 +1023,7 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
       // the stride is the constant 32 unless the plan compresses offsets
       const double s = fp_row<ARITH, VALUED, REL, STAGE>(len, UNI ? (uni ? 1 : 32) : 32, cf, cr, cc, cv, xb, src);
       __stcs(dst + i, s);
+      if (hdst) hdst[i] = s;
     }
     wave_publish(a, b, a.base + (unsigned)l);
   }
@@ -1250,6 +1260,163 @@ __global__ void __launch_bounds__(256, 5) wave_mix_kernel(WaveArgs a, const VT *
     }
     wave_publish(a, b, a.base + (unsigned)l);
   }
+}
+
+// ------------------------------------------------------------------------
+// Mixed-precision PA1 tiles: temporal blocking for matrices larger than L2
+// (the reference's PA1 diamond schedule, mpk2/mpkprep.c:186-233, run in
+// FP32).  A tile is a part plus every vertex within nlevel arcs, its slots
+// sorted by (distance, vertex), so the rows of level l are the prefix
+// with distance <= nlevel - l.  A persistent CTA takes tiles in the plan's
+// order from a ticket and, per tile:
+//   * gathers the tile's level-0 values into shared memory (the halo read
+//     that replaces the reference's MPI exchange);
+//   * loads the local columns and the values of its rows ONCE into
+//     registers (thread t owns rows t and t + kTmThreads of every level),
+//     so the matrix is read once for all nlevel levels;
+//   * computes the levels in place, ping-ponging two shared-memory
+//     vectors, recomputing the skirt rows, and writes the part's own rows
+//     of each level to vv.
+// Rows beyond the registers' reach, or wider than W entries, read their
+// columns and values again at each level (L2 hits).  Row sums: FP32 FMA in
+// CSR order, then the exact scaling by 2^-e: the bits of the wavefront and
+// pipeline mixed forms.
+// ------------------------------------------------------------------------
+struct TileMixArgs {
+  int n, nlevel, npart, max_slots;
+  const int *order;          // tiles in launch order
+  const long *slot_off;      // per tile: first slot (npart + 1)
+  const int *shell;          // per tile: (nlevel + 1) prefix counts by distance
+  const int *slot_vert;      // vertex of each slot
+  const int *slot_coef;      // CSR offset of each slot's row
+  const long *slice_off;     // per tile: first slice
+  const long *ell_off;       // per slice: first entry
+  const uint16_t *ell_col;   // local slot of each entry, 0xFFFF = padding
+  const uint8_t *ell_width;  // per slice
+  const void *val;           // CSR values, float or __nv_bfloat16
+  const float *x;            // level 0 (vf[0..n))
+  float *vf;                 // (nlevel + 1) * n
+  float scale;               // 2^-e
+  unsigned int *ticket;
+  int *err;
+};
+
+constexpr int kTmThreads = 1024;
+constexpr int kTmRows = 2;  // rows per thread held in registers
+
+// A row read from global memory (no register copy): columns of the
+// tile-local ELL, values from the CSR.
+template <typename VT>
+__device__ __forceinline__ float tm_row_global(const TileMixArgs &a, const VT *val, long sl, int lane, int co,
+                                               const float *in) {
+  const int w = a.ell_width[sl];
+  const uint16_t *cp = a.ell_col + a.ell_off[sl] + lane;
+  float s = 0.f;
+  for (int t = 0; t < w; t++) {
+    const int c = cp[32 * t];
+    if (c == 0xFFFF) break;
+    s = __fmaf_rn(to_f32(val[co + t]), in[c], s);
+  }
+  return s;
+}
+
+template <typename VT, int W>
+__global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a) {
+  extern __shared__ __align__(16) float tm_buf[];
+  __shared__ int s_q;
+  float *buf0 = tm_buf, *buf1 = tm_buf + a.max_slots;
+  const VT *val = static_cast<const VT *>(a.val);
+  const int tid = threadIdx.x;
+  for (;;) {
+    __syncthreads();  // the previous tile's buffers and s_q are free
+    if (tid == 0) s_q = (int)atomicAdd(a.ticket, 1u);
+    __syncthreads();
+    const int q = s_q;
+    if (q >= a.npart) return;
+    const int p = a.order[q];
+    const long s0 = a.slot_off[p];
+    const int ns = (int)(a.slot_off[p + 1] - s0);
+    if (ns > a.max_slots) {  // plan invariant; never true for a valid plan
+      if (tid == 0) atomicExch(a.err, kErrBounds);
+      return;
+    }
+    const int *shell = a.shell + (long)p * (a.nlevel + 1);
+    const long sl0 = a.slice_off[p];
+    const int nrow1 = a.nlevel >= 1 ? shell[a.nlevel - 1] : 0;
+    for (int sv = tid; sv < ns; sv += kTmThreads) buf0[sv] = __ldg(a.x + a.slot_vert[s0 + sv]);
+    // this thread's rows: columns (two per word) and values in registers
+    uint32_t cw[kTmRows][(W + 1) / 2];
+    float v[kTmRows][W];
+    int len[kTmRows];
+#pragma unroll
+    for (int j = 0; j < kTmRows; j++) {
+      len[j] = -1;
+      const int r = tid + j * kTmThreads;
+#pragma unroll
+      for (int t = 0; t < (W + 1) / 2; t++) cw[j][t] = 0;
+#pragma unroll
+      for (int t = 0; t < W; t++) v[j][t] = 0.f;
+      if (r < nrow1) {
+        const long sl = sl0 + (r >> 5);
+        const int w = a.ell_width[sl];
+        if (w <= W) {
+          const uint16_t *cp = a.ell_col + a.ell_off[sl] + (r & 31);
+          const int co = a.slot_coef[s0 + r];
+          int L = 0;
+#pragma unroll
+          for (int t = 0; t < W; t++) {
+            const int c = t < w ? (int)__ldg(cp + 32 * t) : 0xFFFF;
+            if (c != 0xFFFF && L == t) {
+              cw[j][t >> 1] |= (uint32_t)c << (16 * (t & 1));
+              v[j][t] = to_f32(val[co + t]);
+              L = t + 1;
+            }
+          }
+          len[j] = L;
+        }
+      }
+    }
+    __syncthreads();
+    const int owned = shell[0];
+    for (int l = 1; l <= a.nlevel; l++) {
+      const float *in = (l & 1) ? buf0 : buf1;
+      float *out = (l & 1) ? buf1 : buf0;
+      const int nrows = shell[a.nlevel - l];
+      float *dst = a.vf + (size_t)l * a.n;
+#pragma unroll
+      for (int j = 0; j < kTmRows; j++) {
+        const int r = tid + j * kTmThreads;
+        if (r < nrows) {
+          float s = 0.f;
+          if (len[j] >= 0) {
+#pragma unroll
+            for (int t = 0; t < W; t++)
+              if (t < len[j]) s = __fmaf_rn(v[j][t], in[(cw[j][t >> 1] >> (16 * (t & 1))) & 0xFFFF], s);
+          } else {
+            s = tm_row_global(a, val, sl0 + (r >> 5), r & 31, a.slot_coef[s0 + r], in);
+          }
+          s *= a.scale;
+          out[r] = s;
+          if (r < owned) __stcs(dst + a.slot_vert[s0 + r], s);
+        }
+      }
+      for (int r = tid + kTmRows * kTmThreads; r < nrows; r += kTmThreads) {
+        float s = tm_row_global(a, val, sl0 + (r >> 5), r & 31, a.slot_coef[s0 + r], in);
+        s *= a.scale;
+        out[r] = s;
+        if (r < owned) __stcs(dst + a.slot_vert[s0 + r], s);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+using TmKernel = void (*)(TileMixArgs);
+inline TmKernel tm_kernel_ptr(int value_type, int w) {
+  if (value_type == MPKG_VALUE_F32)
+    return w == 8 ? tiles_mix_kernel<float, 8> : w == 12 ? tiles_mix_kernel<float, 12> : tiles_mix_kernel<float, 16>;
+  return w == 8 ? tiles_mix_kernel<__nv_bfloat16, 8>
+                : w == 12 ? tiles_mix_kernel<__nv_bfloat16, 12> : tiles_mix_kernel<__nv_bfloat16, 16>;
 }
 
 // ------------------------------------------------------------------------
@@ -1538,6 +1705,11 @@ struct mpkg_plan {
   const void *graph_key = nullptr;
   bool graph_ok = false;
   float *d_fb = nullptr;  // staging of mpkg_exec_batch_host
+  // mixed form on PA1 tiles (temporal blocking)
+  TileMixArgs tm{};
+  bool tm_on = false;
+  int tm_w = 0, tm_grid = 0;
+  size_t tm_smem = 0;
   mpkg_plan *inner = nullptr;  // mixed form: the wavefront layout it runs on
   void *mix_sval = nullptr;    // mixed form: sliced FP32 / BF16 values
   // pdmpk buffers (b_vall, b_in_*, b_out_*, b_cm_* shared with the above)
@@ -1787,7 +1959,7 @@ size_t wave_dyn_smem(const mpkg_plan *p) {
   return w.stage_rel_bytes > 0 ? (size_t)w.stage_rel_bytes + w.stage_len_bytes + 5L * w.stage_slices : 0;
 }
 
-int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st) {
+int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st, double *hv = nullptr) {
   WaveArgs &w = p->wave;
   const unsigned step = (unsigned)p->nlevel + (p->arith == MPKG_ARITH_FIXED ? 2 : 1);
   if (w.base == 0 || w.base > (1u << 30)) {  // first call, or the flags would wrap: start over
@@ -1799,6 +1971,7 @@ int launch_wave(mpkg_plan *p, double *d_vv, cudaStream_t st) {
   }
   WaveArgs a = w;
   a.vv = d_vv;
+  a.hv = hv;
   void *args[] = {&a};
   CUDA_TRY(cudaLaunchCooperativeKernel(wave_kernel_ptr(p), dim3(w.nblk), dim3(256), args, wave_dyn_smem(p), st));
   return kOk;
@@ -3176,6 +3349,127 @@ int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, in
   return kOk;
 }
 
+int mpkg_plan_mixed_tiles(int n, const int *ptr, const int *col, const double *val, const int *part, int npart,
+                          int nlevel, int value_type, mpkg_plan **out) {
+  clear_error();
+  if (!out) return fail(kEInval, "out is null");
+  *out = nullptr;
+  if (!val) return fail(kEInval, "the mixed-precision form needs matrix values");
+  if (value_type != MPKG_VALUE_F32 && value_type != MPKG_VALUE_BF16) return fail(kEInval, "unknown value type");
+  if (!part || npart <= 0) return fail(kEInval, "bad partition");
+  int rc = check_csr(n, ptr, col);
+  if (rc) return rc;
+  if (nlevel <= 0 || nlevel > 31) return fail(kEInval, "nlevel must be in [1, 31]");
+  std::vector<int> pv(part, part + n);
+  for (int q : pv) if (q < 0 || q >= npart) return fail(kERange, "part id out of range");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
+  Csr g;
+  g.n = n;
+  g.ptr.assign(ptr, ptr + n + 1);
+  g.col.assign(col, col + ptr[n]);
+  TilePlan tp;
+  bool on_gpu = false;
+  if ((rc = build_tile_plan_gpu(g, pv, npart, nlevel, &tp, &on_gpu))) return rc;
+  mpkg_plan *p = new_plan();
+  if (!p) return fail(kENoMem, "plan allocation failed");
+  p->exec = MPKG_EXEC_MIXED;
+  p->n = n; p->nlevel = nlevel; p->npart = npart; p->valued = true; p->arith = -1;
+  p->nnz = ptr[n];
+  p->rows_computed = tp.total_rows;
+  p->max_tile_slots = tp.max_slots;
+  p->mix_vt = value_type;
+  rc = cudaGetDevice(&p->device) == cudaSuccess ? kOk : fail(kECuda, "cudaGetDevice failed");
+  if (!rc && cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(kECuda, "stream creation failed");
+  double anorm = 0.0;  // infinity norm -> power-of-two scale, as mpkg_plan_mixed
+  for (int i = 0; i < n; i++) {
+    double r = 0.0;
+    for (int j = ptr[i]; j < ptr[i + 1]; j++) r += std::fabs(val[j]);
+    anorm = std::max(anorm, r);
+  }
+  p->mix_e = anorm > 0 ? (int)std::ceil(std::log2(anorm)) : 0;
+  p->mix.scale = std::ldexp(1.0f, -p->mix_e);
+  TileMixArgs &a = p->tm;
+  a.n = n; a.nlevel = nlevel; a.npart = npart; a.max_slots = tp.max_slots; a.scale = p->mix.scale;
+  int *order = nullptr, *shell = nullptr, *slot_vert = nullptr, *slot_coef = nullptr;
+  long *slot_off = nullptr, *slice_off = nullptr, *ell_off = nullptr;
+  uint16_t *ell_col = nullptr;
+  uint8_t *ell_width = nullptr;
+  if (!rc) rc = dev_copy(p, &order, tp.order.data(), tp.order.size());
+  if (!rc) rc = dev_copy(p, &slot_off, tp.slot_off.data(), tp.slot_off.size());
+  if (!rc) rc = dev_copy(p, &shell, tp.shell.data(), tp.shell.size());
+  if (!rc) rc = dev_copy(p, &slot_vert, tp.slot_vert.data(), tp.slot_vert.size());
+  if (!rc) {
+    std::vector<int> sc(tp.slot_vert.size());
+    for (size_t q = 0; q < sc.size(); q++) sc[q] = ptr[tp.slot_vert[q]];
+    rc = dev_copy(p, &slot_coef, sc.data(), sc.size());
+  }
+  if (!rc) rc = dev_copy(p, &slice_off, tp.slice_off.data(), tp.slice_off.size());
+  if (!rc) rc = dev_copy(p, &ell_off, tp.ell_off.data(), tp.ell_off.size());
+  if (!rc) {
+    std::vector<uint16_t> ec = tp.ell_col;
+    if (ec.empty()) ec.push_back(0xFFFF);
+    rc = dev_copy(p, &ell_col, ec.data(), ec.size());
+  }
+  int wmax = 0;
+  if (!rc) {
+    std::vector<uint8_t> ew = tp.ell_width;
+    for (uint8_t w : ew) wmax = std::max(wmax, (int)w);
+    if (ew.empty()) ew.push_back(0);
+    rc = dev_copy(p, &ell_width, ew.data(), ew.size());
+  }
+  if (!rc) {
+    if (value_type == MPKG_VALUE_F32) {
+      std::vector<float> v(p->nnz);
+      for (long j = 0; j < p->nnz; j++) {
+        v[j] = (float)val[j];
+        if ((double)v[j] != val[j]) p->mix_inexact++;
+      }
+      float *dv = nullptr;
+      rc = dev_copy(p, &dv, v.data(), v.size());
+      a.val = dv;
+    } else {
+      std::vector<__nv_bfloat16> v(p->nnz);
+      for (long j = 0; j < p->nnz; j++) {
+        v[j] = __double2bfloat16(val[j]);
+        if ((double)__bfloat162float(v[j]) != val[j]) p->mix_inexact++;
+      }
+      __nv_bfloat16 *dv = nullptr;
+      rc = dev_copy(p, &dv, v.data(), v.size());
+      a.val = dv;
+    }
+  }
+  unsigned int *ticket = nullptr;
+  if (!rc) rc = dev_alloc(p, &ticket, 1);
+  if (!rc) rc = dev_alloc(p, &p->d_err, 1);
+  if (!rc) {
+    cudaMemset(p->d_err, 0, sizeof(int));
+    a.order = order; a.slot_off = slot_off; a.shell = shell; a.slot_vert = slot_vert; a.slot_coef = slot_coef;
+    a.slice_off = slice_off; a.ell_off = ell_off; a.ell_col = ell_col; a.ell_width = ell_width;
+    a.ticket = ticket; a.err = p->d_err;
+    p->tm_w = wmax <= 8 ? 8 : wmax <= 12 ? 12 : 16;  // wider slices read their rows from L2 at each level
+    p->tm_smem = 2 * (size_t)std::max(tp.max_slots, 1) * sizeof(float);
+    int maxsm = 0, per_sm = 0, nsm = 0;
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
+    if (p->tm_smem > (size_t)maxsm) rc = fail(kERange, "a tile's two level vectors exceed shared memory");
+    const void *fn = reinterpret_cast<const void *>(tm_kernel_ptr(value_type, p->tm_w));
+    if (!rc && (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->tm_smem) !=
+                    cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTmThreads, p->tm_smem) != cudaSuccess))
+      rc = fail(kECuda, "tile kernel attribute set-up failed");
+    if (!rc && per_sm < 1) rc = fail(kERange, "the tile kernel does not fit an SM");
+    p->tm_grid = (int)std::min<long>((long)per_sm * nsm, npart);
+    p->pipe_grid = p->tm_grid;
+    p->tiles_smem = true;
+    p->tm_on = true;
+  }
+  if (rc) { mpkg_plan_destroy(p); return rc; }
+  *out = p;
+  return kOk;
+}
+
 int mpkg_mixed_scale(const mpkg_plan *p, int *exponent, long *inexact_values) {
   if (!p || p->exec != MPKG_EXEC_MIXED) return fail(kEInval, "not a mixed-precision plan");
   if (exponent) *exponent = p->mix_e;
@@ -3191,6 +3485,16 @@ int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream) {
   if (p->epoch >= (1u << 30)) {
     CUDA_TRY(cudaMemsetAsync(p->mix.counts, 0, sizeof(unsigned) * (size_t)(p->nlevel + 1) * p->mix.nchunk, st));
     p->epoch = 1;
+  }
+  if (p->tm_on) {  // PA1 tiles
+    CUDA_TRY(cudaMemsetAsync(p->tm.ticket, 0, sizeof(unsigned int), st));
+    TileMixArgs a = p->tm;
+    a.x = d_vv;
+    a.vf = d_vv;
+    tm_kernel_ptr(p->mix_vt, p->tm_w)<<<p->tm_grid, kTmThreads, p->tm_smem, st>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    p->launches = 1;
+    return kOk;
   }
   if (p->inner) {  // wavefront schedule
     WaveArgs &w = p->inner->wave;
@@ -3290,7 +3594,8 @@ int mpkg_sync(mpkg_plan *p, void *stream) {
   CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
     cudaMemset(p->d_err, 0, sizeof(int));
-    if (p->exec == MPKG_EXEC_PIPE || p->exec == MPKG_EXEC_MIXED) {  // counters are inconsistent after an abort
+    if ((p->exec == MPKG_EXEC_PIPE || p->exec == MPKG_EXEC_MIXED) && p->pipe.counts) {  // counters are
+      // inconsistent after an abort
       cudaMemset(p->pipe.counts, 0, sizeof(unsigned int) * (size_t)(p->nlevel + 1) * p->pipe.ngroups);
       p->epoch = 0;
     }
@@ -3317,6 +3622,21 @@ int mpkg_exec_host(mpkg_plan *p, double *vv) {
     if (cudaPointerGetAttributes(&at, vv) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
       int rc = plan_launch(p, static_cast<double *>(at.devicePointer), p->stream);
       if (rc) return rc;
+      return mpkg_sync(p, p->stream);
+    }
+    cudaGetLastError();  // pageable memory: the copies below
+  }
+  // Page-locked vv on an FP64 wavefront plan: the kernel reads x from the
+  // host mapping and writes every level both to the device copy (which
+  // the next level reads) and through the mapping, so the device->host
+  // traffic overlaps the computation.
+  if (p->exec == MPKG_EXEC_WAVE && (p->arith == MPKG_ARITH_FMA || p->arith == MPKG_ARITH_SEPARATE)) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, vv) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+      if (!p->d_vv) CUDA_TRY(cudaMalloc(&p->d_vv, sizeof(double) * total));
+      int rc = launch_wave(p, p->d_vv, p->stream, static_cast<double *>(at.devicePointer));
+      if (rc) return rc;
+      p->launches = 1;
       return mpkg_sync(p, p->stream);
     }
     cudaGetLastError();  // pageable memory: the copies below

@@ -108,3 +108,96 @@ def test_mixed_values_beyond_l2_bitwise_vs_fp32_oracle(gpu):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     want64 = O.mpk(a.ptr, a.col, a.val, x, k, O.MODE_FMA)
     assert max(rel_errors(v, want64, a.n, k)) <= MIXED_TOL
+
+
+def _mixed_bits(plan, x, k, n):
+    import torch
+    d = torch.full(((k + 1) * n,), float("nan"), dtype=torch.float32, device="cuda")
+    d[:n] = torch.from_numpy(x.astype(np.float32)).cuda()
+    torch.cuda.synchronize()
+    plan.exec_mixed_device(d.data_ptr())
+    plan.sync()
+    return d.cpu().numpy()
+
+
+@pytest.mark.parametrize("case", ["diffusion", "cube", "banded", "bigparts"])
+@pytest.mark.parametrize("vt", [M.VALUE_F32, M.VALUE_BF16])
+def test_mixed_tiles_bitwise_equal_wavefront(case, vt, gpu):
+    """The PA1-tile schedule of the mixed form (temporal blocking) gives
+    the wavefront schedule's bits: FP32 FMA in CSR order, exact 2^-e
+    scaling.  Cases cover register-held rows (9- and 7-point stencils),
+    rows wider than the register budget (random banded, up to 30 entries)
+    and tiles with more rows than the threads hold (large parts)."""
+    k = 6 if case != "bigparts" else 4
+    if case == "diffusion":
+        a = M.Csr.diffusion(192, 160, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=3)
+        part, npart = M.partition_rcb(_grid2(192, 160), 64), 64
+    elif case == "cube":
+        a = M.Csr.laplacian(40, 36, 32, diag=6.0, off=-1.0)
+        part, npart = M.partition_rcb(a.coords, 48), 48
+    elif case == "banded":
+        a = M.Csr.banded(3000, 64, 5, 30, seed=4)
+        npart = 12
+        part = (np.arange(a.n) * npart // a.n).astype(np.int32)
+    else:
+        a = M.Csr.laplacian(64, 64, 4, diag=6.0, off=-1.0)
+        part, npart = M.partition_rcb(a.coords, 4), 4  # 4096-row parts: rows beyond the registers
+    x = M.uniform(11, a.n)
+    tiles = M.Plan.mixed_tiles(a, part, npart, k, vt)
+    wave = M.Plan.mixed(a, k, vt)
+    assert tiles.mixed_scale() == wave.mixed_scale()
+    got, want = _mixed_bits(tiles, x, k, a.n), _mixed_bits(wave, x, k, a.n)
+    tiles.close()
+    wave.close()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
+        f"{np.count_nonzero(got.view(np.uint32) != want.view(np.uint32))} entries differ"
+
+
+def _grid2(nx, ny):
+    i = np.arange(nx * ny)
+    return np.stack([i % nx, i // nx, np.zeros_like(i)], axis=1).astype(np.int32)
+
+
+def test_mixed_tiles_beyond_l2_bitwise_vs_fp32_oracle(gpu):
+    """2048^2 9-point diffusion (151 MB of FP32 values, more than L2) on
+    4096 PA1 tiles: the FP32 oracle's bits, and within 1e-6 of FP64 per
+    power; BF16 values (log-normal coefficients, rounded) within the
+    BF16 storage error of FP64."""
+    a = M.Csr.diffusion(2048, 2048, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=3)
+    k = 8
+    x = M.uniform(4, a.n)
+    part = M.partition_rcb(_grid2(2048, 2048), 4096)
+    plan = M.Plan.mixed_tiles(a, part, 4096, k, M.VALUE_F32)
+    e, _ = plan.mixed_scale()
+    got = _mixed_bits(plan, x, k, a.n).reshape(k + 1, a.n)
+    plan.close()
+    sval = a.val.astype(np.float32) * np.float32(2.0 ** -e)
+    want = O.spmm_f32(a.ptr, a.col, sval, x.astype(np.float32)[:, None], k)[:, :, 0]
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    want64 = O.mpk(a.ptr, a.col, a.val, x, k, O.MODE_FMA)
+    v = got.astype(np.float64) * (2.0 ** (e * np.arange(k + 1)))[:, None]
+    assert max(rel_errors(v, want64, a.n, k)) <= MIXED_TOL
+    pb = M.Plan.mixed_tiles(a, part, 4096, k, M.VALUE_BF16)
+    eb, inexact = pb.mixed_scale()
+    gb = _mixed_bits(pb, x, k, a.n).reshape(k + 1, a.n)
+    pb.close()
+    assert inexact > 0  # log-normal coefficients are not BF16 numbers
+    vb = gb.astype(np.float64) * (2.0 ** (eb * np.arange(k + 1)))[:, None]
+    errs = rel_errors(vb, want64, a.n, k)
+    assert max(errs) <= BF16_TOL, errs
+
+
+BF16_TOL = 2e-2  # BF16 keeps 8 significand bits: about 2^-9 relative per value, k levels of it
+
+
+def test_mixed_bf16_rounded_values_error_vs_fp64(gpu):
+    """BF16 values on the log-normal diffusion matrix (values rounded):
+    the error against the FP64 oracle per power stays within the BF16
+    storage bound."""
+    a = M.Csr.diffusion(512, 512, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=3)
+    k = 8
+    x = M.uniform(4, a.n)
+    v, e, inexact = run_mixed(a, k, M.VALUE_BF16, x)
+    assert inexact > 0
+    errs = rel_errors(v, O.mpk(a.ptr, a.col, a.val, x, k, O.MODE_FMA), a.n, k)
+    assert max(errs) <= BF16_TOL, errs

@@ -272,12 +272,18 @@ def test_fixed_point_wait_times_out_and_recovers(gpu):
     assert max(_rel_errors(_run(plan, x, a.n, 4), want, a.n, 4)) <= TOL
 
 
-@pytest.mark.parametrize("arith", [M.ARITH_DF64, M.ARITH_FIXED])
-def test_host_mapped_execution_matches_device(arith, gpu):
-    """Page-locked host vv runs the ring forms through the host mapping;
-    pageable vv goes through the copies; both give the device path's bits."""
+@pytest.mark.parametrize("valued", [False, True])
+@pytest.mark.parametrize("arith", [M.ARITH_DF64, M.ARITH_FIXED, M.ARITH_FMA, M.ARITH_SEPARATE])
+def test_host_mapped_execution_matches_device(arith, valued, gpu):
+    """Page-locked host vv runs the wavefront through the host mapping (the
+    ring forms keep their levels on the device; the FP64 forms write every
+    level to the device copy and through the mapping); pageable vv goes
+    through the copies; both give the device path's bits, twice in a row."""
     import torch
-    a = M.Csr.laplacian(64, 64, 16).pattern()
+    if arith == M.ARITH_FIXED and valued:
+        pytest.skip("fixed point runs the 1/deg operator only")
+    a = M.Csr.laplacian(64, 64, 16)
+    a = a if valued else a.pattern()
     k = 6
     x = M.uniform(21, a.n)
     plan = M.Plan.wave(a, k, arith=arith)
@@ -289,9 +295,12 @@ def test_host_mapped_execution_matches_device(arith, gpu):
     want = d.cpu().numpy()
     pinned = torch.zeros((k + 1) * a.n, dtype=torch.float64).pin_memory()
     pinned[:a.n] = torch.from_numpy(x)
-    got_pinned = plan.exec_host(pinned.numpy())
+    got_pinned = plan.exec_host(pinned.numpy()).copy()
+    pinned[a.n:] = float("nan")
+    again = plan.exec_host(pinned.numpy())
     got_pageable = _run(plan, x, a.n, k)
     plan.close()
     assert got_pinned.tobytes() == want.tobytes()
+    assert again.tobytes() == want.tobytes()
     assert got_pageable.tobytes() == want.tobytes()
     assert np.array_equal(got_pinned[:a.n], x)  # x is read, not written

@@ -76,6 +76,28 @@ def test_sstep_cg_bases(dims, trained_mlp, gpu):
     assert np.linalg.norm(x_l - x_cg) / np.linalg.norm(x_cg) < 1e-6
 
 
+@pytest.mark.parametrize("dims,seed", [((96, 96, 96), 5), ((64, 64, 64), 6)])
+def test_learned_shifts_need_no_more_iterations_than_lanczos(dims, seed, gpu):
+    """The criterion of the learned part on config-5-like problems (3-D
+    7-point variable-coefficient diffusion, log-normal sigma = 1): with the
+    shipped MLP (trained on the Ritz values of 2000 synthetic matrices),
+    s-step CG (s = 8) reaches 1e-8 in no more outer iterations than with
+    the Lanczos shifts, and in fewer than with the monomial basis."""
+    import os
+    from mpk_gb300.train_shifts import load
+    path = os.path.join(os.path.dirname(M.__file__), "shift_mlp.npz")
+    mlp = load(path)
+    a = M.Csr.diffusion(*dims, sigma=1.0, dominance=0.01, seed=seed)
+    b = M.uniform(7, a.n)
+    _, mono = M.sstep_cg(a, b, 8)
+    _, lan = M.sstep_cg(a, b, 8, shifts=S.from_lanczos(a, 8))
+    _, lrn = M.sstep_cg(a, b, 8, shifts=S.predict(mlp, a))
+    for inf in (mono, lan, lrn):
+        assert inf["converged"] and inf["relres"] <= 1e-8
+    assert lrn["iterations"] <= lan["iterations"]
+    assert lrn["iterations"] < mono["iterations"]
+
+
 def test_sstep_gram_modes_agree(gpu):
     """The FP64 Gram (default) and the double-float Gram take the same
     outer iterations on a diffusion problem and give solutions that agree
