@@ -633,9 +633,9 @@ def main():
     # the other executors and arithmetic forms on the same workload
     variants = {}
     if "variants" in sections:
-        runs = [(ex, ar, None) for ex, ar in (("spmv", "fma"), ("wave", "fma"), ("wave", "df64"), ("wave", "fixed"),
-                                              ("pipe", "fma"), ("pipe", "df64"), ("tiles", "fma"), ("tiles", "df64"),
-                                              ("tasks", "fma"))]
+        runs = [(ex, ar, None) for ex, ar in (("spmv", "fma"), ("wave", "fma"), ("spmv", "df64"), ("wave", "df64"),
+                                              ("spmv", "fixed"), ("wave", "fixed"), ("pipe", "fma"), ("pipe", "df64"),
+                                              ("tiles", "fma"), ("tiles", "df64"), ("tasks", "fma"))]
         runs += [("spmv", "fma", "valued"), ("wave", "fma", "valued"), ("wave", "df64", "valued")]
         ref_val = None
         for ex, ar, op in runs:
@@ -703,6 +703,13 @@ def main():
                 "bound_us": fmas / rate * 1e6, "achieved_fma_per_s": fmas / (ms * 1e-3),
                 "frac": fmas / (ms * 1e-3) / rate}
     base_ms = variants.get("spmv_fma", {}).get("ms_per_step")
+    # the MPK against k separate SpMV launches in the same arithmetic
+    same_arith = {}
+    for ar in ("fma", "df64", "fixed"):
+        t_sp = variants.get(f"spmv_{ar}", {}).get("ms_per_step")
+        t_mpk = ms if (args.exec == "wave" and args.arith == ar) else variants.get(f"wave_{ar}", {}).get("ms_per_step")
+        if t_sp and t_mpk:
+            same_arith[ar] = {"k_spmv_ms": t_sp, "mpk_wave_ms": t_mpk, "speedup": t_sp / t_mpk}
     cfg = dict(shared_config())
     line = {"metric": "MPK powers/sec (FP64, k*n output rows per second)", "value": value,
             "unit": "Grow-powers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -721,6 +728,7 @@ def main():
                                          "still dirty in L2 when the kernel ends are written back after it",
                          "fp64_pipe": fp64},
             "k_spmv_ms": base_ms, "speedup_vs_k_spmv": (base_ms / ms) if base_ms else None,
+            "speedup_vs_k_spmv_same_arith": same_arith,
             "variants": variants, "mixed": mixed, "batched": batched, "sstep": sstep, "prep": prep,
             "gpu_launches": info["launches"] * args.steps,
             "clocks": clk.summary(), "wall_s_timed_region": wall, "tail_calls_for_clock_samples": tail,

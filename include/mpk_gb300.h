@@ -53,7 +53,7 @@ extern "C" {
                                  FP32 pipes, FP64 storage; about 2^-46
                                  relative error per operation */
 #define MPKG_ARITH_FIXED 3    /* 64-bit fixed point (1/deg operator, wavefront
-                                 executor only): exact integer row sums at one
+                                 and k-SpMV executors): exact integer row sums at one
                                  scale 2^S per call, S = 62 - ceil(log2(longest
                                  row)) - e with max|x| < 2^e; error about 2^-S
                                  relative to max|x| per level; FP64 storage */
@@ -124,7 +124,11 @@ int mpkg_plan_pa1(int n, const int *ptr, const int *col, const double *val,
 int mpkg_plan_pipe(int n, const int *ptr, const int *col, const double *val,
                    int nlevel, int chunk, int arith, mpkg_plan **out);
 
-/* k chained SpMV launches (baseline; also the GPU spmv_exec_*). */
+/* k chained SpMV launches (baseline; also the GPU spmv_exec_*).  arith
+ * FMA/SEPARATE: FP64 rows (the reference's bits); DF64 and FIXED: the
+ * wavefront's double-float and fixed-point rows with the levels in a
+ * device ring, so the baseline runs the same arithmetic as the form it is
+ * compared with (same bits as mpkg_plan_wave in that arith). */
 int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val,
                    int nlevel, int arith, mpkg_plan **out);
 
@@ -213,6 +217,21 @@ int mpkg_sstep_gram(int mode);
 #define MPKG_SSTEP_DEVICE_LOOP 0
 #define MPKG_SSTEP_HOST_LOOP 1
 int mpkg_sstep_loop(int mode);
+
+/* How the calling thread's later mpkg_sstep_cg calls build the basis:
+ * MPKG_SSTEP_BASIS_MPK (default; the whole basis of both blocks as ONE
+ * matrix powers launch, the wavefront form: each CTA owns a row range at
+ * every level and waits only for the CTAs owning its columns, bounded
+ * waits) or MPKG_SSTEP_BASIS_STEPS (one SpMV launch per basis step).  Both
+ * give the same bits. */
+#define MPKG_SSTEP_BASIS_MPK 0
+#define MPKG_SSTEP_BASIS_STEPS 1
+int mpkg_sstep_basis(int mode);
+/* Test hook for failure detection: the calling thread's later matrix
+ * powers bases wait for extra_levels levels more than exist, so their
+ * bounded waits give up (about a second) and mpkg_sstep_cg returns
+ * MPKG_ETIMEOUT with the context usable; 0 restores normal waits. */
+int mpkg_sstep_debug_stall(int extra_levels);
 
 /* s-step CG (s <= 10): Newton basis rho_(j+1) = (A - shifts[j]) rho_j /
  * scale (shifts NULL: monomial basis), 2s+1 FP32 basis vectors per outer
@@ -403,6 +422,12 @@ int mpkg_levels(int n, const int *ptr, const int *col, const int *part, int npar
 /* level2wcrs (mpk2/lib.c:504-537). */
 int mpkg_level_weights(int n, const int *ptr, const int *col, const int *level,
                        int *wv, int *we);
+/* The same two computed on the current GPU (host arrays in and out; the
+ * same bytes as the host builds): every part's min-plus fixed point at
+ * once by Jacobi sweeps, and the weights per entry. */
+int mpkg_levels_gpu(int n, const int *ptr, const int *col, const int *part, int npart,
+                    const int *level_org, int *level);
+int mpkg_level_weights_gpu(int n, const int *ptr, const int *col, const int *level, int *wv, int *we);
 /* `skirt` tool output file (mpk2/skirt.c + lib.c:584-654), computed with
  * bounded searches; lev == NULL for PA1. */
 int mpkg_skirt_write(const char *path, int n, const int *ptr, const int *col,

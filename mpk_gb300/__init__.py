@@ -123,6 +123,8 @@ def _declare(L):
         "mpkg_free": (None, [P]),
         "mpkg_levels": (I, [I, P, P, P, I, P, P]),
         "mpkg_level_weights": (I, [I, P, P, P, P, P]),
+        "mpkg_levels_gpu": (I, [I, P, P, P, I, P, P]),
+        "mpkg_level_weights_gpu": (I, [I, P, P, P, P, P]),
         "mpkg_skirt_write": (I, [C.c_char_p, I, P, P, P, I, P, I]),
         "mpkg_tasks": (I, [I, P, P, I, I, I, P, P, I, P, pp, C.POINTER(Lg)]),
         "mpkg_tile_prep": (I, [I, P, P, P, I, I, I, C.POINTER(TilesT)]),
@@ -133,6 +135,8 @@ def _declare(L):
         "mpkg_lapjv": (I, [P, I, P]),
         "mpkg_sstep_gram": (I, [I]),
         "mpkg_sstep_loop": (I, [I]),
+        "mpkg_sstep_basis": (I, [I]),
+        "mpkg_sstep_debug_stall": (I, [I]),
         "mpkg_partition_rcb": (I, [I, P, I, I, P]),
         "mpkg_partition_bfs": (I, [I, P, P, I, P]),
         "mpkg_have_metis": (I, []),
@@ -401,21 +405,25 @@ def partition_bfs(a: Csr, npart):
     return part
 
 
-def levels(a: Csr, part, npart, level_org=None):
-    """comp_level / update_level (mpk2/lib.c:330-412)."""
+def levels(a: Csr, part, npart, level_org=None, on_gpu=False):
+    """comp_level / update_level (mpk2/lib.c:330-412), on the host or the
+    current GPU (same bytes)."""
     part = _i32(part)
     lo = _i32(level_org)
     out = np.empty(a.n, dtype=np.int32)
-    _check(lib().mpkg_levels(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(part), npart, _ptr(lo), _ptr(out)))
+    fn = lib().mpkg_levels_gpu if on_gpu else lib().mpkg_levels
+    _check(fn(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(part), npart, _ptr(lo), _ptr(out)))
     return out
 
 
-def level_weights(a: Csr, level):
-    """level2wcrs (mpk2/lib.c:504-537) -> (wv, we)."""
+def level_weights(a: Csr, level, on_gpu=False):
+    """level2wcrs (mpk2/lib.c:504-537) -> (wv, we), on the host or the
+    current GPU (same bytes)."""
     level = _i32(level)
     wv = np.empty(a.n, dtype=np.int32)
     we = np.empty(a.nnz, dtype=np.int32)
-    _check(lib().mpkg_level_weights(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(level), _ptr(wv), _ptr(we)))
+    fn = lib().mpkg_level_weights_gpu if on_gpu else lib().mpkg_level_weights
+    _check(fn(a.n, _ptr(a.ptr), _ptr(a.col), _ptr(level), _ptr(wv), _ptr(we)))
     return wv, we
 
 
@@ -686,10 +694,11 @@ def cg(a: Csr, b, x0=None, tol=1e-8, max_iter=10000):
 
 GRAM_FP64, GRAM_DF64 = 0, 1
 SSTEP_DEVICE_LOOP, SSTEP_HOST_LOOP = 0, 1
+SSTEP_BASIS_MPK, SSTEP_BASIS_STEPS = 0, 1
 
 
 def sstep_cg(a: Csr, b, s=8, shifts=None, scale=None, x0=None, tol=1e-8, max_outer=2000, gram=GRAM_FP64,
-             loop=SSTEP_DEVICE_LOOP):
+             loop=SSTEP_DEVICE_LOOP, basis=SSTEP_BASIS_MPK):
     """s-step CG with an FP32 Newton basis (shifts None: monomial) scaled
     by `scale` per step (default: the Gershgorin upper bound / 2); the
     Gram matrix in FP64 (GRAM_FP64) or double-float (GRAM_DF64); the
@@ -697,6 +706,7 @@ def sstep_cg(a: Csr, b, s=8, shifts=None, scale=None, x0=None, tol=1e-8, max_out
     the host (one launch and synchronisation per outer iteration)."""
     _check(lib().mpkg_sstep_gram(gram))
     _check(lib().mpkg_sstep_loop(loop))
+    _check(lib().mpkg_sstep_basis(basis))
     x = np.zeros(a.n) if x0 is None else np.array(x0, dtype=np.float64)
     b = _f64(b)
     if scale is None:

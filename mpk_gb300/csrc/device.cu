@@ -1137,6 +1137,67 @@ __device__ __forceinline__ long long double_to_fix(double x, int S) {
   return (long long)(b >> 63 ? 0ull - q : q);
 }
 
+// ------------------------------------------------------------------------
+// k separate SpMV launches in the wavefront's other arithmetic forms (the
+// "k SpMVs" baseline of mpk2/spmvexec.c:8-50 in the same arithmetic as the
+// MPK it is compared with): one thread per CSR row per level, levels kept
+// in a two-slot device ring like the wavefront's, FP64 results written to
+// vv.  Double-float: the rows of wave_df_kernel; fixed point: the rows of
+// wave_fix_kernel with the scale chosen from max|x| per call.
+// ------------------------------------------------------------------------
+template <bool VALUED>
+__global__ void __launch_bounds__(256) spmv_df_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                                                      const float2 *__restrict__ coef2, const float2 *src,
+                                                      float2 *sdst, double *__restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float sh = 0.f, sl = 0.f;
+  const int j0 = ptr[i], j1 = ptr[i + 1];
+  for (int j = j0; j < j1; j++) {
+    const float2 x = src[col[j]];
+    if (VALUED) df_mac(coef2[j], x, sh, sl);
+    else df_acc(x, sh, sl);
+  }
+  float2 v = df_norm(sh, sl);
+  if (!VALUED) v = df_scale(coef2[i], v);
+  sdst[i] = v;
+  y[i] = df_to_double(v);
+}
+
+__global__ void fix_emax_kernel(int n, const double *__restrict__ x, unsigned int *word) {
+  int e = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    e = max(e, (int)(((unsigned long long)__double_as_longlong(x[i]) >> 52) & 0x7FF));
+  e = (int)__reduce_max_sync(0xFFFFFFFFu, (unsigned)e);
+  if ((threadIdx.x & 31) == 0) atomicMax(word, (unsigned)e);
+}
+
+// word[0]: the largest biased exponent of |x|; word[1] receives S
+__global__ void fix_convert_kernel(int n, const double *__restrict__ x, unsigned int *word, int dbits,
+                                   long long *__restrict__ ring) {
+  const int emax = (int)word[0] - 1022;  // max|x| < 2^emax
+  const int S = min(62 - dbits - emax, 1022);
+  if (blockIdx.x == 0 && threadIdx.x == 0) word[1] = (unsigned)S;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    ring[i] = double_to_fix(x[i], S);
+}
+
+__global__ void __launch_bounds__(256) spmv_fix_kernel(int n, const int *__restrict__ ptr,
+                                                       const int *__restrict__ col,
+                                                       const unsigned long long *__restrict__ mul,
+                                                       const unsigned int *__restrict__ word, const long long *src,
+                                                       long long *dst, double *__restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int S = (int)word[1];
+  const int j0 = ptr[i], len = ptr[i + 1] - j0;
+  long long sum = 0;
+  for (int j = 0; j < len; j++) sum += src[col[j0 + j]];
+  const long long q = fix_div(sum, len, mul[len & 255]);
+  dst[i] = q;
+  y[i] = fix_to_double(q, S);
+}
+
 template <bool STAGE>
 __global__ void __launch_bounds__(256, 5) wave_fix_kernel(WaveArgs a) {
   extern __shared__ __align__(16) unsigned char wave_smem[];
@@ -1705,6 +1766,11 @@ struct mpkg_plan {
   const void *graph_key = nullptr;
   bool graph_ok = false;
   float *d_fb = nullptr;  // staging of mpkg_exec_batch_host
+  // k-SpMV in double-float or fixed point: level ring, fixed-point tables
+  void *sp_ring = nullptr;
+  unsigned long long *sp_mul = nullptr;
+  unsigned int *sp_word = nullptr;
+  int sp_dbits = 0;
   // mixed form on PA1 tiles (temporal blocking)
   TileMixArgs tm{};
   bool tm_on = false;
@@ -1760,7 +1826,7 @@ int plan_common(mpkg_plan *p, int n, const int *ptr, const int *col, const doubl
   if (rc) return rc;
   if (nlevel <= 0 || nlevel > 31) return fail(kEInval, "nlevel must be in [1, 31]");
   if (arith == MPKG_ARITH_FIXED && !(allow_fixed && val == nullptr))
-    return fail(kEInval, "fixed-point arithmetic runs the 1/deg operator on the wavefront executor only");
+    return fail(kEInval, "fixed-point arithmetic runs the 1/deg operator only (wavefront and k-SpMV executors)");
   if (arith != MPKG_ARITH_FMA && arith != MPKG_ARITH_SEPARATE && arith != MPKG_ARITH_DF64 &&
       arith != MPKG_ARITH_FIXED)
     return fail(kEInval, "unknown arith mode");
@@ -2285,6 +2351,36 @@ int plan_launch(mpkg_plan *p, double *d_vv, cudaStream_t st) {
       break;
     }
     case MPKG_EXEC_SPMV: {
+      const int n = p->n;
+      const dim3 blk(256), grd((n + 255) / 256);
+      if (p->arith == MPKG_ARITH_DF64) {
+        float2 *ring = static_cast<float2 *>(p->sp_ring);
+        split_kernel<<<592, 256, 0, st>>>(d_vv, ring, n);
+        for (int l = 1; l <= p->nlevel; l++) {
+          const float2 *src = ring + (size_t)((l - 1) & 1) * n;
+          float2 *dst = ring + (size_t)(l & 1) * n;
+          if (p->valued)
+            spmv_df_kernel<true><<<grd, blk, 0, st>>>(n, p->d_ptr, p->d_col, p->d_coef2, src, dst, d_vv + (size_t)l * n);
+          else
+            spmv_df_kernel<false><<<grd, blk, 0, st>>>(n, p->d_ptr, p->d_col, p->d_coef2, src, dst, d_vv + (size_t)l * n);
+        }
+        CUDA_TRY(cudaGetLastError());
+        p->launches = p->nlevel + 1;
+        break;
+      }
+      if (p->arith == MPKG_ARITH_FIXED) {
+        long long *ring = static_cast<long long *>(p->sp_ring);
+        CUDA_TRY(cudaMemsetAsync(p->sp_word, 0, 2 * sizeof(unsigned int), st));
+        fix_emax_kernel<<<592, 256, 0, st>>>(n, d_vv, p->sp_word);
+        fix_convert_kernel<<<592, 256, 0, st>>>(n, d_vv, p->sp_word, p->sp_dbits, ring);
+        for (int l = 1; l <= p->nlevel; l++)
+          spmv_fix_kernel<<<grd, blk, 0, st>>>(n, p->d_ptr, p->d_col, p->sp_mul, p->sp_word,
+                                               ring + (size_t)((l - 1) & 1) * n, ring + (size_t)(l & 1) * n,
+                                               d_vv + (size_t)l * n);
+        CUDA_TRY(cudaGetLastError());
+        p->launches = p->nlevel + 2;
+        break;
+      }
       int rc = launch_spmv(p->n, p->d_ptr, p->d_col, p->d_coef, p->valued, p->nlevel, d_vv, p->arith, st);
       if (rc) return rc;
       p->launches = p->nlevel;
@@ -2495,12 +2591,29 @@ int mpkg_plan_spmv(int n, const int *ptr, const int *col, const double *val, int
   *out = nullptr;
   mpkg_plan *p = new_plan();
   if (!p) return fail(kENoMem, "plan allocation failed");
-  int rc = arith == MPKG_ARITH_DF64 ? fail(kEInval, "the k-SpMV baseline computes in FP64 only")
-                                    : plan_common(p, n, ptr, col, val, nlevel, arith);
+  int rc = plan_common(p, n, ptr, col, val, nlevel, arith, true);
   if (!rc) {
     p->exec = MPKG_EXEC_SPMV;
     p->npart = 1;
     p->rows_computed = (long)n * nlevel;
+  }
+  if (!rc && arith == MPKG_ARITH_DF64) {
+    float2 *ring = nullptr;
+    rc = dev_alloc(p, &ring, (size_t)2 * n);
+    p->sp_ring = ring;
+  }
+  if (!rc && arith == MPKG_ARITH_FIXED) {
+    int maxlen = 0;
+    for (int i = 0; i < n; i++) maxlen = std::max(maxlen, ptr[i + 1] - ptr[i]);
+    if (maxlen > 255) rc = fail(kERange, "fixed-point form: rows are limited to 255 entries");
+    while ((1 << p->sp_dbits) < maxlen) p->sp_dbits++;
+    std::vector<unsigned long long> mul(256, 0);
+    for (int d = 2; d < 256; d++) mul[d] = ~0ull / (unsigned long long)d + 1;  // ceil(2^64 / d)
+    long long *ring = nullptr;
+    if (!rc) rc = dev_copy(p, &p->sp_mul, mul.data(), mul.size());
+    if (!rc) rc = dev_alloc(p, &p->sp_word, 2);
+    if (!rc) rc = dev_alloc(p, &ring, (size_t)2 * n);
+    p->sp_ring = ring;
   }
   if (rc) { mpkg_plan_destroy(p); return rc; }
   *out = p;
@@ -3563,7 +3676,8 @@ int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info) {
   info->rows_computed = p->rows_computed;
   info->device_bytes = p->device_bytes;
   info->launches = p->exec == MPKG_EXEC_TASKS ? p->nphase + 1
-                   : p->exec == MPKG_EXEC_SPMV ? p->nlevel
+                   : p->exec == MPKG_EXEC_SPMV
+                       ? p->nlevel + (p->arith == MPKG_ARITH_DF64 ? 1 : p->arith == MPKG_ARITH_FIXED ? 2 : 0)
                    : p->exec == MPKG_EXEC_BUFS ? 2 + 2 * p->nphase + 1
                    : p->exec == MPKG_EXEC_PDMPK ? 2 + 2 * p->nphase : 1;
   if (p->exec == MPKG_EXEC_WAVE) info->pipe_grid = p->wave_grid;

@@ -163,6 +163,9 @@ struct TilePlan {
 };
 int build_tile_plan(const Csr &g, const std::vector<int> &part, int npart, int nlevel,
                     TilePlan *tp);
+// Tile launch order: breadth-first over the part graph (neighbouring tiles
+// consecutive, so shared halo rows are reused from L2).
+void part_order(const Csr &g, const std::vector<int> &part, int npart, std::vector<int> *order);
 // The same plan built on the current GPU (prep_gpu.cu); falls back to
 // build_tile_plan for balls beyond its capacity and for every error case.
 // *on_gpu tells which ran.

@@ -402,6 +402,48 @@ int build_tasks(const Csr &g, int npart, int nlevel, int nphase,
 }
 
 // PA1 tiles.
+// Launch order of the parts: breadth-first over the part graph (parts
+// adjacent when an entry of one reads a vertex of the other), from a part
+// of least degree, neighbours in ascending id; unconnected parts start new
+// searches.  Consecutive tiles are then neighbours, so the halo rows two
+// tiles share are read while the first tile's are still in L2.  The order
+// only schedules work: every tile computes the same rows whatever it is.
+void part_order(const Csr &g, const std::vector<int> &part, int npart, std::vector<int> *order) {
+  std::vector<std::pair<int, int>> pairs;
+  for (int i = 0; i < g.n; i++)
+    for (int j = g.ptr[i]; j < g.ptr[i + 1]; j++) {
+      const int a = part[i], b = part[g.col[j]];
+      if (a != b) pairs.emplace_back(a, b);
+    }
+  std::sort(pairs.begin(), pairs.end());
+  pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+  std::vector<int> aptr(npart + 1, 0), adj(pairs.size());
+  for (auto &e : pairs) aptr[e.first + 1]++;
+  for (int p = 0; p < npart; p++) aptr[p + 1] += aptr[p];
+  for (size_t k = 0; k < pairs.size(); k++) adj[k] = pairs[k].second;  // sorted by (first, second)
+  std::vector<int> byd(npart);
+  std::iota(byd.begin(), byd.end(), 0);
+  std::stable_sort(byd.begin(), byd.end(),
+                   [&](int a, int b) { return aptr[a + 1] - aptr[a] < aptr[b + 1] - aptr[b]; });
+  std::vector<char> seen(npart, 0);
+  order->clear();
+  order->reserve(npart);
+  for (int s0 : byd) {
+    if (seen[s0]) continue;
+    size_t head = order->size();
+    order->push_back(s0);
+    seen[s0] = 1;
+    while (head < order->size()) {
+      const int p = (*order)[head++];
+      for (int k = aptr[p]; k < aptr[p + 1]; k++)
+        if (!seen[adj[k]]) {
+          seen[adj[k]] = 1;
+          order->push_back(adj[k]);
+        }
+    }
+  }
+}
+
 int build_tile_plan(const Csr &g, const std::vector<int> &part, int npart, int nlevel,
                     TilePlan *tp) {
   const int n = g.n;
@@ -411,8 +453,7 @@ int build_tile_plan(const Csr &g, const std::vector<int> &part, int npart, int n
   transpose(g, &tr);
   auto mem = members_of(part, npart);
   tp->n = n; tp->npart = npart; tp->nlevel = nlevel;
-  tp->order.resize(npart);
-  std::iota(tp->order.begin(), tp->order.end(), 0);
+  part_order(g, part, npart, &tp->order);
   tp->slot_off.assign(npart + 1, 0);
   tp->shell.assign((size_t)npart * (nlevel + 1), 0);
   tp->slot_vert.clear();

@@ -435,8 +435,7 @@ int build_tile_plan_gpu(const Csr &g, const std::vector<int> &part, int npart, i
   for (int p = 0; p < npart; p++)
     if (bsize[p] < 0 || ell[p] < 0) return build_tile_plan(g, part, npart, nlevel, tp);
   tp->n = n; tp->npart = npart; tp->nlevel = nlevel;
-  tp->order.resize(npart);
-  std::iota(tp->order.begin(), tp->order.end(), 0);
+  part_order(g, part, npart, &tp->order);
   tp->shell = shell;
   tp->slot_off.assign(npart + 1, 0);
   tp->slice_off.assign(npart + 1, 0);
@@ -498,9 +497,162 @@ int check_part_host(const Csr &g, const std::vector<int> &part, int npart, int n
   return host_pa1_tasks(g, part, npart, nlevel, tl);
 }
 
+// ---- DMPK phase levels and METIS weights on the GPU -----------------------
+// comp_level / update_level (mpk2/lib.c:330-412): per part, the fixed point
+// of minplus_r from BIG inside the part and init outside (-1, or the
+// previous phase's levels).  Every part's fixed point at once: a vertex
+// reads its own part's values and the fixed init of the others, so the
+// parts never interact.  Jacobi sweeps from BIG descend to the same least
+// values the reference's sweeps reach (the shortest-path fixed point, at
+// most BIG), one launch per sweep until a sweep changes nothing.
+__global__ void level_sweep_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                                   const int *__restrict__ part, const int *__restrict__ init,
+                                   const long long *__restrict__ src, long long *__restrict__ dst,
+                                   int *__restrict__ changed) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    long long t = src[i];
+    const int pi = part[i];
+    for (int j = ptr[i]; j < ptr[i + 1]; j++) {
+      const int c = col[j];
+      const long long v = (part[c] != pi ? (init ? (long long)init[c] : -1LL) : src[c]) + 1;
+      if (v < t) t = v;
+    }
+    dst[i] = t;
+    if (t != src[i]) *changed = 1;
+  }
+}
+
+__global__ void level_minmax_kernel(int n, const int *__restrict__ lev, int *mm) {
+  int lo = 0x7fffffff, hi = -0x7fffffff - 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    lo = min(lo, lev[i]);
+    hi = max(hi, lev[i]);
+  }
+  atomicMin(mm, lo);
+  atomicMax(mm + 1, hi);
+}
+
+// level2wcrs (mpk2/lib.c:504-537): vertex weight max + 1 - l_i; edge weight
+// 1e6 / (l_i + l_j - 2 min + 1) truncated, at least 1 (IEEE division, the
+// host's bits).
+__global__ void level_weight_kernel(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                                    const int *__restrict__ lev, const int *__restrict__ mm, int *__restrict__ wv,
+                                    int *__restrict__ we) {
+  const int mn = mm[0], mx = mm[1];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int l0 = lev[i];
+    wv[i] = mx + 1 - l0;
+    for (int j = ptr[i]; j < ptr[i + 1]; j++) {
+      double w = (double)(l0 + lev[col[j]] - 2 * mn);
+      w = __ddiv_rn(1e+6, __dadd_rn(w, 1.0));
+      we[j] = w < 1.0 ? 1 : __double2int_rz(w);
+    }
+  }
+}
+
+template <typename T>
+struct DevArr {
+  T *p = nullptr;
+  ~DevArr() { cudaFree(p); }
+  cudaError_t alloc(size_t count) { return cudaMalloc((void **)&p, sizeof(T) * std::max<size_t>(count, 1)); }
+  cudaError_t put(const T *src, size_t count) {
+    cudaError_t e = alloc(count);
+    return e != cudaSuccess || !count ? e : cudaMemcpy(p, src, sizeof(T) * count, cudaMemcpyHostToDevice);
+  }
+};
+
+#define PG_TRY(expr)                                                                             \
+  do {                                                                                           \
+    cudaError_t e_ = (expr);                                                                     \
+    if (e_ != cudaSuccess) return fail(kECuda, std::string(#expr ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+int levels_gpu(int n, const int *ptr, const int *col, const int *part, const int *level_org, int *level) {
+  const long nnz = ptr[n];
+  long long big;
+  if (level_org) {
+    int mx = level_org[0];
+    for (int i = 1; i < n; i++) mx = std::max(mx, level_org[i]);
+    big = (long long)mx + n + 1;
+  } else {
+    big = (long long)n + 1;
+  }
+  DevArr<int> dptr, dcol, dpart, dinit, dchg;
+  DevArr<long long> d0, d1;
+  PG_TRY(dptr.put(ptr, (size_t)n + 1));
+  PG_TRY(dcol.put(col, (size_t)nnz));
+  PG_TRY(dpart.put(part, (size_t)n));
+  if (level_org) PG_TRY(dinit.put(level_org, (size_t)n));
+  PG_TRY(dchg.alloc(1));
+  PG_TRY(d0.alloc(n));
+  PG_TRY(d1.alloc(n));
+  std::vector<long long> h(n, big);
+  PG_TRY(cudaMemcpy(d0.p, h.data(), sizeof(long long) * n, cudaMemcpyHostToDevice));
+  const int grid = (int)std::min<long>((n + 255) / 256, 4096);
+  long long *src = d0.p, *dst = d1.p;
+  for (long sweep = 0; sweep <= (long)n + 1; sweep++) {  // a fixed point is reached within n + 1 sweeps
+    int chg = 0;
+    PG_TRY(cudaMemsetAsync(dchg.p, 0, sizeof(int)));
+    level_sweep_kernel<<<grid, 256>>>(n, dptr.p, dcol.p, dpart.p, level_org ? dinit.p : nullptr, src, dst, dchg.p);
+    PG_TRY(cudaGetLastError());
+    PG_TRY(cudaMemcpy(&chg, dchg.p, sizeof(int), cudaMemcpyDeviceToHost));
+    std::swap(src, dst);
+    if (!chg) break;
+  }
+  PG_TRY(cudaMemcpy(h.data(), src, sizeof(long long) * n, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; i++) level[i] = (int)h[i];
+  return kOk;
+}
+
+int level_weights_gpu(int n, const int *ptr, const int *col, const int *level, int *wv, int *we) {
+  const long nnz = ptr[n];
+  DevArr<int> dptr, dcol, dlev, dmm, dwv, dwe;
+  PG_TRY(dptr.put(ptr, (size_t)n + 1));
+  PG_TRY(dcol.put(col, (size_t)nnz));
+  PG_TRY(dlev.put(level, (size_t)n));
+  const int mm0[2] = {0x7fffffff, -0x7fffffff - 1};
+  PG_TRY(dmm.put(mm0, 2));
+  PG_TRY(dwv.alloc(n));
+  PG_TRY(dwe.alloc(nnz));
+  const int grid = (int)std::min<long>((n + 255) / 256, 4096);
+  level_minmax_kernel<<<grid, 256>>>(n, dlev.p, dmm.p);
+  level_weight_kernel<<<grid, 256>>>(n, dptr.p, dcol.p, dlev.p, dmm.p, dwv.p, dwe.p);
+  PG_TRY(cudaGetLastError());
+  PG_TRY(cudaMemcpy(wv, dwv.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if (nnz) PG_TRY(cudaMemcpy(we, dwe.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+  return kOk;
+}
+
 }  // namespace mpkg
 
 extern "C" {
+
+int mpkg_levels_gpu(int n, const int *ptr, const int *col, const int *part, int npart, const int *level_org,
+                    int *level) {
+  using namespace mpkg;
+  clear_error();
+  if (n <= 0 || !ptr || !col || ptr[0] != 0 || !part || !level || npart <= 0) return fail(kEInval, "bad argument");
+  for (int i = 0; i < n; i++)
+    if (ptr[i + 1] < ptr[i]) return fail(kEInval, "ptr must be non-decreasing");
+  for (long j = 0; j < ptr[n]; j++)
+    if (col[j] < 0 || col[j] >= n) return fail(kERange, "column index out of range");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
+  return levels_gpu(n, ptr, col, part, level_org, level);
+}
+
+int mpkg_level_weights_gpu(int n, const int *ptr, const int *col, const int *level, int *wv, int *we) {
+  using namespace mpkg;
+  clear_error();
+  if (n <= 0 || !ptr || !col || ptr[0] != 0 || !level || !wv || !we) return fail(kEInval, "bad argument");
+  for (int i = 0; i < n; i++)
+    if (ptr[i + 1] < ptr[i]) return fail(kEInval, "ptr must be non-decreasing");
+  for (long j = 0; j < ptr[n]; j++)
+    if (col[j] < 0 || col[j] >= n) return fail(kERange, "column index out of range");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(kECuda, "no CUDA device");
+  return level_weights_gpu(n, ptr, col, level, wv, we);
+}
 
 int mpkg_tile_prep(int n, const int *ptr, const int *col, const int *part, int npart, int nlevel, int on_gpu,
                    mpkg_tiles_t *out) {

@@ -235,22 +235,96 @@ __global__ void basis_start_kernel(int n, const double *__restrict__ p, const do
   }
 }
 
-// One Newton step of both blocks: out = (A in - theta in) / sigma, FP32
-// values and accumulation in CSR order; the R block stops one step early.
-__global__ void basis_step_kernel(int n, Sell a, const float *__restrict__ pin, float *__restrict__ pout,
-                                  const float *__restrict__ rin, float *__restrict__ rout, float theta, float rsigma) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float sp = 0.f, sr = 0.f;
-    const long e0 = a.off[i >> 5] + (i & 31);
-    const int l = a.len[i];
-    for (int t = 0; t < l; t++) {
-      const int c = a.col[e0 + 32L * t];
-      const float v = a.valf[e0 + 32L * t];
-      sp = __fmaf_rn(v, pin[c], sp);
-      if (rout) sr = __fmaf_rn(v, rin[c], sr);
+// Row i of one Newton step of both blocks: out = (A in - theta in) / sigma,
+// FP32 values and accumulation in CSR order (the R block when rout is not
+// null).  Both basis builders below run this code, so they give the same
+// bits.  The inputs are plain loads: the matrix-powers form reads levels
+// that other CTAs wrote during the same launch.
+__device__ __forceinline__ void newton_row(int i, const Sell &a, const float *pin, float *pout, const float *rin,
+                                           float *rout, float theta, float rsigma) {
+  float sp = 0.f, sr = 0.f;
+  const long e0 = a.off[i >> 5] + (i & 31);
+  const int l = a.len[i];
+  for (int t = 0; t < l; t++) {
+    const int c = a.col[e0 + 32L * t];
+    const float v = a.valf[e0 + 32L * t];
+    sp = __fmaf_rn(v, pin[c], sp);
+    if (rout) sr = __fmaf_rn(v, rin[c], sr);
+  }
+  pout[i] = __fmul_rn(__fmaf_rn(-theta, pin[i], sp), rsigma);
+  if (rout) rout[i] = __fmul_rn(__fmaf_rn(-theta, rin[i], sr), rsigma);
+}
+
+// One Newton step of both blocks over all rows (one launch per step); the
+// R block stops one step early.
+__global__ void basis_step_kernel(int n, Sell a, const float *pin, float *pout, const float *rin, float *rout,
+                                  float theta, float rsigma) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    newton_row(i, a, pin, pout, rin, rout, theta, rsigma);
+}
+
+// The whole basis [p, rho_1(A) p, ..., rho_s(A) p, r, ..., rho_(s-1)(A) r]
+// as ONE matrix powers launch (the wavefront form): CTA b owns rows
+// [row_lo[b], row_lo[b+1]) (slice aligned, so no cache line holds two
+// CTAs' rows) at every level, and computes level j once the CTAs owning
+// the columns of its rows (a contiguous range) have published level j - 1.
+// The levels are the basis vectors themselves, each a fresh buffer, so no
+// CTA overwrites what another still reads.  Waits are bounded: a wait that
+// gives up sets *err and the launch ends (the host reports MPKG_ETIMEOUT).
+// flags are reset to 0 before every launch.
+struct BasisWave {
+  int n, s, nblk;
+  const int *row_lo;     // nblk + 1
+  const int *dep_lo;     // nblk: first CTA owning a column of CTA b's rows
+  const int *dep_hi;     // nblk: last such CTA
+  unsigned int *flags;   // nblk: last level published
+  int *err;
+  unsigned int stall;    // test hook: extra levels to wait for (never published)
+  float theta[kMaxS], rsig[kMaxS];
+};
+
+constexpr long kBasisSpin = 4000000;  // polls of one flag (~1 s with backoff)
+
+__device__ __forceinline__ unsigned int acquire_u32(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreads) basis_wave_kernel(BasisWave w, Sell a, float *Y) {
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = 0;
+  __syncthreads();
+  const int b = blockIdx.x, r0 = w.row_lo[b], r1 = w.row_lo[b + 1];
+  const size_t n = (size_t)w.n;
+  for (int j = 1; j <= w.s; j++) {
+    if (j > 1) {
+      for (int c = w.dep_lo[b] + (int)threadIdx.x; c <= w.dep_hi[b]; c += blockDim.x) {
+        long spins = 0;
+        while (acquire_u32(w.flags + c) < (unsigned)(j - 1) + w.stall) {
+          if (++spins > kBasisSpin || *((volatile int *)w.err)) {
+            atomicCAS(w.err, 0, 1);
+            s_abort = 1;
+            break;
+          }
+          __nanosleep(spins < 16 ? 32 : 256);
+        }
+      }
+      __syncthreads();
+      if (s_abort) return;
     }
-    pout[i] = (sp - theta * pin[i]) * rsigma;
-    if (rout) rout[i] = (sr - theta * rin[i]) * rsigma;
+    const bool rstep = j < w.s;
+    const float *pin = Y + (size_t)(j - 1) * n;
+    float *pout = Y + (size_t)j * n;
+    const float *rin = rstep ? Y + (size_t)(w.s + j) * n : nullptr;
+    float *rout = rstep ? Y + (size_t)(w.s + 1 + j) * n : nullptr;
+    for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x)
+      newton_row(i, a, pin, pout, rin, rout, w.theta[j - 1], w.rsig[j - 1]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(w.flags + b), "r"((unsigned)j) : "memory");
+    }
   }
 }
 
@@ -267,6 +341,8 @@ __global__ void basis_step_kernel(int n, Sell a, const float *__restrict__ pin, 
 constexpr int kGramRows = 64;
 thread_local bool g_gram_f64 = true;  // mpkg_sstep_gram: FP64 (default) or double-float Gram
 thread_local bool g_device_loop = true;  // mpkg_sstep_loop: device-side (default) or host-side outer loop
+thread_local bool g_basis_mpk = true;    // mpkg_sstep_basis: one matrix powers launch (default) or s launches
+thread_local unsigned g_basis_stall = 0;  // mpkg_sstep_debug_stall
 __device__ __forceinline__ void gram_acc(float a, float b, float &sh, float &sl) {
   const float p = __fmul_rn(a, b), e = __fmaf_rn(a, b, -p);
   const float t = __fadd_rn(sh, p), bp = __fadd_rn(t, -sh);
@@ -646,6 +722,83 @@ bool build_device_loop(GraphRun &gr, F &&body) {
   return true;
 }
 
+// The basis wavefront's layout: slice-aligned CTA row ranges of equal size
+// and, per CTA, the contiguous range of CTAs owning the columns of its rows.
+struct BasisLayout {
+  DevBuf<int> row_lo, dep_lo, dep_hi, err;
+  DevBuf<unsigned int> flags;
+  BasisWave w{};
+  bool coop = false;  // cooperative launch attribute accepted in stream capture
+  int build(int n, const int *ptr, const int *col, int s, const std::vector<double> &th,
+            const std::vector<double> &sg) {
+    int dev = 0, nsm = 0, per_sm = 0;
+    SS_TRY(cudaGetDevice(&dev));
+    SS_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    SS_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_wave_kernel, kThreads, 0));
+    const int nsl = (n + 31) / 32;
+    const int nblk = std::max(1, std::min(per_sm * nsm, nsl));
+    std::vector<int> lo(nblk + 1), dl(nblk), dh(nblk);
+    for (int b = 0; b <= nblk; b++) lo[b] = std::min<long>(n, 32L * ((long)b * nsl / nblk));
+    auto owner = [&](int row) { return (int)(std::upper_bound(lo.begin(), lo.end(), row) - lo.begin()) - 1; };
+    for (int b = 0; b < nblk; b++) {
+      int cmin = lo[b], cmax = std::max(lo[b], lo[b + 1] - 1);
+      for (int i = lo[b]; i < lo[b + 1]; i++)
+        for (int j = ptr[i]; j < ptr[i + 1]; j++) {
+          cmin = std::min(cmin, col[j]);
+          cmax = std::max(cmax, col[j]);
+        }
+      dl[b] = std::min(b, owner(cmin));
+      dh[b] = std::max(b, std::min(nblk - 1, owner(cmax)));
+    }
+    int rc;
+    if ((rc = row_lo.alloc(nblk + 1)) || (rc = dep_lo.alloc(nblk)) || (rc = dep_hi.alloc(nblk)) ||
+        (rc = flags.alloc(nblk)) || (rc = err.alloc(1)))
+      return rc;
+    SS_TRY(cudaMemcpy(row_lo.p, lo.data(), sizeof(int) * (nblk + 1), cudaMemcpyHostToDevice));
+    SS_TRY(cudaMemcpy(dep_lo.p, dl.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice));
+    SS_TRY(cudaMemcpy(dep_hi.p, dh.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice));
+    SS_TRY(cudaMemset(err.p, 0, sizeof(int)));
+    w.n = n; w.s = s; w.nblk = nblk; w.stall = g_basis_stall;
+    w.row_lo = row_lo.p; w.dep_lo = dep_lo.p; w.dep_hi = dep_hi.p; w.flags = flags.p; w.err = err.p;
+    for (int j = 0; j < s; j++) {
+      w.theta[j] = (float)th[j];
+      w.rsig[j] = (float)(1.0 / sg[j]);
+    }
+    return kOk;
+  }
+  cudaError_t launch(const Sell &a, float *Y, cudaStream_t cs) const {
+    cudaError_t e = cudaMemsetAsync(flags.p, 0, sizeof(unsigned int) * (size_t)w.nblk, cs);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)w.nblk);
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = cs;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = coop ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, basis_wave_kernel, w, a, Y);
+  }
+  // Whether a cooperative launch can be captured into a graph here; if not,
+  // the grid (sized by the occupancy calculator, every CTA resident on an
+  // otherwise idle device) is launched plainly and the bounded waits guard it.
+  void probe(const Sell &a, float *Y) {
+    cudaStream_t st = nullptr;
+    cudaGraph_t g = nullptr;
+    coop = false;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); return; }
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      coop = true;
+      const bool ok = launch(a, Y, st) == cudaSuccess;
+      coop = cudaStreamEndCapture(st, &g) == cudaSuccess && ok;
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(st);
+    cudaGetLastError();
+  }
+};
+
 // Page-locked host bytes (int-addressed), released on scope exit.
 struct HostBuf {
   int *p = nullptr;
@@ -877,6 +1030,18 @@ int mpkg_sstep_gram(int mode) {
   return kOk;
 }
 
+int mpkg_sstep_basis(int mode) {
+  if (mode != MPKG_SSTEP_BASIS_MPK && mode != MPKG_SSTEP_BASIS_STEPS) return fail(kEInval, "unknown basis mode");
+  g_basis_mpk = mode == MPKG_SSTEP_BASIS_MPK;
+  return kOk;
+}
+
+int mpkg_sstep_debug_stall(int extra_levels) {
+  if (extra_levels < 0 || extra_levels > 1000) return fail(kEInval, "0 <= extra_levels <= 1000");
+  g_basis_stall = (unsigned)extra_levels;
+  return kOk;
+}
+
 int mpkg_sstep_loop(int mode) {
   clear_error();
   if (mode != MPKG_SSTEP_DEVICE_LOOP && mode != MPKG_SSTEP_HOST_LOOP) return fail(kEInval, "unknown loop mode");
@@ -933,12 +1098,21 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
     return kOk;
   };
   if ((rc = upload_scalars())) return rc;
+  // the basis as one matrix powers launch (default) or s SpMV launches
+  const bool basis_mpk = g_basis_mpk;
+  BasisLayout bl;
+  if (basis_mpk) {
+    if ((rc = bl.build(n, ptr, col, s, th, sg))) return rc;
+    bl.probe(a.sell(), y.p);
+  }
   // one outer iteration: basis, Gram, coefficient steps, update, true
   // residual, scalars for the next iteration
   auto iteration = [&](cudaStream_t cs) {
     float *Y = y.p;
     basis_start_kernel<<<nb, kThreads, 0, cs>>>(n, dp.p, dr.p, dsc.p, Y, Y + (size_t)(s + 1) * n);
-    for (int j = 0; j < s; j++) {
+    if (basis_mpk) {
+      bl.launch(a.sell(), Y, cs);
+    } else for (int j = 0; j < s; j++) {
       const bool rstep = j + 1 < s;
       basis_step_kernel<<<nb, kThreads, 0, cs>>>(n, a.sell(), Y + (size_t)j * n, Y + (size_t)(j + 1) * n,
                                                  rstep ? Y + (size_t)(s + 1 + j) * n : nullptr,
@@ -1088,6 +1262,11 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
   }
   SS_TRY(cudaStreamSynchronize(gr.st));
   SS_TRY(cudaMemcpy(x, dx.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (basis_mpk) {
+    int werr = 0;
+    SS_TRY(cudaMemcpy(&werr, bl.err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (werr) return fail(kETimeout, "s-step basis: a device-side wait exceeded its spin limit");
+  }
   if (info) {
     std::memset(info, 0, sizeof *info);
     info->loop_ms = std::chrono::duration<double, std::milli>(t_loop_end - t_loop).count();

@@ -127,7 +127,11 @@ def test_mixed_tiles_bitwise_equal_wavefront(case, vt, gpu):
     the wavefront schedule's bits: FP32 FMA in CSR order, exact 2^-e
     scaling.  Cases cover register-held rows (9- and 7-point stencils),
     rows wider than the register budget (random banded, up to 30 entries)
-    and tiles with more rows than the threads hold (large parts)."""
+    and tiles with more rows than the threads hold (large parts).  PA1
+    needs a symmetric pattern: the reference's skirt distance follows the
+    columns a row reads (mpk2/lib.c:203-219), and only then does every
+    column of a skirt row lie in the tile (mpk2/mpkprep.c:196-222 checks
+    it)."""
     k = 6 if case != "bigparts" else 4
     if case == "diffusion":
         a = M.Csr.diffusion(192, 160, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=3)
@@ -135,8 +139,13 @@ def test_mixed_tiles_bitwise_equal_wavefront(case, vt, gpu):
     elif case == "cube":
         a = M.Csr.laplacian(40, 36, 32, diag=6.0, off=-1.0)
         part, npart = M.partition_rcb(a.coords, 48), 48
-    elif case == "banded":
-        a = M.Csr.banded(3000, 64, 5, 30, seed=4)
+    elif case == "banded":  # symmetric pattern (PA1 needs one): B + B^T of a random banded B
+        import scipy.sparse as sp
+        bb = M.Csr.banded(3000, 64, 5, 30, seed=4)
+        B = sp.csr_matrix((bb.val, bb.col, bb.ptr), shape=(bb.n, bb.n))
+        S = (B + B.T).tocsr()
+        S.sort_indices()
+        a = M.Csr(S.indptr, S.indices, S.data)
         npart = 12
         part = (np.arange(a.n) * npart // a.n).astype(np.int32)
     else:

@@ -304,3 +304,25 @@ def test_host_mapped_execution_matches_device(arith, valued, gpu):
     assert again.tobytes() == want.tobytes()
     assert got_pageable.tobytes() == want.tobytes()
     assert np.array_equal(got_pinned[:a.n], x)  # x is read, not written
+
+
+@pytest.mark.parametrize("arith,valued", [(M.ARITH_DF64, False), (M.ARITH_DF64, True), (M.ARITH_FIXED, False)])
+def test_kspmv_same_arithmetic_as_wavefront(arith, valued, gpu):
+    """The k-SpMV baseline in double-float and fixed point computes the
+    wavefront's rows in the same arithmetic: the same bits, level for
+    level, and within 1e-13 of the FP64 chain (so that the MPK/k-SpMV
+    speed-up compares like with like)."""
+    a = M.Csr.laplacian(48, 40, 36, diag=6.0, off=-1.0)
+    a = a if valued else a.pattern()
+    k = 8
+    x = M.uniform(31, a.n)
+    sp = M.Plan.spmv(a, k, arith=arith)
+    wv = M.Plan.wave(a, k, arith=arith)
+    got, want = _run(sp, x, a.n, k), _run(wv, x, a.n, k)
+    info = sp.info()
+    sp.close()
+    wv.close()
+    assert got.tobytes() == want.tobytes()
+    ref = O.mpk(a.ptr, a.col, a.val, x, k, O.MODE_FMA)
+    assert max(_rel_errors(got, ref, a.n, k)) <= TOL
+    assert info["launches"] == k + (1 if arith == M.ARITH_DF64 else 2)

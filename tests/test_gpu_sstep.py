@@ -134,3 +134,37 @@ def test_sstep_device_loop_equals_host_loop(gram, gpu):
         assert idev["loop_launches"] == 1  # the device-side loop ran
         assert ihost["loop_launches"] == ihost["iterations"]
     assert idev["iterations"] == 3 and not idev["converged"]
+
+
+@pytest.mark.parametrize("loop", [M.SSTEP_DEVICE_LOOP, M.SSTEP_HOST_LOOP])
+def test_sstep_mpk_basis_equals_step_launches(loop, gpu):
+    """The basis built as one matrix powers launch (wavefront form, the
+    default) gives the bits of the basis built by one SpMV launch per step:
+    same solution, iterations and basis condition number."""
+    a = M.Csr.diffusion(40, 40, 24, sigma=1.0, seed=12)
+    b = M.uniform(6, a.n)
+    sh = S.from_lanczos(a, 8)
+    xm, im = M.sstep_cg(a, b, 8, shifts=sh, loop=loop, basis=M.SSTEP_BASIS_MPK)
+    xs, ist = M.sstep_cg(a, b, 8, shifts=sh, loop=loop, basis=M.SSTEP_BASIS_STEPS)
+    assert xm.tobytes() == xs.tobytes()
+    for key in ("iterations", "mpk_steps", "breakdowns", "converged", "relres", "basis_cond"):
+        assert im[key] == ist[key], key
+    assert im["converged"]
+
+
+def test_sstep_mpk_basis_wait_times_out_and_recovers(gpu):
+    """The basis launch's bounded waits give up on levels that are never
+    published (MPKG_ETIMEOUT, context usable); the next solve is right."""
+    a = M.Csr.diffusion(32, 32, 16, sigma=1.0, seed=13)
+    b = M.uniform(2, a.n)
+    _check = M._check
+    _check(M.lib().mpkg_sstep_debug_stall(50))
+    try:
+        with pytest.raises(M.MpkError) as e:
+            M.sstep_cg(a, b, 4, max_outer=2)
+        assert e.value.code == M.ETIMEOUT
+    finally:
+        _check(M.lib().mpkg_sstep_debug_stall(0))
+    x1, i1 = M.sstep_cg(a, b, 4)
+    x2, i2 = M.sstep_cg(a, b, 4, basis=M.SSTEP_BASIS_STEPS)
+    assert i1["converged"] and x1.tobytes() == x2.tobytes()

@@ -184,3 +184,40 @@ def test_gpu_pa1_tasks_fall_back_beyond_capacity(gpu):
     assert not on
     off2, idx2, _ = M.pa1_tasks(a0.pattern(), part, 2, 3, on_gpu=False)
     assert np.array_equal(off, off2) and np.array_equal(idx, idx2)
+
+
+# ---- DMPK phase levels and METIS weights on the GPU ------------------------
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if int(c.split("_")[3].rstrip("m")) > 0])
+def test_gpu_phase_levels_and_weights_equal_reference(name, gpu):
+    """comp_level / update_level and level2wcrs built on the GPU give the
+    reference tools' levels and weight graphs on every multi-phase golden
+    case (RCB, BFS and METIS partitions)."""
+    g = load_golden(name)
+    a = golden_matrix(name)
+    npart = int(g["npart"])
+    prev = None
+    for ph in range(int(g["nphase"])):
+        lev = M.levels(a, g["parts"][ph], npart, prev, on_gpu=True)
+        assert np.array_equal(lev, g["levels"][ph]), f"phase {ph} levels"
+        wv, we = M.level_weights(a, lev, on_gpu=True)
+        wv_h, we_h = M.level_weights(a, lev)
+        assert np.array_equal(we, g["weights"][ph]) and np.array_equal(wv, wv_h)
+        prev = lev
+
+
+@pytest.mark.gpu
+def test_gpu_phase_levels_identical_to_host_large(gpu):
+    """A 96^3 Laplacian in 512 parts, three phases with different
+    partitions: the GPU levels and weights equal the host build's bytes."""
+    a = M.Csr.laplacian(96, 96, 96).pattern()
+    parts = [M.partition_rcb(a.coords, 512), M.partition_bfs(a, 512),
+             M.partition_rcb(a.coords[:, ::-1].copy(), 512)]
+    prev_g = prev_h = None
+    for p in parts:
+        lg = M.levels(a, p, 512, prev_g, on_gpu=True)
+        lh = M.levels(a, p, 512, prev_h)
+        assert np.array_equal(lg, lh)
+        for x, y in zip(M.level_weights(a, lg, on_gpu=True), M.level_weights(a, lh)):
+            assert np.array_equal(x, y)
+        prev_g, prev_h = lg, lh
