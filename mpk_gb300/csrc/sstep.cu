@@ -237,17 +237,16 @@ __global__ void basis_start_kernel(int n, const double *__restrict__ p, const do
 
 // Row i of one Newton step of both blocks: out = (A in - theta in) / sigma,
 // FP32 values and accumulation in CSR order (the R block when rout is not
-// null).  Both basis builders below run this code, so they give the same
-// bits.  The inputs are plain loads: the matrix-powers form reads levels
-// that other CTAs wrote during the same launch.
-__device__ __forceinline__ void newton_row(int i, const Sell &a, const float *pin, float *pout, const float *rin,
-                                           float *rout, float theta, float rsigma) {
+// null); the row's entry t at cb[32 t] / vb[32 t] (the sliced layout, in
+// global or shared memory).  Both basis builders below run this code, so
+// they give the same bits.  The inputs are plain loads: the matrix-powers
+// form reads levels that other CTAs wrote during the same launch.
+__device__ __forceinline__ void newton_row(int i, int l, const int *cb, const float *vb, const float *pin, float *pout,
+                                           const float *rin, float *rout, float theta, float rsigma) {
   float sp = 0.f, sr = 0.f;
-  const long e0 = a.off[i >> 5] + (i & 31);
-  const int l = a.len[i];
   for (int t = 0; t < l; t++) {
-    const int c = a.col[e0 + 32L * t];
-    const float v = a.valf[e0 + 32L * t];
+    const int c = cb[32 * t];
+    const float v = vb[32 * t];
     sp = __fmaf_rn(v, pin[c], sp);
     if (rout) sr = __fmaf_rn(v, rin[c], sr);
   }
@@ -259,24 +258,29 @@ __device__ __forceinline__ void newton_row(int i, const Sell &a, const float *pi
 // R block stops one step early.
 __global__ void basis_step_kernel(int n, Sell a, const float *pin, float *pout, const float *rin, float *rout,
                                   float theta, float rsigma) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    newton_row(i, a, pin, pout, rin, rout, theta, rsigma);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const long e0 = a.off[i >> 5] + (i & 31);
+    newton_row(i, a.len[i], a.col + e0, a.valf + e0, pin, pout, rin, rout, theta, rsigma);
+  }
 }
 
 // The whole basis [p, rho_1(A) p, ..., rho_s(A) p, r, ..., rho_(s-1)(A) r]
 // as ONE matrix powers launch (the wavefront form): CTA b owns rows
 // [row_lo[b], row_lo[b+1]) (slice aligned, so no cache line holds two
 // CTAs' rows) at every level, and computes level j once the CTAs owning
-// the columns of its rows (a contiguous range) have published level j - 1.
-// The levels are the basis vectors themselves, each a fresh buffer, so no
-// CTA overwrites what another still reads.  Waits are bounded: a wait that
-// gives up sets *err and the launch ends (the host reports MPKG_ETIMEOUT).
-// flags are reset to 0 before every launch.
+// the columns of its rows (an exact list) have published level j - 1.
+// STAGE: the CTA's slab of the sliced matrix (columns and FP32 values) is
+// copied into shared memory once and serves all s levels, so the matrix is
+// read once per basis instead of once per step.  The levels are the basis
+// vectors themselves, each a fresh buffer, so no CTA overwrites what
+// another still reads.  Waits are bounded: a wait that gives up sets *err
+// and the launch ends (the host reports MPKG_ETIMEOUT).  flags are reset
+// to 0 before every launch.
 struct BasisWave {
   int n, s, nblk;
   const int *row_lo;     // nblk + 1
-  const int *dep_lo;     // nblk: first CTA owning a column of CTA b's rows
-  const int *dep_hi;     // nblk: last such CTA
+  const int *dep_ptr;    // nblk + 1: CTA b waits for dep_idx[dep_ptr[b] .. dep_ptr[b+1])
+  const int *dep_idx;
   unsigned int *flags;   // nblk: last level published
   int *err;
   unsigned int stall;    // test hook: extra levels to wait for (never published)
@@ -291,15 +295,31 @@ __device__ __forceinline__ unsigned int acquire_u32(const unsigned int *p) {
   return v;
 }
 
+template <bool STAGE>
 __global__ void __launch_bounds__(kThreads) basis_wave_kernel(BasisWave w, Sell a, float *Y) {
+  extern __shared__ __align__(16) int bw_slab[];
   __shared__ int s_abort;
   if (threadIdx.x == 0) s_abort = 0;
-  __syncthreads();
   const int b = blockIdx.x, r0 = w.row_lo[b], r1 = w.row_lo[b + 1];
   const size_t n = (size_t)w.n;
+  const long e_lo = r0 < r1 ? a.off[r0 >> 5] : 0;
+  int *s_col = bw_slab;
+  float *s_val = nullptr;
+  if (STAGE && r0 < r1) {
+    const long ne = a.off[(r1 + 31) >> 5] - e_lo;  // a multiple of 32 entries
+    s_val = reinterpret_cast<float *>(bw_slab + ne);
+    const int4 *gc = reinterpret_cast<const int4 *>(a.col + e_lo);
+    const float4 *gv = reinterpret_cast<const float4 *>(a.valf + e_lo);
+    for (long q = threadIdx.x; q < ne / 4; q += blockDim.x) {
+      reinterpret_cast<int4 *>(s_col)[q] = gc[q];
+      reinterpret_cast<float4 *>(s_val)[q] = gv[q];
+    }
+  }
+  __syncthreads();
   for (int j = 1; j <= w.s; j++) {
     if (j > 1) {
-      for (int c = w.dep_lo[b] + (int)threadIdx.x; c <= w.dep_hi[b]; c += blockDim.x) {
+      for (int k = w.dep_ptr[b] + (int)threadIdx.x; k < w.dep_ptr[b + 1]; k += blockDim.x) {
+        const int c = w.dep_idx[k];
         long spins = 0;
         while (acquire_u32(w.flags + c) < (unsigned)(j - 1) + w.stall) {
           if (++spins > kBasisSpin || *((volatile int *)w.err)) {
@@ -318,8 +338,14 @@ __global__ void __launch_bounds__(kThreads) basis_wave_kernel(BasisWave w, Sell 
     float *pout = Y + (size_t)j * n;
     const float *rin = rstep ? Y + (size_t)(w.s + j) * n : nullptr;
     float *rout = rstep ? Y + (size_t)(w.s + 1 + j) * n : nullptr;
-    for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x)
-      newton_row(i, a, pin, pout, rin, rout, w.theta[j - 1], w.rsig[j - 1]);
+    for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) {
+      const long e0 = a.off[i >> 5] + (i & 31);
+      if (STAGE)
+        newton_row(i, a.len[i], s_col + (e0 - e_lo), s_val + (e0 - e_lo), pin, pout, rin, rout, w.theta[j - 1],
+                   w.rsig[j - 1]);
+      else
+        newton_row(i, a.len[i], a.col + e0, a.valf + e0, pin, pout, rin, rout, w.theta[j - 1], w.rsig[j - 1]);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
@@ -597,6 +623,7 @@ struct DevCsr {
   int *slen = nullptr, *scol = nullptr;
   double *sval = nullptr;
   float *svalf = nullptr;
+  std::vector<long> soff_h;  // host copy of the slice offsets
   ~DevCsr() {
     cudaFree(ptr); cudaFree(col); cudaFree(val);
     cudaFree(soff); cudaFree(slen); cudaFree(scol); cudaFree(sval); cudaFree(svalf);
@@ -628,6 +655,7 @@ struct DevCsr {
     SS_TRY(cudaMalloc(&sval, sizeof(double) * ne));
     if (f32) SS_TRY(cudaMalloc(&svalf, sizeof(float) * ne));
     SS_TRY(cudaMemcpy(soff, so.data(), sizeof(long) * (nsl + 1), cudaMemcpyHostToDevice));
+    soff_h = so;
     sell_fill_kernel<<<blocks_for(n), kThreads>>>(n, ptr, col, val, soff, slen, scol, sval, svalf);
     SS_TRY(cudaGetLastError());
     return kOk;
@@ -723,43 +751,84 @@ bool build_device_loop(GraphRun &gr, F &&body) {
 }
 
 // The basis wavefront's layout: slice-aligned CTA row ranges of equal size
-// and, per CTA, the contiguous range of CTAs owning the columns of its rows.
+// and, per CTA, the exact list of CTAs owning the columns of its rows;
+// the grid and whether the CTAs' matrix slabs fit shared memory.
 struct BasisLayout {
-  DevBuf<int> row_lo, dep_lo, dep_hi, err;
+  DevBuf<int> row_lo, dep_ptr, dep_idx, err;
   DevBuf<unsigned int> flags;
   BasisWave w{};
-  bool coop = false;  // cooperative launch attribute accepted in stream capture
-  int build(int n, const int *ptr, const int *col, int s, const std::vector<double> &th,
-            const std::vector<double> &sg) {
-    int dev = 0, nsm = 0, per_sm = 0;
+  bool coop = false;   // cooperative launch attribute accepted in stream capture
+  bool stage = false;  // slabs staged in shared memory
+  size_t smem = 0;
+  int build(int n, const int *ptr, const int *col, const std::vector<long> &soff, int s,
+            const std::vector<double> &th, const std::vector<double> &sg) {
+    int dev = 0, nsm = 0, maxsm = 0;
     SS_TRY(cudaGetDevice(&dev));
     SS_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    SS_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_wave_kernel, kThreads, 0));
+    SS_TRY(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     const int nsl = (n + 31) / 32;
-    const int nblk = std::max(1, std::min(per_sm * nsm, nsl));
-    std::vector<int> lo(nblk + 1), dl(nblk), dh(nblk);
-    for (int b = 0; b <= nblk; b++) lo[b] = std::min<long>(n, 32L * ((long)b * nsl / nblk));
-    auto owner = [&](int row) { return (int)(std::upper_bound(lo.begin(), lo.end(), row) - lo.begin()) - 1; };
+    auto split = [&](int nblk, std::vector<int> *lo) {
+      lo->resize(nblk + 1);
+      for (int b = 0; b <= nblk; b++) (*lo)[b] = (int)std::min<long>(n, 32L * ((long)b * nsl / nblk));
+    };
+    // the most CTAs per SM whose slabs fit shared memory (8 .. 1), else
+    // the plain occupancy without staging
+    std::vector<int> lo;
+    int nblk = 0;
+    for (int c = 8; c >= 1 && !stage; c--) {
+      const int nb = std::max(1, std::min(c * nsm, nsl));
+      split(nb, &lo);
+      long maxe = 0;
+      for (int b = 0; b < nb; b++)
+        if (lo[b] < lo[b + 1]) maxe = std::max(maxe, soff[(lo[b + 1] + 31) / 32] - soff[lo[b] / 32]);
+      const size_t bytes = (size_t)maxe * (sizeof(int) + sizeof(float));
+      if (bytes > (size_t)maxsm) continue;
+      int per_sm = 0;
+      if (cudaFuncSetAttribute(basis_wave_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+              cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_wave_kernel<true>, kThreads, bytes) !=
+              cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      if ((long)per_sm * nsm < nb) continue;
+      stage = true;
+      smem = bytes;
+      nblk = nb;
+    }
+    if (!stage) {
+      int per_sm = 0;
+      SS_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_wave_kernel<false>, kThreads, 0));
+      nblk = std::max(1, std::min(per_sm * nsm, nsl));
+      split(nblk, &lo);
+    }
+    // exact dependency lists: the owners of every column of the CTA's rows
+    std::vector<int> owner_of(n), dp(nblk + 1, 0), di;
+    for (int b = 0; b < nblk; b++)
+      for (int i = lo[b]; i < lo[b + 1]; i++) owner_of[i] = b;
+    std::vector<int> mark(nblk, -1);
     for (int b = 0; b < nblk; b++) {
-      int cmin = lo[b], cmax = std::max(lo[b], lo[b + 1] - 1);
       for (int i = lo[b]; i < lo[b + 1]; i++)
         for (int j = ptr[i]; j < ptr[i + 1]; j++) {
-          cmin = std::min(cmin, col[j]);
-          cmax = std::max(cmax, col[j]);
+          const int o = owner_of[col[j]];
+          if (o != b && mark[o] != b) {
+            mark[o] = b;
+            di.push_back(o);
+          }
         }
-      dl[b] = std::min(b, owner(cmin));
-      dh[b] = std::max(b, std::min(nblk - 1, owner(cmax)));
+      std::sort(di.begin() + dp[b], di.end());
+      dp[b + 1] = (int)di.size();
     }
     int rc;
-    if ((rc = row_lo.alloc(nblk + 1)) || (rc = dep_lo.alloc(nblk)) || (rc = dep_hi.alloc(nblk)) ||
+    if ((rc = row_lo.alloc(nblk + 1)) || (rc = dep_ptr.alloc(nblk + 1)) || (rc = dep_idx.alloc(di.size())) ||
         (rc = flags.alloc(nblk)) || (rc = err.alloc(1)))
       return rc;
     SS_TRY(cudaMemcpy(row_lo.p, lo.data(), sizeof(int) * (nblk + 1), cudaMemcpyHostToDevice));
-    SS_TRY(cudaMemcpy(dep_lo.p, dl.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice));
-    SS_TRY(cudaMemcpy(dep_hi.p, dh.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice));
+    SS_TRY(cudaMemcpy(dep_ptr.p, dp.data(), sizeof(int) * (nblk + 1), cudaMemcpyHostToDevice));
+    if (!di.empty()) SS_TRY(cudaMemcpy(dep_idx.p, di.data(), sizeof(int) * di.size(), cudaMemcpyHostToDevice));
     SS_TRY(cudaMemset(err.p, 0, sizeof(int)));
     w.n = n; w.s = s; w.nblk = nblk; w.stall = g_basis_stall;
-    w.row_lo = row_lo.p; w.dep_lo = dep_lo.p; w.dep_hi = dep_hi.p; w.flags = flags.p; w.err = err.p;
+    w.row_lo = row_lo.p; w.dep_ptr = dep_ptr.p; w.dep_idx = dep_idx.p; w.flags = flags.p; w.err = err.p;
     for (int j = 0; j < s; j++) {
       w.theta[j] = (float)th[j];
       w.rsig[j] = (float)(1.0 / sg[j]);
@@ -772,13 +841,15 @@ struct BasisLayout {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)w.nblk);
     cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = stage ? smem : 0;
     cfg.stream = cs;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeCooperative;
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = coop ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, basis_wave_kernel, w, a, Y);
+    return stage ? cudaLaunchKernelEx(&cfg, basis_wave_kernel<true>, w, a, Y)
+                 : cudaLaunchKernelEx(&cfg, basis_wave_kernel<false>, w, a, Y);
   }
   // Whether a cooperative launch can be captured into a graph here; if not,
   // the grid (sized by the occupancy calculator, every CTA resident on an
@@ -1102,7 +1173,7 @@ int mpkg_sstep_cg(int n, const int *ptr, const int *col, const double *val, cons
   const bool basis_mpk = g_basis_mpk;
   BasisLayout bl;
   if (basis_mpk) {
-    if ((rc = bl.build(n, ptr, col, s, th, sg))) return rc;
+    if ((rc = bl.build(n, ptr, col, a.soff_h, s, th, sg))) return rc;
     bl.probe(a.sell(), y.p);
   }
   // one outer iteration: basis, Gram, coefficient steps, update, true
