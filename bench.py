@@ -357,20 +357,36 @@ def bench_mixed(M, torch, a, x, k, exact, args, flush, stream):
         del d64
     best64 = min(fp64, key=fp64.get)
     t64 = fp64[best64]
-    res = {"n": b.n, "nnz": b.nnz, "fp64_ms": fp64, "fp64_best": best64,
-           "algorithmic_bytes_f32": b.nnz * 8 + 4 * (b.n + 1) + 4 * b.n * (k + 1)}
+    peak, _ = peaks()
+    B32 = b.nnz * 8 + 4 * (b.n + 1) + 4 * b.n * (k + 1)
+    res = {"n": b.n, "nnz": b.nnz, "fp64_ms": fp64, "fp64_best": best64, "algorithmic_bytes_f32": B32,
+           "schedules": "wave: the wavefront (every level streams the matrix); tiles: PA1 tiles of 4096 RCB parts "
+                        "(32x32 boxes) + 8-deep skirts, each tile's rows held on chip for all levels"}
+    i = np.arange(b.n)
+    coords = np.stack([i % 2048, i // 2048, np.zeros_like(i)], axis=1).astype(np.int32)
+    tparts = M.partition_rcb(coords, 4096)
+    bits = {}
     for name, vt in (("f32", M.VALUE_F32), ("bf16", M.VALUE_BF16)):
-        p32 = M.Plan.mixed(b, k, vt)
-        e, inexact = p32.mixed_scale()
-        d32 = torch.zeros((k + 1) * b.n, dtype=torch.float32, device="cuda")
-        d32[:b.n] = torch.from_numpy(xb.astype(np.float32)).cuda()
-        t32 = statistics.mean(time_mixed(p32, d32, min(args.steps, 100), args.warmup, flush, stream))
-        errs = mixed_errors(d32.cpu().numpy(), e, ex64, b.n, k)
-        res[name] = {"ms_per_step": t32, "speedup_vs_best_fp64": t64 / t32, "rel_err_per_power": errs,
-                     "values_rounded": inexact, "value": k * b.n / (t32 * 1e-3) / 1e9,
-                     "executor": p32.info()["exec"]}
-        p32.close()
-        del d32
+        for sched in ("wave", "tiles"):
+            p32 = M.Plan.mixed(b, k, vt) if sched == "wave" else M.Plan.mixed_tiles(b, tparts, 4096, k, vt)
+            e, inexact = p32.mixed_scale()
+            d32 = torch.zeros((k + 1) * b.n, dtype=torch.float32, device="cuda")
+            d32[:b.n] = torch.from_numpy(xb.astype(np.float32)).cuda()
+            t32 = statistics.mean(time_mixed(p32, d32, min(args.steps, 100), args.warmup, flush, stream))
+            got = d32.cpu().numpy()
+            errs = mixed_errors(got, e, ex64, b.n, k)
+            bits[(name, sched)] = got.view(np.uint32)
+            info = p32.info()
+            res[f"{name}_{sched}"] = {
+                "ms_per_step": t32, "speedup_vs_best_fp64": t64 / t32, "rel_err_per_power": errs,
+                "values_rounded": inexact, "value": k * b.n / (t32 * 1e-3) / 1e9,
+                "rows_computed_per_output_row": info["rows_computed"] / (b.n * k),
+                "achieved_gbs": B32 / (t32 * 1e-3) / 1e9, "frac_hbm": B32 / (t32 * 1e-3) / 1e9 / peak,
+                "kernel": (("tiles_reg_kernel" if info["tile_regs"] else "tiles_mix_kernel") if sched == "tiles"
+                           else "wave_mix_kernel")}
+            p32.close()
+            del d32
+        res[f"{name}_tiles"]["bit_equal_wave"] = bool(np.array_equal(bits[(name, "wave")], bits[(name, "tiles")]))
     out["diffusion2048_9pt"] = res
     return out
 

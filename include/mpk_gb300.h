@@ -102,6 +102,8 @@ typedef struct {
   int pipe_chunk;       /* PIPE: rows per chunk */
   int pipe_reach;       /* PIPE: dependency reach in chunks */
   int pipe_grid;        /* PIPE: resident CTAs launched */
+  int tile_regs;        /* MIXED on tiles: 1 when every tile's rows are held in
+                           registers (register-resident tile kernel) */
 } mpkg_plan_info_t;
 
 /* Plan over task lists in the reference layout: list t = phase*npart+part

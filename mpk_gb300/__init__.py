@@ -75,7 +75,8 @@ class PlanInfo(C.Structure):
                 ("exec", C.c_int), ("arith", C.c_int), ("valued", C.c_int),
                 ("nnz", C.c_long), ("rows_computed", C.c_long), ("device_bytes", C.c_long),
                 ("launches", C.c_int), ("tiles_in_smem", C.c_int), ("max_tile_slots", C.c_int),
-                ("pipe_chunk", C.c_int), ("pipe_reach", C.c_int), ("pipe_grid", C.c_int)]
+                ("pipe_chunk", C.c_int), ("pipe_reach", C.c_int), ("pipe_grid", C.c_int),
+                ("tile_regs", C.c_int)]
 
 
 def _declare(L):

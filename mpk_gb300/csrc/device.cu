@@ -1384,7 +1384,7 @@ __device__ __forceinline__ float tm_row_global(const TileMixArgs &a, const VT *v
 template <typename VT, int W>
 __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a) {
   extern __shared__ __align__(16) float tm_buf[];
-  __shared__ int s_q;
+  __shared__ int s_q, s_nrows[32];
   float *buf0 = tm_buf, *buf1 = tm_buf + a.max_slots;
   const VT *val = static_cast<const VT *>(a.val);
   const int tid = threadIdx.x;
@@ -1408,11 +1408,13 @@ __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a)
     // this thread's rows: columns (two per word) and values in registers
     uint32_t cw[kTmRows][(W + 1) / 2];
     float v[kTmRows][W];
-    int len[kTmRows];
+    int len[kTmRows], vert[kTmRows];
+    const int owned = shell[0];
 #pragma unroll
     for (int j = 0; j < kTmRows; j++) {
       len[j] = -1;
       const int r = tid + j * kTmThreads;
+      vert[j] = r < owned ? a.slot_vert[s0 + r] : 0;  // the part's own rows are written at every level
 #pragma unroll
       for (int t = 0; t < (W + 1) / 2; t++) cw[j][t] = 0;
 #pragma unroll
@@ -1437,12 +1439,12 @@ __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a)
         }
       }
     }
+    if (tid >= 1 && tid <= a.nlevel) s_nrows[tid] = shell[a.nlevel - tid];  // rows of each level
     __syncthreads();
-    const int owned = shell[0];
     for (int l = 1; l <= a.nlevel; l++) {
       const float *in = (l & 1) ? buf0 : buf1;
       float *out = (l & 1) ? buf1 : buf0;
-      const int nrows = shell[a.nlevel - l];
+      const int nrows = s_nrows[l];
       float *dst = a.vf + (size_t)l * a.n;
 #pragma unroll
       for (int j = 0; j < kTmRows; j++) {
@@ -1458,7 +1460,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a)
           }
           s *= a.scale;
           out[r] = s;
-          if (r < owned) __stcs(dst + a.slot_vert[s0 + r], s);
+          if (r < owned) __stcs(dst + vert[j], s);
         }
       }
       for (int r = tid + kTmRows * kTmThreads; r < nrows; r += kTmThreads) {
@@ -1471,6 +1473,212 @@ __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a)
     }
   }
 }
+
+// ------------------------------------------------------------------------
+// Register-resident PA1 tiles (the mixed form's temporal blocking for
+// tiles of at most kTrThreads * kTrRows computed rows): the plan writes
+// each tile as two contiguous, 16-byte aligned images in execution order,
+//   vert image:   header (ns, nrow1, owned, nslice, shells c_0..c_nlevel)
+//                 + the slots' vertices,
+//   matrix image: [slice][t][lane] byte offsets of the local columns
+//                 (uint16, slot * 4) then [slice][t][lane] values, every
+//                 row padded to W entries with value -0 and the zero slot,
+// so a tile is two bulk copies.  Thread t holds rows t, t + T, t + 2T of
+// every level in registers (value and byte offset per entry), so an entry
+// costs one shared-memory gather and one FMA.  While a tile computes its
+// levels, the next tile's images stream in (TMA bulk copies on two
+// mbarriers) and, once its vertices have landed, its level-0 x is gathered
+// into the third level buffer (cp.async).  Padding entries add
+// fma(-0, +0, s) = s exactly, so the row sums are the FP32 FMA chains in
+// CSR order of the wavefront and pipeline mixed forms, bit for bit.
+// ------------------------------------------------------------------------
+constexpr int kTrThreads = 768;
+constexpr int kTrRows = 3;
+constexpr int kTrHdrInts = 32;  // header of a vert image: 4 counts + c_0..c_nlevel
+
+struct TileRegArgs {
+  int n, nlevel, ntile, zs;      // zs: the zero slot (index of a +0 in every level buffer)
+  const unsigned char *vimg;     // vert images
+  const unsigned char *mimg;     // matrix images
+  const long *voff, *moff;       // per tile (execution order): byte offsets
+  const int *vbytes, *mbytes;    // per tile: image sizes (multiples of 16)
+  int max_vbytes, max_mbytes, buf_floats;
+  const float *x;
+  float *vf;
+  float scale;
+  int *err;
+};
+
+__device__ __forceinline__ bool tr_wait(unsigned long long *bar, unsigned phase, int *err) {
+  long spins = 0;
+  while (!mbar_try(bar, phase)) {
+    if (++spins > kSpinLimit) {  // a copy of this CTA never completed: report, drain with a second bound
+      if (threadIdx.x == 0) atomicCAS(err, 0, kErrTimeout);
+      for (long s2 = 0; s2 < kSpinLimit && !mbar_try(bar, phase); s2++) __nanosleep(256);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// One entry's operands in registers: FP32 values beside packed byte
+// offsets; BF16 values packed with their offset in one word (value bits
+// in the high half are the FP32 value itself).
+template <typename VT, int W>
+struct TrRow;
+template <int W>
+struct TrRow<float, W> {
+  float v[W];
+  uint32_t c[(W + 1) / 2];
+  __device__ __forceinline__ void load(const uint16_t *cols, const float *vals) {
+#pragma unroll
+    for (int t = 0; t < W; t++) v[t] = vals[32 * t];
+#pragma unroll
+    for (int t = 0; t < W; t += 2) {
+      const uint32_t lo = cols[32 * t];
+      const uint32_t hi = t + 1 < W ? (uint32_t)cols[32 * (t + 1)] : 0u;
+      c[t / 2] = lo | (hi << 16);
+    }
+  }
+  __device__ __forceinline__ float sum(const unsigned char *in) const {
+    float s = 0.f;
+#pragma unroll
+    for (int t = 0; t < W; t++) {
+      const uint32_t off = (t & 1) ? (c[t / 2] >> 16) : (c[t / 2] & 0xFFFFu);
+      s = __fmaf_rn(v[t], *reinterpret_cast<const float *>(in + off), s);
+    }
+    return s;
+  }
+};
+template <int W>
+struct TrRow<__nv_bfloat16, W> {
+  uint32_t w[W];
+  __device__ __forceinline__ void load(const uint16_t *cols, const __nv_bfloat16 *vals) {
+    const uint16_t *vb = reinterpret_cast<const uint16_t *>(vals);
+#pragma unroll
+    for (int t = 0; t < W; t++) w[t] = ((uint32_t)vb[32 * t] << 16) | (uint32_t)cols[32 * t];
+  }
+  __device__ __forceinline__ float sum(const unsigned char *in) const {
+    float s = 0.f;
+#pragma unroll
+    for (int t = 0; t < W; t++)
+      s = __fmaf_rn(__uint_as_float(w[t] & 0xFFFF0000u), *reinterpret_cast<const float *>(in + (w[t] & 0xFFFFu)),
+                    s);
+    return s;
+  }
+};
+
+template <typename VT, int W>
+__global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a) {
+  extern __shared__ __align__(128) unsigned char tr_smem[];
+  __shared__ __align__(8) unsigned long long bar_v, bar_m;
+  __shared__ int s_nrows[33];
+  unsigned char *mbuf = tr_smem;                                  // matrix image
+  int *vbuf = reinterpret_cast<int *>(tr_smem + a.max_mbytes);    // vert image
+  float *xb = reinterpret_cast<float *>(tr_smem + a.max_mbytes + a.max_vbytes);
+  const int tid = threadIdx.x, G = gridDim.x;
+  int q = blockIdx.x;
+  if (q >= a.ntile) return;
+  for (int b = 0; b < 3; b++)
+    if (tid == 0) xb[b * a.buf_floats + a.zs] = 0.f;
+  long nvo = 0, nmo = 0;  // thread 0: offsets and sizes of this CTA's next tile, loaded a tile ahead
+  int nvb = 0, nmb = 0;
+  if (tid == 0) {
+    mbar_init(&bar_v);
+    mbar_init(&bar_m);
+    mbar_expect(&bar_v, (unsigned)a.vbytes[q]);
+    bulk_g2s(vbuf, a.vimg + a.voff[q], (unsigned)a.vbytes[q], &bar_v);
+    mbar_expect(&bar_m, (unsigned)a.mbytes[q]);
+    bulk_g2s(mbuf, a.mimg + a.moff[q], (unsigned)a.mbytes[q], &bar_m);
+    if (q + G < a.ntile) {
+      nvo = a.voff[q + G]; nmo = a.moff[q + G]; nvb = a.vbytes[q + G]; nmb = a.mbytes[q + G];
+    }
+  }
+  __syncthreads();
+  unsigned phase = 0;
+  int cur = 0, alt = 1, nxt = 2;
+  // the first tile's level 0
+  if (!tr_wait(&bar_v, phase, a.err)) return;
+  {
+    const int ns = vbuf[0];
+    for (int s = tid; s < ns; s += kTrThreads) cp_async4(xb + s, a.x + vbuf[kTrHdrInts + s]);
+  }
+  const int lane = tid & 31, warp = tid >> 5;
+  constexpr int kWarps = kTrThreads / 32;
+  for (;;) {
+    // this tile: header, vertices and matrix image in shared memory
+    if (!tr_wait(&bar_m, phase, a.err)) return;
+    phase ^= 1u;
+    const int nrow1 = vbuf[1], owned = vbuf[2], nslice = vbuf[3];
+    if (tid >= 1 && tid <= a.nlevel) s_nrows[tid] = vbuf[4 + a.nlevel - tid];
+    TrRow<VT, W> row[kTrRows];
+    int vert[kTrRows];
+    const uint16_t *cols = reinterpret_cast<const uint16_t *>(mbuf);
+    const VT *vals = reinterpret_cast<const VT *>(mbuf + (size_t)nslice * W * 64);
+#pragma unroll
+    for (int j = 0; j < kTrRows; j++) {
+      const int r = tid + j * kTrThreads;
+      vert[j] = r < owned ? vbuf[kTrHdrInts + r] : 0;
+      const long e = ((long)(warp + j * kWarps) * W) * 32 + lane;  // slice r / 32, entry 0
+      if (r < nrow1) row[j].load(cols + e, vals + e);
+    }
+    cp_async_wait_all();  // this tile's level 0 (gathered during the previous tile)
+    __syncthreads();      // both images fully read: the buffers take the next tile
+    const int qn = q + G;
+    const bool has_next = qn < a.ntile;
+    if (tid == 0 && has_next) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect(&bar_v, (unsigned)nvb);
+      bulk_g2s(vbuf, a.vimg + nvo, (unsigned)nvb, &bar_v);
+      mbar_expect(&bar_m, (unsigned)nmb);
+      bulk_g2s(mbuf, a.mimg + nmo, (unsigned)nmb, &bar_m);
+      if (qn + G < a.ntile) {
+        nvo = a.voff[qn + G]; nmo = a.moff[qn + G]; nvb = a.vbytes[qn + G]; nmb = a.mbytes[qn + G];
+      }
+    }
+    const int lg = (a.nlevel + 1) / 2;  // level after which the next tile's x is gathered
+    for (int l = 1; l <= a.nlevel; l++) {
+      const unsigned char *in = reinterpret_cast<const unsigned char *>(xb + ((l & 1) ? cur : alt) * a.buf_floats);
+      float *out = xb + ((l & 1) ? alt : cur) * a.buf_floats;
+      const int nr = s_nrows[l];
+      float *dst = a.vf + (size_t)l * a.n;
+#pragma unroll
+      for (int j = 0; j < kTrRows; j++) {
+        const int r = tid + j * kTrThreads;
+        if (r < nr) {
+          const float s = row[j].sum(in) * a.scale;
+          out[r] = s;
+          if (r < owned) __stcs(dst + vert[j], s);
+        }
+      }
+      if (l == lg && has_next) {
+        if (!tr_wait(&bar_v, phase, a.err)) return;
+        const int ns = vbuf[0];
+        float *xn = xb + nxt * a.buf_floats;
+        for (int s = tid; s < ns; s += kTrThreads) cp_async4(xn + s, a.x + vbuf[kTrHdrInts + s]);
+      }
+      __syncthreads();
+    }
+    if (!has_next) break;
+    const int c0 = cur;
+    cur = nxt; nxt = alt; alt = c0;
+    q = qn;
+  }
+}
+
+using TrKernel = void (*)(TileRegArgs);
+inline TrKernel tr_kernel_ptr(int value_type, int w) {
+  if (value_type == MPKG_VALUE_F32)
+    return w == 5 ? tiles_reg_kernel<float, 5> : w == 9 ? tiles_reg_kernel<float, 9> : tiles_reg_kernel<float, 12>;
+  return w == 5 ? tiles_reg_kernel<__nv_bfloat16, 5>
+                : w == 9 ? tiles_reg_kernel<__nv_bfloat16, 9> : tiles_reg_kernel<__nv_bfloat16, 12>;
+}
+inline int tr_width(int wmax) { return wmax <= 5 ? 5 : wmax <= 9 ? 9 : wmax <= 12 ? 12 : 0; }
 
 using TmKernel = void (*)(TileMixArgs);
 inline TmKernel tm_kernel_ptr(int value_type, int w) {
@@ -1776,6 +1984,10 @@ struct mpkg_plan {
   bool tm_on = false;
   int tm_w = 0, tm_grid = 0;
   size_t tm_smem = 0;
+  TileRegArgs tr{};  // register-resident tiles (replaces tm when every tile fits)
+  bool tr_on = false;
+  int tr_w = 0, tr_grid = 0;
+  size_t tr_smem = 0;
   mpkg_plan *inner = nullptr;  // mixed form: the wavefront layout it runs on
   void *mix_sval = nullptr;    // mixed form: sliced FP32 / BF16 values
   // pdmpk buffers (b_vall, b_in_*, b_out_*, b_cm_* shared with the above)
@@ -3462,6 +3674,107 @@ int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, in
   return kOk;
 }
 
+namespace {
+// The register-resident tile kernel's two images per tile (layout above
+// tiles_reg_kernel), in execution order.  Plans whose tiles do not fit
+// (rows wider than 12 entries, more than kTrThreads * kTrRows computed rows,
+// more than 16383 slots, nlevel > 27, images beyond shared memory) keep
+// tiles_mix_kernel; nothing is built for them.
+int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void *hval, int wmax) {
+  const int k = p->nlevel, W = tr_width(wmax);
+  const int npart = p->npart;
+  const size_t vsz = p->mix_vt == MPKG_VALUE_F32 ? sizeof(float) : sizeof(__nv_bfloat16);
+  if (W == 0 || k > kTrHdrInts - 5 || tp.max_slots > 16383) return kOk;
+  const int zs = tp.max_slots;
+  std::vector<long> voff(npart + 1, 0), moff(npart + 1, 0);
+  std::vector<int> vbytes(npart), mbytes(npart);
+  for (int q = 0; q < npart; q++) {
+    const int pt = tp.order[q];
+    const int ns = (int)(tp.slot_off[pt + 1] - tp.slot_off[pt]);
+    const int nrow1 = tp.shell[(long)pt * (k + 1) + k - 1];
+    if (nrow1 > kTrThreads * kTrRows) return kOk;
+    const int nslice = (nrow1 + 31) / 32;
+    if (tp.slice_off[pt + 1] - tp.slice_off[pt] != nslice) return fail(kEStruct, "tile slices disagree with shells");
+    vbytes[q] = 4 * (kTrHdrInts + (ns + 3) / 4 * 4);
+    mbytes[q] = std::max<int>(16, (int)((size_t)nslice * W * 32 * (2 + vsz)));
+    voff[q + 1] = voff[q] + vbytes[q];
+    moff[q + 1] = moff[q] + mbytes[q];
+  }
+  const int max_v = *std::max_element(vbytes.begin(), vbytes.end());
+  const int max_m = *std::max_element(mbytes.begin(), mbytes.end());
+  const int buf_floats = (zs + 1 + 3) / 4 * 4;
+  const size_t smem = (size_t)max_m + max_v + 3 * (size_t)buf_floats * sizeof(float);
+  int maxsm = 0, nsm = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
+  if (smem > (size_t)maxsm) return kOk;
+  std::vector<unsigned char> vimg(voff[npart]), mimg(moff[npart]);
+  const uint16_t zoff = (uint16_t)(zs * 4);
+  const uint16_t neg0_bf16 = 0x8000;
+  for (int q = 0; q < npart; q++) {
+    const int pt = tp.order[q];
+    const long s0 = tp.slot_off[pt];
+    const int ns = (int)(tp.slot_off[pt + 1] - s0);
+    const int *sh = &tp.shell[(long)pt * (k + 1)];
+    const int nrow1 = sh[k - 1], nslice = (nrow1 + 31) / 32;
+    int *hv = reinterpret_cast<int *>(vimg.data() + voff[q]);
+    hv[0] = ns; hv[1] = nrow1; hv[2] = sh[0]; hv[3] = nslice;
+    for (int d = 0; d <= k; d++) hv[4 + d] = sh[d];
+    for (int s = 0; s < ns; s++) hv[kTrHdrInts + s] = tp.slot_vert[s0 + s];
+    uint16_t *mc = reinterpret_cast<uint16_t *>(mimg.data() + moff[q]);
+    unsigned char *mv = mimg.data() + moff[q] + (size_t)nslice * W * 64;
+    for (int sl = 0; sl < nslice; sl++) {
+      const long gs = tp.slice_off[pt] + sl;
+      const int w = tp.ell_width[gs];
+      for (int t = 0; t < W; t++)
+        for (int lane = 0; lane < 32; lane++) {
+          const int r = sl * 32 + lane;
+          const size_t e = ((size_t)sl * W + t) * 32 + lane;
+          const int c = (r < nrow1 && t < w) ? tp.ell_col[tp.ell_off[gs] + (long)t * 32 + lane] : 0xFFFF;
+          if (c != 0xFFFF && c >= ns) return fail(kEStruct, "tile column outside the halo");
+          mc[e] = c != 0xFFFF ? (uint16_t)(c * 4) : zoff;
+          const long j = c != 0xFFFF ? (long)ptr[tp.slot_vert[s0 + r]] + t : -1;
+          if (vsz == sizeof(float)) {
+            const float x = j >= 0 ? static_cast<const float *>(hval)[j] : -0.0f;
+            std::memcpy(mv + e * 4, &x, 4);
+          } else {
+            uint16_t b = neg0_bf16;
+            if (j >= 0) std::memcpy(&b, static_cast<const __nv_bfloat16 *>(hval) + j, 2);
+            std::memcpy(mv + e * 2, &b, 2);
+          }
+        }
+    }
+  }
+  unsigned char *dvimg = nullptr, *dmimg = nullptr;
+  long *dvoff = nullptr, *dmoff = nullptr;
+  int *dvb = nullptr, *dmb = nullptr;
+  int rc = dev_copy(p, &dvimg, vimg.data(), vimg.size());
+  if (!rc) rc = dev_copy(p, &dmimg, mimg.data(), mimg.size());
+  if (!rc) rc = dev_copy(p, &dvoff, voff.data(), (size_t)npart);
+  if (!rc) rc = dev_copy(p, &dmoff, moff.data(), (size_t)npart);
+  if (!rc) rc = dev_copy(p, &dvb, vbytes.data(), vbytes.size());
+  if (!rc) rc = dev_copy(p, &dmb, mbytes.data(), mbytes.size());
+  if (rc) return rc;
+  const void *fn = reinterpret_cast<const void *>(tr_kernel_ptr(p->mix_vt, W));
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTrThreads, smem) != cudaSuccess)
+    return fail(kECuda, "register tile kernel attribute set-up failed");
+  if (per_sm < 1) return kOk;
+  TileRegArgs &a = p->tr;
+  a.n = p->n; a.nlevel = k; a.ntile = npart; a.zs = zs;
+  a.vimg = dvimg; a.mimg = dmimg; a.voff = dvoff; a.moff = dmoff; a.vbytes = dvb; a.mbytes = dmb;
+  a.max_vbytes = max_v; a.max_mbytes = max_m; a.buf_floats = buf_floats;
+  a.scale = p->mix.scale;
+  a.err = p->d_err;
+  p->tr_w = W;
+  p->tr_smem = smem;
+  p->tr_grid = (int)std::min<long>((long)per_sm * nsm, npart);
+  p->pipe_grid = p->tr_grid;
+  p->tr_on = true;
+  return kOk;
+}
+}  // namespace
+
 int mpkg_plan_mixed_tiles(int n, const int *ptr, const int *col, const double *val, const int *part, int npart,
                           int nlevel, int value_type, mpkg_plan **out) {
   clear_error();
@@ -3532,24 +3845,26 @@ int mpkg_plan_mixed_tiles(int n, const int *ptr, const int *col, const double *v
     if (ew.empty()) ew.push_back(0);
     rc = dev_copy(p, &ell_width, ew.data(), ew.size());
   }
+  std::vector<float> v32;
+  std::vector<__nv_bfloat16> v16;
   if (!rc) {
     if (value_type == MPKG_VALUE_F32) {
-      std::vector<float> v(p->nnz);
+      v32.resize(p->nnz);
       for (long j = 0; j < p->nnz; j++) {
-        v[j] = (float)val[j];
-        if ((double)v[j] != val[j]) p->mix_inexact++;
+        v32[j] = (float)val[j];
+        if ((double)v32[j] != val[j]) p->mix_inexact++;
       }
       float *dv = nullptr;
-      rc = dev_copy(p, &dv, v.data(), v.size());
+      rc = dev_copy(p, &dv, v32.data(), v32.size());
       a.val = dv;
     } else {
-      std::vector<__nv_bfloat16> v(p->nnz);
+      v16.resize(p->nnz);
       for (long j = 0; j < p->nnz; j++) {
-        v[j] = __double2bfloat16(val[j]);
-        if ((double)__bfloat162float(v[j]) != val[j]) p->mix_inexact++;
+        v16[j] = __double2bfloat16(val[j]);
+        if ((double)__bfloat162float(v16[j]) != val[j]) p->mix_inexact++;
       }
       __nv_bfloat16 *dv = nullptr;
-      rc = dev_copy(p, &dv, v.data(), v.size());
+      rc = dev_copy(p, &dv, v16.data(), v16.size());
       a.val = dv;
     }
   }
@@ -3578,6 +3893,8 @@ int mpkg_plan_mixed_tiles(int n, const int *ptr, const int *col, const double *v
     p->tiles_smem = true;
     p->tm_on = true;
   }
+  if (!rc) rc = reg_tiles_setup(p, tp, ptr, value_type == MPKG_VALUE_F32 ? (const void *)v32.data()
+                                                                          : (const void *)v16.data(), wmax);
   if (rc) { mpkg_plan_destroy(p); return rc; }
   *out = p;
   return kOk;
@@ -3598,6 +3915,15 @@ int mpkg_exec_mixed_device(mpkg_plan *p, float *d_vv, void *stream) {
   if (p->epoch >= (1u << 30)) {
     CUDA_TRY(cudaMemsetAsync(p->mix.counts, 0, sizeof(unsigned) * (size_t)(p->nlevel + 1) * p->mix.nchunk, st));
     p->epoch = 1;
+  }
+  if (p->tr_on) {  // PA1 tiles, rows in registers
+    TileRegArgs a = p->tr;
+    a.x = d_vv;
+    a.vf = d_vv;
+    tr_kernel_ptr(p->mix_vt, p->tr_w)<<<p->tr_grid, kTrThreads, p->tr_smem, st>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    p->launches = 1;
+    return kOk;
   }
   if (p->tm_on) {  // PA1 tiles
     CUDA_TRY(cudaMemsetAsync(p->tm.ticket, 0, sizeof(unsigned int), st));
@@ -3690,6 +4016,7 @@ int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info) {
   info->pipe_chunk = p->pipe.chunk;
   info->pipe_reach = p->pipe_reach;
   info->pipe_grid = p->pipe_grid;
+  info->tile_regs = p->tr_on ? 1 : 0;
   return kOk;
 }
 

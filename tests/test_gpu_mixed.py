@@ -162,6 +162,68 @@ def test_mixed_tiles_bitwise_equal_wavefront(case, vt, gpu):
         f"{np.count_nonzero(got.view(np.uint32) != want.view(np.uint32))} entries differ"
 
 
+def _stencil2(nx, ny, offsets, seed):
+    """2-D stencil on nx*ny with the given (dx, dy) offsets (a symmetric
+    set), log-normal off-diagonal values, diagonally dominant rows."""
+    rng = np.random.default_rng(seed)
+    rows, cols = [], []
+    yy, xx = np.divmod(np.arange(nx * ny), nx)
+    for dx, dy in offsets:
+        ok = (xx + dx >= 0) & (xx + dx < nx) & (yy + dy >= 0) & (yy + dy < ny)
+        i = np.nonzero(ok)[0]
+        rows.append(i)
+        cols.append(i + dx + nx * dy)
+    r, c = np.concatenate(rows), np.concatenate(cols)
+    o = np.lexsort((c, r))
+    r, c = r[o], c[o]
+    v = rng.lognormal(0.0, 1.0, r.size)
+    off = r != c
+    v[off] = -v[off]
+    rs = np.bincount(r[off], weights=-v[off], minlength=nx * ny)
+    v[~off] = rs[r[~off]] + 0.01
+    ptr = np.zeros(nx * ny + 1, dtype=np.int64)
+    np.add.at(ptr, r + 1, 1)
+    return M.Csr(np.cumsum(ptr).astype(np.int32), c.astype(np.int32), v)
+
+
+@pytest.mark.parametrize("case", ["lap5", "diff9", "wide11", "k1", "k2", "bigparts"])
+@pytest.mark.parametrize("vt", [M.VALUE_F32, M.VALUE_BF16])
+def test_mixed_register_tiles_bitwise_equal_wavefront(case, vt, gpu):
+    """Tiles whose computed rows fit the register-resident kernel (at most
+    2304 rows of at most 12 entries) run on it, several tiles per CTA,
+    with the next tile's images streaming in while a tile computes; the
+    bits equal the wavefront schedule's.  Row widths 5, 9 and 11 (padded
+    to 12) select the kernel's three widths; k = 1 and 2 cover the x
+    gather right after the first level.  Larger tiles keep the general
+    tile kernel."""
+    k = {"k1": 1, "k2": 2, "wide11": 5, "bigparts": 4}.get(case, 8)
+    if case == "lap5":
+        a = M.Csr.laplacian(300, 200, 1, diag=4.0, off=-1.0)
+        part, npart = M.partition_rcb(_grid2(300, 200), 240), 240
+    elif case == "wide11":
+        offs = [(dx, dy) for dx in (-1, 0, 1) for dy in (-1, 0, 1)] + [(-2, 0), (2, 0)]
+        a = _stencil2(200, 180, offs, seed=7)
+        part, npart = M.partition_rcb(_grid2(200, 180), 300), 300
+    elif case == "bigparts":
+        a = M.Csr.laplacian(64, 64, 4, diag=6.0, off=-1.0)
+        part, npart = M.partition_rcb(a.coords, 4), 4
+    else:
+        nx, ny, npart = (256, 200, 400) if case == "diff9" else (128, 128, 100)
+        a = M.Csr.diffusion(nx, ny, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=5)
+        part = M.partition_rcb(_grid2(nx, ny), npart)
+    x = M.uniform(13, a.n)
+    tiles = M.Plan.mixed_tiles(a, part, npart, k, vt)
+    assert tiles.info()["tile_regs"] == (0 if case == "bigparts" else 1)
+    wave = M.Plan.mixed(a, k, vt)
+    got, want = _mixed_bits(tiles, x, k, a.n), _mixed_bits(wave, x, k, a.n)
+    again = _mixed_bits(tiles, x, k, a.n)  # a second call on the same plan
+    tiles.close()
+    wave.close()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
+        f"{np.count_nonzero(got.view(np.uint32) != want.view(np.uint32))} entries differ"
+    assert np.array_equal(again.view(np.uint32), want.view(np.uint32))
+
+
 def _grid2(nx, ny):
     i = np.arange(nx * ny)
     return np.stack([i % nx, i // nx, np.zeros_like(i)], axis=1).astype(np.int32)
