@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -1476,13 +1478,20 @@ __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a)
 
 // ------------------------------------------------------------------------
 // Register-resident PA1 tiles (the mixed form's temporal blocking for
-// tiles of at most kTrThreads * kTrRows computed rows): the plan writes
-// each tile as two contiguous, 16-byte aligned images in execution order,
-//   vert image:   header (ns, nrow1, owned, nslice, shells c_0..c_nlevel)
-//                 + the slots' vertices,
-//   matrix image: [slice][t][lane] byte offsets of the local columns
-//                 (uint16, slot * 4) then [slice][t][lane] values, every
-//                 row padded to W entries with value -0 and the zero slot,
+// tiles of at most kTrThreads * kTrRows computed rows).  A tile's slot s
+// lives in the level buffers at position (s & ~31) | ((s + rot) & 31), rot
+// chosen per 32-slot group by the plan so that the 32 gathers of one
+// warp-wide load fall into distinct shared-memory banks as far as it can.
+// The plan writes each tile as two contiguous, 16-byte aligned images in
+// execution order,
+//   vert image:   header (positions, nrow1, owned, nslice, shells
+//                 c_0..c_nlevel, rotation count at [31]), the rotation of
+//                 every 32-slot group, then the vertex at every position
+//                 (-1 where no slot sits),
+//   matrix image: [slice][t][lane] byte offsets of the local columns'
+//                 positions (uint16, position * 4) then [slice][t][lane]
+//                 values, every row padded to W entries with value -0 and
+//                 the zero position,
 // so a tile is two bulk copies.  Thread t holds rows t, t + T, t + 2T of
 // every level in registers (value and byte offset per entry), so an entry
 // costs one shared-memory gather and one FMA.  While a tile computes its
@@ -1494,10 +1503,10 @@ __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a)
 // ------------------------------------------------------------------------
 constexpr int kTrThreads = 768;
 constexpr int kTrRows = 3;
-constexpr int kTrHdrInts = 32;  // header of a vert image: 4 counts + c_0..c_nlevel
+constexpr int kTrHdrInts = 32;  // header of a vert image: 4 counts, c_0..c_nlevel, [31] rotation ints
 
 struct TileRegArgs {
-  int n, nlevel, ntile, zs;      // zs: the zero slot (index of a +0 in every level buffer)
+  int n, nlevel, ntile, zs;      // zs: the zero position (a +0 in every level buffer)
   const unsigned char *vimg;     // vert images
   const unsigned char *mimg;     // matrix images
   const long *voff, *moff;       // per tile (execution order): byte offsets
@@ -1605,8 +1614,12 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
   // the first tile's level 0
   if (!tr_wait(&bar_v, phase, a.err)) return;
   {
-    const int ns = vbuf[0];
-    for (int s = tid; s < ns; s += kTrThreads) cp_async4(xb + s, a.x + vbuf[kTrHdrInts + s]);
+    const int npos = vbuf[0];
+    const int *pv = vbuf + kTrHdrInts + vbuf[31];
+    for (int s = tid; s < npos; s += kTrThreads) {
+      const int v = pv[s];
+      if (v >= 0) cp_async4(xb + s, a.x + v);
+    }
   }
   const int lane = tid & 31, warp = tid >> 5;
   constexpr int kWarps = kTrThreads / 32;
@@ -1617,13 +1630,15 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
     const int nrow1 = vbuf[1], owned = vbuf[2], nslice = vbuf[3];
     if (tid >= 1 && tid <= a.nlevel) s_nrows[tid] = vbuf[4 + a.nlevel - tid];
     TrRow<VT, W> row[kTrRows];
-    int vert[kTrRows];
+    int vert[kTrRows], prow[kTrRows];
+    const int *pv = vbuf + kTrHdrInts + vbuf[31];
     const uint16_t *cols = reinterpret_cast<const uint16_t *>(mbuf);
     const VT *vals = reinterpret_cast<const VT *>(mbuf + (size_t)nslice * W * 64);
 #pragma unroll
     for (int j = 0; j < kTrRows; j++) {
       const int r = tid + j * kTrThreads;
-      vert[j] = r < owned ? vbuf[kTrHdrInts + r] : 0;
+      prow[j] = r < nrow1 ? (r & ~31) | ((r + vbuf[kTrHdrInts + (r >> 5)]) & 31) : 0;
+      vert[j] = r < owned ? pv[prow[j]] : 0;
       const long e = ((long)(warp + j * kWarps) * W) * 32 + lane;  // slice r / 32, entry 0
       if (r < nrow1) row[j].load(cols + e, vals + e);
     }
@@ -1652,15 +1667,19 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
         const int r = tid + j * kTrThreads;
         if (r < nr) {
           const float s = row[j].sum(in) * a.scale;
-          out[r] = s;
+          out[prow[j]] = s;
           if (r < owned) __stcs(dst + vert[j], s);
         }
       }
       if (l == lg && has_next) {
         if (!tr_wait(&bar_v, phase, a.err)) return;
-        const int ns = vbuf[0];
+        const int npos = vbuf[0];
+        const int *pn = vbuf + kTrHdrInts + vbuf[31];
         float *xn = xb + nxt * a.buf_floats;
-        for (int s = tid; s < ns; s += kTrThreads) cp_async4(xn + s, a.x + vbuf[kTrHdrInts + s]);
+        for (int s = tid; s < npos; s += kTrThreads) {
+          const int v = pn[s];
+          if (v >= 0) cp_async4(xn + s, a.x + v);
+        }
       }
       __syncthreads();
     }
@@ -3675,17 +3694,77 @@ int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, in
 }
 
 namespace {
+inline uint32_t rotl32(uint32_t m, int r) { return r ? (m << r) | (m >> (32 - r)) : m; }
+
+// Bank rotation of every 32-slot group of one tile: for each warp-wide
+// gather (a slice's entry t at level 1, weighted by the levels the slice
+// computes) the slots it reads are grouped by 32-slot group as bit masks
+// of their offsets; group q's rotation r maps offset o to bank (o + r) & 31.
+// One pass over the groups picks for each the rotation that least overlaps
+// the banks the other groups of the same gathers occupy (coordinate
+// descent from no rotation; ties keep the current one).
+void tile_rotations(const TilePlan &tp, int pt, int k, int nrow1, int nslice, int ns, std::vector<int> *rot_out) {
+  const int nq = (ns + 31) / 32;
+  struct Ent { int wf, q; uint32_t m; int w; };
+  std::vector<Ent> ent;
+  std::vector<int> wf_first;  // entries of gather i: [wf_first[i], wf_first[i+1])
+  const int *sh = &tp.shell[(long)pt * (k + 1)];
+  std::vector<uint32_t> qm(nq, 0u);
+  std::vector<int> touched;
+  for (int sl = 0; sl < nslice; sl++) {
+    int w = 0;
+    for (int l = 1; l <= k; l++) w += sl * 32 < sh[k - l];
+    const long gs = tp.slice_off[pt] + sl;
+    const int width = tp.ell_width[gs];
+    for (int t = 0; t < width; t++) {
+      wf_first.push_back((int)ent.size());
+      touched.clear();
+      for (int lane = 0; lane < 32 && sl * 32 + lane < nrow1; lane++) {
+        const int c = tp.ell_col[tp.ell_off[gs] + (long)t * 32 + lane];
+        if (c == 0xFFFF || c >= ns) continue;
+        if (!qm[c >> 5]) touched.push_back(c >> 5);
+        qm[c >> 5] |= 1u << (c & 31);
+      }
+      if (touched.size() > 1)  // a gather within one group never conflicts
+        for (int q : touched) ent.push_back({(int)wf_first.size() - 1, q, qm[q], w});
+      for (int q : touched) qm[q] = 0u;
+    }
+  }
+  wf_first.push_back((int)ent.size());
+  std::vector<std::vector<int>> byq(nq);
+  for (int e = 0; e < (int)ent.size(); e++) byq[ent[e].q].push_back(e);
+  std::vector<int> &rot = *rot_out;
+  rot.assign(nq, 0);
+  long cost[32];
+  for (int q = 0; q < nq; q++) {
+    if (byq[q].empty()) continue;
+    std::fill(cost, cost + 32, 0L);
+    for (int e : byq[q]) {
+      const Ent &en = ent[e];
+      uint32_t o = 0;
+      for (int e2 = wf_first[en.wf]; e2 < wf_first[en.wf + 1]; e2++)
+        if (e2 != e) o |= rotl32(ent[e2].m, rot[ent[e2].q]);
+      for (int r = 0; r < 32; r++) cost[r] += (long)en.w * __builtin_popcount(rotl32(en.m, r) & o);
+    }
+    int best = rot[q];
+    for (int r = 0; r < 32; r++)
+      if (cost[r] < cost[best]) best = r;
+    rot[q] = best;
+  }
+}
+
 // The register-resident tile kernel's two images per tile (layout above
-// tiles_reg_kernel), in execution order.  Plans whose tiles do not fit
-// (rows wider than 12 entries, more than kTrThreads * kTrRows computed rows,
-// more than 16383 slots, nlevel > 27, images beyond shared memory) keep
-// tiles_mix_kernel; nothing is built for them.
+// tiles_reg_kernel), in execution order, built by all host threads.  Plans
+// whose tiles do not fit (rows wider than 12 entries, more than
+// kTrThreads * kTrRows computed rows, positions beyond 16-bit byte
+// offsets, nlevel > 26, images beyond shared memory) keep tiles_mix_kernel;
+// nothing is built for them.
 int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void *hval, int wmax) {
   const int k = p->nlevel, W = tr_width(wmax);
   const int npart = p->npart;
   const size_t vsz = p->mix_vt == MPKG_VALUE_F32 ? sizeof(float) : sizeof(__nv_bfloat16);
-  if (W == 0 || k > kTrHdrInts - 5 || tp.max_slots > 16383) return kOk;
-  const int zs = tp.max_slots;
+  const int zp = (tp.max_slots + 31) / 32 * 32;  // the zero position, past every tile's positions
+  if (W == 0 || k > kTrHdrInts - 6 || zp * 4 > 65532) return kOk;
   std::vector<long> voff(npart + 1, 0), moff(npart + 1, 0);
   std::vector<int> vbytes(npart), mbytes(npart);
   for (int q = 0; q < npart; q++) {
@@ -3695,32 +3774,39 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
     if (nrow1 > kTrThreads * kTrRows) return kOk;
     const int nslice = (nrow1 + 31) / 32;
     if (tp.slice_off[pt + 1] - tp.slice_off[pt] != nslice) return fail(kEStruct, "tile slices disagree with shells");
-    vbytes[q] = 4 * (kTrHdrInts + (ns + 3) / 4 * 4);
+    const int nq = (ns + 31) / 32;
+    vbytes[q] = 4 * (kTrHdrInts + (nq + 3) / 4 * 4 + nq * 32);
     mbytes[q] = std::max<int>(16, (int)((size_t)nslice * W * 32 * (2 + vsz)));
     voff[q + 1] = voff[q] + vbytes[q];
     moff[q + 1] = moff[q] + mbytes[q];
   }
   const int max_v = *std::max_element(vbytes.begin(), vbytes.end());
   const int max_m = *std::max_element(mbytes.begin(), mbytes.end());
-  const int buf_floats = (zs + 1 + 3) / 4 * 4;
+  const int buf_floats = zp + 4;
   const size_t smem = (size_t)max_m + max_v + 3 * (size_t)buf_floats * sizeof(float);
   int maxsm = 0, nsm = 0, per_sm = 0;
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
   if (smem > (size_t)maxsm) return kOk;
   std::vector<unsigned char> vimg(voff[npart]), mimg(moff[npart]);
-  const uint16_t zoff = (uint16_t)(zs * 4);
-  const uint16_t neg0_bf16 = 0x8000;
-  for (int q = 0; q < npart; q++) {
+  std::atomic<int> bad{0};
+  auto build = [&](int q) {
     const int pt = tp.order[q];
     const long s0 = tp.slot_off[pt];
     const int ns = (int)(tp.slot_off[pt + 1] - s0);
     const int *sh = &tp.shell[(long)pt * (k + 1)];
-    const int nrow1 = sh[k - 1], nslice = (nrow1 + 31) / 32;
+    const int nrow1 = sh[k - 1], nslice = (nrow1 + 31) / 32, nq = (ns + 31) / 32, nqp = (nq + 3) / 4 * 4;
+    std::vector<int> rot;
+    tile_rotations(tp, pt, k, nrow1, nslice, ns, &rot);
+    auto pos = [&](int c) { return (c & ~31) | ((c + rot[c >> 5]) & 31); };
     int *hv = reinterpret_cast<int *>(vimg.data() + voff[q]);
-    hv[0] = ns; hv[1] = nrow1; hv[2] = sh[0]; hv[3] = nslice;
+    hv[0] = nq * 32; hv[1] = nrow1; hv[2] = sh[0]; hv[3] = nslice;
     for (int d = 0; d <= k; d++) hv[4 + d] = sh[d];
-    for (int s = 0; s < ns; s++) hv[kTrHdrInts + s] = tp.slot_vert[s0 + s];
+    hv[31] = nqp;
+    for (int g = 0; g < nq; g++) hv[kTrHdrInts + g] = rot[g];
+    int *pv = hv + kTrHdrInts + nqp;
+    for (int g = 0; g < nq * 32; g++) pv[g] = -1;
+    for (int sl = 0; sl < ns; sl++) pv[pos(sl)] = tp.slot_vert[s0 + sl];
     uint16_t *mc = reinterpret_cast<uint16_t *>(mimg.data() + moff[q]);
     unsigned char *mv = mimg.data() + moff[q] + (size_t)nslice * W * 64;
     for (int sl = 0; sl < nslice; sl++) {
@@ -3731,20 +3817,29 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
           const int r = sl * 32 + lane;
           const size_t e = ((size_t)sl * W + t) * 32 + lane;
           const int c = (r < nrow1 && t < w) ? tp.ell_col[tp.ell_off[gs] + (long)t * 32 + lane] : 0xFFFF;
-          if (c != 0xFFFF && c >= ns) return fail(kEStruct, "tile column outside the halo");
-          mc[e] = c != 0xFFFF ? (uint16_t)(c * 4) : zoff;
+          if (c != 0xFFFF && c >= ns) { bad = 1; return; }
+          mc[e] = (uint16_t)(4 * (c != 0xFFFF ? pos(c) : zp));
           const long j = c != 0xFFFF ? (long)ptr[tp.slot_vert[s0 + r]] + t : -1;
           if (vsz == sizeof(float)) {
             const float x = j >= 0 ? static_cast<const float *>(hval)[j] : -0.0f;
             std::memcpy(mv + e * 4, &x, 4);
           } else {
-            uint16_t b = neg0_bf16;
+            uint16_t b = 0x8000;  // BF16 -0
             if (j >= 0) std::memcpy(&b, static_cast<const __nv_bfloat16 *>(hval) + j, 2);
             std::memcpy(mv + e * 2, &b, 2);
           }
         }
     }
-  }
+  };
+  const int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::atomic<int> next{0};
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nth; t++)
+    pool.emplace_back([&] {
+      for (int q; (q = next.fetch_add(1)) < npart && !bad;) build(q);
+    });
+  for (auto &th : pool) th.join();
+  if (bad) return fail(kEStruct, "tile column outside the halo");
   unsigned char *dvimg = nullptr, *dmimg = nullptr;
   long *dvoff = nullptr, *dmoff = nullptr;
   int *dvb = nullptr, *dmb = nullptr;
@@ -3761,7 +3856,7 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
     return fail(kECuda, "register tile kernel attribute set-up failed");
   if (per_sm < 1) return kOk;
   TileRegArgs &a = p->tr;
-  a.n = p->n; a.nlevel = k; a.ntile = npart; a.zs = zs;
+  a.n = p->n; a.nlevel = k; a.ntile = npart; a.zs = zp;
   a.vimg = dvimg; a.mimg = dmimg; a.voff = dvoff; a.moff = dmoff; a.vbytes = dvb; a.mbytes = dmb;
   a.max_vbytes = max_v; a.max_mbytes = max_m; a.buf_floats = buf_floats;
   a.scale = p->mix.scale;
