@@ -1582,19 +1582,46 @@ struct TrRow<__nv_bfloat16, W> {
   }
 };
 
+// One level of a tile: rows r = tid + j * kTrThreads below nr read the
+// level buffer at byte offset IN of the dynamic shared memory and write the
+// one at OUT (compile-time offsets, so a gather is one shared load with an
+// immediate displacement); the part's own rows also go to dst.
+template <typename VT, int W, int IN, int OUT>
+__device__ __forceinline__ void tr_level(const TrRow<VT, W> (&row)[kTrRows], const int (&prow)[kTrRows],
+                                         const int (&vert)[kTrRows], int nr, int owned, float *dst, float scale,
+                                         unsigned char *smem) {
+#pragma unroll
+  for (int j = 0; j < kTrRows; j++) {
+    const int r = (int)threadIdx.x + j * kTrThreads;
+    if (r < nr) {
+      const float s = row[j].sum(smem + IN) * scale;
+      *reinterpret_cast<float *>(smem + OUT + 4 * prow[j]) = s;
+      if (r < owned) __stcs(dst + vert[j], s);
+    }
+  }
+}
+
+// Level buffers: X0 and X1 at fixed offsets (the levels ping-pong between
+// them), XG receives the next tile's level 0 and is copied to X0 when that
+// tile starts; then the matrix image and the vert image.
+constexpr int kTrXBytes = 16384;  // positions per level buffer: 4096 (the zero position included)
+
 template <typename VT, int W>
 __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a) {
   extern __shared__ __align__(128) unsigned char tr_smem[];
   __shared__ __align__(8) unsigned long long bar_v, bar_m;
   __shared__ int s_nrows[33];
-  unsigned char *mbuf = tr_smem;                                  // matrix image
-  int *vbuf = reinterpret_cast<int *>(tr_smem + a.max_mbytes);    // vert image
-  float *xb = reinterpret_cast<float *>(tr_smem + a.max_mbytes + a.max_vbytes);
+  constexpr int X0 = 0, X1 = kTrXBytes, XG = 2 * kTrXBytes;
+  float *xg = reinterpret_cast<float *>(tr_smem + XG);
+  unsigned char *mbuf = tr_smem + 3 * kTrXBytes;                     // matrix image
+  int *vbuf = reinterpret_cast<int *>(mbuf + a.max_mbytes);          // vert image
   const int tid = threadIdx.x, G = gridDim.x;
   int q = blockIdx.x;
   if (q >= a.ntile) return;
-  for (int b = 0; b < 3; b++)
-    if (tid == 0) xb[b * a.buf_floats + a.zs] = 0.f;
+  if (tid == 0) {
+    reinterpret_cast<float *>(tr_smem + X0)[a.zs] = 0.f;
+    reinterpret_cast<float *>(tr_smem + X1)[a.zs] = 0.f;
+  }
   long nvo = 0, nmo = 0;  // thread 0: offsets and sizes of this CTA's next tile, loaded a tile ahead
   int nvb = 0, nmb = 0;
   if (tid == 0) {
@@ -1610,7 +1637,6 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
   }
   __syncthreads();
   unsigned phase = 0;
-  int cur = 0, alt = 1, nxt = 2;
   // the first tile's level 0
   if (!tr_wait(&bar_v, phase, a.err)) return;
   {
@@ -1618,7 +1644,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
     const int *pv = vbuf + kTrHdrInts + vbuf[31];
     for (int s = tid; s < npos; s += kTrThreads) {
       const int v = pv[s];
-      if (v >= 0) cp_async4(xb + s, a.x + v);
+      if (v >= 0) cp_async4(xg + s, a.x + v);
     }
   }
   const int lane = tid & 31, warp = tid >> 5;
@@ -1627,7 +1653,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
     // this tile: header, vertices and matrix image in shared memory
     if (!tr_wait(&bar_m, phase, a.err)) return;
     phase ^= 1u;
-    const int nrow1 = vbuf[1], owned = vbuf[2], nslice = vbuf[3];
+    const int npos = vbuf[0], nrow1 = vbuf[1], owned = vbuf[2], nslice = vbuf[3];
     if (tid >= 1 && tid <= a.nlevel) s_nrows[tid] = vbuf[4 + a.nlevel - tid];
     TrRow<VT, W> row[kTrRows];
     int vert[kTrRows], prow[kTrRows];
@@ -1656,36 +1682,25 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
         nvo = a.voff[qn + G]; nmo = a.moff[qn + G]; nvb = a.vbytes[qn + G]; nmb = a.mbytes[qn + G];
       }
     }
-    const int lg = (a.nlevel + 1) / 2;  // level after which the next tile's x is gathered
+    for (int s = tid; s < npos; s += kTrThreads) reinterpret_cast<float *>(tr_smem + X0)[s] = xg[s];
+    __syncthreads();
+    const int lg = (a.nlevel + 1) / 2;  // level after which the next tile's x is gathered into XG
     for (int l = 1; l <= a.nlevel; l++) {
-      const unsigned char *in = reinterpret_cast<const unsigned char *>(xb + ((l & 1) ? cur : alt) * a.buf_floats);
-      float *out = xb + ((l & 1) ? alt : cur) * a.buf_floats;
-      const int nr = s_nrows[l];
       float *dst = a.vf + (size_t)l * a.n;
-#pragma unroll
-      for (int j = 0; j < kTrRows; j++) {
-        const int r = tid + j * kTrThreads;
-        if (r < nr) {
-          const float s = row[j].sum(in) * a.scale;
-          out[prow[j]] = s;
-          if (r < owned) __stcs(dst + vert[j], s);
-        }
-      }
+      if (l & 1) tr_level<VT, W, X0, X1>(row, prow, vert, s_nrows[l], owned, dst, a.scale, tr_smem);
+      else tr_level<VT, W, X1, X0>(row, prow, vert, s_nrows[l], owned, dst, a.scale, tr_smem);
       if (l == lg && has_next) {
         if (!tr_wait(&bar_v, phase, a.err)) return;
-        const int npos = vbuf[0];
+        const int nposn = vbuf[0];
         const int *pn = vbuf + kTrHdrInts + vbuf[31];
-        float *xn = xb + nxt * a.buf_floats;
-        for (int s = tid; s < npos; s += kTrThreads) {
+        for (int s = tid; s < nposn; s += kTrThreads) {
           const int v = pn[s];
-          if (v >= 0) cp_async4(xn + s, a.x + v);
+          if (v >= 0) cp_async4(xg + s, a.x + v);
         }
       }
       __syncthreads();
     }
     if (!has_next) break;
-    const int c0 = cur;
-    cur = nxt; nxt = alt; alt = c0;
     q = qn;
   }
 }
@@ -3764,7 +3779,7 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
   const int npart = p->npart;
   const size_t vsz = p->mix_vt == MPKG_VALUE_F32 ? sizeof(float) : sizeof(__nv_bfloat16);
   const int zp = (tp.max_slots + 31) / 32 * 32;  // the zero position, past every tile's positions
-  if (W == 0 || k > kTrHdrInts - 6 || zp * 4 > 65532) return kOk;
+  if (W == 0 || k > kTrHdrInts - 6 || 4 * (zp + 1) > kTrXBytes) return kOk;
   std::vector<long> voff(npart + 1, 0), moff(npart + 1, 0);
   std::vector<int> vbytes(npart), mbytes(npart);
   for (int q = 0; q < npart; q++) {
@@ -3782,8 +3797,8 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
   }
   const int max_v = *std::max_element(vbytes.begin(), vbytes.end());
   const int max_m = *std::max_element(mbytes.begin(), mbytes.end());
-  const int buf_floats = zp + 4;
-  const size_t smem = (size_t)max_m + max_v + 3 * (size_t)buf_floats * sizeof(float);
+  const int buf_floats = kTrXBytes / 4;
+  const size_t smem = 3 * (size_t)kTrXBytes + max_m + max_v;
   int maxsm = 0, nsm = 0, per_sm = 0;
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
