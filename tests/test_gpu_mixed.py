@@ -50,6 +50,45 @@ def test_mixed_bf16_lossless_on_stencil(gpu):
     assert max(errs) <= MIXED_TOL, errs
 
 
+def _conv_diff(nx, ny, c):
+    """Upwind convection-diffusion on nx*ny: centre 4+c, west -1-c, east,
+    south and north -1.  Strongly non-normal for large c (||A||_inf = 8+2c
+    far above the spectral radius)."""
+    yy, xx = np.divmod(np.arange(nx * ny), nx)
+    ents = [((0, -1), -1.0), ((-1, 0), -1.0 - c), ((0, 0), 4.0 + c), ((1, 0), -1.0), ((0, 1), -1.0)]
+    rows, cols, vals = [], [], []
+    for (dx, dy), v in ents:
+        ok = (xx + dx >= 0) & (xx + dx < nx) & (yy + dy >= 0) & (yy + dy < ny)
+        i = np.nonzero(ok)[0]
+        rows.append(i)
+        cols.append(i + dx + nx * dy)
+        vals.append(np.full(i.size, v))
+    r, cc, vv = np.concatenate(rows), np.concatenate(cols), np.concatenate(vals)
+    o = np.lexsort((cc, r))
+    ptr = np.zeros(nx * ny + 1, dtype=np.int64)
+    np.add.at(ptr, r[o] + 1, 1)
+    return M.Csr(np.cumsum(ptr).astype(np.int32), cc[o].astype(np.int32), vv[o])
+
+
+@pytest.mark.parametrize("c", [20.0, 100.0])
+def test_mixed_nonnormal_31_levels_no_underflow(c, gpu):
+    """The static 2^-e scaling (2^e >= ||A||_inf) on a strongly non-normal
+    operator whose levels shrink by about ||A||_inf / rho per power: at
+    the largest nlevel (31) no level entry that is nonzero in FP64 falls
+    to an FP32 subnormal or zero, and every power stays within 1e-6 of
+    FP64.  A basis could underflow only after about
+    126 / log2(2^e / rho) powers."""
+    a = _conv_diff(96, 80, c)
+    k = 31
+    x = M.uniform(9, a.n)
+    v, e, _ = run_mixed(a, k, M.VALUE_F32, x)
+    raw = v / (2.0 ** (e * np.arange(k + 1)))[:, None]
+    want = O.mpk(a.ptr, a.col, a.val, x, k, O.MODE_FMA).reshape(k + 1, a.n)
+    assert not np.any((np.abs(raw[1:]) < np.finfo(np.float32).tiny) & (want[1:] != 0))
+    assert np.abs(raw[k]).max() < 0.1  # the basis shrinks, it does not grow
+    assert max(rel_errors(v, want, a.n, k)) <= MIXED_TOL
+
+
 def test_mixed_scaling_keeps_basis_bounded(gpu):
     a = M.Csr.laplacian(64, 64, 16, diag=6.0, off=-1.0)
     x = np.ones(a.n)
