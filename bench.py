@@ -498,6 +498,10 @@ def bench_sstep(M):
     out["learned_shifts"]["model"] = src
     # the same solve with the Gram matrix summed in double-float on the FP32 pipes
     _, out["learned_shifts_df64_gram"] = M.sstep_cg(a, b, 8, shifts=sh, gram=M.GRAM_DF64)
+    # the same solve with the basis built by one matrix powers launch per
+    # outer iteration (the default builds it with one launch per step)
+    _, out["learned_shifts_mpk_basis"] = M.sstep_cg(a, b, 8, shifts=sh, basis=M.SSTEP_BASIS_MPK)
+    out["basis"] = "one FP32 SpMV launch per Newton step, both blocks per launch (mpk_basis: one wavefront launch)"
     out["gram"] = "FP64 FMAs over the exact FP64 products of the FP32 basis (df64: double-float sums)"
     # the same solve with the outer loop driven from the host (one graph
     # launch and synchronisation per outer iteration)

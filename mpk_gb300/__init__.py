@@ -699,7 +699,7 @@ SSTEP_BASIS_MPK, SSTEP_BASIS_STEPS = 0, 1
 
 
 def sstep_cg(a: Csr, b, s=8, shifts=None, scale=None, x0=None, tol=1e-8, max_outer=2000, gram=GRAM_FP64,
-             loop=SSTEP_DEVICE_LOOP, basis=SSTEP_BASIS_MPK):
+             loop=SSTEP_DEVICE_LOOP, basis=SSTEP_BASIS_STEPS):
     """s-step CG with an FP32 Newton basis (shifts None: monomial) scaled
     by `scale` per step (default: the Gershgorin upper bound / 2); the
     Gram matrix in FP64 (GRAM_FP64) or double-float (GRAM_DF64); the

@@ -1535,47 +1535,31 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Shared-memory load and store at a 32-bit shared address plus a
-// compile-time displacement (one instruction each; the address arithmetic
-// stays in 32 bits).
-template <int D>
-__device__ __forceinline__ float lds_at(uint32_t addr) {
-  float v;
-  asm volatile("ld.shared.f32 %0, [%1+%2];" : "=f"(v) : "r"(addr), "n"(D) : "memory");
-  return v;
-}
-template <int D>
-__device__ __forceinline__ void sts_at(uint32_t addr, float v) {
-  asm volatile("st.shared.f32 [%0+%1], %2;" ::"r"(addr), "n"(D), "f"(v) : "memory");
-}
-
-// One entry's operands in registers: FP32 values beside packed 16-bit
-// shared addresses (the image's byte offset plus the dynamic shared
-// memory's base); BF16 values packed with their address in one word
-// (value bits in the high half are the FP32 value itself).
+// One entry's operands in registers: FP32 values beside packed byte
+// offsets; BF16 values packed with their offset in one word (value bits
+// in the high half are the FP32 value itself).
 template <typename VT, int W>
 struct TrRow;
 template <int W>
 struct TrRow<float, W> {
   float v[W];
   uint32_t c[(W + 1) / 2];
-  __device__ __forceinline__ void load(const uint16_t *cols, const float *vals, uint32_t sb) {
+  __device__ __forceinline__ void load(const uint16_t *cols, const float *vals) {
 #pragma unroll
     for (int t = 0; t < W; t++) v[t] = vals[32 * t];
 #pragma unroll
     for (int t = 0; t < W; t += 2) {
-      const uint32_t lo = cols[32 * t] + sb;
-      const uint32_t hi = t + 1 < W ? (uint32_t)cols[32 * (t + 1)] + sb : 0u;
+      const uint32_t lo = cols[32 * t];
+      const uint32_t hi = t + 1 < W ? (uint32_t)cols[32 * (t + 1)] : 0u;
       c[t / 2] = lo | (hi << 16);
     }
   }
-  template <int IN>
-  __device__ __forceinline__ float sum() const {
+  __device__ __forceinline__ float sum(const unsigned char *in) const {
     float s = 0.f;
 #pragma unroll
     for (int t = 0; t < W; t++) {
-      const uint32_t addr = (t & 1) ? (c[t / 2] >> 16) : (c[t / 2] & 0xFFFFu);
-      s = __fmaf_rn(v[t], lds_at<IN>(addr), s);
+      const uint32_t off = (t & 1) ? (c[t / 2] >> 16) : (c[t / 2] & 0xFFFFu);
+      s = __fmaf_rn(v[t], *reinterpret_cast<const float *>(in + off), s);
     }
     return s;
   }
@@ -1583,35 +1567,35 @@ struct TrRow<float, W> {
 template <int W>
 struct TrRow<__nv_bfloat16, W> {
   uint32_t w[W];
-  __device__ __forceinline__ void load(const uint16_t *cols, const __nv_bfloat16 *vals, uint32_t sb) {
+  __device__ __forceinline__ void load(const uint16_t *cols, const __nv_bfloat16 *vals) {
     const uint16_t *vb = reinterpret_cast<const uint16_t *>(vals);
 #pragma unroll
-    for (int t = 0; t < W; t++) w[t] = ((uint32_t)vb[32 * t] << 16) | ((uint32_t)cols[32 * t] + sb);
+    for (int t = 0; t < W; t++) w[t] = ((uint32_t)vb[32 * t] << 16) | (uint32_t)cols[32 * t];
   }
-  template <int IN>
-  __device__ __forceinline__ float sum() const {
+  __device__ __forceinline__ float sum(const unsigned char *in) const {
     float s = 0.f;
 #pragma unroll
     for (int t = 0; t < W; t++)
-      s = __fmaf_rn(__uint_as_float(w[t] & 0xFFFF0000u), lds_at<IN>(w[t] & 0xFFFFu), s);
+      s = __fmaf_rn(__uint_as_float(w[t] & 0xFFFF0000u), *reinterpret_cast<const float *>(in + (w[t] & 0xFFFFu)),
+                    s);
     return s;
   }
 };
 
 // One level of a tile: rows r = tid + j * kTrThreads below nr read the
 // level buffer at byte offset IN of the dynamic shared memory and write the
-// one at OUT (compile-time displacements: a gather is one shared load);
-// the part's own rows also go to dst.  prow holds each row's shared
-// address in the buffer at offset 0.
+// one at OUT (compile-time offsets, so a gather is one shared load with an
+// immediate displacement); the part's own rows also go to dst.
 template <typename VT, int W, int IN, int OUT>
-__device__ __forceinline__ void tr_level(const TrRow<VT, W> (&row)[kTrRows], const uint32_t (&prow)[kTrRows],
-                                         const int (&vert)[kTrRows], int nr, int owned, float *dst, float scale) {
+__device__ __forceinline__ void tr_level(const TrRow<VT, W> (&row)[kTrRows], const int (&prow)[kTrRows],
+                                         const int (&vert)[kTrRows], int nr, int owned, float *dst, float scale,
+                                         unsigned char *smem) {
 #pragma unroll
   for (int j = 0; j < kTrRows; j++) {
     const int r = (int)threadIdx.x + j * kTrThreads;
     if (r < nr) {
-      const float s = row[j].template sum<IN>() * scale;
-      sts_at<OUT>(prow[j], s);
+      const float s = row[j].sum(smem + IN) * scale;
+      *reinterpret_cast<float *>(smem + OUT + 4 * prow[j]) = s;
       if (r < owned) __stcs(dst + vert[j], s);
     }
   }
@@ -1634,12 +1618,6 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
   const int tid = threadIdx.x, G = gridDim.x;
   int q = blockIdx.x;
   if (q >= a.ntile) return;
-  // shared addresses of the level buffers are kept in 16 bits
-  const uint32_t sb = smem_u32(tr_smem);
-  if (sb + 2 * kTrXBytes > 65536u) {
-    if (tid == 0) atomicExch(a.err, kErrBounds);
-    return;
-  }
   if (tid == 0) {
     reinterpret_cast<float *>(tr_smem + X0)[a.zs] = 0.f;
     reinterpret_cast<float *>(tr_smem + X1)[a.zs] = 0.f;
@@ -1678,19 +1656,17 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
     const int npos = vbuf[0], nrow1 = vbuf[1], owned = vbuf[2], nslice = vbuf[3];
     if (tid >= 1 && tid <= a.nlevel) s_nrows[tid] = vbuf[4 + a.nlevel - tid];
     TrRow<VT, W> row[kTrRows];
-    int vert[kTrRows];
-    uint32_t prow[kTrRows];
+    int vert[kTrRows], prow[kTrRows];
     const int *pv = vbuf + kTrHdrInts + vbuf[31];
     const uint16_t *cols = reinterpret_cast<const uint16_t *>(mbuf);
     const VT *vals = reinterpret_cast<const VT *>(mbuf + (size_t)nslice * W * 64);
 #pragma unroll
     for (int j = 0; j < kTrRows; j++) {
       const int r = tid + j * kTrThreads;
-      const int ps = r < nrow1 ? (r & ~31) | ((r + vbuf[kTrHdrInts + (r >> 5)]) & 31) : 0;
-      prow[j] = sb + 4 * (uint32_t)ps;
-      vert[j] = r < owned ? pv[ps] : 0;
+      prow[j] = r < nrow1 ? (r & ~31) | ((r + vbuf[kTrHdrInts + (r >> 5)]) & 31) : 0;
+      vert[j] = r < owned ? pv[prow[j]] : 0;
       const long e = ((long)(warp + j * kWarps) * W) * 32 + lane;  // slice r / 32, entry 0
-      if (r < nrow1) row[j].load(cols + e, vals + e, sb);
+      if (r < nrow1) row[j].load(cols + e, vals + e);
     }
     cp_async_wait_all();  // this tile's level 0 (gathered during the previous tile)
     __syncthreads();      // both images fully read: the buffers take the next tile
@@ -1711,8 +1687,8 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
     const int lg = (a.nlevel + 1) / 2;  // level after which the next tile's x is gathered into XG
     for (int l = 1; l <= a.nlevel; l++) {
       float *dst = a.vf + (size_t)l * a.n;
-      if (l & 1) tr_level<VT, W, X0, X1>(row, prow, vert, s_nrows[l], owned, dst, a.scale);
-      else tr_level<VT, W, X1, X0>(row, prow, vert, s_nrows[l], owned, dst, a.scale);
+      if (l & 1) tr_level<VT, W, X0, X1>(row, prow, vert, s_nrows[l], owned, dst, a.scale, tr_smem);
+      else tr_level<VT, W, X1, X0>(row, prow, vert, s_nrows[l], owned, dst, a.scale, tr_smem);
       if (l == lg && has_next) {
         if (!tr_wait(&bar_v, phase, a.err)) return;
         const int nposn = vbuf[0];

@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(kThreads) basis_wave_kernel(BasisWave w, Sell 
 constexpr int kGramRows = 64;
 thread_local bool g_gram_f64 = true;  // mpkg_sstep_gram: FP64 (default) or double-float Gram
 thread_local bool g_device_loop = true;  // mpkg_sstep_loop: device-side (default) or host-side outer loop
-thread_local bool g_basis_mpk = true;    // mpkg_sstep_basis: one matrix powers launch (default) or s launches
+thread_local bool g_basis_mpk = false;   // mpkg_sstep_basis: s launches (default) or one matrix powers launch
 thread_local unsigned g_basis_stall = 0;  // mpkg_sstep_debug_stall
 __device__ __forceinline__ void gram_acc(float a, float b, float &sh, float &sl) {
   const float p = __fmul_rn(a, b), e = __fmaf_rn(a, b, -p);
