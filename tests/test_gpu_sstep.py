@@ -161,10 +161,10 @@ def test_sstep_mpk_basis_wait_times_out_and_recovers(gpu):
     _check(M.lib().mpkg_sstep_debug_stall(50))
     try:
         with pytest.raises(M.MpkError) as e:
-            M.sstep_cg(a, b, 4, max_outer=2)
+            M.sstep_cg(a, b, 4, max_outer=2, basis=M.SSTEP_BASIS_MPK)
         assert e.value.code == M.ETIMEOUT
     finally:
         _check(M.lib().mpkg_sstep_debug_stall(0))
-    x1, i1 = M.sstep_cg(a, b, 4)
+    x1, i1 = M.sstep_cg(a, b, 4, basis=M.SSTEP_BASIS_MPK)
     x2, i2 = M.sstep_cg(a, b, 4, basis=M.SSTEP_BASIS_STEPS)
     assert i1["converged"] and x1.tobytes() == x2.tobytes()
