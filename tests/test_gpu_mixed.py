@@ -263,6 +263,42 @@ def test_mixed_register_tiles_bitwise_equal_wavefront(case, vt, gpu):
     assert np.array_equal(again.view(np.uint32), want.view(np.uint32))
 
 
+@pytest.mark.parametrize("vt", [M.VALUE_F32, M.VALUE_BF16])
+def test_mixed_register_tiles_empty_rows_vs_fp32_oracle(vt, gpu):
+    """The register tile kernel on isolated vertices (empty rows: every
+    entry is padding, the sum stays +0 as the FP32 chain's), bit for bit
+    against the FP32 oracle on the stored values scaled by the exact 2^-e
+    (FP32 values) and against the wavefront schedule (BF16 values).  A
+    partition with an unused part id is refused, as by every PA1 plan."""
+    k = 6
+    base = M.Csr.laplacian(48, 40, 1, diag=4.0, off=-1.0)
+    drop = {0, 77, 500, 1919}
+    rows = [set() if i in drop else set(base.col[base.ptr[i]:base.ptr[i + 1]].tolist()) - drop
+            for i in range(base.n)]
+    ptr = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+    col = np.concatenate([sorted(r) for r in rows]).astype(np.int32)
+    val = np.where(col == np.repeat(np.arange(base.n), np.diff(ptr)), 4.0, -1.0)
+    a = M.Csr(ptr, col, val)
+    part, npart = M.partition_rcb(_grid2(48, 40), 20), 20
+    with pytest.raises(M.MpkError) as e:
+        M.Plan.mixed_tiles(a, (2 * part).astype(np.int32), 2 * npart, k, vt)
+    assert e.value.code == M.EINVAL
+    x = M.uniform(21, a.n)
+    plan = M.Plan.mixed_tiles(a, part.astype(np.int32), npart, k, vt)
+    assert plan.info()["tile_regs"] == 1
+    e, _ = plan.mixed_scale()
+    got = _mixed_bits(plan, x, k, a.n).reshape(k + 1, a.n)
+    plan.close()
+    if vt == M.VALUE_F32:
+        sval = a.val.astype(np.float32) * np.float32(2.0 ** -e)
+        want = O.spmm_f32(a.ptr, a.col, sval, x.astype(np.float32)[:, None], k)[:, :, 0]
+    else:
+        wave = M.Plan.mixed(a, k, vt)
+        want = _mixed_bits(wave, x, k, a.n).reshape(k + 1, a.n)
+        wave.close()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
 def _grid2(nx, ny):
     i = np.arange(nx * ny)
     return np.stack([i % nx, i // nx, np.zeros_like(i)], axis=1).astype(np.int32)
