@@ -244,7 +244,31 @@ __global__ void basis_start_kernel(int n, const double *__restrict__ p, const do
 __device__ __forceinline__ void newton_row(int i, int l, const int *cb, const float *vb, const float *pin, float *pout,
                                            const float *rin, float *rout, float theta, float rsigma) {
   float sp = 0.f, sr = 0.f;
-  for (int t = 0; t < l; t++) {
+  int t = 0;
+  if (l <= 8) {  // all of a short row's loads in flight together: columns, then both gathers
+    int c[8];
+    float v[8], xp[8], xr[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (u < l) {
+        c[u] = cb[32 * u];
+        v[u] = vb[32 * u];
+      }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (u < l) {
+        xp[u] = pin[c[u]];
+        xr[u] = rout ? rin[c[u]] : 0.f;
+      }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (u < l) {
+        sp = __fmaf_rn(v[u], xp[u], sp);
+        if (rout) sr = __fmaf_rn(v[u], xr[u], sr);
+      }
+    t = l;
+  }
+  for (; t < l; t++) {
     const int c = cb[32 * t];
     const float v = vb[32 * t];
     sp = __fmaf_rn(v, pin[c], sp);
