@@ -397,7 +397,7 @@ def bench_batch(M, torch, args, flush, stream):
     k=6, one persistent graph-replayed launch, autotuned."""
     import scipy.sparse as sp
     k, nrhs = 6, 16
-    mats = M.batch_workload(256, seed=0)
+    mats = M.batch_workload(args.batch_mats, seed=0)
     N = sum(m.n for m in mats)
     nnz = sum(m.nnz for m in mats)
     t0 = time.perf_counter()
@@ -423,7 +423,8 @@ def bench_batch(M, torch, args, flush, stream):
     ms = statistics.median(times)
     vb = d.view(k + 1, N, nrhs)
     errs = [0.0] * k
-    sample = [0, 1, 2, 3, 128, 129, 254, 255]
+    nm = len(mats)
+    sample = sorted({j % nm for j in (0, 1, 2, 3, nm // 2, nm // 2 + 1, nm - 2, nm - 1)})
     row0 = np.concatenate([[0], np.cumsum([m.n for m in mats])])
     for j in sample:  # error of the FP32 form against FP64, per power
         m = mats[j]
@@ -437,11 +438,11 @@ def bench_batch(M, torch, args, flush, stream):
     peak, _ = peaks()
     info = plan.batch_info()
     plan.close()
-    return {"workload": "256 matrices, n log-uniform [1e3, 2e5] (half random 2-D/3-D stencils, half random banded "
+    return {"workload": f"{nm} matrices, n log-uniform [1e3, 2e5] (half random 2-D/3-D stencils, half random banded "
                         "bw 64, 5-30 nnz/row), 16 RHS FP32, k=6", "rows": N, "nnz": nnz, "ms_per_step": ms,
             "value": N * nrhs * k / (ms * 1e-3) / 1e9, "unit": "G row-RHS powers/s",
             "algorithmic_bytes": B, "achieved_gbs": B / (ms * 1e-3) / 1e9, "frac_hbm": B / (ms * 1e-3) / 1e9 / peak,
-            "rel_err_per_power_vs_fp64": errs, "error_sample": "8 of the 256 matrices, all 16 RHS",
+            "rel_err_per_power_vs_fp64": errs, "error_sample": f"{len(sample)} of the {nm} matrices, all 16 RHS",
             "plan_s": plan_s, "tuned": {kk: info[kk] for kk in ("lanes_per_row", "vector_width", "group_bytes",
                                                                "ngroup", "grid", "graph", "candidates", "tune_ms")},
             "gpu_launches_per_step": 1}
@@ -576,6 +577,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true", help="time only the selected executor")
     ap.add_argument("--sections", default="variants,mixed,batched,sstep,prep",
                     help="comma list of the extra sections to run (variants, mixed, batched, sstep, prep; 'none')")
+    ap.add_argument("--batch-mats", type=int, default=256,
+                    help="matrices of the batched section (256 = the workload; fewer for a profiler capture)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     sections = set() if args.no_variants else {t.strip() for t in args.sections.split(",")} - {"none", ""}
