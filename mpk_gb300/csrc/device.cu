@@ -1488,8 +1488,9 @@ __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a)
 //                 c_0..c_nlevel, rotation count at [31]), the rotation of
 //                 every 32-slot group, then the vertex at every position
 //                 (-1 where no slot sits),
-//   matrix image: [slice][t][lane] byte offsets of the local columns'
-//                 positions (uint16, position * 4) then [slice][t][lane]
+//   matrix image: [slice][t / 2][lane] pairs of byte offsets of the local
+//                 columns' positions (uint16 each, position * 4; entry t in
+//                 half t & 1 of the word) then [slice][t][lane]
 //                 values, every row padded to W entries with value -0 and
 //                 the zero position,
 // so a tile is two bulk copies.  Thread t holds rows t, t + T, t + 2T of
@@ -1544,15 +1545,11 @@ template <int W>
 struct TrRow<float, W> {
   float v[W];
   uint32_t c[(W + 1) / 2];
-  __device__ __forceinline__ void load(const uint16_t *cols, const float *vals) {
+  __device__ __forceinline__ void load(const uint32_t *cols, const float *vals) {
 #pragma unroll
     for (int t = 0; t < W; t++) v[t] = vals[32 * t];
 #pragma unroll
-    for (int t = 0; t < W; t += 2) {
-      const uint32_t lo = cols[32 * t];
-      const uint32_t hi = t + 1 < W ? (uint32_t)cols[32 * (t + 1)] : 0u;
-      c[t / 2] = lo | (hi << 16);
-    }
+    for (int p = 0; p < (W + 1) / 2; p++) c[p] = cols[32 * p];
   }
   __device__ __forceinline__ float sum(const unsigned char *in) const {
     float s = 0.f;
@@ -1567,10 +1564,10 @@ struct TrRow<float, W> {
 template <int W>
 struct TrRow<__nv_bfloat16, W> {
   uint32_t w[W];
-  __device__ __forceinline__ void load(const uint16_t *cols, const __nv_bfloat16 *vals) {
+  __device__ __forceinline__ void load(const uint32_t *cols, const __nv_bfloat16 *vals) {
     const uint16_t *vb = reinterpret_cast<const uint16_t *>(vals);
 #pragma unroll
-    for (int t = 0; t < W; t++) w[t] = ((uint32_t)vb[32 * t] << 16) | (uint32_t)cols[32 * t];
+    for (int t = 0; t < W; t++) w[t] = ((uint32_t)vb[32 * t] << 16) | ((cols[32 * (t / 2)] >> (16 * (t & 1))) & 0xFFFFu);
   }
   __device__ __forceinline__ float sum(const unsigned char *in) const {
     float s = 0.f;
@@ -1658,15 +1655,15 @@ __global__ void __launch_bounds__(kTrThreads, 1) tiles_reg_kernel(TileRegArgs a)
     TrRow<VT, W> row[kTrRows];
     int vert[kTrRows], prow[kTrRows];
     const int *pv = vbuf + kTrHdrInts + vbuf[31];
-    const uint16_t *cols = reinterpret_cast<const uint16_t *>(mbuf);
-    const VT *vals = reinterpret_cast<const VT *>(mbuf + (size_t)nslice * W * 64);
+    const uint32_t *cols = reinterpret_cast<const uint32_t *>(mbuf);  // two entries' offsets per word
+    const VT *vals = reinterpret_cast<const VT *>(mbuf + (size_t)nslice * ((W + 1) / 2) * 128);
 #pragma unroll
     for (int j = 0; j < kTrRows; j++) {
       const int r = tid + j * kTrThreads;
       prow[j] = r < nrow1 ? (r & ~31) | ((r + vbuf[kTrHdrInts + (r >> 5)]) & 31) : 0;
       vert[j] = r < owned ? pv[prow[j]] : 0;
-      const long e = ((long)(warp + j * kWarps) * W) * 32 + lane;  // slice r / 32, entry 0
-      if (r < nrow1) row[j].load(cols + e, vals + e);
+      const long sl = warp + j * kWarps;  // slice r / 32
+      if (r < nrow1) row[j].load(cols + (sl * ((W + 1) / 2)) * 32 + lane, vals + (sl * W) * 32 + lane);
     }
     cp_async_wait_all();  // this tile's level 0 (gathered during the previous tile)
     __syncthreads();      // both images fully read: the buffers take the next tile
@@ -3791,7 +3788,7 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
     if (tp.slice_off[pt + 1] - tp.slice_off[pt] != nslice) return fail(kEStruct, "tile slices disagree with shells");
     const int nq = (ns + 31) / 32;
     vbytes[q] = 4 * (kTrHdrInts + (nq + 3) / 4 * 4 + nq * 32);
-    mbytes[q] = std::max<int>(16, (int)((size_t)nslice * W * 32 * (2 + vsz)));
+    mbytes[q] = std::max<int>(16, (int)((size_t)nslice * 32 * (4 * ((W + 1) / 2) + W * vsz)));
     voff[q + 1] = voff[q] + vbytes[q];
     moff[q + 1] = moff[q] + mbytes[q];
   }
@@ -3822,8 +3819,8 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
     int *pv = hv + kTrHdrInts + nqp;
     for (int g = 0; g < nq * 32; g++) pv[g] = -1;
     for (int sl = 0; sl < ns; sl++) pv[pos(sl)] = tp.slot_vert[s0 + sl];
-    uint16_t *mc = reinterpret_cast<uint16_t *>(mimg.data() + moff[q]);
-    unsigned char *mv = mimg.data() + moff[q] + (size_t)nslice * W * 64;
+    uint16_t *mc = reinterpret_cast<uint16_t *>(mimg.data() + moff[q]);  // [slice][t / 2][lane][t & 1]
+    unsigned char *mv = mimg.data() + moff[q] + (size_t)nslice * ((W + 1) / 2) * 128;
     for (int sl = 0; sl < nslice; sl++) {
       const long gs = tp.slice_off[pt] + sl;
       const int w = tp.ell_width[gs];
@@ -3833,7 +3830,8 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
           const size_t e = ((size_t)sl * W + t) * 32 + lane;
           const int c = (r < nrow1 && t < w) ? tp.ell_col[tp.ell_off[gs] + (long)t * 32 + lane] : 0xFFFF;
           if (c != 0xFFFF && c >= ns) { bad = 1; return; }
-          mc[e] = (uint16_t)(4 * (c != 0xFFFF ? pos(c) : zp));
+          mc[(((size_t)sl * ((W + 1) / 2) + t / 2) * 32 + lane) * 2 + (t & 1)] =
+              (uint16_t)(4 * (c != 0xFFFF ? pos(c) : zp));
           const long j = c != 0xFFFF ? (long)ptr[tp.slot_vert[s0 + r]] + t : -1;
           if (vsz == sizeof(float)) {
             const float x = j >= 0 ? static_cast<const float *>(hval)[j] : -0.0f;
