@@ -1522,6 +1522,7 @@ struct TileRegArgs {
 __device__ __forceinline__ bool tr_wait(unsigned long long *bar, unsigned phase, int *err) {
   long spins = 0;
   while (!mbar_try(bar, phase)) {
+    if (spins > 16) __nanosleep(64);
     if (++spins > kSpinLimit) {  // a copy of this CTA never completed: report, drain with a second bound
       if (threadIdx.x == 0) atomicCAS(err, 0, kErrTimeout);
       for (long s2 = 0; s2 < kSpinLimit && !mbar_try(bar, phase); s2++) __nanosleep(256);
