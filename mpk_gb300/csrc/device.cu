@@ -1498,7 +1498,8 @@ __global__ void __launch_bounds__(kTmThreads, 1) tiles_mix_kernel(TileMixArgs a)
 // costs one shared-memory gather and one FMA.  While a tile computes its
 // levels, the next tile's images stream in (TMA bulk copies on two
 // mbarriers) and, once its vertices have landed, its level-0 x is gathered
-// into the third level buffer (cp.async).  Padding entries add
+// into a third buffer (cp.async), copied into the first level buffer when
+// that tile starts.  Padding entries add
 // fma(-0, +0, s) = s exactly, so the row sums are the FP32 FMA chains in
 // CSR order of the wavefront and pipeline mixed forms, bit for bit.
 // ------------------------------------------------------------------------
