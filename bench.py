@@ -360,15 +360,15 @@ def bench_mixed(M, torch, a, x, k, exact, args, flush, stream):
     peak, _ = peaks()
     B32 = b.nnz * 8 + 4 * (b.n + 1) + 4 * b.n * (k + 1)
     res = {"n": b.n, "nnz": b.nnz, "fp64_ms": fp64, "fp64_best": best64, "algorithmic_bytes_f32": B32,
-           "schedules": "wave: the wavefront (every level streams the matrix); tiles: PA1 tiles of 4096 RCB parts "
-                        "(32x32 boxes) + 8-deep skirts, each tile's rows held on chip for all levels"}
+           "schedules": "wave: the wavefront (every level streams the matrix); tiles: PA1 tiles (RCB parts, part "
+                        "size chosen by the plan's autotuner among 384..1536 rows) + 8-deep skirts, each tile's rows "
+                        "held on chip for all levels"}
     i = np.arange(b.n)
     coords = np.stack([i % 2048, i // 2048, np.zeros_like(i)], axis=1).astype(np.int32)
-    tparts = M.partition_rcb(coords, 4096)
     bits = {}
     for name, vt in (("f32", M.VALUE_F32), ("bf16", M.VALUE_BF16)):
         for sched in ("wave", "tiles"):
-            p32 = M.Plan.mixed(b, k, vt) if sched == "wave" else M.Plan.mixed_tiles(b, tparts, 4096, k, vt)
+            p32 = M.Plan.mixed(b, k, vt) if sched == "wave" else M.Plan.mixed_tiles_tuned(b, coords, k, vt)
             e, inexact = p32.mixed_scale()
             d32 = torch.zeros((k + 1) * b.n, dtype=torch.float32, device="cuda")
             d32[:b.n] = torch.from_numpy(xb.astype(np.float32)).cuda()
@@ -384,6 +384,9 @@ def bench_mixed(M, torch, a, x, k, exact, args, flush, stream):
                 "achieved_gbs": B32 / (t32 * 1e-3) / 1e9, "frac_hbm": B32 / (t32 * 1e-3) / 1e9 / peak,
                 "kernel": (("tiles_reg_kernel" if info["tile_regs"] else "tiles_mix_kernel") if sched == "tiles"
                            else "wave_mix_kernel")}
+            if sched == "tiles":
+                res[f"{name}_{sched}"].update(parts=info["npart"], part_sizes_timed=info["tune_candidates"],
+                                              tune_ms=info["tune_ms"])
             p32.close()
             del d32
         res[f"{name}_tiles"]["bit_equal_wave"] = bool(np.array_equal(bits[(name, "wave")], bits[(name, "tiles")]))

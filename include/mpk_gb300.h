@@ -104,6 +104,8 @@ typedef struct {
   int pipe_grid;        /* PIPE: resident CTAs launched */
   int tile_regs;        /* MIXED on tiles: 1 when every tile's rows are held in
                            registers (register-resident tile kernel) */
+  int tune_candidates;  /* mpkg_plan_mixed_tiles_tuned: part sizes timed */
+  double tune_ms;       /* mpkg_plan_mixed_tiles_tuned: time spent choosing */
 } mpkg_plan_info_t;
 
 /* Plan over task lists in the reference layout: list t = phase*npart+part
@@ -340,6 +342,16 @@ int mpkg_plan_mixed(int n, const int *ptr, const int *col, const double *val, in
  * a tile's two FP32 level vectors exceed shared memory (use more parts). */
 int mpkg_plan_mixed_tiles(int n, const int *ptr, const int *col, const double *val, const int *part, int npart,
                           int nlevel, int value_type, mpkg_plan **out);
+/* mpkg_plan_mixed_tiles with the part size chosen by measurement (no
+ * counterpart in the reference, whose part count is an input): for part
+ * sizes of 384, 512, 768, 1024 and 1536 rows it partitions the vertices by
+ * recursive coordinate bisection of coords (n x dim ints), builds the
+ * tile plan, times three executions on scratch vectors and keeps the
+ * fastest plan (info: npart, tune_candidates, tune_ms).  Same bits as
+ * mpkg_plan_mixed_tiles on that partition; MPKG_ERANGE when no size
+ * gives a plan. */
+int mpkg_plan_mixed_tiles_tuned(int n, const int *ptr, const int *col, const double *val, const int *coords, int dim,
+                                int nlevel, int value_type, mpkg_plan **out);
 /* e of the plan's scaling and the number of values the storage type
  * cannot represent exactly (0 means lossless, e.g. BF16 on stencils). */
 int mpkg_mixed_scale(const mpkg_plan *p, int *exponent, long *inexact_values);

@@ -76,7 +76,7 @@ class PlanInfo(C.Structure):
                 ("nnz", C.c_long), ("rows_computed", C.c_long), ("device_bytes", C.c_long),
                 ("launches", C.c_int), ("tiles_in_smem", C.c_int), ("max_tile_slots", C.c_int),
                 ("pipe_chunk", C.c_int), ("pipe_reach", C.c_int), ("pipe_grid", C.c_int),
-                ("tile_regs", C.c_int)]
+                ("tile_regs", C.c_int), ("tune_candidates", C.c_int), ("tune_ms", C.c_double)]
 
 
 def _declare(L):
@@ -149,6 +149,7 @@ def _declare(L):
         "mpkg_gen_banded": (I, [Lg, I, I, I, C.c_uint64, C.POINTER(I), C.POINTER(Lg), pp, pp, pp]),
         "mpkg_plan_mixed": (I, [I, P, P, P, I, I, pp]),
         "mpkg_plan_mixed_tiles": (I, [I, P, P, P, P, I, I, I, pp]),
+        "mpkg_plan_mixed_tiles_tuned": (I, [I, P, P, P, P, I, I, I, pp]),
         "mpkg_mixed_scale": (I, [P, C.POINTER(I), C.POINTER(Lg)]),
         "mpkg_exec_mixed_device": (I, [P, P, P]),
         "mpkg_bufs_prepare": (I, [C.c_char_p]),
@@ -577,6 +578,15 @@ class Plan:
         part = _i32(part)
         return cls._make(lib().mpkg_plan_mixed_tiles, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val), _ptr(part),
                          npart, nlevel, value_type, a=a, nlevel=nlevel)
+
+    @classmethod
+    def mixed_tiles_tuned(cls, a: Csr, coords, nlevel, value_type=VALUE_F32):
+        """Plan.mixed_tiles with the part size chosen by timing RCB
+        partitions of coords (n x dim) into parts of 384..1536 rows;
+        info() gives the chosen npart."""
+        coords = _i32(coords)
+        return cls._make(lib().mpkg_plan_mixed_tiles_tuned, a.n, _ptr(a.ptr), _ptr(a.col), _ptr(a.val),
+                         _ptr(coords), coords.shape[1], nlevel, value_type, a=a, nlevel=nlevel)
 
     def mixed_scale(self):
         """(e, number of values the storage type rounds)."""

@@ -2017,6 +2017,8 @@ struct mpkg_plan {
   bool tm_on = false;
   int tm_w = 0, tm_grid = 0;
   size_t tm_smem = 0;
+  double tune_ms = 0.0;    // mpkg_plan_mixed_tiles_tuned: time spent choosing the part size
+  int tune_candidates = 0;  // part sizes it timed
   TileRegArgs tr{};  // register-resident tiles (replaces tm when every tile fits)
   bool tr_on = false;
   int tr_w = 0, tr_grid = 0;
@@ -4010,6 +4012,72 @@ int mpkg_plan_mixed_tiles(int n, const int *ptr, const int *col, const double *v
   return kOk;
 }
 
+int mpkg_plan_mixed_tiles_tuned(int n, const int *ptr, const int *col, const double *val, const int *coords, int dim,
+                                int nlevel, int value_type, mpkg_plan **out) {
+  clear_error();
+  if (!out) return fail(kEInval, "out is null");
+  *out = nullptr;
+  if (n <= 0 || !coords || dim <= 0) return fail(kEInval, "bad coordinates");
+  const std::vector<int> cvec(coords, coords + (long)n * dim);
+  float *scratch = nullptr;
+  if (cudaMalloc(&scratch, sizeof(float) * (size_t)n * (nlevel + 1)) != cudaSuccess)
+    return fail(kENoMem, "autotune scratch");
+  cudaMemset(scratch, 0, sizeof(float) * (size_t)n * (nlevel + 1));  // timing only: the values do not matter
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  mpkg_plan *best = nullptr;
+  float best_ms = 0.f;
+  int tried = 0, last_rc = kOk;
+  std::string last_msg;
+  const auto t_start = std::chrono::steady_clock::now();
+  for (int rows : {384, 512, 768, 1024, 1536}) {  // part sizes, rows per part
+    const int npart = std::max(1, (n + rows - 1) / rows);
+    std::vector<int> part;
+    if (partition_rcb(n, cvec, dim, npart, &part) != kOk) continue;
+    mpkg_plan *p = nullptr;
+    int rc = mpkg_plan_mixed_tiles(n, ptr, col, val, part.data(), npart, nlevel, value_type, &p);
+    if (rc) {  // e.g. the tiles' level vectors exceed shared memory: the next size
+      last_rc = rc;
+      last_msg = mpkg_last_error();
+      continue;
+    }
+    tried++;
+    float ms = 0.f;
+    for (int w = 0; w < 2 && !rc; w++) rc = mpkg_exec_mixed_device(p, scratch, p->stream);
+    if (!rc && cudaEventRecord(e0, p->stream) != cudaSuccess) rc = fail(kECuda, "event record");
+    for (int w = 0; w < 3 && !rc; w++) rc = mpkg_exec_mixed_device(p, scratch, p->stream);
+    if (!rc && cudaEventRecord(e1, p->stream) != cudaSuccess) rc = fail(kECuda, "event record");
+    if (!rc) rc = mpkg_sync(p, p->stream);
+    if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = fail(kECuda, "event time");
+    if (rc) {
+      mpkg_plan_destroy(p);
+      if (best) mpkg_plan_destroy(best);
+      best = nullptr;
+      break;
+    }
+    if (!best || ms < best_ms) {
+      if (best) mpkg_plan_destroy(best);
+      best = p;
+      best_ms = ms;
+    } else {
+      mpkg_plan_destroy(p);
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(scratch);
+  if (!best) {
+    if (tried == 0 && last_rc) return fail(last_rc, last_msg.c_str());
+    return last_rc ? fail(last_rc, last_msg.c_str()) : fail(kERange, "no part size gives a tile plan");
+  }
+  best->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  best->tune_candidates = tried;
+  clear_error();
+  *out = best;
+  return kOk;
+}
+
 int mpkg_mixed_scale(const mpkg_plan *p, int *exponent, long *inexact_values) {
   if (!p || p->exec != MPKG_EXEC_MIXED) return fail(kEInval, "not a mixed-precision plan");
   if (exponent) *exponent = p->mix_e;
@@ -4127,6 +4195,8 @@ int mpkg_plan_info(const mpkg_plan *p, mpkg_plan_info_t *info) {
   info->pipe_reach = p->pipe_reach;
   info->pipe_grid = p->pipe_grid;
   info->tile_regs = p->tr_on ? 1 : 0;
+  info->tune_candidates = p->tune_candidates;
+  info->tune_ms = p->tune_ms;
   return kOk;
 }
 

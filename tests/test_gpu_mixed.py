@@ -263,6 +263,26 @@ def test_mixed_register_tiles_bitwise_equal_wavefront(case, vt, gpu):
     assert np.array_equal(again.view(np.uint32), want.view(np.uint32))
 
 
+def test_mixed_tiles_tuned_part_size(gpu):
+    """The part-size autotuner times RCB partitions into parts of 384 to
+    1536 rows and keeps the fastest tile plan; whatever it picks gives
+    the wavefront's bits."""
+    a = M.Csr.diffusion(256, 200, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=6)
+    k = 8
+    plan = M.Plan.mixed_tiles_tuned(a, _grid2(256, 200), k, M.VALUE_F32)
+    inf = plan.info()
+    assert inf["tune_candidates"] >= 3 and inf["tune_ms"] > 0
+    assert inf["npart"] in {-(-a.n // rows) for rows in (384, 512, 768, 1024, 1536)}
+    assert inf["tile_regs"] == 1
+    x = M.uniform(17, a.n)
+    got = _mixed_bits(plan, x, k, a.n)
+    plan.close()
+    wave = M.Plan.mixed(a, k, M.VALUE_F32)
+    want = _mixed_bits(wave, x, k, a.n)
+    wave.close()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
 @pytest.mark.parametrize("vt", [M.VALUE_F32, M.VALUE_BF16])
 def test_mixed_register_tiles_empty_rows_vs_fp32_oracle(vt, gpu):
     """The register tile kernel on isolated vertices (empty rows: every
