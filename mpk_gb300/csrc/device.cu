@@ -3850,11 +3850,15 @@ int reg_tiles_setup(mpkg_plan *p, const TilePlan &tp, const int *ptr, const void
   };
   const int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   std::atomic<int> next{0};
+  auto work = [&] {
+    for (int q; (q = next.fetch_add(1)) < npart && !bad;) build(q);
+  };
   std::vector<std::thread> pool;
-  for (int t = 0; t < nth; t++)
-    pool.emplace_back([&] {
-      for (int q; (q = next.fetch_add(1)) < npart && !bad;) build(q);
-    });
+  try {
+    for (int t = 1; t < nth; t++) pool.emplace_back(work);
+  } catch (const std::exception &) {  // no more threads: the caller's thread does the rest
+  }
+  work();
   for (auto &th : pool) th.join();
   if (bad) return fail(kEStruct, "tile column outside the halo");
   unsigned char *dvimg = nullptr, *dmimg = nullptr;
