@@ -330,8 +330,28 @@ mpkg_plan *plan_for(mpk_t *mg, const double *val, int kind) {
   }
   off[nl] = (long)idx.size();
   mpkg_plan *p = nullptr;
-  int rc = mpkg_plan_tasks(mg->n, mg->g0->ptr, mg->g0->col, val, mg->npart, mg->nlevel, mg->nphase,
-                           off.data(), idx.data(), legacy_arith(), &p);
+  // Task lists that cover every (level, vertex) write every entry of vv
+  // levels 1..nlevel, each with its row's FMA chain in CSR order whichever
+  // task computes it; the wavefront computes each entry once and gives the
+  // same bits, so it runs such lists (PA1 and every complete DMPK list
+  // set).  Lists that leave entries untouched keep the task executor.
+  const long n = mg->n, cells = n * mg->nlevel;
+  std::vector<unsigned char> cov((size_t)cells, 0);
+  long covered = 0;
+  for (long v : idx) {
+    const long l = v / n, i = v - l * n;
+    if (l >= 1 && l <= mg->nlevel && !cov[(size_t)((l - 1) * n + i)]) {
+      cov[(size_t)((l - 1) * n + i)] = 1;
+      covered++;
+    }
+  }
+  int rc = 1;
+  if (covered == cells) {
+    rc = mpkg_plan_wave(mg->n, mg->g0->ptr, mg->g0->col, val, mg->nlevel, legacy_arith(), &p);
+    if (rc) clear_error();
+  }
+  if (rc) rc = mpkg_plan_tasks(mg->n, mg->g0->ptr, mg->g0->col, val, mg->npart, mg->nlevel, mg->nphase,
+                               off.data(), idx.data(), legacy_arith(), &p);
   if (rc) return nullptr;
   g_plans[key] = p;
   return p;
