@@ -1539,8 +1539,7 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // One entry's operands in registers: FP32 values beside packed byte
-// offsets; BF16 values packed with their offset in one word (value bits
-// in the high half are the FP32 value itself).
+// offsets.
 template <typename VT, int W>
 struct TrRow;
 template <int W>
@@ -1564,20 +1563,16 @@ struct TrRow<float, W> {
   }
 };
 template <int W>
-struct TrRow<__nv_bfloat16, W> {
-  uint32_t w[W];
+struct TrRow<__nv_bfloat16, W> : TrRow<float, W> {
+  // BF16 values widened once, as the tile enters the registers (a BF16
+  // value is the high half of its FP32 bit pattern): the level loop is the
+  // FP32 one, and only the image in HBM and shared memory is narrower.
   __device__ __forceinline__ void load(const uint32_t *cols, const __nv_bfloat16 *vals) {
     const uint16_t *vb = reinterpret_cast<const uint16_t *>(vals);
 #pragma unroll
-    for (int t = 0; t < W; t++) w[t] = ((uint32_t)vb[32 * t] << 16) | ((cols[32 * (t / 2)] >> (16 * (t & 1))) & 0xFFFFu);
-  }
-  __device__ __forceinline__ float sum(const unsigned char *in) const {
-    float s = 0.f;
+    for (int t = 0; t < W; t++) this->v[t] = __uint_as_float((uint32_t)vb[32 * t] << 16);
 #pragma unroll
-    for (int t = 0; t < W; t++)
-      s = __fmaf_rn(__uint_as_float(w[t] & 0xFFFF0000u), *reinterpret_cast<const float *>(in + (w[t] & 0xFFFFu)),
-                    s);
-    return s;
+    for (int p = 0; p < (W + 1) / 2; p++) this->c[p] = cols[32 * p];
   }
 };
 
