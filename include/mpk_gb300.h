@@ -401,9 +401,10 @@ int mpkg_debug_pipe_stall(mpkg_plan *p, int extra_levels);
  * checked on the device before anything is computed: a column outside
  * [0, n) returns MPKG_ERANGE, a ptr that decreases or does not start at 0
  * (or a matrix without entries) MPKG_EINVAL, and vv is then left as it was;
- * col and val must hold ptr[n] entries.  It calls no allocating routine.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) with that device current; make that
- * first call before any stream capture.  All calls share the one array and
+ * col and val must hold ptr[n] entries.  It calls no allocating routine.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the one array and
  * it keeps the last call's contents (each call clears what must start at
  * zero), so calls that overlap on the GPU race.  The call waits for its
  * kernels (stream may be NULL) and returns MPKG_ETIMEOUT if a bounded wait
