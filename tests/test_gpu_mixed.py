@@ -225,7 +225,7 @@ def _stencil2(nx, ny, offsets, seed):
     return M.Csr(np.cumsum(ptr).astype(np.int32), c.astype(np.int32), v)
 
 
-@pytest.mark.parametrize("case", ["lap5", "diff9", "wide11", "k1", "k2", "k12", "bigparts"])
+@pytest.mark.parametrize("case", ["lap5", "diff9", "wide11", "k1", "k2", "k12", "k20", "bigparts"])
 @pytest.mark.parametrize("vt", [M.VALUE_F32, M.VALUE_BF16])
 def test_mixed_register_tiles_bitwise_equal_wavefront(case, vt, gpu):
     """Tiles whose computed rows fit the register-resident kernel (at most
@@ -233,9 +233,9 @@ def test_mixed_register_tiles_bitwise_equal_wavefront(case, vt, gpu):
     with the next tile's images streaming in while a tile computes; the
     bits equal the wavefront schedule's.  Row widths 5, 9 and 11 (padded
     to 12) select the kernel's three widths; k = 1 and 2 cover the x
-    gather right after the first level, k = 12 small parts with deep
-    skirts.  Larger tiles keep the general tile kernel."""
-    k = {"k1": 1, "k2": 2, "k12": 12, "wide11": 5, "bigparts": 4}.get(case, 8)
+    gather right after the first level, k = 12 and 20 small parts with
+    deep skirts (20 levels of shells in the tile header).  Larger tiles keep the general tile kernel."""
+    k = {"k1": 1, "k2": 2, "k12": 12, "k20": 20, "wide11": 5, "bigparts": 4}.get(case, 8)
     if case == "lap5":
         a = M.Csr.laplacian(300, 200, 1, diag=4.0, off=-1.0)
         part, npart = M.partition_rcb(_grid2(300, 200), 240), 240
@@ -247,7 +247,8 @@ def test_mixed_register_tiles_bitwise_equal_wavefront(case, vt, gpu):
         a = M.Csr.laplacian(64, 64, 4, diag=6.0, off=-1.0)
         part, npart = M.partition_rcb(a.coords, 4), 4
     else:
-        nx, ny, npart = {"diff9": (256, 200, 400), "k12": (128, 128, 256)}.get(case, (128, 128, 100))
+        nx, ny, npart = {"diff9": (256, 200, 400), "k12": (128, 128, 256),
+                         "k20": (96, 96, 1152)}.get(case, (128, 128, 100))
         a = M.Csr.diffusion(nx, ny, sigma=1.0, wx=1.0, wy=0.1, wdiag=0.5, dominance=0.01, seed=5)
         part = M.partition_rcb(_grid2(nx, ny), npart)
     x = M.uniform(13, a.n)
