@@ -853,10 +853,12 @@ __device__ __forceinline__ bool wave_wait(const WaveArgs &a, int b, unsigned int
   return *s_abort == 0;
 }
 
+// Release of a CTA's level: the barrier orders the CTA's row writes before
+// thread 0's store, and the store's release (a GPU-scope acq_rel fence
+// followed by the store) is cumulative over them, so no separate fence.
 __device__ __forceinline__ void wave_publish(const WaveArgs &a, int b, unsigned int v) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.flags + b), "r"(v) : "memory");
   }
 }
@@ -1831,9 +1833,8 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
         }
         VecF<VW>::st(dst + (size_t)i * nrhs, acc);
       }
-      __syncthreads();
+      __syncthreads();  // as in wave_publish: the release store is cumulative
       if (threadIdx.x == 0) {
-        __threadfence();
         asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.flags + b), "r"(tag + (unsigned)l) : "memory");
       }
     }
