@@ -404,7 +404,9 @@ def bench_batch(M, torch, args, flush, stream):
     N = sum(m.n for m in mats)
     nnz = sum(m.nnz for m in mats)
     t0 = time.perf_counter()
-    plan = M.Plan.batch(mats, nrhs, k, tune=True)
+    mode = {"tune": True, "default": False, "staged": M.BATCH_STAGED, "staged2": M.BATCH_STAGED2,
+            "staged4": M.BATCH_STAGED4}[args.batch_mode]
+    plan = M.Plan.batch(mats, nrhs, k, tune=mode)
     plan_s = time.perf_counter() - t0
     X = M.uniform(1, N * nrhs).astype(np.float32)
     d = torch.zeros((k + 1) * N * nrhs, dtype=torch.float32, device="cuda")
@@ -446,8 +448,10 @@ def bench_batch(M, torch, args, flush, stream):
             "value": N * nrhs * k / (ms * 1e-3) / 1e9, "unit": "G row-RHS powers/s",
             "algorithmic_bytes": B, "achieved_gbs": B / (ms * 1e-3) / 1e9, "frac_hbm": B / (ms * 1e-3) / 1e9 / peak,
             "rel_err_per_power_vs_fp64": errs, "error_sample": f"{len(sample)} of the {nm} matrices, all 16 RHS",
-            "plan_s": plan_s, "tuned": {kk: info[kk] for kk in ("lanes_per_row", "vector_width", "group_bytes",
-                                                               "ngroup", "grid", "graph", "candidates", "tune_ms")},
+            "plan_s": plan_s, "mode": args.batch_mode,
+            "tuned": {kk: info[kk] for kk in ("lanes_per_row", "vector_width", "group_bytes", "ngroup", "grid",
+                                              "threads", "staged", "window_bytes", "graph", "candidates",
+                                              "tune_ms")},
             "gpu_launches_per_step": 1}
 
 
@@ -580,6 +584,9 @@ def main():
     ap.add_argument("--no-variants", action="store_true", help="time only the selected executor")
     ap.add_argument("--sections", default="variants,mixed,batched,sstep,prep",
                     help="comma list of the extra sections to run (variants, mixed, batched, sstep, prep; 'none')")
+    ap.add_argument("--batch-mode", default="tune", choices=["tune", "default", "staged", "staged2", "staged4"],
+                    help="batched section's kernel configuration: autotuned (the workload) or one fixed "
+                         "configuration (for a profiler capture)")
     ap.add_argument("--batch-mats", type=int, default=256,
                     help="matrices of the batched section (256 = the workload; fewer for a profiler capture)")
     args = ap.parse_args()

@@ -160,9 +160,21 @@ int mpkg_plan_wave_ctas(int n, const int *ptr, const int *col, const double *val
  * (nlevel+1) * N * nrhs, N = sum of n[m]; level l of matrix m starts at
  * (l*N + row0[m]) * nrhs, row0[m] = n[0] + ... + n[m-1], each row's nrhs
  * values contiguous; level 0 is the input.  Entries are accumulated with
- * FP32 FMA in CSR order.  tune != 0 times every kernel configuration
- * (lanes per row x vector width, L2 group size, CTAs per SM) on these
- * matrices at plan time and keeps the fastest. */
+ * FP32 FMA in CSR order.  tune = MPKG_BATCH_TUNE times every kernel
+ * configuration (lanes per row x vector width, L2 group size, CTAs per SM,
+ * and for nrhs a multiple of 4 the kernel that stages each CTA's window of
+ * the previous level in shared memory) on these matrices at plan time and
+ * keeps the fastest; MPKG_BATCH_DEFAULT takes the first configuration
+ * untimed, MPKG_BATCH_STAGED / MPKG_BATCH_STAGED2 / MPKG_BATCH_STAGED4 the
+ * staged kernel at one, two or four CTAs per SM untimed (EINVAL when nrhs
+ * is not a multiple of 4).  All configurations give the same bits. */
+enum {
+  MPKG_BATCH_DEFAULT = 0,
+  MPKG_BATCH_TUNE = 1,
+  MPKG_BATCH_STAGED = 2,
+  MPKG_BATCH_STAGED2 = 3,
+  MPKG_BATCH_STAGED4 = 4
+};
 int mpkg_plan_batch(int nmat, const int *n, const int *const *ptr, const int *const *col, const float *const *val,
                     int nrhs, int nlevel, int tune, mpkg_plan **out);
 typedef struct {
@@ -175,6 +187,9 @@ typedef struct {
   int candidates;                  /* configurations timed by the autotuner */
   double tune_ms;                  /* autotuning time at plan creation */
   long device_bytes;
+  int staged;                      /* 1: previous level windowed in shared memory */
+  int threads;                     /* CTA size */
+  long window_bytes;               /* staged: shared-memory window per CTA */
 } mpkg_batch_info_t;
 int mpkg_batch_info(const mpkg_plan *p, mpkg_batch_info_t *info);
 /* d_vb: device buffer as above (16-byte aligned), level 0 filled. */

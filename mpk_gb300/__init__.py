@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(_HERE, "libmpk_gb300.so")
 
 OK, EINVAL, EIO, EFORMAT, ESTRUCT, ECUDA, ETIMEOUT, ENOMEM, ERANGE = 0, -1, -2, -3, -4, -5, -6, -7, -8
 ARITH_FMA, ARITH_SEPARATE, ARITH_DF64, ARITH_FIXED = 0, 1, 2, 3
+BATCH_DEFAULT, BATCH_TUNE, BATCH_STAGED, BATCH_STAGED2, BATCH_STAGED4 = 0, 1, 2, 3, 4
 EXEC_TASKS, EXEC_TILES, EXEC_PIPE, EXEC_SPMV, EXEC_BUFS, EXEC_MIXED, EXEC_PDMPK, EXEC_WAVE, EXEC_BATCH = \
     0, 1, 2, 3, 4, 5, 6, 7, 8
 PD_PART_BLOCKSHIFT, PD_PART_BFS, PD_PART_METIS = 0, 1, 2
@@ -61,7 +62,8 @@ class BatchInfo(C.Structure):
     _fields_ = [("nmat", C.c_int), ("nrhs", C.c_int), ("nlevel", C.c_int), ("rows", C.c_long), ("nnz", C.c_long),
                 ("lanes_per_row", C.c_int), ("vector_width", C.c_int), ("group_bytes", C.c_long),
                 ("ngroup", C.c_int), ("grid", C.c_int), ("graph", C.c_int), ("candidates", C.c_int),
-                ("tune_ms", C.c_double), ("device_bytes", C.c_long)]
+                ("tune_ms", C.c_double), ("device_bytes", C.c_long), ("staged", C.c_int), ("threads", C.c_int),
+                ("window_bytes", C.c_long)]
 
 
 class CgInfo(C.Structure):
@@ -610,7 +612,10 @@ class Plan:
     @classmethod
     def batch(cls, mats, nrhs, nlevel, tune=True):
         """Batched block-vector form over a list of Csr (values cast to
-        FP32): one persistent launch replayed as a CUDA graph."""
+        FP32): one persistent launch replayed as a CUDA graph.  tune: True
+        (BATCH_TUNE, time every configuration), False (BATCH_DEFAULT), or
+        BATCH_STAGED / BATCH_STAGED2 / BATCH_STAGED4 (the shared-memory
+        window kernel at one, two or four CTAs per SM, untimed)."""
         keep = []
         n = np.array([m.n for m in mats], dtype=np.int32)
         arrs = []
@@ -624,7 +629,8 @@ class Plan:
         vals = (C.c_void_p * len(mats))(*[t[2].ctypes.data for t in keep])
         h = C.c_void_p()
         _check(lib().mpkg_plan_batch(len(mats), _ptr(n), C.cast(ptrs, C.c_void_p), C.cast(cols, C.c_void_p),
-                                     C.cast(vals, C.c_void_p), nrhs, nlevel, 1 if tune else 0, C.byref(h)))
+                                     C.cast(vals, C.c_void_p), nrhs, nlevel,
+                                     int(tune) if not isinstance(tune, bool) else (1 if tune else 0), C.byref(h)))
         p = Plan.__new__(Plan)
         p._h = h
         p.n, p.nlevel, p.nrhs = int(n.sum()), nlevel, nrhs

@@ -1741,6 +1741,7 @@ struct BatchArgs {
   const int *dep_idx;          // dep_idx[dep_ptr[g*nblk+b] ..), the other CTAs owning its columns
   unsigned int *flags;
   int *err;
+  const int *win;              // staged form: ngroup * nblk pairs [w0, w1) of previous-level rows in smem
 };
 
 template <int VW>
@@ -1834,6 +1835,106 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
         VecF<VW>::st(dst + (size_t)i * nrhs, acc);
       }
       __syncthreads();  // as in wave_publish: the release store is cumulative
+      if (threadIdx.x == 0) {
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.flags + b), "r"(tag + (unsigned)l) : "memory");
+      }
+    }
+  }
+}
+
+// The batched rows with the previous level staged in shared memory.  Per
+// (group, level) the CTA copies rows [w0, w1) of the previous level (its
+// own rows and the halo its columns reach, as far as the window holds)
+// with one bulk copy on an mbarrier; an entry whose column falls in the
+// window reads shared memory, any other reads global memory through the
+// same generic load.  Rows of the window that no row of the CTA reads may
+// be stale: they are never used.  Same rows, CSR order and FMAs as
+// batch_kernel, so the same bits.
+template <int LPR, int VW>
+__global__ void __launch_bounds__(1024) batch_stage_kernel(BatchArgs a) {
+  extern __shared__ __align__(128) float bs_win[];
+  __shared__ int s_abort;
+  __shared__ __align__(8) unsigned long long s_bar;
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    mbar_init(&s_bar);
+  }
+  __syncthreads();
+  unsigned phase = 0;
+  const int b = blockIdx.x, nrhs = LPR * VW;
+  const int lane = (int)threadIdx.x % LPR, rpp = (int)blockDim.x / LPR;
+  for (int g = 0; g < a.ngroup; g++) {
+    const int r0 = a.row_lo[(size_t)g * (a.nblk + 1) + b], r1 = a.row_lo[(size_t)g * (a.nblk + 1) + b + 1];
+    const unsigned tag = a.base + (unsigned)g * (unsigned)(a.nlevel + 1);
+    const int dlo = a.dep_ptr[(size_t)g * a.nblk + b], dhi = a.dep_ptr[(size_t)g * a.nblk + b + 1];
+    const int w0 = a.win[2 * ((size_t)g * a.nblk + b)], w1 = a.win[2 * ((size_t)g * a.nblk + b) + 1];
+    const unsigned wn = (unsigned)(w1 - w0);
+    for (int l = 1; l <= a.nlevel; l++) {
+      if (l > 1) {  // the CTAs owning this range's columns have published level l-1 of group g
+        for (int k = dlo + (int)threadIdx.x; k < dhi; k += blockDim.x) {
+          const int c = a.dep_idx[k];
+          long spins = 0;
+          while (ld_acquire(a.flags + c) < tag + (unsigned)(l - 1) + a.stall) {
+            if (++spins > kSpinLimit || *((volatile int *)a.err)) {
+              atomicCAS(a.err, 0, kErrTimeout);
+              s_abort = 1;
+              break;
+            }
+            __nanosleep(spins < 16 ? 32 : 256);
+          }
+        }
+        __syncthreads();
+        if (s_abort) return;
+      }
+      const float *src = a.vb + (size_t)(l - 1) * a.N * nrhs;
+      if (wn > 0) {
+        if (threadIdx.x == 0) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the window first
+          const unsigned bytes = wn * (unsigned)nrhs * 4u;
+          mbar_expect(&s_bar, bytes);
+          bulk_g2s(bs_win, src + (size_t)w0 * nrhs, bytes, &s_bar);
+        }
+        if (!tr_wait(&s_bar, phase, a.err)) return;
+        phase ^= 1u;
+      }
+      const float *gl = src + lane * VW;
+      const float *wl = bs_win + lane * VW;
+      float *dst = a.vb + (size_t)l * a.N * nrhs + lane * VW;
+      for (int i = r0 + (int)threadIdx.x / LPR; i < r1; i += rpp) {
+        float acc[VW];
+#pragma unroll
+        for (int u = 0; u < VW; u++) acc[u] = 0.0f;
+        const int q0 = __ldg(a.ptr + i), q1 = __ldg(a.ptr + i + 1);
+        int q = q0;
+        for (; q + 4 <= q1; q += 4) {
+          const float *xp[4];
+          float v[4], xv[4][VW];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const int c = __ldg(a.col + q + u);
+            v[u] = __ldg(a.val + q + u);
+            const unsigned o = (unsigned)(c - w0);
+            xp[u] = o < wn ? wl + (size_t)o * nrhs : gl + (size_t)c * nrhs;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) VecF<VW>::ld(xp[u], xv[u]);
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int w = 0; w < VW; w++) acc[w] = __fmaf_rn(v[u], xv[u][w], acc[w]);
+        }
+        for (; q < q1; q++) {
+          float x0[VW];
+          const int c = __ldg(a.col + q);
+          const float v0 = __ldg(a.val + q);
+          const unsigned o = (unsigned)(c - w0);
+          VecF<VW>::ld(o < wn ? wl + (size_t)o * nrhs : gl + (size_t)c * nrhs, x0);
+#pragma unroll
+          for (int u = 0; u < VW; u++) acc[u] = __fmaf_rn(v0, x0[u], acc[u]);
+        }
+        VecF<VW>::st(dst + (size_t)i * nrhs, acc);
+      }
+      __syncthreads();  // rows written and the window read; the release store is cumulative
       if (threadIdx.x == 0) {
         asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.flags + b), "r"(tag + (unsigned)l) : "memory");
       }
@@ -1995,6 +2096,9 @@ struct mpkg_plan {
   // batched block-vector form
   BatchArgs batch{};
   int batch_lpr = 0, batch_vw = 0, batch_nmat = 0;
+  int batch_threads = 256;   // CTA size of the persistent launch
+  bool batch_staged = false; // batch_stage_kernel: previous level windowed in shared memory
+  size_t batch_smem = 0;     // its window bytes per CTA
   long batch_group_bytes = 0;
   double batch_tune_ms = 0.0;
   int batch_candidates = 0;
@@ -2298,6 +2402,13 @@ BatchKernel batch_kernel_for(int lpr, int vw) {
   return nullptr;
 }
 
+BatchKernel batch_stage_kernel_for(int lpr, int vw) {
+#define MPKG_BK(L, V) if (lpr == L && vw == V) return batch_stage_kernel<L, V>;
+  MPKG_BK(1, 4) MPKG_BK(2, 4) MPKG_BK(4, 4) MPKG_BK(8, 4) MPKG_BK(16, 4) MPKG_BK(32, 4)
+#undef MPKG_BK
+  return nullptr;
+}
+
 // Host description of the concatenated matrices.
 struct BatchHost {
   long N = 0;
@@ -2308,9 +2419,12 @@ struct BatchHost {
 
 // Groups of consecutive matrices within `budget` bytes (matrix + two
 // levels of vectors); per group, CTA row ranges of equal nonzeros and the
-// CTAs owning each range's columns.
-void batch_layout(const BatchHost &h, int nrhs, long budget, int grid, std::vector<int> *row_lo,
-                  std::vector<int> *dptr, std::vector<int> *didx, int *ngroup) {
+// CTAs owning each range's columns.  With cap_rows > 0, also each (group,
+// CTA)'s window [w0, w1) of previous-level rows for shared memory: the span
+// of its columns when that fits cap_rows rows, else cap_rows rows around
+// its own rows (columns beyond are read from global memory).
+void batch_layout(const BatchHost &h, int nrhs, long budget, int grid, long cap_rows, std::vector<int> *row_lo,
+                  std::vector<int> *dptr, std::vector<int> *didx, std::vector<int> *win, int *ngroup) {
   const int nmat = (int)h.mat_row0.size() - 1;
   std::vector<long> g0(1, 0);
   long bytes = 0;
@@ -2327,6 +2441,7 @@ void batch_layout(const BatchHost &h, int nrhs, long budget, int grid, std::vect
   *ngroup = (int)g0.size() - 1;
   row_lo->assign((size_t)*ngroup * (grid + 1), 0);
   dptr->assign((size_t)*ngroup * grid + 1, 0);
+  win->assign((size_t)*ngroup * grid * 2, 0);
   didx->clear();
   std::vector<int> seen(grid, -1);
   for (int g = 0; g < *ngroup; g++) {
@@ -2353,6 +2468,22 @@ void batch_layout(const BatchHost &h, int nrhs, long budget, int grid, std::vect
       }
       std::sort(didx->begin() + first, didx->end());
       (*dptr)[u + 1] = (int)didx->size();
+      if (cap_rows > 0 && lo[b + 1] > lo[b]) {
+        long cmin = lo[b], cmax = lo[b + 1] - 1;
+        for (long q = h.ptr[lo[b]]; q < h.ptr[lo[b + 1]]; q++) {
+          cmin = std::min<long>(cmin, h.col[q]);
+          cmax = std::max<long>(cmax, h.col[q]);
+        }
+        long w0 = cmin, w1 = cmax + 1;
+        if (w1 - w0 > cap_rows) {  // around the own rows, within the column span
+          const long own = lo[b + 1] - lo[b];
+          w0 = own >= cap_rows ? lo[b] : std::max(cmin, lo[b] - (cap_rows - own) / 2);
+          w1 = std::min(cmax + 1, w0 + cap_rows);
+          w0 = std::max(cmin, w1 - cap_rows);
+        }
+        (*win)[2 * u] = (int)w0;
+        (*win)[2 * u + 1] = (int)w1;
+      }
     }
     std::fill(seen.begin(), seen.end(), -1);
   }
@@ -2378,14 +2509,18 @@ int batch_launch_raw(mpkg_plan *p, float *d_vb, cudaStream_t st, bool capture) {
   if (capture) CUDA_TRY(cudaMemsetAsync(a.flags, 0, sizeof(unsigned int) * (size_t)a.nblk, st));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(a.nblk);
-  cfg.blockDim = dim3(256);
+  cfg.blockDim = dim3(p->batch_threads);
+  cfg.dynamicSmemBytes = p->batch_staged ? p->batch_smem : 0;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  CUDA_TRY(cudaLaunchKernelEx(&cfg, batch_kernel_for(p->batch_lpr, p->batch_vw), a));
+  CUDA_TRY(cudaLaunchKernelEx(&cfg,
+                              p->batch_staged ? batch_stage_kernel_for(p->batch_lpr, p->batch_vw)
+                                              : batch_kernel_for(p->batch_lpr, p->batch_vw),
+                              a));
   return kOk;
 }
 
@@ -3236,22 +3371,30 @@ extern "C" {
 namespace {
 
 // Device state of one (lpr, vw, budget, grid) configuration of a batch plan.
-int batch_configure(mpkg_plan *p, const BatchHost &h, int lpr, int vw, long budget, int grid) {
-  std::vector<int> lo, dlo, dhi;
+int batch_configure(mpkg_plan *p, const BatchHost &h, int lpr, int vw, long budget, int grid, bool staged,
+                    int threads, size_t smem) {
+  std::vector<int> lo, dlo, dhi, win;
   int ngroup = 0;
-  batch_layout(h, p->batch.nrhs, budget, grid, &lo, &dlo, &dhi, &ngroup);
+  const long cap_rows = staged ? (long)(smem / (4 * (size_t)p->batch.nrhs)) : 0;
+  batch_layout(h, p->batch.nrhs, budget, grid, cap_rows, &lo, &dlo, &dhi, &win, &ngroup);
   BatchArgs &a = p->batch;
   // previous layout arrays are freed with the plan (owned list); small
-  int *d_lo = nullptr, *d_dlo = nullptr, *d_dhi = nullptr;
+  int *d_lo = nullptr, *d_dlo = nullptr, *d_dhi = nullptr, *d_win = nullptr;
   unsigned int *d_flags = nullptr;
   int rc = dev_copy(p, &d_lo, lo.data(), lo.size());
   if (!rc) rc = dev_copy(p, &d_dlo, dlo.data(), dlo.size());
   if (!rc) rc = dev_copy(p, &d_dhi, dhi.data(), dhi.size());
+  if (!rc && staged) rc = dev_copy(p, &d_win, win.data(), win.size());
   if (!rc) rc = dev_alloc(p, &d_flags, (size_t)grid);
+  if (!rc && staged &&
+      cudaFuncSetAttribute((const void *)batch_stage_kernel_for(lpr, vw),
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    rc = fail(kECuda, "shared memory attribute");
   if (rc) return rc;
-  a.row_lo = d_lo; a.dep_ptr = d_dlo; a.dep_idx = d_dhi; a.flags = d_flags;
+  a.row_lo = d_lo; a.dep_ptr = d_dlo; a.dep_idx = d_dhi; a.flags = d_flags; a.win = d_win;
   a.nblk = grid; a.ngroup = ngroup; a.base = 0;
   p->batch_lpr = lpr; p->batch_vw = vw; p->batch_group_bytes = budget;
+  p->batch_staged = staged; p->batch_threads = threads; p->batch_smem = staged ? smem : 0;
   p->pipe_grid = grid;
   if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
   if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
@@ -3269,6 +3412,7 @@ int mpkg_plan_batch(int nmat, const int *n, const int *const *ptr, const int *co
   *out = nullptr;
   if (nlevel <= 0 || nlevel > 64) return fail(kEInval, "nlevel must be in [1, 64]");
   if (nrhs <= 0 || nrhs > 128 || (nrhs & (nrhs - 1)) != 0) return fail(kEInval, "nrhs must be a power of two <= 128");
+  if (tune < MPKG_BATCH_DEFAULT || tune > MPKG_BATCH_STAGED4) return fail(kEInval, "unknown tune mode");
   BatchHost h;
   h.mat_row0.assign(nmat + 1, 0);
   long nnz = 0;
@@ -3322,8 +3466,9 @@ int mpkg_plan_batch(int nmat, const int *n, const int *const *ptr, const int *co
   int nsm = 0;
   if (!rc && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
     rc = fail(kECuda, "device query failed");
-  // candidates: lanes x vector width covering nrhs, group budget, CTAs per SM
-  struct Cand { int lpr, vw; long budget; int grid; };
+  // candidates: lanes x vector width covering nrhs, group budget, CTAs per
+  // SM; and the staged kernel at one or two CTAs per SM
+  struct Cand { int lpr, vw; long budget; int grid; bool staged; int threads; size_t smem; };
   std::vector<Cand> cands;
   for (int vw : {4, 2, 1}) {
     if (nrhs % vw) continue;
@@ -3335,13 +3480,49 @@ int mpkg_plan_batch(int nmat, const int *n, const int *const *ptr, const int *co
     if (rc || per_sm <= 0) continue;
     for (long budget : {32L << 20, 64L << 20, 1L << 40})
       for (int occ : {per_sm, std::max(1, per_sm / 2)}) {
-        cands.push_back({lpr, vw, budget, std::max(1, std::min<int>(occ * nsm, (int)std::min<long>(h.N, INT32_MAX)))});
+        cands.push_back({lpr, vw, budget, std::max(1, std::min<int>(occ * nsm, (int)std::min<long>(h.N, INT32_MAX))),
+                         false, 256, 0});
         if (occ == std::max(1, per_sm / 2)) break;
       }
   }
+  if (!rc && nrhs % 4 == 0 && nrhs / 4 <= 32) {
+    int sm_per_sm = 0, sm_optin = 0;
+    if (cudaDeviceGetAttribute(&sm_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sm_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device) != cudaSuccess)
+      rc = fail(kECuda, "device query failed");
+    for (int ctas : {1, 2, 4}) {
+      if (rc) break;
+      const int threads = 1024 / ctas;
+      // a window of whole rows within the SM's share, less the static part and the per-CTA reserve
+      size_t smem = std::min<size_t>((size_t)sm_optin, (size_t)sm_per_sm / ctas) - 2048;
+      smem -= smem % (4 * (size_t)nrhs);
+      BatchKernel k = batch_stage_kernel_for(nrhs / 4, 4);
+      int per_sm = 0;
+      if (cudaFuncSetAttribute((const void *)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+              cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      if (per_sm <= 0) continue;
+      for (long budget : {32L << 20, 64L << 20, 1L << 40})
+        cands.push_back({nrhs / 4, 4, budget, std::max(1, std::min<int>(per_sm * nsm, (int)std::min<long>(h.N, INT32_MAX))),
+                         true, threads, smem});
+    }
+  }
   if (!rc && cands.empty()) rc = fail(kEInval, "no kernel configuration for this nrhs");
-  Cand best = cands.empty() ? Cand{1, 1, 0, 1} : cands[0];
-  if (!rc && tune && cands.size() > 1) {
+  Cand best = cands.empty() ? Cand{1, 1, 0, 1, false, 256, 0} : cands[0];
+  if (!rc && tune >= MPKG_BATCH_STAGED) {  // untimed staged configuration
+    const int want_threads = tune == MPKG_BATCH_STAGED ? 1024 : tune == MPKG_BATCH_STAGED2 ? 512 : 256;
+    bool found = false;
+    for (const Cand &c : cands)
+      if (c.staged && c.threads == want_threads && c.budget == (64L << 20)) {
+        best = c;
+        found = true;
+        break;
+      }
+    if (!found) rc = fail(kEInval, "no staged configuration for this nrhs and device");
+  } else if (!rc && tune == MPKG_BATCH_TUNE && cands.size() > 1) {
     // time every candidate on the plan's own matrices (zero input; the
     // arithmetic does not depend on the values)
     float *scratch = nullptr;
@@ -3356,7 +3537,7 @@ int mpkg_plan_batch(int nmat, const int *n, const int *const *ptr, const int *co
     auto t_start = std::chrono::steady_clock::now();
     for (const Cand &c : cands) {
       if (rc) break;
-      if ((rc = batch_configure(p, h, c.lpr, c.vw, c.budget, c.grid))) break;
+      if ((rc = batch_configure(p, h, c.lpr, c.vw, c.budget, c.grid, c.staged, c.threads, c.smem))) break;
       for (int w = 0; w < 2 && !rc; w++) rc = batch_launch_raw(p, scratch, p->stream, false);
       if (!rc && cudaEventRecord(e0, p->stream) != cudaSuccess) rc = fail(kECuda, "event record");
       for (int w = 0; w < 3 && !rc; w++) rc = batch_launch_raw(p, scratch, p->stream, false);
@@ -3373,7 +3554,8 @@ int mpkg_plan_batch(int nmat, const int *n, const int *const *ptr, const int *co
     if (scratch) cudaFree(scratch);
   }
   p->batch_candidates = (int)cands.size();
-  if (!rc) rc = batch_configure(p, h, best.lpr, best.vw, best.budget, best.grid);
+  if (!rc)
+    rc = batch_configure(p, h, best.lpr, best.vw, best.budget, best.grid, best.staged, best.threads, best.smem);
   if (rc) { mpkg_plan_destroy(p); return rc; }
   *out = p;
   return kOk;
@@ -3396,6 +3578,9 @@ int mpkg_batch_info(const mpkg_plan *p, mpkg_batch_info_t *info) {
   info->candidates = p->batch_candidates;
   info->tune_ms = p->batch_tune_ms;
   info->device_bytes = p->device_bytes;
+  info->staged = p->batch_staged ? 1 : 0;
+  info->threads = p->batch_threads;
+  info->window_bytes = (long)p->batch_smem;
   return kOk;
 }
 

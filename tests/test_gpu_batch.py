@@ -30,7 +30,7 @@ def _oracle(mats, X, nlevel):
 
 
 @pytest.mark.parametrize("nrhs", [4, 16, 32])
-@pytest.mark.parametrize("tune", [False, True])
+@pytest.mark.parametrize("tune", [False, True, M.BATCH_STAGED, M.BATCH_STAGED2, M.BATCH_STAGED4])
 def test_batch_bitwise_vs_oracle(small_batch, nrhs, tune, gpu):
     mats, k = small_batch, 6
     X = _inputs(mats, nrhs, 7)
@@ -43,6 +43,37 @@ def test_batch_bitwise_vs_oracle(small_batch, nrhs, tune, gpu):
     info = plan.batch_info()
     assert info["lanes_per_row"] * info["vector_width"] == nrhs
     assert info["nmat"] == len(mats) and info["rows"] == X.shape[0]
+    if not isinstance(tune, bool):
+        assert info["staged"] == 1
+        assert info["threads"] == {M.BATCH_STAGED: 1024, M.BATCH_STAGED2: 512, M.BATCH_STAGED4: 256}[tune]
+
+
+@pytest.mark.parametrize("mode", [M.BATCH_STAGED, M.BATCH_STAGED2, M.BATCH_STAGED4])
+@pytest.mark.parametrize("nrhs", [4, 32])
+def test_batch_staged_partial_windows(mode, nrhs, gpu):
+    """3-D stencils whose z-neighbours lie beyond the shared-memory window
+    (at 32 right-hand sides the window holds 0.4-1.8 K rows, the
+    z-stride is 1.6-2.5 K rows on each side; at 4 most spans fit): the
+    entries outside it are read from global memory, the bits stay the
+    oracle's.  Rows of 40-60 entries take the row loop's tail path."""
+    mats = [M.Csr.laplacian(40, 40, 40, diag=6.0, off=-1.0), M.Csr.diffusion(50, 50, 24, sigma=0.5, seed=3),
+            M.Csr.banded(5000, 64, 5, 30, seed=5), M.Csr.laplacian(7, 3, 1, diag=4.0, off=-1.0),
+            M.Csr.banded(3000, 64, 40, 60, seed=6)]
+    k = 5
+    X = _inputs(mats, nrhs, 11)
+    plan = M.Plan.batch(mats, nrhs, k, tune=mode)
+    info = plan.batch_info()
+    assert info["staged"] == 1 and info["window_bytes"] > 0
+    vb = np.zeros((k + 1,) + X.shape, dtype=np.float32)
+    vb[0] = X
+    plan.exec_batch_host(vb)
+    assert vb.tobytes() == _oracle(mats, X, k).tobytes()
+
+
+def test_batch_staged_needs_four_rhs(small_batch, gpu):
+    with pytest.raises(M.MpkError) as e:
+        M.Plan.batch(small_batch, 2, 3, tune=M.BATCH_STAGED)
+    assert e.value.code == M.EINVAL
 
 
 def test_batch_error_vs_fp64(small_batch, gpu):
@@ -81,13 +112,14 @@ def test_batch_graph_replay_device(small_batch, gpu):
     assert d.cpu().numpy().tobytes() == _oracle(mats, X, k).tobytes()
 
 
-def test_batch_wait_times_out_and_recovers(small_batch, gpu):
+@pytest.mark.parametrize("mode", [False, M.BATCH_STAGED, M.BATCH_STAGED4])
+def test_batch_wait_times_out_and_recovers(small_batch, mode, gpu):
     """The batched form's bounded waits give up on a flag that is never set
     (ETIMEOUT) and the same plan, its graph captured again, then runs bit
     for bit."""
     mats, k = small_batch, 6
     X = _inputs(mats, 16, 9)
-    plan = M.Plan.batch(mats, 16, k, tune=False)
+    plan = M.Plan.batch(mats, 16, k, tune=mode)
     plan.debug_stall(100)
     vb = np.zeros((k + 1,) + X.shape, dtype=np.float32)
     vb[0] = X
