@@ -70,6 +70,23 @@ def test_batch_staged_partial_windows(mode, nrhs, gpu):
     assert vb.tobytes() == _oracle(mats, X, k).tobytes()
 
 
+@pytest.mark.parametrize("nrhs", [64, 128])
+def test_batch_staged_wide_rows(small_batch, nrhs, gpu):
+    """16 and 32 lanes per row (float4 each) in the window kernel: the
+    window holds 0.2-0.9 K rows of 256-512 bytes, the bits stay the
+    oracle's."""
+    mats, k = small_batch[:6], 3
+    X = _inputs(mats, nrhs, 13)
+    for mode in (M.BATCH_STAGED2, M.BATCH_STAGED4):
+        plan = M.Plan.batch(mats, nrhs, k, tune=mode)
+        info = plan.batch_info()
+        assert info["staged"] == 1 and info["lanes_per_row"] == nrhs // 4
+        vb = np.zeros((k + 1,) + X.shape, dtype=np.float32)
+        vb[0] = X
+        plan.exec_batch_host(vb)
+        assert vb.tobytes() == _oracle(mats, X, k).tobytes()
+
+
 def test_batch_staged_needs_four_rhs(small_batch, gpu):
     with pytest.raises(M.MpkError) as e:
         M.Plan.batch(small_batch, 2, 3, tune=M.BATCH_STAGED)
