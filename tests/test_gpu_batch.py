@@ -73,7 +73,7 @@ def test_batch_staged_partial_windows(mode, nrhs, gpu):
 @pytest.mark.parametrize("nrhs", [64, 128])
 def test_batch_staged_wide_rows(small_batch, nrhs, gpu):
     """16 and 32 lanes per row (float4 each) in the window kernel: the
-    window holds 0.2-0.9 K rows of 256-512 bytes, the bits stay the
+    window holds 110-450 rows of 256-512 bytes, the bits stay the
     oracle's."""
     mats, k = small_batch[:6], 3
     X = _inputs(mats, nrhs, 13)
