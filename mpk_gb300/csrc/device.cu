@@ -550,51 +550,6 @@ __device__ __forceinline__ float2 pipe_row_df(int q0, int q1, const int *cols, c
   return df_norm(sh, sl);
 }
 
-template <bool VALUED>
-__global__ void __launch_bounds__(kPipeThreads, 8) pipe_df_kernel(PipeArgs a) {
-  extern __shared__ __align__(16) unsigned char pipe_smem[];
-  int *rptr = reinterpret_cast<int *>(pipe_smem);
-  int *cols_buf = reinterpret_cast<int *>(pipe_smem + pipe_cols_offset(a.chunk));
-  float2 *vals_buf = reinterpret_cast<float2 *>(pipe_smem + pipe_vals_offset(a.chunk, a.max_chunk_nnz));
-  __shared__ unsigned int s_chunk;
-  __shared__ int s_abort;
-  __shared__ __align__(8) unsigned long long s_bar;
-  unsigned phase = 0;
-  if (threadIdx.x == 0 && a.bulk_ok) mbar_init(&s_bar);
-  __syncthreads();
-  for (;;) {
-    int *cols;
-    float2 *vals;
-    const int c = pipe_take<float2, VALUED>(a, a.coef2, rptr, cols_buf, vals_buf, &cols, &vals, &s_bar, &phase,
-                                            &s_chunk, &s_abort);
-    if (c < 0) return;
-    const int r0 = c * a.chunk;
-    const int nr = min(a.chunk, a.n - r0);
-    const int r = threadIdx.x;
-    const bool active = r < nr;
-    const float2 cf = (!VALUED && active) ? a.coef2[r0 + r] : make_float2(0.f, 0.f);
-    const int q0 = rptr[r], q1 = active ? rptr[r + 1] : q0;
-    const int glo = a.gdep_lo[c], ghi = a.gdep_hi[c];
-    for (int l = 1; l <= a.nlevel; l++) {
-      if (l > 1 && !pipe_wait(a, glo, ghi, l - 1, &s_abort)) return;
-      float2 v;
-      if (l == 1) {  // level 1 reads x (FP64) and splits each gathered value
-        float sh = 0.f, sl = 0.f;
-        for (int q = q0; q < q1; q++) df_mac(VALUED ? vals[q] : cf, df_split(a.x[cols[q]]), sh, sl);
-        v = df_norm(sh, sl);
-      } else {
-        const float2 *src = a.ring + (long)((l - 1) & 1) * a.n;
-        v = pipe_row_df<VALUED>(q0, q1, cols, vals, cf, src);
-      }
-      if (active) {
-        a.ring[(long)(l & 1) * a.n + r0 + r] = v;
-        a.vv[(long)l * a.n + r0 + r] = df_to_double(v);
-      }
-      pipe_publish(a, c, l);
-    }
-  }
-}
-
 // ------------------------------------------------------------------------
 // Dataflow pipeline.  Work items are (chunk, level) pairs in a precomputed
 // topological order: key = chunk + D*(level-1), D larger than the
