@@ -849,11 +849,6 @@ __device__ __forceinline__ int ld_off(const short *p) {
   return (int)__ldg(p);
 }
 
-template <bool REL>
-__device__ __forceinline__ int wave_col(const WaveArgs &a, long e, int i) {
-  return REL ? i + (int)__ldg(a.srel + e) : __ldg(a.scol + e);
-}
-
 // One row's sum over its entries (CSR order): the row's int16 offsets are
 // RS apart (32: per-lane layout, a constant after inlining; 1: a slice's
 // shared list), values and int32 columns 32 apart.  Up to 8 (12 for FP32) entries have all their
