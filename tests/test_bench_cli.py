@@ -34,3 +34,12 @@ def test_profile_commands_use_known_flags():
                     assert w in out, f"{name}: {w}"
                 if w in ("&&", ">", "2>&1"):
                     break
+
+
+def test_profile_commands_run_committed_files_only():
+    """The commands in profiles/ name no working-directory scripts."""
+    prof = os.path.join(ROOT, "profiles")
+    for name in sorted(os.listdir(prof)):
+        if name.endswith(".md"):
+            text = open(os.path.join(prof, name)).read()
+            assert "_work/" not in text, name
