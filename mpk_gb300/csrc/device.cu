@@ -934,6 +934,8 @@ __device__ __forceinline__ float mix_row(int len, int RS, const short *cr, const
   return s;
 }
 
+constexpr int kWaveXGroups = 8;  // host execution: CTA groups that copy x in turn
+
 // FP64 rows (fma or separate multiply/add, CSR order as the reference).
 // A warp computes one 32-row slice; CTA row ranges start on slices.  The
 // previous level is read from vv: every address of it is fresh in this
@@ -952,6 +954,28 @@ __global__ void __launch_bounds__(256, 4) wave_kernel(WaveArgs a) {
   const unsigned char *s_len = wave_smem + a.stage_rel_bytes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (a.hv) {  // x from the host mapping into the device copy, own rows
+    // in kWaveXGroups groups of CTAs taken in order: group g copies once
+    // group g-1 has published level 0, so the first groups' levels already
+    // travel down the host link (which carries both directions at once)
+    // while the later groups' x still travels up
+    const int grp = (int)((long)b * kWaveXGroups / a.nblk);
+    if (grp > 0) {
+      const int c0 = (int)(((long)(grp - 1) * a.nblk + kWaveXGroups - 1) / kWaveXGroups);
+      const int c1 = (int)(((long)grp * a.nblk + kWaveXGroups - 1) / kWaveXGroups);
+      for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x) {
+        long spins = 0;
+        while (ld_acquire(a.flags + c) < a.base + a.stall) {
+          if (++spins > kSpinLimit || *((volatile int *)a.err)) {
+            atomicCAS(a.err, 0, kErrTimeout);
+            s_abort = 1;
+            break;
+          }
+          __nanosleep(spins < 16 ? 32 : 256);
+        }
+      }
+      __syncthreads();
+      if (s_abort) return;
+    }
     for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) a.vv[i] = a.hv[i];
     wave_publish(a, b, a.base);
   }
